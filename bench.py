@@ -1,0 +1,327 @@
+"""Benchmark: particle push + charge scatter on the 2049x1025 / 64M-ion ES-PIC workload.
+
+One step = KineticMaterial.updateFields() for the ion species on the GPU: E gather,
+velocity update, move, surface/exit handling, deterministic int64 node scatter, density
+finalisation, plus the automatic cell sort every 8 steps (amortised inside the timed
+steps).  Metric: particle-steps/s (whole job).  The particle arrays (64M x 24 B =
+1.6 GB) are far larger than L2 (129 MB), so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference algorithm's CPU restatement (the oracle port; the
+Java reference cannot run here) on the host cores with a bounded sample of the same
+workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s (push+scatter); Poisson ms/solve to 1e-6 residual"
+UNIT = "particle-steps/s"
+# algorithmic bytes: per particle-step read cell, fx, fy, vx, vy (20 B) + write them (20 B);
+# per node per push launch: E read (8 B) + int64 count read-modify-write via atomics (16 B)
+BYTES_PER_PARTICLE = 40
+BYTES_PER_NODE_PUSH = 24
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def setup_workload(n_particles, seed=0):
+    from starfish_gb300 import workloads as W
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    cfg = W.config1(n_particles)
+    spec = cfg.mesh
+    _, efi, efj = W.electrode_efield(spec)
+    dom = GpuDomain(spec, device=0)
+    dom.set_efield(efi, efj)
+    km = KineticMaterial(dom, cfg.ion.mass, cfg.ion.charge, cfg.ion.spwt,
+                         capacity=int(n_particles * 1.02) + 1024)
+    chunk = 8 * 1024 * 1024
+    for c0 in range(0, n_particles, chunk):
+        m = min(chunk, n_particles - c0)
+        pos, vel = W.uniform_maxwellian(spec, cfg.ion, m, seed + c0)
+        km.add_particles(pos, vel, rewind=True, dt=cfg.dt)
+    km.sort()
+    return cfg, dom, km, efi, efj
+
+
+def cpu_baseline_sample(cfg, efi, efj, n_sample, threads, steps=1, seed=1):
+    """The oracle port (reference algorithm, FP64 AoS) on a bounded sample of the workload."""
+    from oracle import oracle as O
+    from starfish_gb300 import workloads as W
+    spec = cfg.mesh
+    m = O.OMesh(spec.ni, spec.nj, spec.x0, spec.dh, spec.domain, spec.node_type, spec.face_type)
+    pos, vel = W.uniform_maxwellian(spec, cfg.ion, n_sample, seed)
+    P = np.zeros((n_sample, 12))
+    P[:, 0:2] = pos[:, 0:2]
+    P[:, 3:6] = vel
+    P[:, 6] = (pos[:, 0] - spec.x0[0]) / spec.dh[0]
+    P[:, 7] = (pos[:, 1] - spec.x0[1]) / spec.dh[1]
+    P[:, 9] = cfg.ion.spwt
+    P[:, 10] = 1
+    vol = O.node_volumes(m)
+    segs = O.seg_table(spec.seg_xy, spec.seg_btype, O.SURF_ABSORB)
+    if spec.node_seg_ptr is None:
+        spec.node_seg_ptr, spec.node_seg_idx = O.node_segments(m, spec.seg_xy)
+    done = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        n_alive = int((P[:, 10] == 1).sum())
+        O.push(m, efi, efj, cfg.ion.charge, cfg.ion.mass, cfg.dt, segs, spec.node_seg_ptr,
+               spec.node_seg_idx, P, threads=threads)
+        O.update_fields(m, vol, P)
+        done += n_alive
+    t = time.perf_counter() - t0
+    return done / t, t
+
+
+def run_reference(args):
+    """Reference arm: the CPU restatement with all host threads, same workload and metric."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from starfish_gb300 import workloads as W
+    cfg = W.config1(64 * 1024 * 1024)
+    _, efi, efj = W.electrode_efield(cfg.mesh)
+    threads = os.cpu_count() or 1
+    n_sample = 4 * 1024 * 1024
+    for _ in range(max(args.warmup, 0) and 1):
+        cpu_baseline_sample(cfg, efi, efj, n_sample // 8, threads, 1)
+    vals = []
+    for k in range(args.steps):
+        v, t = cpu_baseline_sample(cfg, efi, efj, n_sample, threads, 1, seed=k + 1)
+        vals.append((v, t))
+    total_ps = n_sample * args.steps
+    total_t = sum(t for _, t in vals)
+    value = total_ps / total_t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * 64 * 1024 * 1024 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": cfg.name, "mesh": [cfg.mesh.ni, cfg.mesh.nj],
+                   "particles": 64 * 1024 * 1024, "dt": cfg.dt,
+                   "sample_particles_per_step": n_sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n_sample} particles of the 64M workload per step, "
+                                   f"{args.steps} steps, push on {threads} threads + serial scatter"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--particles", type=int, default=64 * 1024 * 1024)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from starfish_gb300 import build as B
+    B.build()
+
+    cfg, dom, km, efi, efj = setup_workload(args.particles, seed=1000 * rank)
+    ext = torch.cuda.ExternalStream(dom.stream())
+    W_ = max(args.warmup, 3) if args.warmup >= 0 else 3
+    for _ in range(W_):
+        km.update_fields(cfg.dt, stats=False)
+
+    # ---- timed region: device-resident particles (value) ----
+    dom.timing(True)
+    dom.timing_reset()
+    launches0 = dom.launches()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    np_start = km.get_np()
+    psteps = 0
+    ev0.record(ext)
+    for _ in range(args.steps):
+        psteps += np_start
+        st = km.update_fields(cfg.dt, stats=False)
+        np_start = st["np"]
+    ev1.record(ext)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    launches = dom.launches() - launches0
+    push_ms, push_n = dom.kernel_time("push")
+    fin_ms, fin_n = dom.kernel_time("finalize")
+    sort_ms, sort_n = dom.kernel_time("sort")
+    slow_ms, slow_n = dom.kernel_time("push_slow")
+    dom.timing(False)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot = torch.tensor([float(psteps)], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(tot)
+        psteps_all = tot.item()
+    else:
+        psteps_all = float(psteps)
+    ms = t.item()
+    value = psteps_all / (ms / 1e3)
+
+    # ---- end-to-end through the C ABI with host buffers ----
+    efi_h = torch.from_numpy(efi.copy()).pin_memory().numpy()
+    efj_h = torch.from_numpy(efj.copy()).pin_memory().numpy()
+    nd_h = torch.zeros(cfg.mesh.nn, dtype=torch.float64).pin_memory().numpy()
+    import ctypes as C
+    from starfish_gb300 import abi
+    lib = dom.lib
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    np_start = km.get_np()
+    e_steps = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e_steps += np_start
+        dom.check(lib.sf_set_efield(dom.ctx, abi.ptr(efi_h), abi.ptr(efj_h)))
+        st = abi.PushStats()
+        dom.check(lib.sf_push_deposit(dom.ctx, km.sid, cfg.dt, abi.PUSH_STATS, C.byref(st)))
+        dom.check(lib.sf_get_field(dom.ctx, abi.FIELD_ND, km.sid, abi.ptr(nd_h)))
+        np_start = st.np
+    e2e_s = time.perf_counter() - t0
+    e2e_val = e_steps * world / e2e_s
+
+    peak, peak_kind = measured_peaks()
+    nn = cfg.mesh.nn
+    avg_np = psteps / max(args.steps, 1)
+    push_avg_ms = push_ms / max(push_n, 1)
+    alg_bytes = BYTES_PER_PARTICLE * avg_np + BYTES_PER_NODE_PUSH * nn
+    achieved = alg_bytes / (push_avg_ms / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "push_traffic.json")
+    if os.path.exists(tf):
+        try:
+            tr = json.load(open(tf))
+            traffic = tr["bytes_per_particle"] * avg_np + tr.get("bytes_per_node", 0) * nn
+        except Exception:
+            traffic = None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": W_, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": cfg.name, "mesh": [cfg.mesh.ni, cfg.mesh.nj], "dx_m": cfg.mesh.dh[0],
+                   "particles_per_gpu": args.particles, "dt_s": cfg.dt, "sort_interval": 8,
+                   "l2": "inputs larger than L2 (1.6 GB of particles per step)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "k_push", "alg_bytes_per_launch": alg_bytes,
+                     "avg_launch_ms": push_avg_ms},
+        "kernel_ms": {"push": push_ms / max(push_n, 1), "push_slow": slow_ms / max(slow_n, 1),
+                      "finalize": fin_ms / max(fin_n, 1), "sort": sort_ms / max(sort_n, 1),
+                      "sort_launches": sort_n},
+        "clocks": clk,
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * nn,
+                "d2h_bytes_per_step": 8 * nn + 64},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        n_sample = 4 * 1024 * 1024
+        v, t = cpu_baseline_sample(cfg, efi, efj, n_sample, threads, steps=2)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{n_sample} particles of the 64M workload, 2 steps "
+                                          f"(push on {threads} threads, serial scatter), {t:.1f} s"}
+    dom.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

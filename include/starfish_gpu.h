@@ -1,0 +1,220 @@
+/*
+ * starfish_gpu.h -- C ABI of libstarfish_gpu.so, the GB300 (sm_103a) hot path of
+ * Starfish's ES-PIC/DSMC time step.
+ *
+ * The Java host reaches these entry points through JNI (or the FFM API) from
+ * GPU-backed subclasses registered under the reference's own plugin names
+ * (KINETIC, POISSON, DSMC, MCC).  Each entry point below names the reference
+ * method it replaces (paths relative to the Starfish project root,
+ * src/starfish/...).
+ *
+ * Conventions
+ *  - Every function returns an int status: SF_OK (0) or one of SF_ERR_*.
+ *    sf_last_error(ctx) gives a one-line message for the last failure.  No
+ *    function exits the process or blocks without bound.
+ *  - Node arrays are j-major, u = j*ni + i (Mesh.IJtoN, core/domain/Mesh.java:893-897),
+ *    the order of Vec.deflate (core/common/Vec.java:165-180).  Cell arrays are
+ *    j-major over (ni-1)*(nj-1) cells.
+ *  - Host pointers are caller-owned and only read/written during the call.
+ *    Device state (particles, fields, solver) is owned by the context.
+ *  - A context is not thread-safe; all work is issued on one CUDA stream per
+ *    context and every call returns after its work is complete.
+ */
+#ifndef STARFISH_GPU_H
+#define STARFISH_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sf_ctx sf_ctx;
+
+/* ---- status codes ---------------------------------------------------------- */
+#define SF_OK 0
+#define SF_ERR_ARG 1           /* invalid argument / unsupported configuration   */
+#define SF_ERR_CUDA 2          /* CUDA runtime error                              */
+#define SF_ERR_NOT_CONVERGED 3 /* solver hit its iteration cap (Solver.java:384)  */
+#define SF_ERR_DIVERGED 4      /* NaN/Inf residual (Solver.calculateResidue 437)  */
+#define SF_ERR_TIMEOUT 5       /* a bounded device wait gave up                   */
+#define SF_ERR_OOM 6           /* device allocation failed / capacity exceeded    */
+#define SF_ERR_STATE 7         /* call out of order (e.g. no field set yet)       */
+
+/* ---- enumerations, numerically equal to the reference's codes ------------------ */
+/* DomainModule.DomainType */
+#define SF_DOMAIN_XY 0
+#define SF_DOMAIN_RZ 1
+#define SF_DOMAIN_ZR 2
+/* Mesh.NodeType (core/domain/Mesh.java:172-173) */
+#define SF_NODE_OPEN (-1)
+#define SF_NODE_DIRICHLET 0
+#define SF_NODE_INSULATOR 1
+#define SF_NODE_INTERNAL 2
+/* Mesh.DomainBoundaryType (core/domain/Mesh.java:140-141) */
+#define SF_DB_OPEN (-1)
+#define SF_DB_DIRICHLET 0
+#define SF_DB_NEUMANN 1
+#define SF_DB_PERIODIC 2
+#define SF_DB_SYMMETRY 3
+#define SF_DB_MESH 4
+#define SF_DB_SINK 5
+#define SF_DB_CIRCUIT 6
+/* Mesh.Face (core/domain/Mesh.java:107-108) */
+#define SF_FACE_RIGHT 0
+#define SF_FACE_TOP 1
+#define SF_FACE_LEFT 2
+#define SF_FACE_BOTTOM 3
+/* Boundary.BoundaryType (core/boundaries/Boundary.java:124-125) */
+#define SF_BT_DIRICHLET 0
+#define SF_BT_OPEN 1
+#define SF_BT_SINK 2
+#define SF_BT_VIRTUAL 3
+/* Surface impact handlers (interactions/SurfaceInteraction.java:29-36).
+ * SF_SURF_PASS: the boundary has no material, the particle is not stopped
+ * (KineticMaterial.java:570-571). */
+#define SF_SURF_PASS (-1)
+#define SF_SURF_ABSORB 0
+#define SF_SURF_NONE 1
+#define SF_SURF_SPECULAR 2
+#define SF_SURF_DIFFUSE 3
+/* field selectors for sf_get_field */
+#define SF_FIELD_ND 0      /* number density of a species (Material.getDen)          */
+#define SF_FIELD_U 1       /* mean velocity components (KineticMaterial U/V/W)        */
+#define SF_FIELD_V 2
+#define SF_FIELD_W 3
+#define SF_FIELD_COUNT 4   /* raw deposited weight per node, sum of w*S (no 1/V)      */
+#define SF_FIELD_NODE_VOL 5 /* node volumes in use (Mesh.node_vol)                      */
+#define SF_FIELD_PHI 10    /* potential (DomainModule phi)                            */
+#define SF_FIELD_RHO 11    /* charge density used by the last solve                    */
+#define SF_FIELD_EFI 12    /* electric field components (DomainModule efi/efj)         */
+#define SF_FIELD_EFJ 13
+#define SF_FIELD_NE 14     /* Boltzmann electron density                               */
+
+/* ---- mesh --------------------------------------------------------------------- */
+typedef struct {
+  int32_t ni, nj;            /* nodes (UniformMesh)                                  */
+  double x0[2];              /* origin (UniformMesh.x0)                              */
+  double dh[2];              /* spacing (UniformMesh.dh)                             */
+  int32_t domain_type;       /* SF_DOMAIN_*                                          */
+  const int8_t* node_type;   /* ni*nj SF_NODE_* codes (Mesh.node[i][j].type)         */
+  const double* bc_value;    /* ni*nj Dirichlet values (Mesh.node[i][j].bc_value) or NULL */
+  const double* node_vol;    /* ni*nj node volumes (Mesh.node_vol) or NULL = computed */
+  const int8_t* face_type;   /* 4*max(ni,nj) SF_DB_* codes, rows in SF_FACE_* order;
+                                RIGHT/LEFT rows indexed by j, TOP/BOTTOM rows by i   */
+  int32_t n_segments;        /* linear boundary segments (LinearSegment)             */
+  const double* seg_xy;      /* 4 per segment: x1, y1, x2, y2                        */
+  const int32_t* seg_btype;  /* SF_BT_* of the owning boundary                       */
+  const int32_t* node_seg_ptr; /* ni*nj+1 CSR of Mesh.node[i][j].segments            */
+  const int32_t* node_seg_idx; /* (Mesh.setNodeControlVolumes, Mesh.java:1217-1296)  */
+} sf_mesh_desc;
+
+/* Per-step totals returned by the push, as ParticleMover accumulates them
+ * (KineticMaterial.java:406-413, summed over movers at :244-256), before the
+ * multiplication by the species mass. */
+typedef struct {
+  double n_sum;        /* sum of mpw over surviving particles                 */
+  double p_sum[3];     /* sum of mpw*v                                         */
+  double e_sum;        /* sum of mpw*|v| (Vec.mag3, as in the reference)        */
+  double boundary_charge; /* sum of mpw*q over absorbed particles (SourceModule.boundary_charge) */
+  int64_t np;          /* particles alive after the step                        */
+  int64_t n_removed;   /* particles removed this step                           */
+  int64_t n_slow;      /* particles that took the exact surface/exit path       */
+  int64_t n_bounce_limited; /* particles that used all 10 bounces               */
+} sf_push_stats;
+
+/* Creates a context on CUDA device `device` for one uniform mesh.
+ * Replaces: Mesh/UniformMesh set-up as seen by KineticMaterial and Solver
+ * (UniformMesh.java:55-72, Mesh.initNodes 364-402, Solver.init 153-189). */
+int sf_ctx_create(const sf_mesh_desc* mesh, int device, sf_ctx** out);
+int sf_ctx_destroy(sf_ctx* ctx);
+/* Last error message of a context (or of the last failed sf_ctx_create when ctx is NULL). */
+const char* sf_last_error(const sf_ctx* ctx);
+/* Library version string. */
+const char* sf_version(void);
+
+/* Host-side helper: per-node lists of the segments whose box test passes, as
+ * Mesh.setNodeControlVolumes builds node[i][j].segments (core/domain/Mesh.java:1217-1296).
+ * Call with ptr == idx == NULL to get *nnz; then ptr has ni*nj+1 and idx *nnz entries.
+ * Needs no GPU.  A Java host passes its own lists instead. */
+int sf_build_node_segments(int32_t ni, int32_t nj, const double* x0, const double* dh,
+                           int32_t n_segments, const double* seg_xy, int32_t* ptr, int32_t* idx,
+                           int64_t* nnz);
+
+/* ---- species and particles ------------------------------------------------- */
+/* Registers a kinetic species (KineticMaterial ctor; mass in kg, charge in C,
+ * spwt = specific weight Material.spwt0).  capacity: maximum particles held.
+ * nd_back: background density added after the scatter (Material.java:618-632). */
+int sf_species_add(sf_ctx* ctx, double charge, double mass, double spwt, int64_t capacity,
+                   double nd_back, int32_t* sid);
+/* Automatic cell sort every `interval` pushes (default 8; 0 = only explicit sorts).
+ * Sorting keeps the deposit's shared-memory tiles compact and drops removed slots. */
+int sf_species_set_sort_interval(sf_ctx* ctx, int32_t sid, int32_t interval);
+/* Surface handler of the boundary owning segment `seg` for this species
+ * (MaterialInteraction list, Material.performSurfaceInteraction, Material.java:279-336).
+ * vth: boundary thermal speed for SF_SURF_DIFFUSE (Boundary.getVth); c_rest, c_accom:
+ * MaterialInteraction coefficients.  Default for every segment: SF_SURF_ABSORB. */
+int sf_species_set_surface(sf_ctx* ctx, int32_t sid, int32_t seg, int32_t model, double vth,
+                           double c_rest, double c_accom);
+/* Appends particles from physical positions (KineticMaterial.addParticle, KineticMaterial.java:759-802):
+ * lc = XtoL(pos), clamped to the mesh; if rewind != 0 the velocity is rewound by -dt/2
+ * with the current electric field (needs sf_set_efield / a Poisson solve first).
+ * pos, vel: n*3 doubles; mpw: n weights or NULL (= spwt; only uniform weights are held). */
+int sf_particles_append(sf_ctx* ctx, int32_t sid, int64_t n, const double* pos, const double* vel,
+                        const double* mpw, int32_t rewind, double dt);
+/* Appends particles given logical coordinates (Particle.lc, n*2) instead of positions;
+ * no rewind.  Used to load identical state into the GPU and the reference. */
+int sf_particles_append_lc(sf_ctx* ctx, int32_t sid, int64_t n, const double* lc,
+                           const double* vel);
+/* Number of particles currently held (alive). */
+int sf_particles_count(sf_ctx* ctx, int32_t sid, int64_t* np);
+/* Copies particles to the host in storage order: lc (n*2), vel (n*3); dead slots are
+ * skipped.  cap = capacity of the host arrays; *n_out = particles written. */
+int sf_particles_download(sf_ctx* ctx, int32_t sid, int64_t cap, double* lc, double* vel,
+                          int64_t* n_out);
+/* Counting sort of a species by cell; drops removed particles (the cell binning of
+ * DSMC.perform(mesh), DSMC.java:194-231, done once for all users). */
+int sf_particles_sort(sf_ctx* ctx, int32_t sid);
+/* Removes all particles of a species. */
+int sf_particles_clear(sf_ctx* ctx, int32_t sid);
+
+/* ---- fields ----------------------------------------------------------------- */
+/* Sets the electric field used by the push (DomainModule efi/efj, FP64 host -> FP32 device). */
+int sf_set_efield(sf_ctx* ctx, const double* efi, const double* efj);
+/* Copies a node field to the host (FP64, ni*nj). */
+int sf_get_field(sf_ctx* ctx, int32_t field, int32_t sid, double* out);
+
+/* ---- push + scatter ---------------------------------------------------------- */
+/* One time step of KineticMaterial.updateFields() for one species on one mesh:
+ * ParticleMover.run (KineticMaterial.java:299-422) -- E gather, v += q/m E dt, move,
+ * ProcessBoundary (:471-750) surface hits and domain exits -- followed by the node
+ * scatter of updateFields(md) (:168-197) into a deterministic int64 fixed-point
+ * grid and the density nd = sum(w S)/V + nd_back.
+ * flags: SF_PUSH_STATS computes sf_push_stats (reads vz); SF_PUSH_MOMENTS also
+ * deposits the u/v/w moments.  stats may be NULL. */
+#define SF_PUSH_STATS 1
+#define SF_PUSH_MOMENTS 2
+int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_stats* stats);
+/* Surface flux / mass deposit accumulated by the push since the last reset, per
+ * segment and split over the segment ends exactly like the Field1D scatter of
+ * Material.addSurfaceMomentum / addSurfaceMassDeposit (Material.java:759-796):
+ * out arrays hold 2 doubles per segment (weight at the start / end node). */
+int sf_get_surface_flux(sf_ctx* ctx, int32_t sid, double* flux, double* deposit);
+int sf_reset_surface_flux(sf_ctx* ctx, int32_t sid);
+
+/* ---- measurement ---------------------------------------------------------- */
+/* The CUDA stream (cudaStream_t) all work of the context is issued on. */
+int sf_ctx_get_stream(sf_ctx* ctx, void** stream);
+/* Per-kernel CUDA-event timing on the context stream (off by default).  When on,
+ * each hot kernel launch is bracketed by events and its device time accumulated
+ * under its name ("push", "push_slow", "sort", "finalize", "poisson_residual", ...). */
+int sf_timing_enable(sf_ctx* ctx, int32_t on);
+int sf_timing_get(sf_ctx* ctx, const char* kernel, double* total_ms, int64_t* launches);
+int sf_timing_reset(sf_ctx* ctx);
+/* Number of kernels this context has launched since creation (or the last reset). */
+int sf_launch_count(sf_ctx* ctx, int64_t* launches, int32_t reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STARFISH_GPU_H */

@@ -1,0 +1,267 @@
+// sf_internal.h -- shared declarations of libstarfish_gpu.so (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/starfish_gpu.h"
+
+namespace sf {
+
+// ---------------------------------------------------------------------------------
+// Errors: every ABI entry point catches sf::Error and turns it into a status code.
+// ---------------------------------------------------------------------------------
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define SF_CUDA(x)                                                                    \
+  do {                                                                                \
+    cudaError_t e_ = (x);                                                             \
+    if (e_ != cudaSuccess)                                                            \
+      throw ::sf::Error(e_ == cudaErrorMemoryAllocation ? SF_ERR_OOM : SF_ERR_CUDA,  \
+                        std::string(#x) + ": " + cudaGetErrorString(e_));             \
+  } while (0)
+
+#define SF_REQUIRE(cond, code, msg)                          \
+  do {                                                       \
+    if (!(cond)) throw ::sf::Error((code), std::string(msg)); \
+  } while (0)
+
+constexpr uint32_t DEAD = 0xFFFFFFFFu;   // cell word of a removed particle
+constexpr double QE = 1.60217646e-19;    // Constants.QE  (core/common/Constants.java:22)
+constexpr double EPS0 = 8.85418782e-12;  // Constants.EPS0
+constexpr double KB = 1.3806503e-23;     // Constants.K
+constexpr double PI = 3.14159265358979323846;
+constexpr double FLT_EPS_REF = 1e-7;     // Constants.FLT_EPS
+// Deposit fixed point: one particle of weight spwt contributes S * 2^31 (S in [0,1]).
+constexpr double DEP_SCALE = 2147483648.0;
+// Moment fixed point: S * v * 2^16 per (m/s).
+constexpr double MOM_SCALE = 65536.0;
+
+// Segment end points x1, y1, x2, y2 (16-byte aligned for vector loads).
+struct alignas(16) Seg4 {
+  double x, y, z, w;
+};
+
+// Packed cell word: (j << 16) | i.  Meshes are limited to 65535 nodes per direction.
+__host__ __device__ inline uint32_t pack_cell(int i, int j) { return ((uint32_t)j << 16) | (uint32_t)i; }
+__host__ __device__ inline int cell_i(uint32_t c) { return (int)(c & 0xFFFFu); }
+__host__ __device__ inline int cell_j(uint32_t c) { return (int)(c >> 16); }
+
+// ---------------------------------------------------------------------------------
+// Device views (plain structs passed by value to kernels)
+// ---------------------------------------------------------------------------------
+struct MeshView {
+  int ni, nj, nmax, domain;
+  double x0[2], dh[2];
+  float inv_dx, inv_dy;
+  const float2* E;              // ni*nj (efi, efj) FP32
+  const uint8_t* seg_dist;      // ni*nj Chebyshev distance to the nearest node listing a
+                                // DIRICHLET/SINK segment (255 = none within 255)
+  const int* node_seg_ptr;      // ni*nj+1
+  const int* node_seg_idx;
+  const Seg4* seg_xy;        // x1, y1, x2, y2
+  const int* seg_btype;
+  const int8_t* face_type;      // 4*nmax
+  const double* node_vol;       // ni*nj
+  int nseg;
+};
+
+struct SurfaceView {
+  const int* model;     // per segment SF_SURF_*
+  const float4* param;  // vth, c_rest, c_accom, unused
+  double* flux;         // 2 per segment
+  double* deposit;      // 2 per segment
+};
+
+struct ParticlesView {
+  uint32_t* cell;
+  float2* frac;
+  float2* vxy;
+  float* vz;
+  int64_t n;  // slots in use
+};
+
+// ---------------------------------------------------------------------------------
+// Philox4x32-10 counter-based RNG (Salmon, Moraes, Dror, Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC'11).  Streams are keyed by (seed, purpose) and
+// counted by (particle or cell index, step, draw).
+// ---------------------------------------------------------------------------------
+struct Philox {
+  uint4 ctr;
+  uint2 key;
+  uint4 buf;
+  int left;
+  __device__ Philox(uint64_t seed, uint32_t stream, uint64_t index, uint32_t step) {
+    key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32) ^ (stream * 0x9E3779B9u));
+    ctr = make_uint4((uint32_t)index, (uint32_t)(index >> 32), step, 0u);
+    left = 0;
+  }
+  __device__ static inline void round1(uint4& c, const uint2 k) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+  }
+  __device__ inline uint4 block() {
+    uint4 c = ctr;
+    uint2 k = key;
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+      round1(c, k);
+      k.x += 0x9E3779B9u;
+      k.y += 0xBB67AE85u;
+    }
+    ctr.w++;
+    return c;
+  }
+  __device__ inline uint32_t next_u32() {
+    if (left == 0) {
+      buf = block();
+      left = 4;
+    }
+    uint32_t v = (left == 4) ? buf.x : (left == 3) ? buf.y : (left == 2) ? buf.z : buf.w;
+    left--;
+    return v;
+  }
+  // uniform in [0,1) with 53 random bits
+  __device__ inline double uniform() {
+    uint32_t a = next_u32() >> 5, b = next_u32() >> 6;
+    return ((double)a * 67108864.0 + (double)b) * (1.0 / 9007199254740992.0);
+  }
+  // uniform in [0,1) with 24 random bits
+  __device__ inline float uniformf() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
+};
+
+// RNG stream identifiers
+enum : uint32_t { RNG_SURFACE = 1, RNG_DSMC = 2, RNG_MCC = 3, RNG_INJECT = 4 };
+
+}  // namespace sf
+
+// ---------------------------------------------------------------------------------
+// Host-side context
+// ---------------------------------------------------------------------------------
+struct SfSpecies {
+  double charge = 0, mass = 1, spwt = 1, nd_back = 0;
+  int64_t cap = 0;
+  int64_t n = 0;         // slots in use (alive + removed, until the next sort)
+  int64_t n_dead = 0;    // removed slots among n
+  bool sorted = false;   // slots are in cell order with no removed slots
+  sf::ParticlesView cur{}, alt{};
+  unsigned long long* count = nullptr;  // ni*nj fixed-point deposit
+  long long* mom = nullptr;             // 3*ni*nj fixed-point moments
+  double* nd = nullptr;                 // ni*nj number density
+  double* uvw = nullptr;                // 3*ni*nj mean velocity
+  bool moments_valid = false;
+  int* seg_model = nullptr;
+  float4* seg_param = nullptr;
+  double* flux = nullptr;     // 2*nseg
+  double* deposit = nullptr;  // 2*nseg
+  uint32_t step = 0;          // pushes done (RNG counter)
+  int sort_interval = 8;      // automatic sort every N pushes (0 = never)
+  int pushes_since_sort = 1 << 30;
+};
+
+struct SfPoisson;  // sf_poisson.cu
+
+// CUDA-event timing of named kernels on the context stream
+struct SfTimer {
+  bool on = false;
+  struct Rec {
+    std::string name;
+    double ms = 0;
+    int64_t launches = 0;
+  };
+  std::vector<Rec> recs;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;  // rec index, events
+  std::vector<cudaEvent_t> pool;
+};
+
+struct sf_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  std::string err;
+  // mesh (host copies)
+  int ni = 0, nj = 0, nmax = 0, domain = 0;
+  double x0[2] = {0, 0}, dh[2] = {1, 1};
+  std::vector<int8_t> node_type, face_type;
+  std::vector<double> bc_value, node_vol;
+  int nseg = 0;
+  std::vector<double> seg_xy;
+  std::vector<int> seg_btype;
+  // device mesh
+  float2* E = nullptr;
+  bool efield_set = false;
+  uint8_t* seg_dist = nullptr;
+  int* node_seg_ptr = nullptr;
+  int* node_seg_idx = nullptr;
+  sf::Seg4* d_seg_xy = nullptr;
+  int* d_seg_btype = nullptr;
+  int8_t* d_face_type = nullptr;
+  double* d_node_vol = nullptr;
+  // scratch
+  int* slow_idx = nullptr;        // capacity = max species capacity
+  int64_t slow_cap = 0;
+  unsigned long long* counters = nullptr;  // [0] slow count, [1] removed, [2] bounce-limited
+  double* stats_partial = nullptr;         // per-block partial sums
+  int stats_blocks = 0;
+  int* bins = nullptr;                     // (ncells+1) sort bins
+  int* bins_tmp = nullptr;
+  int* scan_blocks = nullptr;
+  double* host_pinned = nullptr;           // small pinned staging area
+  double* dscratch = nullptr;              // ni*nj FP64 scratch (field transfers)
+  std::vector<SfSpecies*> species;
+  SfPoisson* poisson = nullptr;
+  uint64_t seed = 0x5eed5eedULL;
+  int64_t launches = 0;   // kernels launched
+  SfTimer timer;
+
+  sf::MeshView mesh_view() const;
+  int ncells() const { return (ni - 1) * (nj - 1); }
+};
+
+// helpers shared between translation units
+void sf_poisson_destroy_internal(sf_ctx* ctx);                       // sf_poisson.cu
+int sf_poisson_get_field_internal(sf_ctx* ctx, int field, double* out);  // sf_poisson.cu
+namespace sf {
+void launch_sort(sf_ctx* ctx, SfSpecies* sp);
+void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments);
+SfSpecies* get_species(sf_ctx* ctx, int sid);
+void ensure_scratch(sf_ctx* ctx, int64_t particles);
+// Timing scope: brackets the kernels launched inside with events when timing is on.
+struct TimedScope {
+  sf_ctx* ctx;
+  int rec = -1;
+  cudaEvent_t a = nullptr, b = nullptr;
+  TimedScope(sf_ctx* c, const char* name);
+  ~TimedScope();
+};
+void timer_collect(sf_ctx* ctx);  // after a stream sync: accumulate pending event pairs
+inline int grid_for(int64_t n, int block, int max_blocks) {
+  int64_t g = (n + block - 1) / block;
+  if (g > max_blocks) g = max_blocks;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+}  // namespace sf
+
+// Wraps an ABI body: converts exceptions into status codes and records the message.
+#define SF_API_BEGIN try {
+#define SF_API_END(ctx)                                      \
+  }                                                          \
+  catch (const sf::Error& e) {                               \
+    if (ctx) (ctx)->err = e.what();                          \
+    return e.code;                                           \
+  }                                                          \
+  catch (const std::exception& e) {                          \
+    if (ctx) (ctx)->err = e.what();                          \
+    return SF_ERR_ARG;                                       \
+  }                                                          \
+  return SF_OK;

@@ -1,0 +1,786 @@
+// sf_push.cu -- particle push + node scatter (the KineticMaterial hot path).
+//
+// One call of sf_push_deposit() does, for one species, what
+// KineticMaterial.updateFields() does per step (core/materials/KineticMaterial.java:117-197):
+//   ParticleMover.run (:299-422)   E gather, v += q/m E dt, x += v dt, ProcessBoundary
+//   updateFields(md)  (:168-197)   node scatter of the particle weights (+ u/v/w moments)
+//   Material.update   (Material.java:618-632)  nd = sum(w S)/V + nd_back
+//
+// Kernels
+//   k_push     fused push + deposit over cell-sorted SoA particles.  Particles whose
+//              move neither leaves the mesh nor comes near a surface segment (checked
+//              with a per-node distance map) finish here; each block accumulates its
+//              tile's deposit in shared memory (warp-aggregated with match/reduce) and
+//              flushes it with one 64-bit atomic per touched node.
+//   k_push_slow  the remaining particles ("slow queue"), in FP64 with the reference's
+//              exact surface-hit and domain-exit logic, up to 10 bounces.
+//   k_finalize  int64 fixed-point counts -> FP64 density (and mean velocities).
+// The deposit is an integer sum, so node densities are bit-identical run to run.
+#include <climits>
+#include <cmath>
+
+#include "sf_internal.h"
+
+using namespace sf;
+
+namespace {
+
+constexpr int PB = 256;            // threads per block
+constexpr int PPT = 4;             // particles per thread per tile
+constexpr int TILE = PB * PPT;     // particles per block tile
+constexpr int SBOX = 4096;         // shared-memory deposit box (nodes)
+
+struct PushArgs {
+  float qm_dt;        // (q/m) dt
+  float dt_dx, dt_dy; // dt/dx, dt/dy
+  float dt;
+  float dx, dy;
+  float r0x, r0y;     // mesh origin (radius origin for RZ / ZR)
+  double dt64;
+  double qm;          // q/m
+  double charge, spwt;
+  uint64_t seed;
+  uint32_t step;
+};
+
+__device__ __forceinline__ unsigned quant(float w) {
+  // S in [0,1] -> round(S * 2^31); S = 1 gives 2^31 which fits in 32 bits
+  return __float2uint_rn(w * 2147483648.0f);
+}
+
+// Bilinear weights of the scatter (Field2D.scatter, core/domain/Field2D.java:244-295):
+// XY plain; RZ/ZR with Ruyten's eq. 4.2 in the radial direction, written relative to
+// the cell's lower radius rm so that FP32 keeps its precision away from the axis:
+//   d = 1 - (1-f)(4 rm + (2-f) dr) / (2 (2 rm + dr))
+template <int DOM>
+__device__ __forceinline__ void scatter_weights(float fx, float fy, int i, int j, const PushArgs& a,
+                                                float& di, float& dj) {
+  di = fx;
+  dj = fy;
+  if (DOM == SF_DOMAIN_RZ) {
+    float rm = a.r0x + (float)i * a.dx;
+    di = 1.f - 0.5f * (1.f - fx) * (4.f * rm + (2.f - fx) * a.dx) / (2.f * rm + a.dx);
+  } else if (DOM == SF_DOMAIN_ZR) {
+    float rm = a.r0y + (float)j * a.dy;
+    dj = 1.f - 0.5f * (1.f - fy) * (4.f * rm + (2.f - fy) * a.dy) / (2.f * rm + a.dy);
+  }
+}
+
+__device__ __forceinline__ float2 gather_E(const MeshView& m, int i, int j, float fx, float fy) {
+  // Field2D.gather (Field2D.java:318-350); at lc = n-1 the cell is n-2 with fraction 1,
+  // which gives gather_safe's value (:371-390).
+  int u = j * m.ni + i;
+  float2 e00 = __ldg(&m.E[u]), e10 = __ldg(&m.E[u + 1]);
+  float2 e11 = __ldg(&m.E[u + m.ni + 1]), e01 = __ldg(&m.E[u + m.ni]);
+  float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w11 = fx * fy, w01 = (1.f - fx) * fy;
+  float2 e;
+  e.x = w00 * e00.x + w10 * e10.x + w11 * e11.x + w01 * e01.x;
+  e.y = w00 * e00.y + w10 * e10.y + w11 * e11.y + w01 * e01.y;
+  return e;
+}
+
+struct Kahan {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+};
+
+// ---------------------------------------------------------------------------------
+// fused push + deposit
+// ---------------------------------------------------------------------------------
+template <int DOM, bool STATS, bool MOM>
+__global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushArgs a,
+                                              unsigned long long* __restrict__ count,
+                                              long long* __restrict__ mom, int* __restrict__ slow_idx,
+                                              unsigned long long* __restrict__ counters,
+                                              double* __restrict__ stats_partial) {
+  __shared__ unsigned long long acc[SBOX];
+  __shared__ int sred[4][PB / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned FULL = 0xffffffffu;
+  const size_t nn = (size_t)m.ni * m.nj;
+  Kahan st_px, st_py, st_pz, st_e;
+  unsigned st_n = 0;
+
+  for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < P.n; t0 += (int64_t)gridDim.x * TILE) {
+    int pi[PPT], pj[PPT];
+    float pfx[PPT], pfy[PPT];
+    float pv[PPT][3];
+    bool dep[PPT];
+    int imin = INT_MAX, imax = -1, jmin = INT_MAX, jmax = -1;
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+      const int64_t p = t0 + k * PB + threadIdx.x;
+      dep[k] = false;
+      pi[k] = pj[k] = 0;
+      pfx[k] = pfy[k] = 0.f;
+      if (p < P.n) {
+        const uint32_t c = P.cell[p];
+        if (c != DEAD) {
+          const int i = cell_i(c), j = cell_j(c);
+          const float2 f = P.frac[p];
+          float2 v = P.vxy[p];
+          // velocity update (KineticMaterial.java:336-346); B = 0
+          const float2 e = gather_E(m, i, j, f.x, f.y);
+          v.x += a.qm_dt * e.x;
+          v.y += a.qm_dt * e.y;
+          float vz = (DOM != SF_DOMAIN_XY || STATS || MOM) ? P.vz[p] : 0.f;
+          // move in logical coordinates (x += v dt; XtoL)
+          float nfx, nfy, nvx = v.x, nvy = v.y, nvz = vz;
+          if (DOM == SF_DOMAIN_XY) {
+            nfx = f.x + v.x * a.dt_dx;
+            nfy = f.y + v.y * a.dt_dy;
+          } else if (DOM == SF_DOMAIN_ZR) {
+            // rotateToZR (KineticMaterial.java:444-462) relative to the cell radius rj
+            nfx = f.x + v.x * a.dt_dx;
+            const float rj = a.r0y + (float)j * a.dy;
+            const float A = vz * a.dt;
+            const float dl = f.y * a.dy + v.y * a.dt;
+            const float B = rj + dl;
+            const float R = sqrtf(A * A + B * B);
+            const float den = R + rj;
+            const float rrel = den > 0.f ? (A * A + dl * (2.f * rj + dl)) / den : 0.f;
+            nfy = rrel / a.dy;
+            const float cs = R > 0.f ? B / R : 1.f, sn = R > 0.f ? A / R : 0.f;
+            nvy = cs * v.y + sn * vz;
+            nvz = -sn * v.y + cs * vz;
+          } else {
+            // rotateToRZ (KineticMaterial.java:424-442), radius along x
+            nfy = f.y + v.y * a.dt_dy;
+            const float ri = a.r0x + (float)i * a.dx;
+            const float A = vz * a.dt;
+            const float dl = f.x * a.dx + v.x * a.dt;
+            const float B = ri + dl;
+            const float R = sqrtf(A * A + B * B);
+            const float den = R + ri;
+            const float rrel = den > 0.f ? (A * A + dl * (2.f * ri + dl)) / den : 0.f;
+            nfx = rrel / a.dx;
+            const float cs = R > 0.f ? B / R : 1.f, sn = R > 0.f ? A / R : 0.f;
+            nvx = cs * v.x + sn * vz;
+            nvz = -sn * v.x + cs * vz;
+          }
+          float fdi = floorf(nfx), fdj = floorf(nfy);
+          nfx -= fdi;
+          nfy -= fdj;
+          if (nfx >= 1.f) { nfx -= 1.f; fdi += 1.f; }
+          if (nfy >= 1.f) { nfy -= 1.f; fdj += 1.f; }
+          const int di = (int)fdi, dj = (int)fdj;
+          const int i2 = i + di, j2 = j + dj;
+          const int span = max(abs(di), abs(dj)) + 1;
+          const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
+          const bool clear = (int)__ldg(&m.seg_dist[j * m.ni + i]) > span;
+          if (inside && clear) {
+            P.cell[p] = pack_cell(i2, j2);
+            P.frac[p] = make_float2(nfx, nfy);
+            P.vxy[p] = make_float2(nvx, nvy);
+            if (DOM != SF_DOMAIN_XY) P.vz[p] = nvz;
+            dep[k] = true;
+            pi[k] = i2;
+            pj[k] = j2;
+            pfx[k] = nfx;
+            pfy[k] = nfy;
+            pv[k][0] = nvx;
+            pv[k][1] = nvy;
+            pv[k][2] = nvz;
+            imin = min(imin, i2);
+            imax = max(imax, i2);
+            jmin = min(jmin, j2);
+            jmax = max(jmax, j2);
+            if (STATS) {
+              st_n++;
+              st_px.add(nvx);
+              st_py.add(nvy);
+              st_pz.add(nvz);
+              st_e.add(sqrtf(nvx * nvx + nvy * nvy + nvz * nvz));
+            }
+          } else {
+            // exact path later: keep the old position, store the updated velocity
+            P.vxy[p] = v;
+            const unsigned long long slot = atomicAdd(&counters[0], 1ULL);
+            slow_idx[slot] = (int)p;
+          }
+        }
+      }
+    }
+    // ---- block bounding box of this tile's deposits ----
+    imin = __reduce_min_sync(FULL, imin);
+    jmin = __reduce_min_sync(FULL, jmin);
+    imax = __reduce_max_sync(FULL, imax);
+    jmax = __reduce_max_sync(FULL, jmax);
+    if (lane == 0) {
+      sred[0][wid] = imin;
+      sred[1][wid] = jmin;
+      sred[2][wid] = imax;
+      sred[3][wid] = jmax;
+    }
+    __syncthreads();
+    imin = sred[0][0];
+    jmin = sred[1][0];
+    imax = sred[2][0];
+    jmax = sred[3][0];
+#pragma unroll
+    for (int w = 1; w < PB / 32; w++) {
+      imin = min(imin, sred[0][w]);
+      jmin = min(jmin, sred[1][w]);
+      imax = max(imax, sred[2][w]);
+      jmax = max(jmax, sred[3][w]);
+    }
+    const int bw = imax - imin + 2, bh = jmax - jmin + 2;
+    const bool any = imax >= 0;
+    const bool use_smem = any && (bw * bh <= SBOX);
+    if (use_smem) {
+      for (int q = threadIdx.x; q < bw * bh; q += PB) acc[q] = 0ULL;
+    }
+    __syncthreads();
+    if (any) {
+#pragma unroll
+      for (int k = 0; k < PPT; k++) {
+        // scatter skip rule at the far mesh edges (lc >= n-1 is not scattered)
+        bool d = dep[k] && !((pfx[k] >= 1.f && pi[k] == m.ni - 2) || (pfy[k] >= 1.f && pj[k] == m.nj - 2));
+        float wx, wy;
+        scatter_weights<DOM>(pfx[k], pfy[k], pi[k], pj[k], a, wx, wy);
+        const unsigned q00 = d ? quant((1.f - wx) * (1.f - wy)) : 0u;
+        const unsigned q10 = d ? quant(wx * (1.f - wy)) : 0u;
+        const unsigned q11 = d ? quant(wx * wy) : 0u;
+        const unsigned q01 = d ? quant((1.f - wx) * wy) : 0u;
+        if (MOM && d) {
+          const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
+          const int base = pj[k] * m.ni + pi[k];
+          const int off[4] = {0, 1, m.ni + 1, m.ni};
+#pragma unroll
+          for (int cc = 0; cc < 4; cc++)
+#pragma unroll
+            for (int dd = 0; dd < 3; dd++)
+              atomicAdd((unsigned long long*)&mom[dd * nn + base + off[cc]],
+                        (unsigned long long)__float2ll_rn(s[cc] * pv[k][dd] * 65536.0f));
+        }
+        if (use_smem) {
+          const unsigned key = d ? (unsigned)((pj[k] - jmin) * bw + (pi[k] - imin)) : 0xFFFFFFFFu;
+          const unsigned grp = __match_any_sync(FULL, key);
+          const unsigned lo00 = __reduce_add_sync(grp, q00 & 0xFFFFu), hi00 = __reduce_add_sync(grp, q00 >> 16);
+          const unsigned lo10 = __reduce_add_sync(grp, q10 & 0xFFFFu), hi10 = __reduce_add_sync(grp, q10 >> 16);
+          const unsigned lo11 = __reduce_add_sync(grp, q11 & 0xFFFFu), hi11 = __reduce_add_sync(grp, q11 >> 16);
+          const unsigned lo01 = __reduce_add_sync(grp, q01 & 0xFFFFu), hi01 = __reduce_add_sync(grp, q01 >> 16);
+          if (d && lane == __ffs(grp) - 1) {
+            atomicAdd(&acc[key], ((unsigned long long)hi00 << 16) + lo00);
+            atomicAdd(&acc[key + 1], ((unsigned long long)hi10 << 16) + lo10);
+            atomicAdd(&acc[key + bw + 1], ((unsigned long long)hi11 << 16) + lo11);
+            atomicAdd(&acc[key + bw], ((unsigned long long)hi01 << 16) + lo01);
+          }
+        } else {
+          const unsigned key = d ? (unsigned)(pj[k] * m.ni + pi[k]) : 0xFFFFFFFFu;
+          const unsigned grp = __match_any_sync(FULL, key);
+          const unsigned lo00 = __reduce_add_sync(grp, q00 & 0xFFFFu), hi00 = __reduce_add_sync(grp, q00 >> 16);
+          const unsigned lo10 = __reduce_add_sync(grp, q10 & 0xFFFFu), hi10 = __reduce_add_sync(grp, q10 >> 16);
+          const unsigned lo11 = __reduce_add_sync(grp, q11 & 0xFFFFu), hi11 = __reduce_add_sync(grp, q11 >> 16);
+          const unsigned lo01 = __reduce_add_sync(grp, q01 & 0xFFFFu), hi01 = __reduce_add_sync(grp, q01 >> 16);
+          if (d && lane == __ffs(grp) - 1) {
+            atomicAdd(&count[key], ((unsigned long long)hi00 << 16) + lo00);
+            atomicAdd(&count[key + 1], ((unsigned long long)hi10 << 16) + lo10);
+            atomicAdd(&count[key + m.ni + 1], ((unsigned long long)hi11 << 16) + lo11);
+            atomicAdd(&count[key + m.ni], ((unsigned long long)hi01 << 16) + lo01);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (use_smem) {
+      for (int q = threadIdx.x; q < bw * bh; q += PB) {
+        const unsigned long long v = acc[q];
+        if (v) atomicAdd(&count[(size_t)(jmin + q / bw) * m.ni + imin + q % bw], v);
+      }
+    }
+    __syncthreads();
+  }
+  if (STATS) {
+    // block reduction of the per-thread sums (FP64 from here on)
+    double vals[5] = {(double)st_n, (double)st_px.s - st_px.c, (double)st_py.s - st_py.c,
+                      (double)st_pz.s - st_pz.c, (double)st_e.s - st_e.c};
+    __shared__ double sd[5][PB / 32];
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+      double x = vals[q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULL, x, o);
+      if (lane == 0) sd[q][wid] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+      double x = 0;
+      for (int w = 0; w < PB / 32; w++) x += sd[threadIdx.x][w];
+      stats_partial[(size_t)blockIdx.x * 8 + threadIdx.x] = x;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// exact path (FP64): ProcessBoundary with surface segments and domain faces
+// ---------------------------------------------------------------------------------
+struct Seg64 {
+  double x1[2], x2[2];
+};
+
+__device__ inline void seg_intersect(const Seg4 s, const double p3[2], const double p4[2], double t[2]) {
+  // LinearSegment.intersect + InfiniteLineIntersect (core/boundaries/LinearSegment.java:113-179)
+  const double x1 = s.x, y1 = s.y, x2 = s.z, y2 = s.w;
+  const double x3 = p3[0], y3 = p3[1], x4 = p4[0], y4 = p4[1];
+  double den = (x1 - x2) * (y3 - y4) - (y1 - y2) * (x3 - x4);
+  if (den == 0) { t[0] = -1; t[1] = -1; return; }
+  double xp0 = ((x1 * y2 - y1 * x2) * (x3 - x4) - (x1 - x2) * (x3 * y4 - y3 * x4)) / den;
+  double xp1 = ((x1 * y2 - y1 * x2) * (y3 - y4) - (y1 - y2) * (x3 * y4 - y3 * x4)) / den;
+  if (fabs(x2 - x1) > 1e-6) t[0] = (xp0 - x1) / (x2 - x1);
+  else t[0] = (xp1 - y1) / (y2 - y1);
+  if (t[0] < -FLT_EPS_REF || t[0] > (1 + FLT_EPS_REF)) { t[0] = -1; t[1] = -1; return; }
+  if (fabs(x4 - x3) > 1e-6) t[1] = (xp0 - x3) / (x4 - x3);
+  else t[1] = (xp1 - y3) / (y4 - y3);
+  if (t[1] < -FLT_EPS_REF || t[1] > (1 + FLT_EPS_REF)) { t[0] = -1; t[1] = -1; return; }
+  t[0] = fmin(fmax(t[0], 0.0), 1.0);
+  t[1] = fmin(fmax(t[1], 0.0), 1.0);
+}
+
+__device__ inline void seg_normal_tangent(const Seg4 s, double n[3], double tg[3]) {
+  // LinearSegment constructor (LinearSegment.java:22-46)
+  double dx = s.z - s.x, dy = s.w - s.y;
+  double len = sqrt(dx * dx + dy * dy);
+  dx /= len;
+  dy /= len;
+  tg[0] = dx; tg[1] = dy; tg[2] = 0;
+  n[0] = -dy; n[1] = dx; n[2] = 0;
+}
+
+__device__ double sample_maxw_speed(Philox& r, double v_th) {
+  // Utils.SampleMaxwSpeed (core/common/Utils.java:69-87), rejection bounded at 10^4 tries
+  double bin_max = 6 * v_th;
+  double a = 4 / (sqrt(PI) * v_th * v_th * v_th);
+  double fm_max = 4 / (sqrt(PI) * v_th) * exp(-1.0);
+  double v = v_th;
+  for (int tries = 0; tries < 10000; tries++) {
+    v = r.uniform() * bin_max;
+    double fm = a * v * v * exp(-v * v / (v_th * v_th));
+    if ((fm / fm_max) > r.uniform()) return v;
+  }
+  return v;
+}
+
+struct SlowArgs {
+  SurfaceView sv;
+  unsigned long long* counters;
+  double* stats_slow;   // 5 sums + boundary charge
+};
+
+// returns alive; follows KineticMaterial.ProcessBoundary (KineticMaterial.java:471-750)
+__device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const PushArgs& a, double pos[2],
+                                 double vel[3], double lc[2], double& pdt, const double old[2],
+                                 const double lc_old[2], Philox& rng, bool& periodic) {
+  const double dt0 = pdt;
+  pdt = 0;
+  int i_min = (int)fmin(lc[0], lc_old[0]), i_max = (int)fmax(lc[0], lc_old[0]);
+  int j_min = (int)fmin(lc[1], lc_old[1]), j_max = (int)fmax(lc[1], lc_old[1]);
+  if (i_min < 0) i_min = 0;
+  if (j_min < 0) j_min = 0;
+  if (i_max >= m.ni) i_max = m.ni - 1;
+  if (j_max >= m.nj) j_max = m.nj - 1;
+  double tp_min = 2.0, tsurf_min = 0;
+  int seg_min = -1;
+  for (int i = i_min; i <= i_max; i++)
+    for (int j = j_min; j <= j_max; j++) {
+      const int u = j * m.ni + i;
+      for (int k = m.node_seg_ptr[u]; k < m.node_seg_ptr[u + 1]; k++) {
+        const int s = m.node_seg_idx[k];
+        const int bt = m.seg_btype[s];
+        if (bt != SF_BT_DIRICHLET && bt != SF_BT_SINK) continue;
+        const Seg4 sxy = m.seg_xy[s];
+        double t[2];
+        seg_intersect(sxy, old, pos, t);
+        const double t_part = t[1];
+        if (t_part > 0) {
+          double n[3], tg[3];
+          seg_normal_tangent(sxy, n, tg);
+          const double acs = (n[0] * vel[0] + n[1] * vel[1]) / sqrt(vel[0] * vel[0] + vel[1] * vel[1]);
+          if (t_part < FLT_EPS_REF && acs > 0) continue;
+          if (t_part < tp_min) {
+            tp_min = t_part;
+            tsurf_min = t[0];
+            seg_min = s;
+          }
+        }
+      }
+    }
+  bool alive = true;
+  if (seg_min >= 0) {
+    tp_min *= 0.9999;
+    pos[0] = old[0] + tp_min * (pos[0] - old[0]);
+    pos[1] = old[1] + tp_min * (pos[1] - old[1]);
+    lc[0] = (pos[0] - m.x0[0]) / m.dh[0];
+    lc[1] = (pos[1] - m.x0[1]) / m.dh[1];
+    pdt = dt0 * (1 - tp_min);
+    if (lc[0] < 0 && lc[0] > -FLT_EPS_REF) lc[0] = 0;
+    if (lc[1] < 0 && lc[1] > -FLT_EPS_REF) lc[1] = 0;
+    const int model = sa.sv.model[seg_min];
+    const Seg4 sxy = m.seg_xy[seg_min];
+    double n[3], tg[3];
+    seg_normal_tangent(sxy, n, tg);
+    switch (model) {
+      case SF_SURF_PASS:
+      case SF_SURF_NONE: alive = true; break;
+      case SF_SURF_SPECULAR: {  // SurfaceInteraction.java:104-150
+        const double mag = sqrt(vel[0] * vel[0] + vel[1] * vel[1]) * 1.4142135623730951;
+        vel[0] += n[0] * mag;
+        vel[1] += n[1] * mag;
+        alive = true;
+        break;
+      }
+      case SF_SURF_DIFFUSE: {  // SurfaceInteraction.java:153-213 (cosine emission)
+        const float4 pr = sa.sv.param[seg_min];
+        const double v_refl = sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]) * pr.y;
+        const double v_diff = sample_maxw_speed(rng, pr.x);
+        const double v_mag = v_refl + pr.z * (v_diff - v_refl);
+        // Vec.lambertianVector (core/common/Vec.java:450-471)
+        double cosphi = sqrt(1.0 - rng.uniform());
+        if (cosphi > 0.99999) cosphi = 0.99999;
+        const double theta = 2 * PI * rng.uniform();
+        const double sinphi = sqrt(1.0 - cosphi * cosphi);
+        const double c_t = cos(theta) * sinphi, c_n = cosphi, c_p = sin(theta) * sinphi;
+        const double pz[3] = {0, 0, 1};
+        for (int q = 0; q < 3; q++) vel[q] = v_mag * (c_t * tg[q] + c_n * n[q] + c_p * pz[q]);
+        alive = true;
+        break;
+      }
+      default: alive = false; break;  // ABSORB
+    }
+    if (!alive) atomicAdd(&sa.stats_slow[5], a.spwt * a.charge);
+    if (m.seg_btype[seg_min] == SF_BT_SINK) alive = false;
+    atomicAdd(&sa.sv.flux[2 * seg_min], a.spwt * (1 - tsurf_min));
+    atomicAdd(&sa.sv.flux[2 * seg_min + 1], a.spwt * tsurf_min);
+    if (!alive) {
+      atomicAdd(&sa.sv.deposit[2 * seg_min], a.spwt * (1 - tsurf_min));
+      atomicAdd(&sa.sv.deposit[2 * seg_min + 1], a.spwt * tsurf_min);
+      return false;
+    }
+  }
+  if (lc[0] < 0 || lc[1] < 0 || lc[0] >= m.ni - 1 || lc[1] >= m.nj - 1) {
+    double t_right = 99, t_top = 99, t_left = 99, t_bottom = 99;
+    if (lc[0] >= m.ni - 1) t_right = (m.ni - 1.0 - lc_old[0]) / (lc[0] - lc_old[0]);
+    if (lc[1] >= m.nj - 1) t_top = (m.nj - 1.0 - lc_old[1]) / (lc[1] - lc_old[1]);
+    if (lc[0] < 0) t_left = lc_old[0] / (lc_old[0] - lc[0]);
+    if (lc[1] < 0) t_bottom = lc_old[1] / (lc_old[1] - lc[1]);
+    int face = SF_FACE_RIGHT;
+    double t = t_right;
+    if (t_top < t) { face = SF_FACE_TOP; t = t_top; }
+    if (t_left < t) { face = SF_FACE_LEFT; t = t_left; }
+    if (t_bottom < t) { face = SF_FACE_BOTTOM; t = t_bottom; }
+    lc[0] = lc_old[0] + t * (lc[0] - lc_old[0]);
+    lc[1] = lc_old[1] + t * (lc[1] - lc_old[1]);
+    if (lc[0] < 0) lc[0] = 0;
+    else if (lc[0] > m.ni - 1) lc[0] = m.ni - 1;
+    if (lc[1] < 0) lc[1] = 0;
+    else if (lc[1] > m.nj - 1) lc[1] = m.nj - 1;
+    pos[0] = m.x0[0] + lc[0] * m.dh[0];
+    pos[1] = m.x0[1] + lc[1] * m.dh[1];
+    pdt = dt0 * (1 - t);
+    int i = (int)lc[0], j = (int)lc[1];
+    if (face == SF_FACE_TOP) j++;
+    if (face == SF_FACE_RIGHT) i++;
+    if (i < 0) i = 0;
+    if (j < 0) j = 0;
+    if (i >= m.ni - 1) i = m.ni - 1;
+    if (j >= m.nj - 1) j = m.nj - 1;
+    const int idx = (face == SF_FACE_LEFT || face == SF_FACE_RIGHT) ? j : i;
+    const int type = m.face_type[face * m.nmax + idx];
+    switch (type) {
+      case SF_DB_SYMMETRY: {  // Vec.mirror about UniformMesh.faceNormal
+        double n[3] = {0, 0, 0};
+        if (face == SF_FACE_LEFT) n[0] = 1;
+        else if (face == SF_FACE_RIGHT) n[0] = -1;
+        else if (face == SF_FACE_BOTTOM) n[1] = 1;
+        else n[1] = -1;
+        const double tm = vel[0] * n[0] + vel[1] * n[1] + vel[2] * n[2];
+        for (int q = 0; q < 3; q++) {
+          const double tq = n[q] * tm;
+          vel[q] = -tq + (vel[q] - tq);
+        }
+        return true;
+      }
+      case SF_DB_PERIODIC: {
+        const double Lx = (m.ni - 1) * m.dh[0], Ly = (m.nj - 1) * m.dh[1];
+        if (face == SF_FACE_LEFT) pos[0] += Lx;
+        else if (face == SF_FACE_RIGHT) pos[0] -= Lx;
+        else if (face == SF_FACE_BOTTOM) pos[1] += Ly;
+        else pos[1] -= Ly;
+        periodic = true;
+        return true;
+      }
+      default: return false;  // OPEN, DIRICHLET, NEUMANN, SINK, MESH, CIRCUIT
+    }
+  }
+  return alive;
+}
+
+template <int DOM>
+__global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, PushArgs a, SlowArgs sa,
+                                                   const int* __restrict__ slow_idx,
+                                                   unsigned long long* __restrict__ count,
+                                                   long long* __restrict__ mom, int mom_on) {
+  const unsigned long long nslow = sa.counters[0];
+  const size_t nn = (size_t)m.ni * m.nj;
+  for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; t < nslow;
+       t += (unsigned long long)gridDim.x * blockDim.x) {
+    const int64_t p = slow_idx[t];
+    const uint32_t c = P.cell[p];
+    const float2 f = P.frac[p];
+    const float2 v = P.vxy[p];
+    double lc[2] = {cell_i(c) + (double)f.x, cell_j(c) + (double)f.y};
+    double pos[2] = {m.x0[0] + lc[0] * m.dh[0], m.x0[1] + lc[1] * m.dh[1]};
+    double vel[3] = {v.x, v.y, (double)P.vz[p]};
+    double pdt = a.dt64;
+    Philox rng(a.seed, RNG_SURFACE, (uint64_t)p, a.step);
+    int bounces = 0;
+    bool alive = true, periodic = false;
+    while (pdt > 0 && bounces++ < 10) {
+      const double old[2] = {pos[0], pos[1]};
+      const double lc_old[2] = {lc[0], lc[1]};
+      pos[0] += vel[0] * pdt;
+      pos[1] += vel[1] * pdt;
+      if (DOM == SF_DOMAIN_RZ) {
+        const double A = vel[2] * pdt, B = pos[0];
+        const double R = sqrt(A * A + B * B);
+        const double cs = R > 0 ? B / R : 1.0, sn = R > 0 ? A / R : 0.0;
+        const double v1 = vel[0], v2 = vel[2];
+        pos[0] = R;
+        vel[0] = cs * v1 + sn * v2;
+        vel[2] = -sn * v1 + cs * v2;
+      } else if (DOM == SF_DOMAIN_ZR) {
+        const double A = vel[2] * pdt, B = pos[1];
+        const double R = sqrt(A * A + B * B);
+        const double cs = R > 0 ? B / R : 1.0, sn = R > 0 ? A / R : 0.0;
+        const double v1 = vel[1], v2 = vel[2];
+        pos[1] = R;
+        vel[1] = cs * v1 + sn * v2;
+        vel[2] = -sn * v1 + cs * v2;
+      }
+      lc[0] = (pos[0] - m.x0[0]) / m.dh[0];
+      lc[1] = (pos[1] - m.x0[1]) / m.dh[1];
+      periodic = false;
+      alive = process_boundary(m, sa, a, pos, vel, lc, pdt, old, lc_old, rng, periodic);
+      if (!alive) break;
+    }
+    if (!alive) {
+      P.cell[p] = DEAD;
+      atomicAdd(&sa.counters[1], 1ULL);
+      continue;
+    }
+    if (pdt > 0) atomicAdd(&sa.counters[2], 1ULL);  // remaining time is dropped
+    if (periodic) {
+      lc[0] = fmin(fmax((pos[0] - m.x0[0]) / m.dh[0], 0.0), m.ni - 1.0);
+      lc[1] = fmin(fmax((pos[1] - m.x0[1]) / m.dh[1], 0.0), m.nj - 1.0);
+    }
+    int i = (int)lc[0], j = (int)lc[1];
+    if (i > m.ni - 2) i = m.ni - 2;
+    if (j > m.nj - 2) j = m.nj - 2;
+    if (i < 0) i = 0;
+    if (j < 0) j = 0;
+    const float fx = (float)(lc[0] - i), fy = (float)(lc[1] - j);
+    P.cell[p] = pack_cell(i, j);
+    P.frac[p] = make_float2(fx, fy);
+    P.vxy[p] = make_float2((float)vel[0], (float)vel[1]);
+    P.vz[p] = (float)vel[2];
+    atomicAdd(&sa.stats_slow[0], 1.0);
+    atomicAdd(&sa.stats_slow[1], vel[0]);
+    atomicAdd(&sa.stats_slow[2], vel[1]);
+    atomicAdd(&sa.stats_slow[3], vel[2]);
+    atomicAdd(&sa.stats_slow[4], sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]));
+    if ((fx >= 1.f && i == m.ni - 2) || (fy >= 1.f && j == m.nj - 2)) continue;  // scatter skip rule
+    float wx, wy;
+    scatter_weights<DOM>(fx, fy, i, j, a, wx, wy);
+    const size_t u = (size_t)j * m.ni + i;
+    atomicAdd(&count[u], (unsigned long long)quant((1.f - wx) * (1.f - wy)));
+    atomicAdd(&count[u + 1], (unsigned long long)quant(wx * (1.f - wy)));
+    atomicAdd(&count[u + m.ni + 1], (unsigned long long)quant(wx * wy));
+    atomicAdd(&count[u + m.ni], (unsigned long long)quant((1.f - wx) * wy));
+    if (mom_on) {
+      const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
+      const size_t off[4] = {0, 1, (size_t)m.ni + 1, (size_t)m.ni};
+      const float vv[3] = {(float)vel[0], (float)vel[1], (float)vel[2]};
+      for (int cc = 0; cc < 4; cc++)
+        for (int dd = 0; dd < 3; dd++)
+          atomicAdd((unsigned long long*)&mom[dd * nn + u + off[cc]],
+                    (unsigned long long)__float2ll_rn(s[cc] * vv[dd] * 65536.0f));
+    }
+  }
+}
+
+// int64 fixed point -> density (Field2D.scaleByVol, Field2D.java:418-431) and mean
+// velocities (Field2D.divideByField, :403-414)
+__global__ void k_finalize(int nn, const unsigned long long* __restrict__ count, const long long* __restrict__ mom,
+                           const double* __restrict__ vol, double w_scale, double nd_back,
+                           double* __restrict__ nd, double* __restrict__ uvw, int mom_on) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x) {
+    const unsigned long long c = count[u];
+    nd[u] = (double)c * w_scale / vol[u] + nd_back;
+    if (mom_on) {
+      for (int d = 0; d < 3; d++)
+        uvw[(size_t)d * nn + u] = c ? ((double)mom[(size_t)d * nn + u] / MOM_SCALE) / ((double)c / DEP_SCALE) : 0.0;
+    }
+  }
+}
+
+__global__ void k_sum_partials(const double* part, int nblocks, double* out) {
+  // deterministic sum of per-block partials; one thread per quantity
+  int q = threadIdx.x;
+  if (q >= 5) return;
+  double s = 0;
+  for (int b = 0; b < nblocks; b++) s += part[(size_t)b * 8 + q];
+  out[q] = s;
+}
+
+struct KernelCfg {
+  int blocks_per_sm = 0;
+};
+
+template <int DOM, bool STATS, bool MOM>
+void launch_push_t(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid) {
+  k_push<DOM, STATS, MOM><<<grid, PB, 0, ctx->stream>>>(ctx->mesh_view(), sp->cur, a, sp->count, sp->mom,
+                                                      ctx->slow_idx, ctx->counters, ctx->stats_partial);
+}
+
+template <int DOM>
+void launch_push_dom(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid, bool stats, bool mom) {
+  if (stats && mom) launch_push_t<DOM, true, true>(ctx, sp, a, grid);
+  else if (stats) launch_push_t<DOM, true, false>(ctx, sp, a, grid);
+  else if (mom) launch_push_t<DOM, false, true>(ctx, sp, a, grid);
+  else launch_push_t<DOM, false, false>(ctx, sp, a, grid);
+}
+
+}  // namespace
+
+namespace sf {
+
+void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments) {
+  int nn = ctx->ni * ctx->nj;
+  ctx->launches++;
+  k_finalize<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+      nn, sp->count, sp->mom, ctx->d_node_vol, sp->spwt / DEP_SCALE, sp->nd_back, sp->nd, sp->uvw, moments ? 1 : 0);
+}
+
+}  // namespace sf
+
+extern "C" int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_stats* stats) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(dt > 0, SF_ERR_ARG, "dt must be positive");
+  SF_REQUIRE(ctx->efield_set, SF_ERR_STATE, "electric field not set (sf_set_efield or a Poisson solve)");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const bool want_stats = (flags & SF_PUSH_STATS) != 0;
+  const bool mom = (flags & SF_PUSH_MOMENTS) != 0;
+  // automatic cell sort every sort_interval pushes (the counter starts at the interval,
+  // so the first push of a species sorts)
+  if (sp->sort_interval > 0 && sp->pushes_since_sort >= sp->sort_interval) launch_sort(ctx, sp);
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  cudaStream_t s = ctx->stream;
+  SF_CUDA(cudaMemsetAsync(sp->count, 0, sizeof(unsigned long long) * nn, s));
+  if (mom) SF_CUDA(cudaMemsetAsync(sp->mom, 0, sizeof(long long) * 3 * nn, s));
+  SF_CUDA(cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * 8, s));
+  // stats_partial tail (after the per-block area) holds the slow-path sums
+  double* slow_stats = ctx->stats_partial + (size_t)8 * (ctx->stats_blocks - 1);
+  SF_CUDA(cudaMemsetAsync(ctx->stats_partial, 0, sizeof(double) * 8 * (size_t)ctx->stats_blocks, s));
+
+  PushArgs a;
+  a.qm_dt = (float)(sp->charge / sp->mass * dt);
+  a.dt_dx = (float)(dt / ctx->dh[0]);
+  a.dt_dy = (float)(dt / ctx->dh[1]);
+  a.dt = (float)dt;
+  a.dx = (float)ctx->dh[0];
+  a.dy = (float)ctx->dh[1];
+  a.r0x = (float)ctx->x0[0];
+  a.r0y = (float)ctx->x0[1];
+  a.dt64 = dt;
+  a.qm = sp->charge / sp->mass;
+  a.charge = sp->charge;
+  a.spwt = sp->spwt;
+  a.seed = ctx->seed;
+  a.step = sp->step;
+
+  int tiles = (int)((sp->n + TILE - 1) / TILE);
+  int grid = std::max(1, std::min(tiles, ctx->stats_blocks - 1));
+  if (sp->n > 0) {
+    {
+    TimedScope ts(ctx, "push");
+    ctx->launches++;
+    switch (ctx->domain) {
+      case SF_DOMAIN_XY: launch_push_dom<SF_DOMAIN_XY>(ctx, sp, a, grid, want_stats, mom); break;
+      case SF_DOMAIN_RZ: launch_push_dom<SF_DOMAIN_RZ>(ctx, sp, a, grid, want_stats, mom); break;
+      default: launch_push_dom<SF_DOMAIN_ZR>(ctx, sp, a, grid, want_stats, mom); break;
+    }
+    }
+    SF_CUDA(cudaGetLastError());
+    SlowArgs sa;
+    sa.sv.model = sp->seg_model;
+    sa.sv.param = sp->seg_param;
+    sa.sv.flux = sp->flux;
+    sa.sv.deposit = sp->deposit;
+    sa.counters = ctx->counters;
+    sa.stats_slow = slow_stats;
+    const int sgrid = ctx->num_sms * 4;
+    TimedScope ts(ctx, "push_slow");
+    ctx->launches++;
+    switch (ctx->domain) {
+      case SF_DOMAIN_XY:
+        k_push_slow<SF_DOMAIN_XY><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, ctx->slow_idx, sp->count, sp->mom, mom);
+        break;
+      case SF_DOMAIN_RZ:
+        k_push_slow<SF_DOMAIN_RZ><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, ctx->slow_idx, sp->count, sp->mom, mom);
+        break;
+      default:
+        k_push_slow<SF_DOMAIN_ZR><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, ctx->slow_idx, sp->count, sp->mom, mom);
+        break;
+    }
+    SF_CUDA(cudaGetLastError());
+  }
+  {
+    TimedScope ts(ctx, "finalize");
+    launch_finalize(ctx, sp, mom);
+  }
+  SF_CUDA(cudaGetLastError());
+  double* h = ctx->host_pinned;
+  unsigned long long hc[4];
+  SF_CUDA(cudaMemcpyAsync(hc, ctx->counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  if (want_stats) {
+    k_sum_partials<<<1, 32, 0, s>>>(ctx->stats_partial, grid, ctx->dscratch);
+    ctx->launches++;
+    SF_CUDA(cudaMemcpyAsync(h, ctx->dscratch, sizeof(double) * 5, cudaMemcpyDeviceToHost, s));
+    SF_CUDA(cudaMemcpyAsync(h + 8, slow_stats, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
+  }
+  SF_CUDA(cudaStreamSynchronize(s));
+  timer_collect(ctx);
+  sp->n_dead += (int64_t)hc[1];
+  sp->step++;
+  sp->pushes_since_sort++;
+  sp->moments_valid = mom;
+  if (hc[1] > 0) sp->sorted = false;
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    if (want_stats) {
+      stats->n_sum = (h[0] + h[8]) * sp->spwt;
+      for (int d = 0; d < 3; d++) stats->p_sum[d] = (h[1 + d] + h[9 + d]) * sp->spwt;
+      stats->e_sum = (h[4] + h[12]) * sp->spwt;
+      stats->boundary_charge = h[13];
+    }
+    stats->np = sp->n - sp->n_dead;
+    stats->n_removed = (int64_t)hc[1];
+    stats->n_slow = (int64_t)hc[0];
+    stats->n_bounce_limited = (int64_t)hc[2];
+  }
+  SF_API_END(ctx)
+}
+
+extern "C" int sf_species_set_sort_interval(sf_ctx* ctx, int32_t sid, int32_t interval) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(interval >= 0, SF_ERR_ARG, "interval must be >= 0");
+  sp->sort_interval = interval;
+  SF_API_END(ctx)
+}

@@ -1,0 +1,153 @@
+"""Host-side classes that mirror the reference's plugin surface on top of the C ABI.
+
+``GpuDomain`` stands for the DomainModule/Mesh a Starfish run holds,
+``KineticMaterial`` for core/materials/KineticMaterial.java (method names and
+argument meaning follow the reference: addParticle, updateFields, getDen ...),
+``PoissonSolver`` for pic/PoissonSolver.java, ``DSMC``/``MCC`` for
+collisions/DSMC.java and MCC.java.  Every method is one or a few C-ABI calls; no
+computation happens here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .workloads import MeshSpec
+
+
+class GpuDomain:
+    def __init__(self, spec: MeshSpec, device: int = 0):
+        self.lib = abi.load()
+        self.spec = spec
+        self._desc = spec.desc()
+        h = C.c_void_p()
+        rc = self.lib.sf_ctx_create(C.byref(self._desc), device, C.byref(h))
+        abi.check(rc, None)
+        self.ctx = h
+        self.ni, self.nj = spec.ni, spec.nj
+
+    def check(self, rc):
+        abi.check(rc, self.ctx)
+
+    def set_efield(self, efi, efj):
+        efi = np.ascontiguousarray(efi, np.float64)
+        efj = np.ascontiguousarray(efj, np.float64)
+        self.check(self.lib.sf_set_efield(self.ctx, abi.ptr(efi), abi.ptr(efj)))
+
+    def get_field(self, field, sid=0):
+        out = np.zeros(self.ni * self.nj)
+        self.check(self.lib.sf_get_field(self.ctx, field, sid, abi.ptr(out)))
+        return out
+
+    def stream(self):
+        s = C.c_void_p()
+        self.check(self.lib.sf_ctx_get_stream(self.ctx, C.byref(s)))
+        return s.value
+
+    def timing(self, on=True):
+        self.check(self.lib.sf_timing_enable(self.ctx, int(on)))
+
+    def timing_reset(self):
+        self.check(self.lib.sf_timing_reset(self.ctx))
+
+    def kernel_time(self, name):
+        ms = C.c_double()
+        n = C.c_int64()
+        self.check(self.lib.sf_timing_get(self.ctx, name.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def launches(self, reset=False):
+        n = C.c_int64()
+        self.check(self.lib.sf_launch_count(self.ctx, C.byref(n), int(reset)))
+        return n.value
+
+    def close(self):
+        if self.ctx:
+            self.lib.sf_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class KineticMaterial:
+    """GPU-resident kinetic species (KineticMaterial, core/materials/KineticMaterial.java)."""
+
+    def __init__(self, domain: GpuDomain, mass, charge, spwt, capacity, nd_back=0.0):
+        self.d = domain
+        sid = C.c_int32()
+        domain.check(domain.lib.sf_species_add(domain.ctx, charge, mass, spwt, int(capacity),
+                                               nd_back, C.byref(sid)))
+        self.sid = sid.value
+        self.mass, self.charge, self.spwt = mass, charge, spwt
+
+    # KineticMaterial.addParticle(pos, vel) with the -dt/2 velocity rewind
+    def add_particles(self, pos, vel, rewind=True, dt=0.0):
+        pos = np.ascontiguousarray(pos, np.float64)
+        vel = np.ascontiguousarray(vel, np.float64)
+        n = pos.shape[0]
+        self.d.check(self.d.lib.sf_particles_append(self.d.ctx, self.sid, n, abi.ptr(pos),
+                                                    abi.ptr(vel), None, int(rewind), float(dt)))
+
+    def add_particles_lc(self, lc, vel):
+        lc = np.ascontiguousarray(lc, np.float64)
+        vel = np.ascontiguousarray(vel, np.float64)
+        self.d.check(self.d.lib.sf_particles_append_lc(self.d.ctx, self.sid, lc.shape[0],
+                                                       abi.ptr(lc), abi.ptr(vel)))
+
+    def set_surface(self, seg, model, vth=0.0, c_rest=1.0, c_accom=1.0):
+        self.d.check(self.d.lib.sf_species_set_surface(self.d.ctx, self.sid, seg, model, vth,
+                                                       c_rest, c_accom))
+
+    def set_sort_interval(self, k):
+        self.d.check(self.d.lib.sf_species_set_sort_interval(self.d.ctx, self.sid, int(k)))
+
+    def sort(self):
+        self.d.check(self.d.lib.sf_particles_sort(self.d.ctx, self.sid))
+
+    def clear(self):
+        self.d.check(self.d.lib.sf_particles_clear(self.d.ctx, self.sid))
+
+    # KineticMaterial.updateFields(): push + scatter
+    def update_fields(self, dt, stats=True, moments=False):
+        st = abi.PushStats()
+        flags = (abi.PUSH_STATS if stats else 0) | (abi.PUSH_MOMENTS if moments else 0)
+        self.d.check(self.d.lib.sf_push_deposit(self.d.ctx, self.sid, float(dt), flags,
+                                                C.byref(st)))
+        return st.as_dict()
+
+    def get_np(self):
+        n = C.c_int64()
+        self.d.check(self.d.lib.sf_particles_count(self.d.ctx, self.sid, C.byref(n)))
+        return n.value
+
+    def get_den(self):
+        return self.d.get_field(abi.FIELD_ND, self.sid)
+
+    def get_count(self):
+        return self.d.get_field(abi.FIELD_COUNT, self.sid)
+
+    def get_uvw(self):
+        return tuple(self.d.get_field(f, self.sid) for f in (abi.FIELD_U, abi.FIELD_V, abi.FIELD_W))
+
+    def download(self):
+        n = self.get_np()
+        lc = np.zeros((max(n, 1), 2))
+        vel = np.zeros((max(n, 1), 3))
+        got = C.c_int64()
+        self.d.check(self.d.lib.sf_particles_download(self.d.ctx, self.sid, n, abi.ptr(lc),
+                                                      abi.ptr(vel), C.byref(got)))
+        return lc[:got.value], vel[:got.value]
+
+    def surface_flux(self):
+        ns = self.d.spec.seg_xy.reshape(-1, 4).shape[0]
+        flux = np.zeros(max(2 * ns, 1))
+        dep = np.zeros(max(2 * ns, 1))
+        self.d.check(self.d.lib.sf_get_surface_flux(self.d.ctx, self.sid, abi.ptr(flux),
+                                                    abi.ptr(dep)))
+        return flux[:2 * ns], dep[:2 * ns]

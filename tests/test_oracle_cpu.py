@@ -1,0 +1,142 @@
+"""CPU checks of the oracle: known answers from the Java SE specification and from physics.
+
+The reference ships no tests or golden vectors; these pin the oracle instead.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from starfish_gb300 import workloads as W
+
+
+def test_java_random_known_values():
+    # java.util.Random(0).nextDouble() sequence (Java SE API LCG; widely published values)
+    r = O.jrandom_doubles(0, 2)
+    assert r[0] == pytest.approx(0.730967787376657, abs=1e-15)
+    assert r[1] == pytest.approx(0.24053641567148587, abs=1e-15)
+    assert O.jrandom_doubles(42, 1)[0] == pytest.approx(0.7275636800328681, abs=1e-15)
+
+
+def test_sampler_moments():
+    # Utils.SampleMaxw3D: sum of 12 uniforms, scaled by v_th * 1.2 * sqrt(1/2)
+    v = O.sample_maxw3d(1, 200000, 1000.0)
+    sig = 1000.0 * 1.2 * np.sqrt(0.5)
+    assert abs(v.mean()) < 5 * sig / np.sqrt(v.size)
+    assert v.std() == pytest.approx(sig, rel=5e-3)
+    s = O.sample_maxw_speed(2, 100000, 1000.0)
+    # Maxwell speed distribution f ~ v^2 exp(-v^2/vth^2): mean = 2 vth / sqrt(pi)
+    assert s.mean() == pytest.approx(2 * 1000.0 / np.sqrt(np.pi), rel=1e-2)
+
+
+def test_bird_gamma():
+    import math
+    for x in (0.5, 1.0, 1.5, 1.69, 2.5, 3.3):
+        assert O.bird_gamma(x) == pytest.approx(math.gamma(x), rel=2e-4)
+
+
+def _omesh(spec):
+    return O.OMesh(spec.ni, spec.nj, spec.x0, spec.dh, spec.domain, spec.node_type, spec.face_type)
+
+
+def test_node_volumes_cover_domain():
+    spec = W.es_pic_mesh(21, 11, 1e-3)
+    vol = O.node_volumes(_omesh(spec))
+    Lx, Ly = spec.lengths()
+    assert vol.sum() == pytest.approx(Lx * Ly, rel=1e-12)
+
+
+def test_operator_structure_xy():
+    """The FVM assembly reduces to the 5-point Laplacian inside, identity on Dirichlet
+    nodes, central differences for the gradient (Solver.java:451-611)."""
+    spec = W.es_pic_mesh(15, 9, 1e-3, electrode_halfwidth=1.5e-3)
+    op = O.assemble(_omesh(spec))
+    p, c, v = op["A"]
+    ni = spec.ni
+    dx = spec.dh[0]
+    for j in range(1, spec.nj - 1):
+        for i in range(1, ni - 1):
+            u = j * ni + i
+            row = dict(zip(c[p[u]:p[u + 1]], v[p[u]:p[u + 1]]))
+            if op["fixed"][u]:
+                assert row == {u: 1.0}
+                continue
+            assert set(row) == {u, u - 1, u + 1, u - ni, u + ni}
+            assert row[u] * dx * dx == pytest.approx(-4.0, rel=1e-12)
+            for k in (u - 1, u + 1, u - ni, u + ni):
+                assert row[k] * dx * dx == pytest.approx(1.0, rel=1e-12)
+
+
+def test_poisson_linear_limit_matches_laplace():
+    """With a negligible electron density the NR solve is Laplace's equation; between
+    phi = 1 on the left wall and 0 on the right with Neumann top/bottom the solution is linear."""
+    ni, nj, dh = 17, 9, 1e-3
+    nmax = max(ni, nj)
+    node_type = np.full((nj, ni), O.NODE_OPEN, np.int8)
+    node_type[:, 0] = node_type[:, -1] = O.NODE_DIRICHLET
+    face = np.zeros((4, nmax), np.int8)
+    face[O.F_TOP, :] = O.DB_SYMMETRY
+    face[O.F_BOTTOM, :] = O.DB_SYMMETRY
+    bc = np.zeros((nj, ni))
+    bc[:, 0] = 1.0
+    m = O.OMesh(ni, nj, [0, 0], [dh, dh], O.DOM_XY, node_type.reshape(-1), face)
+    phi0 = np.zeros(ni * nj)
+    phi, it, out = O.poisson_nl(m, bc.reshape(-1), np.zeros(ni * nj), 1e-20, 2.0, 0.0, 8.85418782e-12,
+                                phi0, max_it=20000, tol=1e-12, nl_max_it=50, nl_tol=1e-10)
+    exact = np.tile(1.0 - np.arange(ni) / (ni - 1), nj)
+    assert np.max(np.abs(phi - exact)) < 1e-6
+
+
+def test_push_ballistic_uniform_field():
+    """No surfaces, uniform E: one push moves x by (v + qE/m dt) dt exactly."""
+    spec = W.es_pic_mesh(41, 21, 1e-3, walls=O.DB_OPEN, electrode_halfwidth=1e-4)
+    spec.seg_xy = np.zeros((0, 4))
+    m = _omesh(spec)
+    n = 100
+    rng = np.random.default_rng(0)
+    parts = np.zeros((n, 12))
+    lc = np.column_stack([rng.uniform(10, 30, n), rng.uniform(5, 15, n)])
+    parts[:, 6:8] = lc
+    parts[:, 0:2] = lc * 1e-3
+    parts[:, 3] = 50.0
+    parts[:, 4] = -20.0
+    parts[:, 9] = 1.0
+    parts[:, 10] = 1
+    E = 1000.0
+    efi = np.full(spec.nn, E)
+    efj = np.zeros(spec.nn)
+    q, mass, dt = 1.6e-19, 1.6e-26, 1e-6
+    alive, stats, _, _ = O.push(m, efi, efj, q, mass, dt, np.zeros((0, 9)), np.zeros(spec.nn + 1),
+                                np.zeros(0), parts)
+    assert alive == n
+    vx = 50.0 + q / mass * E * dt
+    assert np.allclose(parts[:, 3], vx, rtol=1e-14)
+    assert np.allclose(parts[:, 6], lc[:, 0] + vx * dt / 1e-3, rtol=0, atol=1e-10)
+    assert np.allclose(parts[:, 7], lc[:, 1] - 20.0 * dt / 1e-3, rtol=0, atol=1e-10)
+    assert stats[0] == pytest.approx(n)
+
+
+def test_scatter_conserves_weight():
+    spec = W.es_pic_mesh(21, 11, 1e-3)
+    m = _omesh(spec)
+    vol = O.node_volumes(m)
+    rng = np.random.default_rng(1)
+    n = 1000
+    parts = np.zeros((n, 12))
+    parts[:, 6] = rng.uniform(0, 19.999, n)
+    parts[:, 7] = rng.uniform(0, 9.999, n)
+    parts[:, 9] = 3.0
+    parts[:, 10] = 1
+    den = O.update_fields(m, vol, parts)
+    assert (den * vol).sum() == pytest.approx(3.0 * n, rel=1e-12)
+
+
+def test_node_segments_box_rule():
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    ptr, idx = O.node_segments(_omesh(spec), spec.seg_xy)
+    # every listed node lies within 2 cells of the electrode square
+    ni = spec.ni
+    nodes = np.repeat(np.arange(spec.nn), np.diff(ptr))
+    i, j = nodes % ni, nodes // ni
+    xlo, xhi = spec.seg_xy[:, 0].min() / 1e-3, spec.seg_xy[:, 0].max() / 1e-3
+    assert i.min() >= np.floor(xlo) - 2 and i.max() <= np.ceil(xhi) + 2
+    assert len(idx) > 0

@@ -2,7 +2,7 @@
 
 One step = KineticMaterial.updateFields() for the ion species on the GPU: E gather,
 velocity update, move, surface/exit handling, deterministic int64 node scatter, density
-finalisation, plus the automatic cell sort every 8 steps (amortised inside the timed
+finalisation, plus the automatic cell sort every 16 steps (amortised inside the timed
 steps).  Metric: particle-steps/s (whole job).  The particle arrays (64M x 24 B =
 1.6 GB) are far larger than L2 (129 MB), so no L2 flush is needed between steps.
 
@@ -294,7 +294,7 @@ def main():
         "warmup": W_, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": cfg.name, "mesh": [cfg.mesh.ni, cfg.mesh.nj], "dx_m": cfg.mesh.dh[0],
-                   "particles_per_gpu": args.particles, "dt_s": cfg.dt, "sort_interval": 8,
+                   "particles_per_gpu": args.particles, "dt_s": cfg.dt, "sort_interval": 16,
                    "l2": "inputs larger than L2 (1.6 GB of particles per step)",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

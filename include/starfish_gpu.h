@@ -147,7 +147,7 @@ int sf_build_node_segments(int32_t ni, int32_t nj, const double* x0, const doubl
  * nd_back: background density added after the scatter (Material.java:618-632). */
 int sf_species_add(sf_ctx* ctx, double charge, double mass, double spwt, int64_t capacity,
                    double nd_back, int32_t* sid);
-/* Automatic cell sort every `interval` pushes (default 8; 0 = only explicit sorts).
+/* Automatic cell sort every `interval` pushes (default 16; 0 = only explicit sorts).
  * Sorting keeps the deposit's shared-memory tiles compact and drops removed slots. */
 int sf_species_set_sort_interval(sf_ctx* ctx, int32_t sid, int32_t interval);
 /* Surface handler of the boundary owning segment `seg` for this species

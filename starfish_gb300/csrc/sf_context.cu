@@ -37,6 +37,7 @@ sf::MeshView sf_ctx::mesh_view() const {
   m.face_type = d_face_type;
   m.node_vol = d_node_vol;
   m.nseg = nseg;
+  m.all_delete = all_delete ? 1 : 0;
   return m;
 }
 
@@ -218,53 +219,153 @@ __global__ void k_rewind(MeshView m, ParticlesView p, int64_t base, int n, float
   p.vxy[d] = v;
 }
 
-// Warp-aggregated increment of bins[key] by 1 for each participating lane; returns the
-// lane's rank among lanes with the same key plus the bin's previous value when
-// `want_offset` (used by the scatter pass).
-__device__ inline int warp_agg_inc(int* bins, uint32_t key, bool active) {
-  unsigned full = __activemask();
-  uint32_t k = active ? key : 0xFFFFFFFFu;
-  unsigned grp = __match_any_sync(full, k);
-  int leader = __ffs(grp) - 1;
-  int lane = threadIdx.x & 31;
-  int rank = __popc(grp & ((1u << lane) - 1));
-  int base = 0;
-  if (active && lane == leader) base = atomicAdd(&bins[key], __popc(grp));
-  base = __shfl_sync(full, base, leader);
-  return base + rank;
-}
-
 __global__ void k_pack_efield(int nn, const double* __restrict__ efi, const double* __restrict__ efj,
                               float2* __restrict__ E) {
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x)
     E[u] = make_float2((float)efi[u], (float)efj[u]);
 }
 
-__global__ void k_hist(ParticlesView p, int ni, int* bins) {
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < p.n; base += stride) {
-    int64_t k = base + threadIdx.x;
-    uint32_t c = (k < p.n) ? p.cell[k] : DEAD;
-    bool act = c != DEAD;
-    uint32_t lin = act ? (uint32_t)(cell_j(c) * (ni - 1) + cell_i(c)) : 0;
-    warp_agg_inc(bins, lin, act);
+// Counting sort by cell key.  Each block takes chunks of SORT_CHUNK particles and
+// counts their keys in a shared-memory hash table (open addressing, linear probing;
+// a chunk has at most SORT_CHUNK distinct keys and the table twice as many slots, so a
+// probe always ends).  Global memory is then touched once per distinct key per chunk
+// instead of once per particle.
+constexpr int SORT_B = 256;
+constexpr int SORT_IPT = 8;
+constexpr int SORT_CHUNK = SORT_B * SORT_IPT;
+constexpr int SORT_HBITS = 12;
+constexpr int SORT_HSIZE = 1 << SORT_HBITS;  // 4096 >= 2 * SORT_CHUNK
+constexpr unsigned EMPTY_KEY = 0xFFFFFFFFu;
+
+__device__ inline unsigned hash_slot(unsigned key) { return (key * 2654435761u) >> (32 - SORT_HBITS); }
+
+// returns the slot of key, inserting it if absent
+__device__ inline unsigned hash_insert(unsigned* hkey, unsigned key) {
+  unsigned s = hash_slot(key);
+  for (int probe = 0; probe < SORT_HSIZE; probe++) {
+    unsigned k = hkey[s];
+    if (k == key) return s;
+    if (k == EMPTY_KEY) {
+      unsigned prev = atomicCAS(&hkey[s], EMPTY_KEY, key);
+      if (prev == EMPTY_KEY || prev == key) return s;
+    }
+    s = (s + 1) & (SORT_HSIZE - 1);
+  }
+  return SORT_HSIZE;  // unreachable: the table has more slots than a chunk has keys
+}
+
+__global__ void __launch_bounds__(SORT_B) k_sort_hist(ParticlesView p, int ntx, int* bins) {
+  __shared__ unsigned hkey[SORT_HSIZE];
+  __shared__ unsigned hcnt[SORT_HSIZE];
+  for (int64_t base = (int64_t)blockIdx.x * SORT_CHUNK; base < p.n; base += (int64_t)gridDim.x * SORT_CHUNK) {
+    for (int q = threadIdx.x; q < SORT_HSIZE; q += SORT_B) {
+      hkey[q] = EMPTY_KEY;
+      hcnt[q] = 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SORT_IPT; k++) {
+      const int64_t q = base + k * SORT_B + threadIdx.x;
+      const uint32_t c = (q < p.n) ? p.cell[q] : DEAD;
+      if (c == DEAD) continue;
+      const unsigned slot = hash_insert(hkey, cell_key(cell_i(c), cell_j(c), ntx));
+      if (slot < SORT_HSIZE) atomicAdd(&hcnt[slot], 1u);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < SORT_HSIZE; q += SORT_B)
+      if (hcnt[q]) atomicAdd(&bins[hkey[q]], (int)hcnt[q]);
+    __syncthreads();
   }
 }
 
-__global__ void k_scatter_sorted(ParticlesView src, ParticlesView dst, int ni, int* cursor) {
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < src.n; base += stride) {
-    int64_t k = base + threadIdx.x;
-    uint32_t c = (k < src.n) ? src.cell[k] : DEAD;
-    bool act = c != DEAD;
-    uint32_t lin = act ? (uint32_t)(cell_j(c) * (ni - 1) + cell_i(c)) : 0;
-    int d = warp_agg_inc(cursor, lin, act);
-    if (act) {
-      dst.cell[d] = c;
-      dst.frac[d] = src.frac[k];
-      dst.vxy[d] = src.vxy[k];
-      dst.vz[d] = src.vz[k];
+// Scatter pass: the chunk is first regrouped in shared memory by key (chunk-local
+// offsets from a scan of the per-key counts), then written out so that consecutive
+// threads store consecutive slots of each key's run -- coalesced writes instead of one
+// partial sector per particle.
+constexpr size_t SORT_SCATTER_SMEM =
+    (size_t)SORT_HSIZE * 3 * sizeof(unsigned) +
+    (size_t)SORT_CHUNK * (sizeof(uint32_t) + sizeof(float2) + sizeof(float2) + sizeof(float) + sizeof(int));
+
+__global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, ParticlesView dst, int ntx, int* cursor) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* s_frac = reinterpret_cast<float2*>(smem_raw);
+  float2* s_vxy = s_frac + SORT_CHUNK;
+  unsigned* hkey = reinterpret_cast<unsigned*>(s_vxy + SORT_CHUNK);
+  unsigned* hcnt = hkey + SORT_HSIZE;  // counts, then the key run's first output slot
+  unsigned* hoff = hcnt + SORT_HSIZE;  // chunk-local offset of each key
+  uint32_t* s_cell = hoff + SORT_HSIZE;
+  float* s_vz = reinterpret_cast<float*>(s_cell + SORT_CHUNK);
+  int* s_dst = reinterpret_cast<int*>(s_vz + SORT_CHUNK);
+  __shared__ int warp_tot[SORT_B / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int SPT = SORT_HSIZE / SORT_B;  // slots per thread in the scan
+  for (int64_t base = (int64_t)blockIdx.x * SORT_CHUNK; base < src.n; base += (int64_t)gridDim.x * SORT_CHUNK) {
+    for (int q = threadIdx.x; q < SORT_HSIZE; q += SORT_B) {
+      hkey[q] = EMPTY_KEY;
+      hcnt[q] = 0u;
     }
+    __syncthreads();
+    unsigned slot[SORT_IPT], rank[SORT_IPT];
+#pragma unroll
+    for (int k = 0; k < SORT_IPT; k++) {
+      const int64_t q = base + k * SORT_B + threadIdx.x;
+      const uint32_t c = (q < src.n) ? src.cell[q] : DEAD;
+      slot[k] = SORT_HSIZE;
+      if (c == DEAD) continue;
+      slot[k] = hash_insert(hkey, cell_key(cell_i(c), cell_j(c), ntx));
+      if (slot[k] < SORT_HSIZE) rank[k] = atomicAdd(&hcnt[slot[k]], 1u);
+    }
+    __syncthreads();
+    // exclusive scan of the counts over the table -> chunk-local offsets
+    unsigned loc[SPT];
+    unsigned tsum = 0;
+#pragma unroll
+    for (int q = 0; q < SPT; q++) {
+      loc[q] = tsum;
+      tsum += hcnt[threadIdx.x * SPT + q];
+    }
+    unsigned x = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[wid] = (int)x;
+    __syncthreads();
+    unsigned wpre = 0;
+    for (int w = 0; w < wid; w++) wpre += (unsigned)warp_tot[w];
+    const unsigned tpre = wpre + x - tsum;
+#pragma unroll
+    for (int q = 0; q < SPT; q++) hoff[threadIdx.x * SPT + q] = tpre + loc[q];
+    __syncthreads();
+    // reserve each key's run in the output; hcnt becomes the run's first slot
+    for (int q = threadIdx.x; q < SORT_HSIZE; q += SORT_B)
+      if (hcnt[q]) hcnt[q] = (unsigned)atomicAdd(&cursor[hkey[q]], (int)hcnt[q]);
+    __syncthreads();
+    // stage the chunk in key order
+#pragma unroll
+    for (int k = 0; k < SORT_IPT; k++) {
+      if (slot[k] >= SORT_HSIZE) continue;
+      const int64_t q = base + k * SORT_B + threadIdx.x;
+      const unsigned l = hoff[slot[k]] + rank[k];
+      s_cell[l] = src.cell[q];
+      s_frac[l] = src.frac[q];
+      s_vxy[l] = src.vxy[q];
+      s_vz[l] = src.vz[q];
+      s_dst[l] = (int)(hcnt[slot[k]] + rank[k]);
+    }
+    __syncthreads();
+    // live particles in the chunk = sum of the warp totals of the scan
+    unsigned nl = 0;
+    for (int w = 0; w < SORT_B / 32; w++) nl += (unsigned)warp_tot[w];
+    for (unsigned l = threadIdx.x; l < nl; l += SORT_B) {
+      const int d = s_dst[l];
+      dst.cell[d] = s_cell[l];
+      dst.frac[d] = s_frac[l];
+      dst.vxy[d] = s_vxy[l];
+      dst.vz[d] = s_vz[l];
+    }
+    __syncthreads();
   }
 }
 
@@ -365,22 +466,29 @@ static void exclusive_scan(sf_ctx* ctx, int* data, int n) {
 }
 
 void launch_sort(sf_ctx* ctx, SfSpecies* sp) {
-  int nc = ctx->ncells();
+  const int nk = ctx->nkeys;
   TimedScope ts(ctx, "sort");
-  SF_CUDA(cudaMemsetAsync(ctx->bins, 0, sizeof(int) * (size_t)(nc + 1), ctx->stream));
+  SF_CUDA(cudaMemsetAsync(ctx->bins, 0, sizeof(int) * (size_t)(nk + 1), ctx->stream));
   if (sp->n > 0) {
     ctx->launches += 5;
-    int g = grid_for(sp->n, 256, ctx->num_sms * 8);
-    k_hist<<<g, 256, 0, ctx->stream>>>(sp->cur, ctx->ni, ctx->bins);
-    exclusive_scan(ctx, ctx->bins, nc + 1);  // bins[nc] = total alive
-    SF_CUDA(cudaMemcpyAsync(ctx->bins_tmp, ctx->bins, sizeof(int) * (size_t)(nc + 1),
+    int g = grid_for((sp->n + SORT_CHUNK - 1) / SORT_CHUNK, 1, ctx->num_sms * 6);
+    k_sort_hist<<<g, SORT_B, 0, ctx->stream>>>(sp->cur, ctx->ntx, ctx->bins);
+    exclusive_scan(ctx, ctx->bins, nk + 1);  // bins[key] = first slot of the cell, bins[nk] = total
+    SF_CUDA(cudaMemcpyAsync(ctx->bins_tmp, ctx->bins, sizeof(int) * (size_t)(nk + 1),
                             cudaMemcpyDeviceToDevice, ctx->stream));
     ParticlesView dst = sp->alt;
     dst.n = sp->n;
-    k_scatter_sorted<<<g, 256, 0, ctx->stream>>>(sp->cur, dst, ctx->ni, ctx->bins_tmp);
+    static bool attr_set = false;
+    if (!attr_set) {
+      SF_CUDA(cudaFuncSetAttribute(k_sort_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)SORT_SCATTER_SMEM));
+      attr_set = true;
+    }
+    const int gs = grid_for((sp->n + SORT_CHUNK - 1) / SORT_CHUNK, 1, ctx->num_sms * 2);
+    k_sort_scatter<<<gs, SORT_B, SORT_SCATTER_SMEM, ctx->stream>>>(sp->cur, dst, ctx->ntx, ctx->bins_tmp);
     SF_CUDA(cudaGetLastError());
     int total = 0;
-    SF_CUDA(cudaMemcpyAsync(&total, ctx->bins + nc, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    SF_CUDA(cudaMemcpyAsync(&total, ctx->bins + nk, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     SF_CUDA(cudaStreamSynchronize(ctx->stream));
     std::swap(sp->cur, sp->alt);
     sp->cur.n = total;
@@ -445,6 +553,14 @@ int sf_ctx_create(const sf_mesh_desc* md, int device, sf_ctx** out) {
                  "unsupported node type (INSULATOR nodes are not supported)");
     }
     ctx->face_type.assign(md->face_type, md->face_type + 4 * (size_t)ctx->nmax);
+    ctx->all_delete = true;
+    for (int f = 0; f < 4; f++) {
+      const int len = (f == SF_FACE_LEFT || f == SF_FACE_RIGHT) ? md->nj : md->ni;
+      for (int k = 0; k < len; k++) {
+        const int t = ctx->face_type[(size_t)f * ctx->nmax + k];
+        if (t == SF_DB_SYMMETRY || t == SF_DB_PERIODIC) ctx->all_delete = false;
+      }
+    }
     ctx->bc_value.assign(nn, 0.0);
     if (md->bc_value) std::copy(md->bc_value, md->bc_value + nn, ctx->bc_value.begin());
     if (md->node_vol) {
@@ -487,10 +603,13 @@ int sf_ctx_create(const sf_mesh_desc* md, int device, sf_ctx** out) {
     SF_CUDA(cudaMalloc(&ctx->counters, sizeof(unsigned long long) * 8));
     ctx->stats_blocks = ctx->num_sms * 8;
     SF_CUDA(cudaMalloc(&ctx->stats_partial, sizeof(double) * 8 * (size_t)ctx->stats_blocks));
-    int nc = ctx->ncells();
-    SF_CUDA(cudaMalloc(&ctx->bins, sizeof(int) * (size_t)(nc + 1)));
-    SF_CUDA(cudaMalloc(&ctx->bins_tmp, sizeof(int) * (size_t)(nc + 1)));
-    SF_CUDA(cudaMalloc(&ctx->scan_blocks, sizeof(int) * (size_t)((nc + 1) / SCAN_TILE + 2)));
+    ctx->ntx = (ctx->ni - 1 + 15) / 16;
+    ctx->nty = (ctx->nj - 1 + 15) / 16;
+    ctx->nkeys = ctx->ntx * ctx->nty * 256;
+    int nk = ctx->nkeys;
+    SF_CUDA(cudaMalloc(&ctx->bins, sizeof(int) * (size_t)(nk + 1)));
+    SF_CUDA(cudaMalloc(&ctx->bins_tmp, sizeof(int) * (size_t)(nk + 1)));
+    SF_CUDA(cudaMalloc(&ctx->scan_blocks, sizeof(int) * (size_t)((nk + 1) / SCAN_TILE + 2)));
     SF_CUDA(cudaMallocHost(&ctx->host_pinned, sizeof(double) * 64));
     SF_CUDA(cudaMalloc(&ctx->dscratch, sizeof(double) * nn * 2));
     SF_CUDA(cudaStreamSynchronize(ctx->stream));

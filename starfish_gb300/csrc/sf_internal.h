@@ -53,6 +53,16 @@ struct alignas(16) Seg4 {
 __host__ __device__ inline uint32_t pack_cell(int i, int j) { return ((uint32_t)j << 16) | (uint32_t)i; }
 __host__ __device__ inline int cell_i(uint32_t c) { return (int)(c & 0xFFFFu); }
 __host__ __device__ inline int cell_j(uint32_t c) { return (int)(c >> 16); }
+// Sort key of a cell: 16x16-cell tiles in row-major tile order, row-major inside a tile,
+// so that a run of sorted particles is compact in both directions.
+__host__ __device__ inline uint32_t cell_key(int i, int j, int ntx) {
+  return ((uint32_t)((j >> 4) * ntx + (i >> 4)) << 8) | ((uint32_t)(j & 15) << 4) | (uint32_t)(i & 15);
+}
+__host__ __device__ inline void key_cell(uint32_t key, int ntx, int& i, int& j) {
+  const int t = (int)(key >> 8);
+  i = (t % ntx) * 16 + (int)(key & 15u);
+  j = (t / ntx) * 16 + (int)((key >> 4) & 15u);
+}
 
 // ---------------------------------------------------------------------------------
 // Device views (plain structs passed by value to kernels)
@@ -71,6 +81,7 @@ struct MeshView {
   const int8_t* face_type;      // 4*nmax
   const double* node_vol;       // ni*nj
   int nseg;
+  int all_delete;               // every domain face removes exiting particles
 };
 
 struct SurfaceView {
@@ -164,7 +175,7 @@ struct SfSpecies {
   double* flux = nullptr;     // 2*nseg
   double* deposit = nullptr;  // 2*nseg
   uint32_t step = 0;          // pushes done (RNG counter)
-  int sort_interval = 8;      // automatic sort every N pushes (0 = never)
+  int sort_interval = 16;     // automatic sort every N pushes (0 = never)
   int pushes_since_sort = 1 << 30;
 };
 
@@ -199,6 +210,9 @@ struct sf_ctx {
   // device mesh
   float2* E = nullptr;
   bool efield_set = false;
+  bool all_delete = false;  // no SYMMETRY / PERIODIC face anywhere
+  int ntx = 0, nty = 0;     // 16x16-cell tiles of the sort key
+  int nkeys = 0;            // ntx*nty*256
   uint8_t* seg_dist = nullptr;
   int* node_seg_ptr = nullptr;
   int* node_seg_idx = nullptr;

@@ -10,10 +10,11 @@
 //   k_push     fused push + deposit over cell-sorted SoA particles.  Particles whose
 //              move neither leaves the mesh nor comes near a surface segment (checked
 //              with a per-node distance map) finish here; each block accumulates its
-//              tile's deposit in shared memory (warp-aggregated with match/reduce) and
-//              flushes it with one 64-bit atomic per touched node.
-//   k_push_slow  the remaining particles ("slow queue"), in FP64 with the reference's
-//              exact surface-hit and domain-exit logic, up to 10 bounces.
+//              tile's deposit in shared memory (32-bit halves of the fixed-point value)
+//              and flushes it with one 64-bit atomic per touched node.
+//   k_push_slow  the remaining particles ("slow queue"): an FP32 test first clears those
+//              whose path misses every candidate segment; the rest run in FP64 with the
+//              reference's exact surface-hit and domain-exit logic, up to 10 bounces.
 //   k_finalize  int64 fixed-point counts -> FP64 density (and mean velocities).
 // The deposit is an integer sum, so node densities are bit-identical run to run.
 #include <climits>
@@ -92,13 +93,20 @@ struct Kahan {
 // ---------------------------------------------------------------------------------
 // fused push + deposit
 // ---------------------------------------------------------------------------------
+// Deposit accumulation: each particle adds round(S * 2^31) to its four corner nodes.
+// Inside a block the tile's box of nodes is accumulated in shared memory as two 32-bit
+// halves (low/high 16 bits of the fixed-point value), so that plain 32-bit shared
+// atomics cannot overflow (<= 1024 particles per tile), then flushed with one 64-bit
+// global atomic per touched node.  Tiles whose box does not fit (unsorted input) fall
+// back to 64-bit global atomics per corner.
 template <int DOM, bool STATS, bool MOM>
 __global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushArgs a,
                                               unsigned long long* __restrict__ count,
                                               long long* __restrict__ mom, int* __restrict__ slow_idx,
                                               unsigned long long* __restrict__ counters,
                                               double* __restrict__ stats_partial) {
-  __shared__ unsigned long long acc[SBOX];
+  __shared__ unsigned acc_lo[SBOX];
+  __shared__ unsigned acc_hi[SBOX];
   __shared__ int sred[4][PB / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
@@ -112,23 +120,42 @@ __global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushAr
     float pv[PPT][3];
     bool dep[PPT];
     int imin = INT_MAX, imax = -1, jmin = INT_MAX, jmax = -1;
+    // load phase: all of the thread's particles are requested before any is used, so
+    // each warp keeps PPT independent streams of loads in flight (streaming hints keep
+    // L2 for the field and the deposit grid)
+    uint32_t lcell[PPT];
+    float2 lfrac[PPT], lvxy[PPT];
+    float lvz[PPT];
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+      const int64_t p = t0 + k * PB + threadIdx.x;
+      lcell[k] = DEAD;
+      lvz[k] = 0.f;
+      if (p < P.n) {
+        lcell[k] = __ldcs(&P.cell[p]);
+        lfrac[k] = __ldcs(&P.frac[p]);
+        lvxy[k] = __ldcs(&P.vxy[p]);
+        if (DOM != SF_DOMAIN_XY || STATS || MOM) lvz[k] = __ldcs(&P.vz[p]);
+      }
+    }
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
       const int64_t p = t0 + k * PB + threadIdx.x;
       dep[k] = false;
       pi[k] = pj[k] = 0;
       pfx[k] = pfy[k] = 0.f;
+      int status = 0;  // 1 finished here, 2 exact path, 3 removed at a domain face
       if (p < P.n) {
-        const uint32_t c = P.cell[p];
+        const uint32_t c = lcell[k];
         if (c != DEAD) {
           const int i = cell_i(c), j = cell_j(c);
-          const float2 f = P.frac[p];
-          float2 v = P.vxy[p];
+          const float2 f = lfrac[k];
+          float2 v = lvxy[k];
           // velocity update (KineticMaterial.java:336-346); B = 0
           const float2 e = gather_E(m, i, j, f.x, f.y);
           v.x += a.qm_dt * e.x;
           v.y += a.qm_dt * e.y;
-          float vz = (DOM != SF_DOMAIN_XY || STATS || MOM) ? P.vz[p] : 0.f;
+          float vz = lvz[k];
           // move in logical coordinates (x += v dt; XtoL)
           float nfx, nfy, nvx = v.x, nvy = v.y, nvz = vz;
           if (DOM == SF_DOMAIN_XY) {
@@ -174,10 +201,11 @@ __global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushAr
           const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
           const bool clear = (int)__ldg(&m.seg_dist[j * m.ni + i]) > span;
           if (inside && clear) {
-            P.cell[p] = pack_cell(i2, j2);
-            P.frac[p] = make_float2(nfx, nfy);
-            P.vxy[p] = make_float2(nvx, nvy);
-            if (DOM != SF_DOMAIN_XY) P.vz[p] = nvz;
+            __stcs(&P.cell[p], pack_cell(i2, j2));
+            __stcs(&P.frac[p], make_float2(nfx, nfy));
+            __stcs(&P.vxy[p], make_float2(nvx, nvy));
+            if (DOM != SF_DOMAIN_XY) __stcs(&P.vz[p], nvz);
+            status = 1;
             dep[k] = true;
             pi[k] = i2;
             pj[k] = j2;
@@ -197,14 +225,28 @@ __global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushAr
               st_pz.add(nvz);
               st_e.add(sqrtf(nvx * nvx + nvy * nvy + nvz * nvz));
             }
+          } else if (!inside && clear && m.all_delete) {
+            // no candidate segment on the way and every domain face removes particles
+            // (KineticMaterial.java:614-746: OPEN/DIRICHLET/... return false)
+            P.cell[p] = DEAD;
+            status = 3;
           } else {
             // exact path later: keep the old position, store the updated velocity
             P.vxy[p] = v;
-            const unsigned long long slot = atomicAdd(&counters[0], 1ULL);
-            slow_idx[slot] = (int)p;
+            status = 2;
           }
         }
       }
+      const unsigned ms = __ballot_sync(FULL, status == 2);
+      if (ms) {
+        const int leader = __ffs(ms) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(ms));
+        base = __shfl_sync(FULL, base, leader);
+        if (status == 2) slow_idx[base + __popc(ms & ((1u << lane) - 1u))] = (int)p;
+      }
+      const unsigned md = __ballot_sync(FULL, status == 3);
+      if (md && lane == __ffs(md) - 1) atomicAdd(&counters[1], (unsigned long long)__popc(md));
     }
     // ---- block bounding box of this tile's deposits ----
     imin = __reduce_min_sync(FULL, imin);
@@ -233,21 +275,23 @@ __global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushAr
     const bool any = imax >= 0;
     const bool use_smem = any && (bw * bh <= SBOX);
     if (use_smem) {
-      for (int q = threadIdx.x; q < bw * bh; q += PB) acc[q] = 0ULL;
+      for (int q = threadIdx.x; q < bw * bh; q += PB) {
+        acc_lo[q] = 0u;
+        acc_hi[q] = 0u;
+      }
     }
     __syncthreads();
     if (any) {
 #pragma unroll
       for (int k = 0; k < PPT; k++) {
         // scatter skip rule at the far mesh edges (lc >= n-1 is not scattered)
-        bool d = dep[k] && !((pfx[k] >= 1.f && pi[k] == m.ni - 2) || (pfy[k] >= 1.f && pj[k] == m.nj - 2));
+        const bool d = dep[k] && !((pfx[k] >= 1.f && pi[k] == m.ni - 2) || (pfy[k] >= 1.f && pj[k] == m.nj - 2));
+        if (!d) continue;
         float wx, wy;
         scatter_weights<DOM>(pfx[k], pfy[k], pi[k], pj[k], a, wx, wy);
-        const unsigned q00 = d ? quant((1.f - wx) * (1.f - wy)) : 0u;
-        const unsigned q10 = d ? quant(wx * (1.f - wy)) : 0u;
-        const unsigned q11 = d ? quant(wx * wy) : 0u;
-        const unsigned q01 = d ? quant((1.f - wx) * wy) : 0u;
-        if (MOM && d) {
+        const unsigned q[4] = {quant((1.f - wx) * (1.f - wy)), quant(wx * (1.f - wy)), quant(wx * wy),
+                               quant((1.f - wx) * wy)};
+        if (MOM) {
           const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
           const int base = pj[k] * m.ni + pi[k];
           const int off[4] = {0, 1, m.ni + 1, m.ni};
@@ -259,38 +303,25 @@ __global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushAr
                         (unsigned long long)__float2ll_rn(s[cc] * pv[k][dd] * 65536.0f));
         }
         if (use_smem) {
-          const unsigned key = d ? (unsigned)((pj[k] - jmin) * bw + (pi[k] - imin)) : 0xFFFFFFFFu;
-          const unsigned grp = __match_any_sync(FULL, key);
-          const unsigned lo00 = __reduce_add_sync(grp, q00 & 0xFFFFu), hi00 = __reduce_add_sync(grp, q00 >> 16);
-          const unsigned lo10 = __reduce_add_sync(grp, q10 & 0xFFFFu), hi10 = __reduce_add_sync(grp, q10 >> 16);
-          const unsigned lo11 = __reduce_add_sync(grp, q11 & 0xFFFFu), hi11 = __reduce_add_sync(grp, q11 >> 16);
-          const unsigned lo01 = __reduce_add_sync(grp, q01 & 0xFFFFu), hi01 = __reduce_add_sync(grp, q01 >> 16);
-          if (d && lane == __ffs(grp) - 1) {
-            atomicAdd(&acc[key], ((unsigned long long)hi00 << 16) + lo00);
-            atomicAdd(&acc[key + 1], ((unsigned long long)hi10 << 16) + lo10);
-            atomicAdd(&acc[key + bw + 1], ((unsigned long long)hi11 << 16) + lo11);
-            atomicAdd(&acc[key + bw], ((unsigned long long)hi01 << 16) + lo01);
+          const int l = (pj[k] - jmin) * bw + (pi[k] - imin);
+          const int off[4] = {0, 1, bw + 1, bw};
+#pragma unroll
+          for (int cc = 0; cc < 4; cc++) {
+            atomicAdd(&acc_lo[l + off[cc]], q[cc] & 0xFFFFu);
+            atomicAdd(&acc_hi[l + off[cc]], q[cc] >> 16);
           }
         } else {
-          const unsigned key = d ? (unsigned)(pj[k] * m.ni + pi[k]) : 0xFFFFFFFFu;
-          const unsigned grp = __match_any_sync(FULL, key);
-          const unsigned lo00 = __reduce_add_sync(grp, q00 & 0xFFFFu), hi00 = __reduce_add_sync(grp, q00 >> 16);
-          const unsigned lo10 = __reduce_add_sync(grp, q10 & 0xFFFFu), hi10 = __reduce_add_sync(grp, q10 >> 16);
-          const unsigned lo11 = __reduce_add_sync(grp, q11 & 0xFFFFu), hi11 = __reduce_add_sync(grp, q11 >> 16);
-          const unsigned lo01 = __reduce_add_sync(grp, q01 & 0xFFFFu), hi01 = __reduce_add_sync(grp, q01 >> 16);
-          if (d && lane == __ffs(grp) - 1) {
-            atomicAdd(&count[key], ((unsigned long long)hi00 << 16) + lo00);
-            atomicAdd(&count[key + 1], ((unsigned long long)hi10 << 16) + lo10);
-            atomicAdd(&count[key + m.ni + 1], ((unsigned long long)hi11 << 16) + lo11);
-            atomicAdd(&count[key + m.ni], ((unsigned long long)hi01 << 16) + lo01);
-          }
+          const size_t u = (size_t)pj[k] * m.ni + pi[k];
+          const size_t off[4] = {0, 1, (size_t)m.ni + 1, (size_t)m.ni};
+#pragma unroll
+          for (int cc = 0; cc < 4; cc++) atomicAdd(&count[u + off[cc]], (unsigned long long)q[cc]);
         }
       }
     }
     __syncthreads();
     if (use_smem) {
       for (int q = threadIdx.x; q < bw * bh; q += PB) {
-        const unsigned long long v = acc[q];
+        const unsigned long long v = ((unsigned long long)acc_hi[q] << 16) + acc_lo[q];
         if (v) atomicAdd(&count[(size_t)(jmin + q / bw) * m.ni + imin + q % bw], v);
       }
     }
@@ -372,6 +403,43 @@ struct SlowArgs {
   double* stats_slow;   // 5 sums + boundary charge
 };
 
+// Visits the DIRICHLET/SINK segments that KineticMaterial.ProcessBoundary collects for
+// the node box [i_min..i_max] x [j_min..j_max] (KineticMaterial.java:480-515); f(s)
+// returning true stops the walk.  With few segments all of them are visited directly:
+// a segment met by a path inside the box passes within 1.01 cells of a box node, so
+// Mesh.setNodeControlVolumes lists it there and the set of possible hits is the same.
+// With many segments the node lists are walked, testing each segment once (a short
+// list of visited ids; repeats beyond it are harmless re-tests).
+constexpr int SMALL_NSEG = 64;
+template <typename F>
+__device__ inline void for_each_candidate(const MeshView& m, int i_min, int i_max, int j_min, int j_max, F&& f) {
+  if (m.nseg <= SMALL_NSEG) {
+    for (int s = 0; s < m.nseg; s++) {
+      const int bt = m.seg_btype[s];
+      if (bt != SF_BT_DIRICHLET && bt != SF_BT_SINK) continue;
+      if (f(s)) return;
+    }
+    return;
+  }
+  constexpr int SEEN = 16;
+  int seen[SEEN];
+  int nseen = 0;
+  for (int i = i_min; i <= i_max; i++)
+    for (int j = j_min; j <= j_max; j++) {
+      const int u = j * m.ni + i;
+      for (int k = m.node_seg_ptr[u]; k < m.node_seg_ptr[u + 1]; k++) {
+        const int s = m.node_seg_idx[k];
+        const int bt = m.seg_btype[s];
+        if (bt != SF_BT_DIRICHLET && bt != SF_BT_SINK) continue;
+        bool dup = false;
+        for (int q = 0; q < nseen; q++) dup |= (seen[q] == s);
+        if (dup) continue;
+        if (nseen < SEEN) seen[nseen++] = s;
+        if (f(s)) return;
+      }
+    }
+}
+
 // returns alive; follows KineticMaterial.ProcessBoundary (KineticMaterial.java:471-750)
 __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const PushArgs& a, double pos[2],
                                  double vel[3], double lc[2], double& pdt, const double old[2],
@@ -386,30 +454,24 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
   if (j_max >= m.nj) j_max = m.nj - 1;
   double tp_min = 2.0, tsurf_min = 0;
   int seg_min = -1;
-  for (int i = i_min; i <= i_max; i++)
-    for (int j = j_min; j <= j_max; j++) {
-      const int u = j * m.ni + i;
-      for (int k = m.node_seg_ptr[u]; k < m.node_seg_ptr[u + 1]; k++) {
-        const int s = m.node_seg_idx[k];
-        const int bt = m.seg_btype[s];
-        if (bt != SF_BT_DIRICHLET && bt != SF_BT_SINK) continue;
-        const Seg4 sxy = m.seg_xy[s];
-        double t[2];
-        seg_intersect(sxy, old, pos, t);
-        const double t_part = t[1];
-        if (t_part > 0) {
-          double n[3], tg[3];
-          seg_normal_tangent(sxy, n, tg);
-          const double acs = (n[0] * vel[0] + n[1] * vel[1]) / sqrt(vel[0] * vel[0] + vel[1] * vel[1]);
-          if (t_part < FLT_EPS_REF && acs > 0) continue;
-          if (t_part < tp_min) {
-            tp_min = t_part;
-            tsurf_min = t[0];
-            seg_min = s;
-          }
-        }
+  for_each_candidate(m, i_min, i_max, j_min, j_max, [&](int s) {
+    const Seg4 sxy = m.seg_xy[s];
+    double t[2];
+    seg_intersect(sxy, old, pos, t);
+    const double t_part = t[1];
+    if (t_part > 0) {
+      double n[3], tg[3];
+      seg_normal_tangent(sxy, n, tg);
+      const double acs = (n[0] * vel[0] + n[1] * vel[1]) / sqrt(vel[0] * vel[0] + vel[1] * vel[1]);
+      if (t_part < FLT_EPS_REF && acs > 0) return false;
+      if (t_part < tp_min) {
+        tp_min = t_part;
+        tsurf_min = t[0];
+        seg_min = s;
       }
     }
+    return false;
+  });
   bool alive = true;
   if (seg_min >= 0) {
     tp_min *= 0.9999;
@@ -520,12 +582,89 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
   return alive;
 }
 
+// Deposit of one particle with 64-bit global atomics (the slow path's particles), same
+// fixed point and edge rule as the fused kernel.
 template <int DOM>
-__global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, PushArgs a, SlowArgs sa,
+__device__ inline void deposit_global_t(const MeshView& m, unsigned long long* count, long long* mom, int mom_on,
+                                        int i, int j, float fx, float fy, float wx, float wy, float vx, float vy,
+                                        float vz, size_t nn) {
+  if ((fx >= 1.f && i == m.ni - 2) || (fy >= 1.f && j == m.nj - 2)) return;  // scatter skip rule
+  const size_t u = (size_t)j * m.ni + i;
+  const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
+  const size_t off[4] = {0, 1, (size_t)m.ni + 1, (size_t)m.ni};
+  for (int cc = 0; cc < 4; cc++) atomicAdd(&count[u + off[cc]], (unsigned long long)quant(s[cc]));
+  if (mom_on) {
+    const float vv[3] = {vx, vy, vz};
+    for (int cc = 0; cc < 4; cc++)
+      for (int dd = 0; dd < 3; dd++)
+        atomicAdd((unsigned long long*)&mom[dd * nn + u + off[cc]],
+                  (unsigned long long)__float2ll_rn(s[cc] * vv[dd] * 65536.0f));
+  }
+}
+#define deposit_global deposit_global_t<DOM>
+
+// Conservative FP32 test of a move from (i + fx, j + fy) to (i + gx, j + gy) in cells:
+// false means the path cannot meet any DIRICHLET/SINK segment listed on the nodes of
+// its box (the candidate set of KineticMaterial.ProcessBoundary, :480-515), so the
+// reference would find no hit.  Near-parallel or near-touching cases answer true and
+// go to the exact FP64 path.
+__device__ bool may_hit_fp32(const MeshView& m, int i, int j, float fx, float fy, float gx, float gy) {
+  int i_min = i + (int)floorf(fminf(fx, gx)), i_max = i + (int)floorf(fmaxf(fx, gx));
+  int j_min = j + (int)floorf(fminf(fy, gy)), j_max = j + (int)floorf(fmaxf(fy, gy));
+  i_min = max(i_min, 0);
+  j_min = max(j_min, 0);
+  i_max = min(i_max, m.ni - 1);
+  j_max = min(j_max, m.nj - 1);
+  const float rx = gx - fx, ry = gy - fy;
+  const float rl = fabsf(rx) + fabsf(ry);
+  const double idx = 1.0 / m.dh[0], idy = 1.0 / m.dh[1];
+  bool hit = false;
+  for_each_candidate(m, i_min, i_max, j_min, j_max, [&](int sgi) {
+    const Seg4 sg = m.seg_xy[sgi];
+    // end points in cells relative to node (i, j)
+    const float ax = (float)((sg.x - m.x0[0]) * idx - i), ay = (float)((sg.y - m.x0[1]) * idy - j);
+    const float bx = (float)((sg.z - m.x0[0]) * idx - i), by = (float)((sg.w - m.x0[1]) * idy - j);
+    const float sx = bx - ax, sy = by - ay;
+    const float sl = fabsf(sx) + fabsf(sy);
+    const float den = rx * sy - ry * sx;
+    const float qx = ax - fx, qy = ay - fy;
+    const float tn = qx * sy - qy * sx;  // t_part * den
+    const float un = qx * ry - qy * rx;  // t_seg * den
+    const float lim = fabsf(den);
+    const float tol = 1e-3f * lim + 1e-4f * (rl + 1.f) * (sl + 1.f) * (1.f + fabsf(qx) + fabsf(qy));
+    if (lim <= tol) return hit = true;  // (near) parallel
+    const float sgn = den > 0.f ? 1.f : -1.f;
+    const float t1 = tn * sgn, t0 = un * sgn;
+    if (t1 >= -tol && t1 <= lim + tol && t0 >= -tol && t0 <= lim + tol) return hit = true;
+    return false;
+  });
+  return hit;
+}
+
+template <int DOM>
+__global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, PushArgs a, SlowArgs sg,
                                                    const int* __restrict__ slow_idx,
                                                    unsigned long long* __restrict__ count,
                                                    long long* __restrict__ mom, int mom_on) {
-  const unsigned long long nslow = sa.counters[0];
+  // Totals, counters and (for small geometries) per-segment surface sums are first
+  // accumulated per block in shared memory and flushed once at the end: the exact
+  // path's particles hit the same few segments, so global atomics would serialise.
+  __shared__ double s_stats[8];
+  __shared__ double s_seg[4 * SMALL_NSEG];
+  __shared__ unsigned long long s_cnt[4];
+  const bool seg_local = m.nseg <= SMALL_NSEG;
+  for (int q = threadIdx.x; q < 8; q += blockDim.x) s_stats[q] = 0.0;
+  for (int q = threadIdx.x; q < 4 * SMALL_NSEG; q += blockDim.x) s_seg[q] = 0.0;
+  if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0ULL;
+  __syncthreads();
+  const unsigned long long nslow = sg.counters[0];
+  SlowArgs sa = sg;
+  sa.stats_slow = s_stats;
+  sa.counters = s_cnt;
+  if (seg_local) {
+    sa.sv.flux = s_seg;
+    sa.sv.deposit = s_seg + 2 * SMALL_NSEG;
+  }
   const size_t nn = (size_t)m.ni * m.nj;
   for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; t < nslow;
        t += (unsigned long long)gridDim.x * blockDim.x) {
@@ -533,6 +672,41 @@ __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, 
     const uint32_t c = P.cell[p];
     const float2 f = P.frac[p];
     const float2 v = P.vxy[p];
+    if (DOM == SF_DOMAIN_XY) {
+      // FP32 pre-filter: a particle whose path certainly misses every candidate segment
+      // and stays in the mesh finishes exactly like the fast path
+      const int i = cell_i(c), j = cell_j(c);
+      const float gx = f.x + v.x * a.dt_dx, gy = f.y + v.y * a.dt_dy;
+      if (!may_hit_fp32(m, i, j, f.x, f.y, gx, gy)) {
+        float fdi = floorf(gx), fdj = floorf(gy);
+        float nfx = gx - fdi, nfy = gy - fdj;
+        if (nfx >= 1.f) { nfx -= 1.f; fdi += 1.f; }
+        if (nfy >= 1.f) { nfy -= 1.f; fdj += 1.f; }
+        const int i2 = i + (int)fdi, j2 = j + (int)fdj;
+        const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
+        if (inside) {
+          const float vz = P.vz[p];
+          P.cell[p] = pack_cell(i2, j2);
+          P.frac[p] = make_float2(nfx, nfy);
+          atomicAdd(&sa.counters[3], 1ULL);
+          atomicAdd(&sa.stats_slow[0], 1.0);
+          atomicAdd(&sa.stats_slow[1], (double)v.x);
+          atomicAdd(&sa.stats_slow[2], (double)v.y);
+          atomicAdd(&sa.stats_slow[3], (double)vz);
+          atomicAdd(&sa.stats_slow[4], (double)sqrtf(v.x * v.x + v.y * v.y + vz * vz));
+          float wx, wy;
+          scatter_weights<DOM>(nfx, nfy, i2, j2, a, wx, wy);
+          deposit_global(m, count, mom, mom_on, i2, j2, nfx, nfy, wx, wy, v.x, v.y, vz, nn);
+          continue;
+        }
+        if (m.all_delete) {
+          P.cell[p] = DEAD;
+          atomicAdd(&sa.counters[1], 1ULL);
+          atomicAdd(&sa.counters[3], 1ULL);
+          continue;
+        }
+      }
+    }
     double lc[2] = {cell_i(c) + (double)f.x, cell_j(c) + (double)f.y};
     double pos[2] = {m.x0[0] + lc[0] * m.dh[0], m.x0[1] + lc[1] * m.dh[1]};
     double vel[3] = {v.x, v.y, (double)P.vz[p]};
@@ -593,24 +767,20 @@ __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, 
     atomicAdd(&sa.stats_slow[2], vel[1]);
     atomicAdd(&sa.stats_slow[3], vel[2]);
     atomicAdd(&sa.stats_slow[4], sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]));
-    if ((fx >= 1.f && i == m.ni - 2) || (fy >= 1.f && j == m.nj - 2)) continue;  // scatter skip rule
     float wx, wy;
     scatter_weights<DOM>(fx, fy, i, j, a, wx, wy);
-    const size_t u = (size_t)j * m.ni + i;
-    atomicAdd(&count[u], (unsigned long long)quant((1.f - wx) * (1.f - wy)));
-    atomicAdd(&count[u + 1], (unsigned long long)quant(wx * (1.f - wy)));
-    atomicAdd(&count[u + m.ni + 1], (unsigned long long)quant(wx * wy));
-    atomicAdd(&count[u + m.ni], (unsigned long long)quant((1.f - wx) * wy));
-    if (mom_on) {
-      const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
-      const size_t off[4] = {0, 1, (size_t)m.ni + 1, (size_t)m.ni};
-      const float vv[3] = {(float)vel[0], (float)vel[1], (float)vel[2]};
-      for (int cc = 0; cc < 4; cc++)
-        for (int dd = 0; dd < 3; dd++)
-          atomicAdd((unsigned long long*)&mom[dd * nn + u + off[cc]],
-                    (unsigned long long)__float2ll_rn(s[cc] * vv[dd] * 65536.0f));
-    }
+    deposit_global(m, count, mom, mom_on, i, j, fx, fy, wx, wy, (float)vel[0], (float)vel[1], (float)vel[2], nn);
   }
+  __syncthreads();
+  for (int q = threadIdx.x; q < 6; q += blockDim.x)
+    if (s_stats[q] != 0.0) atomicAdd(&sg.stats_slow[q], s_stats[q]);
+  if (threadIdx.x >= 1 && threadIdx.x < 4 && s_cnt[threadIdx.x])
+    atomicAdd(&sg.counters[threadIdx.x], s_cnt[threadIdx.x]);
+  if (seg_local)
+    for (int q = threadIdx.x; q < 2 * m.nseg; q += blockDim.x) {
+      if (s_seg[q] != 0.0) atomicAdd(&sg.sv.flux[q], s_seg[q]);
+      if (s_seg[2 * SMALL_NSEG + q] != 0.0) atomicAdd(&sg.sv.deposit[q], s_seg[2 * SMALL_NSEG + q]);
+    }
 }
 
 // int64 fixed point -> density (Field2D.scaleByVol, Field2D.java:418-431) and mean
@@ -724,7 +894,7 @@ extern "C" int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flag
     sa.sv.deposit = sp->deposit;
     sa.counters = ctx->counters;
     sa.stats_slow = slow_stats;
-    const int sgrid = ctx->num_sms * 4;
+    const int sgrid = ctx->num_sms * 16;
     TimedScope ts(ctx, "push_slow");
     ctx->launches++;
     switch (ctx->domain) {

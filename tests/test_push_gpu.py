@@ -102,7 +102,12 @@ def test_push_deposit_matches_oracle_c0(gpulib, seed):
     for d in range(3):
         assert r["st"]["p_sum"][d] == pytest.approx(r["ost"][1 + d], rel=1e-5, abs=1e-5 * r["ost"][4])
     assert r["st"]["e_sum"] == pytest.approx(r["ost"][4], rel=1e-5)
-    assert np.allclose(r["gdep"], r["odep"], rtol=1e-9, atol=1e-9 * ion.spwt)
+    # absorbed weight per segment is exact; its split over the segment ends follows the
+    # hit point, which moves with the FP32 velocity update (1e-8 relative)
+    seg_g = r["gdep"].reshape(-1, 2).sum(axis=1)
+    seg_o = r["odep"].reshape(-1, 2).sum(axis=1)
+    assert np.allclose(seg_g, seg_o, rtol=1e-12)
+    assert np.allclose(r["gdep"], r["odep"], rtol=1e-6)
     assert r["st"]["n_slow"] > 0 and r["st"]["n_removed"] > 0
 
 
@@ -113,7 +118,7 @@ def test_push_symmetry_and_open_faces(gpulib):
     spec.face_type[abi.FACE_RIGHT, :] = abi.DB_OPEN
     ion = W.IonSpecies(v_drift=-3000.0)
     _, efi, efj = W.electrode_efield(spec)
-    efj = efj - 2e4   # push ions into the bottom face
+    efj = efj - 2e3   # push ions into the bottom face (0.1 cell per step extra)
     r = run_case(spec, ion, 20000, 5, 5e-7, efi, efj)
     P = r["P"]
     keep = P[:, 10] == 1
@@ -168,3 +173,37 @@ def test_deposit_conserves_weight(gpulib):
     total = km.get_count().sum()
     assert abs(total - n) <= 2 * n * 2.0 ** -31 * 4 + 1e-6
     dom.close()
+
+
+def _tile_key(lc, ni, nj):
+    i = np.minimum(np.floor(lc[:, 0]).astype(np.int64), ni - 2)
+    j = np.minimum(np.floor(lc[:, 1]).astype(np.int64), nj - 2)
+    ntx = (ni - 1 + 15) // 16
+    return (((j >> 4) * ntx + (i >> 4)) << 8) | ((j & 15) << 4) | (i & 15)
+
+
+def test_cell_sort_orders_and_keeps_particles(gpulib):
+    """The counting sort (DSMC.perform(mesh) binning, DSMC.java:194-231) keeps every
+    particle, drops removed ones and leaves cell keys in non-decreasing order."""
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    spec = W.es_pic_mesh(301, 151, 1e-3, electrode_halfwidth=1e-2)
+    ion = W.IonSpecies()
+    _, efi, efj = W.electrode_efield(spec)
+    pos, vel = W.uniform_maxwellian(spec, ion, 300000, 11)
+    dom = GpuDomain(spec)
+    dom.set_efield(efi, efj)
+    km = KineticMaterial(dom, ion.mass, ion.charge, ion.spwt, capacity=400000)
+    km.set_sort_interval(0)
+    km.add_particles(pos, vel, rewind=False)
+    lc0, v0 = km.download()
+    km.update_fields(5e-7)          # removes some particles (electrode, walls)
+    lc1, v1 = km.download()
+    km.sort()
+    lc2, v2 = km.download()
+    dom.close()
+    assert lc2.shape[0] == lc1.shape[0] < lc0.shape[0]
+    k = _tile_key(lc2, spec.ni, spec.nj)
+    assert np.all(np.diff(k) >= 0)
+    a = np.lexsort(np.column_stack([lc1, v1]).T)
+    b = np.lexsort(np.column_stack([lc2, v2]).T)
+    assert np.array_equal(np.column_stack([lc1, v1])[a], np.column_stack([lc2, v2])[b])

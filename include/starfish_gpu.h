@@ -202,6 +202,55 @@ int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_
 int sf_get_surface_flux(sf_ctx* ctx, int32_t sid, double* flux, double* deposit);
 int sf_reset_surface_flux(sf_ctx* ctx, int32_t sid);
 
+/* ---- field solve ------------------------------------------------------------ */
+/* Parameters of the nonlinear Poisson solve with Boltzmann electrons
+ * (PoissonSolver, pic/PoissonSolver.java:49-107; defaults SolverModule.java:55-87). */
+typedef struct {
+  double n0;        /* reference electron density (m^-3), PoissonSolver.den0            */
+  double kTe0;      /* electron temperature (eV), PoissonSolver.kTe0                    */
+  double phi0;      /* reference potential (V), PoissonSolver.phi0                      */
+  double eps;       /* permittivity, Constants.EPS0 * eps_r                             */
+  double tol;       /* target FP64 residual ||R||_2 / N (LinearSolverGS metric, :111-125) */
+  int32_t max_it;   /* cap on Newton / refinement iterations                            */
+  int32_t cycles;   /* multigrid V-cycles per Newton iteration (inner FP32 solve)       */
+  int32_t use_learned; /* 1: start from the learned predictor when it is trained       */
+  int32_t linear;   /* 1: linear Poisson (no electron term), PoissonSolver linear_mode  */
+} sf_poisson_params;
+
+typedef struct {
+  int32_t newton_it;        /* outer (FP64 residual) iterations taken                  */
+  int32_t vcycles;          /* inner multigrid cycles                                   */
+  double residual;          /* final ||R||_2 / N (FP64)                                  */
+  double residual_inf;      /* final max |R|                                             */
+  double initial_residual;  /* ||R||_2 / N of the initial guess                          */
+  double ms;                /* device time of the solve (CUDA events)                    */
+} sf_solve_stats;
+
+/* SolverModule.updateRho (core/solver/SolverModule.java:144-171): rho = sum over the
+ * context's kinetic species of charge * nd, on the device. */
+int sf_update_rho(sf_ctx* ctx);
+/* Replaces the Dirichlet values (BoundaryModule.updateBoundaries -> DomainModule.updateBCvalues,
+ * used for time-varying electrodes).  bc: ni*nj. */
+int sf_set_bc_values(sf_ctx* ctx, const double* bc);
+/* PoissonSolver.update -> solvePotentialNL -> Solver.solveNonLinearNR
+ * (PoissonSolver.java:110-252, Solver.java:293-387): solves
+ *   A phi = -rho/eps + (e n0/eps) exp((phi - phi0)/kTe)     (non-fixed rows)
+ * to ||R||_2/N < tol in FP64: Newton on the Boltzmann term with FP64 residuals and
+ * updates, each correction from FP32 geometric multigrid V-cycles.  rho: host charge
+ * density (ni*nj) or NULL to use the device rho (sf_update_rho).  phi: host initial
+ * guess and result, or NULL to keep the potential on the device (the previous solution
+ * is then the initial guess).  Returns SF_ERR_NOT_CONVERGED / SF_ERR_DIVERGED as
+ * Solver.java:384-385 and :437-439 report them. */
+int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, double* phi,
+                  sf_solve_stats* stats);
+/* PotentialSolver.updateGradientField (pic/PotentialSolver.java:56-70): E = -grad(phi)
+ * (Solver.evaluateGradient, Solver.java:789-814), kept on the device for the push and
+ * optionally copied to efi/efj (ni*nj each, may be NULL). */
+int sf_efield(sf_ctx* ctx, double* efi, double* efj);
+/* BoltzmannElectronsMaterial.electronModelBoltzmann (BoltzmannElectronsMaterial.java:179-215):
+ * n_e = max(1, n0 exp((phi - phi0)/kTe)) into ne (ni*nj, may be NULL: device only). */
+int sf_boltzmann(sf_ctx* ctx, double* ne);
+
 /* ---- measurement ---------------------------------------------------------- */
 /* The CUDA stream (cudaStream_t) all work of the context is issued on. */
 int sf_ctx_get_stream(sf_ctx* ctx, void** stream);

@@ -747,10 +747,16 @@ double row_mult(const Row& r, const double* x) {
 // residual ||Ax-b||_2 / N checked every 25 iterations before the sweep.
 int gs_solve(const std::vector<Row>& A, double* x, const double* b, int n, int max_it, double tol,
              double* out_norm) {
-  std::vector<double> diag(n);
+  // rows flattened once (same values and column order as the sparse rows)
+  std::vector<int> ptr(n + 1, 0), col;
+  std::vector<double> val, diag(n, 0.0);
   for (int u = 0; u < n; u++) {
-    auto it = A[u].find(u);
-    diag[u] = (it == A[u].end()) ? 0 : it->second;
+    for (auto& kv : A[u]) {
+      col.push_back(kv.first);
+      val.push_back(kv.second);
+      if (kv.first == u) diag[u] = kv.second;
+    }
+    ptr[u + 1] = (int)col.size();
   }
   int it = 1;
   double norm = 1e66;
@@ -758,7 +764,9 @@ int gs_solve(const std::vector<Row>& A, double* x, const double* b, int n, int m
     if (it % 25 == 0) {
       double s = 0;
       for (int u = 0; u < n; u++) {
-        double r = row_mult(A[u], x) - b[u];
+        double r = 0;
+        for (int k = ptr[u]; k < ptr[u + 1]; k++) r += val[k] * x[col[k]];
+        r -= b[u];
         s += r * r;
       }
       norm = std::sqrt(s) / n;
@@ -766,8 +774,8 @@ int gs_solve(const std::vector<Row>& A, double* x, const double* b, int n, int m
     }
     for (int u = 0; u < n; u++) {
       double tau = 0;
-      for (auto& kv : A[u])
-        if (kv.first != u) tau += kv.second * x[kv.first];
+      for (int k = ptr[u]; k < ptr[u + 1]; k++)
+        if (col[k] != u) tau += val[k] * x[col[k]];
       if (std::fabs(diag[u]) < 1e-8) continue;
       double g = (b[u] - tau) / diag[u];
       x[u] = x[u] + 1.4 * (g - x[u]);

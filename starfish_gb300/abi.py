@@ -62,13 +62,16 @@ class PushStats(C.Structure):
 class PoissonParams(C.Structure):
     _fields_ = [("n0", C.c_double), ("kTe0", C.c_double), ("phi0", C.c_double),
                 ("eps", C.c_double), ("tol", C.c_double), ("max_it", C.c_int32),
-                ("nl_max_it", C.c_int32), ("use_learned", C.c_int32), ("flags", C.c_int32)]
+                ("cycles", C.c_int32), ("use_learned", C.c_int32), ("linear", C.c_int32)]
 
 
 class SolveStats(C.Structure):
     _fields_ = [("newton_it", C.c_int32), ("vcycles", C.c_int32), ("residual", C.c_double),
                 ("residual_inf", C.c_double), ("initial_residual", C.c_double),
                 ("ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 EXPORTS = {
@@ -104,6 +107,12 @@ EXPORTS = {
                                 C.POINTER(C.c_int64)]),
     "sf_timing_reset": (C.c_int, [C.c_void_p]),
     "sf_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.c_int32]),
+    "sf_update_rho": (C.c_int, [C.c_void_p]),
+    "sf_set_bc_values": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sf_poisson_nl": (C.c_int, [C.c_void_p, C.POINTER(PoissonParams), C.c_void_p, C.c_void_p,
+                                C.POINTER(SolveStats)]),
+    "sf_efield": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sf_boltzmann": (C.c_int, [C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

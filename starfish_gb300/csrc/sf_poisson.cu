@@ -1,8 +1,854 @@
-// sf_poisson.cu -- placeholder until the Poisson solver lands.
+// sf_poisson.cu -- nonlinear Poisson solve with Boltzmann electrons, electric field.
+//
+// The reference (pic/PoissonSolver.java:110-252, core/solver/Solver.java:293-387,
+// LinearSolverGS.java:74-152) assembles an FVM matrix A (5-point on a uniform XY mesh,
+// identity rows on Dirichlet nodes, one-sided gradient rows on open mesh faces), then
+// runs Newton on  F(x) = A x - b0 - (e n0/eps) exp((x - phi0)/kTe)  with J = A - diag(P),
+// solving each J y = F by SOR.
+//
+// Here the same operator is applied in closed form (no matrix is stored) and the solve
+// is built for GB300, whose FP64 rate is a small fraction of its FP32 rate:
+//   * outer loop in FP64: residual F, its norm and the update x -= y -- the quantities
+//     whose precision decides the converged potential (iterative refinement);
+//   * inner correction in FP32: flexible conjugate gradients preconditioned by one
+//     geometric multigrid V(2,2)-cycle (red-black Gauss-Seidel, full weighting, bilinear
+//     prolongation).  A plain V-cycle converges poorly here because the coarse grids
+//     see the embedded electrode only approximately; CG removes those few slow modes.
+//     The operator is made symmetric by scaling the open-face (one-sided gradient) rows
+//     by 1/h, which leaves its solution unchanged.
+// The coarse end of the hierarchy (<= COARSE_NODES nodes) runs inside one CTA out of
+// shared memory, so a V-cycle is a handful of launches.  All inner scalars stay on the
+// device; the host reads one FP64 residual norm per Newton step.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
 #include "sf_internal.h"
 
-void sf_poisson_destroy_internal(sf_ctx*) {}
-int sf_poisson_get_field_internal(sf_ctx* ctx, int, double*) {
-  ctx->err = "field solver not initialised";
-  return SF_ERR_STATE;
+using namespace sf;
+
+namespace {
+
+// node classes of the closed-form operator
+enum : uint8_t { NC_INTERIOR = 0, NC_FIXED = 1, NC_NLEFT = 2, NC_NRIGHT = 3, NC_NBOTTOM = 4, NC_NTOP = 5 };
+
+constexpr int COARSE_NODES = 8600;  // a level this small and everything below run in one CTA
+constexpr int MAX_LEVELS = 16;
+
+struct LevelView {
+  int ni, nj;
+  float cx, cy;  // 1/dx^2, 1/dy^2
+  float* y;
+  float* r;
+  float* P;
+  float* t;      // residual scratch
+  const uint8_t* type;
+};
+
+struct CoarseDesc {  // levels [0, n) of the single-CTA solve; level 0 is read from global memory
+  int n;
+  int ni[MAX_LEVELS], nj[MAX_LEVELS];
+  float cx[MAX_LEVELS], cy[MAX_LEVELS];
+  int off[MAX_LEVELS];  // node offset of each level in the shared arrays
+  int total;
+  int coarsest_sweeps;
+};
+
+__host__ __device__ inline uint8_t node_class(bool fixed, int i, int j, int ni, int nj) {
+  if (fixed) return NC_FIXED;
+  if (i == 0) return NC_NLEFT;
+  if (i == ni - 1) return NC_NRIGHT;
+  if (j == 0) return NC_NBOTTOM;
+  if (j == nj - 1) return NC_NTOP;
+  return NC_INTERIOR;
 }
+
+// ------------------------------------------------------------------------------------
+// symmetric FP32 operator J (open-face rows scaled by 1/h): pieces shared by the
+// global-memory and the shared-memory levels
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ float apply_J(uint8_t t, const float* y, float P, int u, int ni, float cx, float cy) {
+  const float yc = y[u];
+  switch (t) {
+    case NC_FIXED: return yc;
+    case NC_NLEFT: return cx * (y[u + 1] - yc);
+    case NC_NRIGHT: return cx * (y[u - 1] - yc);
+    case NC_NBOTTOM: return cy * (y[u + ni] - yc);
+    case NC_NTOP: return cy * (y[u - ni] - yc);
+    default: return cx * (y[u - 1] + y[u + 1] - 2.f * yc) + cy * (y[u - ni] + y[u + ni] - 2.f * yc) - P * yc;
+  }
+}
+
+// Gauss-Seidel value of node u (solves its row of J y = r for y[u])
+__device__ __forceinline__ float gs_value(uint8_t t, const float* y, float r, float P, int u, int ni, float cx,
+                                          float cy) {
+  switch (t) {
+    case NC_FIXED: return r;
+    case NC_NLEFT: return y[u + 1] - r / cx;
+    case NC_NRIGHT: return y[u - 1] - r / cx;
+    case NC_NBOTTOM: return y[u + ni] - r / cy;
+    case NC_NTOP: return y[u - ni] - r / cy;
+    default: return (cx * (y[u - 1] + y[u + 1]) + cy * (y[u - ni] + y[u + ni]) - r) / (2.f * cx + 2.f * cy + P);
+  }
+}
+
+// full weighting inside, injection on the boundary rows (halved: the scaled open-face
+// row of a grid twice as coarse carries half the weight), zero on fixed coarse nodes
+__device__ __forceinline__ float restrict_value(const float* tf, uint8_t tc, int I, int J, int nif, int nic, int njc) {
+  if (tc == NC_FIXED) return 0.f;
+  const int i = 2 * I, j = 2 * J;
+  const int u = j * nif + i;
+  if (I == 0 || J == 0 || I == nic - 1 || J == njc - 1) return 0.5f * tf[u];
+  return 0.0625f * (4.f * tf[u] + 2.f * (tf[u - 1] + tf[u + 1] + tf[u - nif] + tf[u + nif]) +
+                    (tf[u - nif - 1] + tf[u - nif + 1] + tf[u + nif - 1] + tf[u + nif + 1]));
+}
+
+__device__ __forceinline__ float prolong_value(const float* yc, int i, int j, int nic) {
+  const int I = i >> 1, J = j >> 1;
+  const int uc = J * nic + I;
+  const bool oi = i & 1, oj = j & 1;
+  if (!oi && !oj) return yc[uc];
+  if (oi && !oj) return 0.5f * (yc[uc] + yc[uc + 1]);
+  if (!oi && oj) return 0.5f * (yc[uc] + yc[uc + nic]);
+  return 0.25f * (yc[uc] + yc[uc + 1] + yc[uc + nic] + yc[uc + nic + 1]);
+}
+
+// ------------------------------------------------------------------------------------
+// global-memory level kernels
+// ------------------------------------------------------------------------------------
+__global__ void k_smooth(LevelView L, int color) {
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= L.nj) return;
+  const int i = 2 * k + ((j + color) & 1);
+  if (i >= L.ni) return;
+  const int u = j * L.ni + i;
+  L.y[u] = gs_value(L.type[u], L.y, L.r[u], L.P[u], u, L.ni, L.cx, L.cy);
+}
+
+__global__ void k_resid(LevelView L) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= L.ni || j >= L.nj) return;
+  const int u = j * L.ni + i;
+  L.t[u] = L.r[u] - apply_J(L.type[u], L.y, L.P[u], u, L.ni, L.cx, L.cy);
+}
+
+__global__ void k_restrict(LevelView F, LevelView Cl) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  if (I >= Cl.ni || J >= Cl.nj) return;
+  const int uc = J * Cl.ni + I;
+  Cl.r[uc] = restrict_value(F.t, Cl.type[uc], I, J, F.ni, Cl.ni, Cl.nj);
+  Cl.y[uc] = 0.f;
+}
+
+__global__ void k_prolong(LevelView Cl, LevelView F) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= F.ni || j >= F.nj) return;
+  const int u = j * F.ni + i;
+  if (F.type[u] == NC_FIXED) return;
+  F.y[u] += prolong_value(Cl.y, i, j, Cl.ni);
+}
+
+// coarse-grid P: injection of the fine linearisation coefficient
+__global__ void k_restrict_P(LevelView F, LevelView Cl) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int J = blockIdx.y * blockDim.y + threadIdx.y;
+  if (I >= Cl.ni || J >= Cl.nj) return;
+  Cl.P[J * Cl.ni + I] = F.P[(2 * J) * F.ni + 2 * I];
+}
+
+// ------------------------------------------------------------------------------------
+// single-CTA V-cycle over the coarse end of the hierarchy (shared memory)
+// ------------------------------------------------------------------------------------
+// rb: red then black (pre-smoothing); otherwise black then red (post-smoothing), so the
+// V-cycle is a symmetric preconditioner
+__device__ void cta_smooth(float* y, const float* r, const float* P, const uint8_t* ty, int ni, int nj, float cx,
+                           float cy, int sweeps, bool rb) {
+  const int n = ni * nj;
+  for (int s = 0; s < sweeps; s++)
+    for (int c = 0; c < 2; c++) {
+      const int color = rb ? c : 1 - c;
+      for (int u = threadIdx.x; u < n; u += blockDim.x) {
+        const int j = u / ni, i = u - j * ni;
+        if (((i + j) & 1) != color) continue;
+        y[u] = gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy);
+      }
+      __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseDesc D, LevelView top, int nu1, int nu2) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  float* Y = reinterpret_cast<float*>(sm);
+  float* R = Y + D.total;
+  float* PP = R + D.total;
+  float* T = PP + D.total;
+  uint8_t* TY = reinterpret_cast<uint8_t*>(T + D.total);
+  const int n0 = D.ni[0] * D.nj[0];
+  for (int u = threadIdx.x; u < n0; u += blockDim.x) {
+    Y[u] = 0.f;
+    R[u] = top.r[u];
+    PP[u] = top.P[u];
+    TY[u] = top.type[u];
+  }
+  __syncthreads();
+  // coarser levels: type and P by injection
+  for (int l = 1; l < D.n; l++) {
+    const int nic = D.ni[l], njc = D.nj[l], nif = D.ni[l - 1];
+    const int oc = D.off[l], of = D.off[l - 1];
+    for (int u = threadIdx.x; u < nic * njc; u += blockDim.x) {
+      const int J = u / nic, I = u - J * nic;
+      const int uf = of + (2 * J) * nif + 2 * I;
+      TY[oc + u] = node_class(TY[uf] == NC_FIXED, I, J, nic, njc);
+      PP[oc + u] = PP[uf];
+    }
+    __syncthreads();
+  }
+  // descend
+  for (int l = 0; l < D.n - 1; l++) {
+    const int o = D.off[l], ni = D.ni[l], nj = D.nj[l];
+    cta_smooth(Y + o, R + o, PP + o, TY + o, ni, nj, D.cx[l], D.cy[l], nu1, true);
+    for (int u = threadIdx.x; u < ni * nj; u += blockDim.x)
+      T[o + u] = R[o + u] - apply_J(TY[o + u], Y + o, PP[o + u], u, ni, D.cx[l], D.cy[l]);
+    __syncthreads();
+    const int oc = D.off[l + 1], nic = D.ni[l + 1], njc = D.nj[l + 1];
+    for (int u = threadIdx.x; u < nic * njc; u += blockDim.x) {
+      const int J = u / nic, I = u - J * nic;
+      R[oc + u] = restrict_value(T + o, TY[oc + u], I, J, ni, nic, njc);
+      Y[oc + u] = 0.f;
+    }
+    __syncthreads();
+  }
+  // coarsest: symmetric sweep pairs
+  {
+    const int l = D.n - 1, o = D.off[l];
+    for (int s = 0; s < D.coarsest_sweeps; s++) {
+      cta_smooth(Y + o, R + o, PP + o, TY + o, D.ni[l], D.nj[l], D.cx[l], D.cy[l], 1, true);
+      cta_smooth(Y + o, R + o, PP + o, TY + o, D.ni[l], D.nj[l], D.cx[l], D.cy[l], 1, false);
+    }
+  }
+  // ascend
+  for (int l = D.n - 2; l >= 0; l--) {
+    const int o = D.off[l], ni = D.ni[l], nj = D.nj[l];
+    const int oc = D.off[l + 1], nic = D.ni[l + 1];
+    for (int u = threadIdx.x; u < ni * nj; u += blockDim.x) {
+      if (TY[o + u] == NC_FIXED) continue;
+      const int j = u / ni, i = u - j * ni;
+      Y[o + u] += prolong_value(Y + oc, i, j, nic);
+    }
+    __syncthreads();
+    cta_smooth(Y + o, R + o, PP + o, TY + o, ni, nj, D.cx[l], D.cy[l], nu2, false);
+  }
+  for (int u = threadIdx.x; u < n0; u += blockDim.x) top.y[u] = Y[u];
+}
+
+// ------------------------------------------------------------------------------------
+// FP64 outer loop
+// ------------------------------------------------------------------------------------
+struct NlArgs {
+  int ni, nj;
+  double cx, cy, dx, dy;  // 1/dx^2, 1/dy^2, dx, dy
+  double C_n0;            // (e/eps) n0
+  double inv_kTe, phi0;
+  int linear;
+};
+
+constexpr int RB = 256;
+
+__device__ inline void block_sum2(double a, double b, double* part, bool max2) {
+  __shared__ double sh[2][RB / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    const double bb = __shfl_down_sync(0xffffffffu, b, o);
+    b = max2 ? fmax(b, bb) : b + bb;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sh[0][wid] = a;
+    sh[1][wid] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0, y = 0;
+    for (int w = 0; w < RB / 32; w++) {
+      x += sh[0][w];
+      y = max2 ? fmax(y, sh[1][w]) : y + sh[1][w];
+    }
+    part[2 * blockIdx.x] = x;
+    part[2 * blockIdx.x + 1] = y;
+  }
+}
+
+// F = A x - b0 - (e n0/eps) exp((x - phi0)/kTe) on interior rows, x - bc on fixed rows,
+// the one-sided gradient on open-face rows (b = 0 there, as Solver.java:322-338 sets);
+// P = d(exp term)/dx.  F (open-face rows scaled by 1/h for the symmetric inner system)
+// and P go to the FP32 level 0; per block sum F^2 and max |F| of the unscaled F.
+__global__ void __launch_bounds__(RB) k_nl_residual(NlArgs a, const double* __restrict__ x,
+                                                    const double* __restrict__ b0, const uint8_t* __restrict__ type,
+                                                    float* __restrict__ F32, float* __restrict__ P32,
+                                                    double* __restrict__ partial) {
+  const int n = a.ni * a.nj;
+  double s2 = 0.0, smax = 0.0;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    const uint8_t t = type[u];
+    const double xc = x[u];
+    double F, Fs, P = 0.0;
+    switch (t) {
+      case NC_FIXED: F = Fs = xc - b0[u]; break;
+      case NC_NLEFT: F = (x[u + 1] - xc) / a.dx; Fs = F / a.dx; break;
+      case NC_NRIGHT: F = (xc - x[u - 1]) / a.dx; Fs = -F / a.dx; break;
+      case NC_NBOTTOM: F = (x[u + a.ni] - xc) / a.dy; Fs = F / a.dy; break;
+      case NC_NTOP: F = (xc - x[u - a.ni]) / a.dy; Fs = -F / a.dy; break;
+      default: {
+        const double Ax = a.cx * (x[u - 1] + x[u + 1] - 2.0 * xc) + a.cy * (x[u - a.ni] + x[u + a.ni] - 2.0 * xc);
+        double ex = 0.0;
+        if (!a.linear) {
+          ex = a.C_n0 * exp((xc - a.phi0) * a.inv_kTe);
+          P = ex * a.inv_kTe;
+        }
+        F = Fs = Ax - (b0[u] + ex);
+      }
+    }
+    F32[u] = (float)Fs;
+    P32[u] = (float)P;
+    s2 += F * F;
+    smax = fmax(smax, fabs(F));
+  }
+  block_sum2(s2, smax, partial, true);
+}
+
+__global__ void k_reduce_partials(const double* partial, int nb, double* out, int max2) {
+  __shared__ double s2[256], sm[256];
+  double a2 = 0, am = 0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    a2 += partial[2 * b];
+    am = max2 ? fmax(am, partial[2 * b + 1]) : am + partial[2 * b + 1];
+  }
+  s2[threadIdx.x] = a2;
+  sm[threadIdx.x] = am;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      s2[threadIdx.x] += s2[threadIdx.x + w];
+      sm[threadIdx.x] = max2 ? fmax(sm[threadIdx.x], sm[threadIdx.x + w]) : sm[threadIdx.x] + sm[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = s2[0];
+    out[1] = sm[0];
+  }
+}
+
+// ---- flexible preconditioned CG on J y = F (FP32 vectors, FP64 dot products) -------
+// scalars: sc[0] = r.z, sc[1] = p.Jp, sc[2] = alpha, sc[3] = beta, sc[4..5] = reduction out
+enum { SC_RZ = 0, SC_PQ = 1, SC_ALPHA = 2, SC_BETA = 3, SC_RED = 4 };
+
+// q = J p and the partial sums of p.q
+__global__ void __launch_bounds__(RB) k_cg_matvec(LevelView L, const float* __restrict__ p, float* __restrict__ q,
+                                                  double* __restrict__ partial) {
+  const int n = L.ni * L.nj;
+  double s = 0.0;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    const float qu = apply_J(L.type[u], p, L.P[u], u, L.ni, L.cx, L.cy);
+    q[u] = qu;
+    s += (double)p[u] * (double)qu;
+  }
+  block_sum2(s, 0.0, partial, false);
+}
+
+// x += alpha p, r -= alpha q, zo = z
+__global__ void k_cg_axpy(int n, const double* __restrict__ sc, const float* __restrict__ p, const float* __restrict__ q,
+                          float* __restrict__ x, float* __restrict__ r, const float* __restrict__ z, float* __restrict__ zo) {
+  const float al = (float)sc[SC_ALPHA];
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    x[u] += al * p[u];
+    r[u] -= al * q[u];
+    zo[u] = z[u];
+  }
+}
+
+// partial sums of r.z and r.(z - zo)
+__global__ void __launch_bounds__(RB) k_cg_dots(int n, const float* __restrict__ r, const float* __restrict__ z,
+                                                const float* __restrict__ zo, double* __restrict__ partial) {
+  double a = 0.0, b = 0.0;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    const double ru = r[u], zu = z[u];
+    a += ru * zu;
+    b += ru * (zu - (double)zo[u]);
+  }
+  block_sum2(a, b, partial, false);
+}
+
+// scalar updates of the CG recurrence (one thread)
+__global__ void k_cg_scalars(double* sc, int stage) {
+  if (threadIdx.x != 0) return;
+  if (stage == 0) {            // after the first preconditioning: rz = r.z
+    sc[SC_RZ] = sc[SC_RED];
+  } else if (stage == 1) {     // after p.q: alpha = rz / pq
+    sc[SC_PQ] = sc[SC_RED];
+    sc[SC_ALPHA] = (sc[SC_PQ] != 0.0) ? sc[SC_RZ] / sc[SC_PQ] : 0.0;
+  } else {                     // after r.z, r.(z-zo): Polak-Ribiere beta, new rz
+    sc[SC_BETA] = (sc[SC_RZ] != 0.0) ? sc[SC_RED + 1] / sc[SC_RZ] : 0.0;
+    sc[SC_RZ] = sc[SC_RED];
+  }
+}
+
+// p = z + beta p  (beta = 0 for the first direction)
+__global__ void k_cg_pupdate(int n, const double* __restrict__ sc, int first, const float* __restrict__ z,
+                             float* __restrict__ p) {
+  const float be = first ? 0.f : (float)sc[SC_BETA];
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) p[u] = z[u] + be * p[u];
+}
+
+__global__ void k_update_phi(int n, double* __restrict__ x, const float* __restrict__ y) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) x[u] -= (double)y[u];
+}
+
+__global__ void k_build_b0(int n, const double* __restrict__ rho, const double* __restrict__ bc,
+                           const uint8_t* __restrict__ type, double inv_eps, double* __restrict__ b0) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    const uint8_t t = type[u];
+    b0[u] = (t == NC_FIXED) ? bc[u] : (t == NC_INTERIOR ? -rho[u] * inv_eps : 0.0);
+  }
+}
+
+__global__ void k_fix_phi(int n, double* __restrict__ x, const double* __restrict__ bc, const uint8_t* __restrict__ type) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
+    if (type[u] == NC_FIXED) x[u] = bc[u];
+}
+
+// E = -grad(phi): central differences inside, one-sided on the mesh edges
+// (the rows Solver.getNodeGradient assembles, Solver.java:559-611)
+__global__ void k_efield(int ni, int nj, double inv_dx, double inv_dy, const double* __restrict__ phi,
+                         double* __restrict__ efi, double* __restrict__ efj, float2* __restrict__ E) {
+  const int n = ni * nj;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    const int j = u / ni, i = u - j * ni;
+    double gi, gj;
+    if (i == 0) gi = (phi[u + 1] - phi[u]) * inv_dx;
+    else if (i == ni - 1) gi = (phi[u] - phi[u - 1]) * inv_dx;
+    else gi = (phi[u + 1] - phi[u - 1]) * (0.5 * inv_dx);
+    if (j == 0) gj = (phi[u + ni] - phi[u]) * inv_dy;
+    else if (j == nj - 1) gj = (phi[u] - phi[u - ni]) * inv_dy;
+    else gj = (phi[u + ni] - phi[u - ni]) * (0.5 * inv_dy);
+    efi[u] = -gi;
+    efj[u] = -gj;
+    E[u] = make_float2((float)(-gi), (float)(-gj));
+  }
+}
+
+__global__ void k_boltzmann(int n, const double* __restrict__ phi, double n0, double inv_kTe, double phi0,
+                            double* __restrict__ ne) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    double d = n0 * exp((phi[u] - phi0) * inv_kTe);
+    ne[u] = d < 1.0 ? 1.0 : d;
+  }
+}
+
+__global__ void k_rho_add(int n, const double* __restrict__ nd, double q, double* __restrict__ rho) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) rho[u] += q * nd[u];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------
+struct SfPoisson {
+  int ni = 0, nj = 0;
+  double *phi = nullptr, *b0 = nullptr, *rho = nullptr, *bc = nullptr, *ne = nullptr;
+  double *efi = nullptr, *efj = nullptr, *partial = nullptr, *red = nullptr, *sc = nullptr;
+  float *cg_x = nullptr, *cg_p = nullptr, *cg_q = nullptr, *cg_zo = nullptr;
+  uint8_t* type0 = nullptr;
+  std::vector<LevelView> lv;
+  std::vector<void*> allocs;
+  int cs = 0;  // first level of the single-CTA solve
+  CoarseDesc cd{};
+  size_t coarse_smem = 0;
+  int red_blocks = 0;
+  bool rho_set = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  sf_poisson_params prm{};
+  bool have_prm = false;
+};
+
+static void* dalloc(SfPoisson* ps, size_t bytes) {
+  void* p = nullptr;
+  SF_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+  ps->allocs.push_back(p);
+  return p;
+}
+
+static SfPoisson* poisson_get(sf_ctx* ctx) {
+  if (ctx->poisson) return ctx->poisson;
+  SF_REQUIRE(ctx->domain == SF_DOMAIN_XY, SF_ERR_ARG,
+             "the Poisson solve supports XY meshes (axisymmetric meshes use a given field)");
+  SfPoisson* ps = new SfPoisson();
+  ctx->poisson = ps;
+  const int ni = ctx->ni, nj = ctx->nj;
+  const size_t nn = (size_t)ni * nj;
+  ps->ni = ni;
+  ps->nj = nj;
+  ps->phi = (double*)dalloc(ps, 8 * nn);
+  ps->b0 = (double*)dalloc(ps, 8 * nn);
+  ps->rho = (double*)dalloc(ps, 8 * nn);
+  ps->bc = (double*)dalloc(ps, 8 * nn);
+  ps->ne = (double*)dalloc(ps, 8 * nn);
+  ps->efi = (double*)dalloc(ps, 8 * nn);
+  ps->efj = (double*)dalloc(ps, 8 * nn);
+  ps->cg_x = (float*)dalloc(ps, 4 * nn);
+  ps->cg_p = (float*)dalloc(ps, 4 * nn);
+  ps->cg_q = (float*)dalloc(ps, 4 * nn);
+  ps->cg_zo = (float*)dalloc(ps, 4 * nn);
+  ps->type0 = (uint8_t*)dalloc(ps, nn);
+  ps->red_blocks = ctx->num_sms * 4;
+  ps->partial = (double*)dalloc(ps, 16 * (size_t)ps->red_blocks);
+  ps->red = (double*)dalloc(ps, 16);
+  ps->sc = (double*)dalloc(ps, 8 * 8);
+  SF_CUDA(cudaMemsetAsync(ps->phi, 0, 8 * nn, ctx->stream));
+  SF_CUDA(cudaMemsetAsync(ps->rho, 0, 8 * nn, ctx->stream));
+  SF_CUDA(cudaMemcpyAsync(ps->bc, ctx->bc_value.data(), 8 * nn, cudaMemcpyHostToDevice, ctx->stream));
+  // node classes of the fine level (fixed = Dirichlet or internal nodes, Mesh.isDirichletNode)
+  std::vector<uint8_t> t0(nn);
+  for (int j = 0; j < nj; j++)
+    for (int i = 0; i < ni; i++) {
+      const int nt = ctx->node_type[(size_t)j * ni + i];
+      t0[(size_t)j * ni + i] = node_class(nt == SF_NODE_DIRICHLET || nt == SF_NODE_INTERNAL, i, j, ni, nj);
+    }
+  SF_CUDA(cudaMemcpyAsync(ps->type0, t0.data(), nn, cudaMemcpyHostToDevice, ctx->stream));
+  // multigrid hierarchy: halve while both node counts are odd (2m+1) and >= 5
+  std::vector<std::vector<uint8_t>> types;
+  types.push_back(t0);
+  int lni = ni, lnj = nj;
+  double ldx = ctx->dh[0], ldy = ctx->dh[1];
+  for (int l = 0; l < MAX_LEVELS; l++) {
+    LevelView L;
+    L.ni = lni;
+    L.nj = lnj;
+    L.cx = (float)(1.0 / (ldx * ldx));
+    L.cy = (float)(1.0 / (ldy * ldy));
+    const size_t n = (size_t)lni * lnj;
+    L.y = (float*)dalloc(ps, 4 * n);
+    L.r = (float*)dalloc(ps, 4 * n);
+    L.P = (float*)dalloc(ps, 4 * n);
+    L.t = (float*)dalloc(ps, 4 * n);
+    if (l == 0) {
+      L.type = ps->type0;
+    } else {
+      uint8_t* ty = (uint8_t*)dalloc(ps, n);
+      SF_CUDA(cudaMemcpyAsync(ty, types[l].data(), n, cudaMemcpyHostToDevice, ctx->stream));
+      L.type = ty;
+    }
+    SF_CUDA(cudaMemsetAsync(L.y, 0, 4 * n, ctx->stream));
+    SF_CUDA(cudaMemsetAsync(L.P, 0, 4 * n, ctx->stream));
+    ps->lv.push_back(L);
+    const bool can = ((lni - 1) % 2 == 0) && ((lnj - 1) % 2 == 0) && lni >= 5 && lnj >= 5;
+    if (!can) break;
+    const int cni = (lni - 1) / 2 + 1, cnj = (lnj - 1) / 2 + 1;
+    std::vector<uint8_t> tc((size_t)cni * cnj);
+    for (int J = 0; J < cnj; J++)
+      for (int I = 0; I < cni; I++)
+        tc[(size_t)J * cni + I] = node_class(types[l][(size_t)(2 * J) * lni + 2 * I] == NC_FIXED, I, J, cni, cnj);
+    types.push_back(tc);
+    lni = cni;
+    lnj = cnj;
+    ldx *= 2;
+    ldy *= 2;
+  }
+  // first level small enough for the single-CTA coarse solve
+  const int nl = (int)ps->lv.size();
+  ps->cs = nl - 1;
+  for (int l = 0; l < nl; l++)
+    if ((size_t)ps->lv[l].ni * ps->lv[l].nj <= (size_t)COARSE_NODES) {
+      ps->cs = l;
+      break;
+    }
+  CoarseDesc& D = ps->cd;
+  D.n = nl - ps->cs;
+  int off = 0;
+  for (int k = 0; k < D.n; k++) {
+    const LevelView& L = ps->lv[ps->cs + k];
+    D.ni[k] = L.ni;
+    D.nj[k] = L.nj;
+    D.cx[k] = L.cx;
+    D.cy[k] = L.cy;
+    D.off[k] = off;
+    off += L.ni * L.nj;
+  }
+  D.total = off;
+  const LevelView& Lc = ps->lv[nl - 1];
+  D.coarsest_sweeps = std::min(200, std::max(10, std::max(Lc.ni, Lc.nj)));
+  ps->coarse_smem = (size_t)D.total * (4 * sizeof(float) + 1) + 16;
+  SF_REQUIRE(ps->coarse_smem <= 220 * 1024, SF_ERR_ARG,
+             "mesh not coarsenable to a level that fits in shared memory (use (2^k)m+1 nodes per direction)");
+  SF_CUDA(cudaFuncSetAttribute(k_coarse_vcycle, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps->coarse_smem));
+  SF_CUDA(cudaEventCreate(&ps->ev0));
+  SF_CUDA(cudaEventCreate(&ps->ev1));
+  SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  return ps;
+}
+
+static inline dim3 grid2(int ni, int nj, dim3 blk) { return dim3((ni + blk.x - 1) / blk.x, (nj + blk.y - 1) / blk.y); }
+
+static void restrict_P(sf_ctx* ctx, SfPoisson* ps) {
+  const dim3 blk(32, 8);
+  for (int l = 0; l < ps->cs; l++) {
+    k_restrict_P<<<grid2(ps->lv[l + 1].ni, ps->lv[l + 1].nj, blk), blk, 0, ctx->stream>>>(ps->lv[l], ps->lv[l + 1]);
+    ctx->launches++;
+  }
+}
+
+// z = M^-1 r: one V(nu1,nu2)-cycle on level 0 from zero, r = lv[0].r, z -> lv[0].y
+static void vcycle(sf_ctx* ctx, SfPoisson* ps, int nu1, int nu2) {
+  cudaStream_t s = ctx->stream;
+  const dim3 blk(32, 8);
+  if (ps->cs > 0) SF_CUDA(cudaMemsetAsync(ps->lv[0].y, 0, 4 * (size_t)ps->lv[0].ni * ps->lv[0].nj, s));
+  for (int l = 0; l < ps->cs; l++) {
+    const LevelView& L = ps->lv[l];
+    const dim3 gs((L.ni / 2 + 1 + blk.x - 1) / blk.x, (L.nj + blk.y - 1) / blk.y);
+    for (int k = 0; k < nu1; k++) {
+      k_smooth<<<gs, blk, 0, s>>>(L, 0);
+      k_smooth<<<gs, blk, 0, s>>>(L, 1);
+      ctx->launches += 2;
+    }
+    k_resid<<<grid2(L.ni, L.nj, blk), blk, 0, s>>>(L);
+    k_restrict<<<grid2(ps->lv[l + 1].ni, ps->lv[l + 1].nj, blk), blk, 0, s>>>(L, ps->lv[l + 1]);
+    ctx->launches += 2;
+  }
+  k_coarse_vcycle<<<1, 1024, ps->coarse_smem, s>>>(ps->cd, ps->lv[ps->cs], nu1, nu2);
+  ctx->launches++;
+  for (int l = ps->cs - 1; l >= 0; l--) {
+    const LevelView& L = ps->lv[l];
+    k_prolong<<<grid2(L.ni, L.nj, blk), blk, 0, s>>>(ps->lv[l + 1], L);
+    ctx->launches++;
+    const dim3 gs((L.ni / 2 + 1 + blk.x - 1) / blk.x, (L.nj + blk.y - 1) / blk.y);
+    for (int k = 0; k < nu2; k++) {
+      k_smooth<<<gs, blk, 0, s>>>(L, 1);
+      k_smooth<<<gs, blk, 0, s>>>(L, 0);
+      ctx->launches += 2;
+    }
+  }
+}
+
+static void reduce(sf_ctx* ctx, SfPoisson* ps, double* out, int max2) {
+  k_reduce_partials<<<1, 256, 0, ctx->stream>>>(ps->partial, ps->red_blocks, out, max2);
+  ctx->launches++;
+}
+
+// iters steps of flexible PCG on J y = F (F = lv[0].r, overwritten as the CG residual);
+// the correction is left in cg_x
+static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters) {
+  cudaStream_t s = ctx->stream;
+  const LevelView& L0 = ps->lv[0];
+  const int n = L0.ni * L0.nj;
+  const int g = grid_for(n, 256, ctx->num_sms * 8);
+  SF_CUDA(cudaMemsetAsync(ps->cg_x, 0, 4 * (size_t)n, s));
+  vcycle(ctx, ps, 2, 2);  // z0
+  SF_CUDA(cudaMemsetAsync(ps->cg_zo, 0, 4 * (size_t)n, s));
+  k_cg_dots<<<ps->red_blocks, RB, 0, s>>>(n, L0.r, L0.y, ps->cg_zo, ps->partial);
+  reduce(ctx, ps, ps->sc + SC_RED, 0);
+  k_cg_scalars<<<1, 32, 0, s>>>(ps->sc, 0);
+  k_cg_pupdate<<<g, 256, 0, s>>>(n, ps->sc, 1, L0.y, ps->cg_p);
+  ctx->launches += 3;
+  for (int k = 0; k < iters; k++) {
+    k_cg_matvec<<<ps->red_blocks, RB, 0, s>>>(L0, ps->cg_p, ps->cg_q, ps->partial);
+    reduce(ctx, ps, ps->sc + SC_RED, 0);
+    k_cg_scalars<<<1, 32, 0, s>>>(ps->sc, 1);
+    k_cg_axpy<<<g, 256, 0, s>>>(n, ps->sc, ps->cg_p, ps->cg_q, ps->cg_x, L0.r, L0.y, ps->cg_zo);
+    ctx->launches += 3;
+    if (k == iters - 1) break;
+    vcycle(ctx, ps, 2, 2);
+    k_cg_dots<<<ps->red_blocks, RB, 0, s>>>(n, L0.r, L0.y, ps->cg_zo, ps->partial);
+    reduce(ctx, ps, ps->sc + SC_RED, 0);
+    k_cg_scalars<<<1, 32, 0, s>>>(ps->sc, 2);
+    k_cg_pupdate<<<g, 256, 0, s>>>(n, ps->sc, 0, L0.y, ps->cg_p);
+    ctx->launches += 3;
+  }
+}
+
+void sf_poisson_destroy_internal(sf_ctx* ctx) {
+  SfPoisson* ps = ctx->poisson;
+  if (!ps) return;
+  for (void* p : ps->allocs) cudaFree(p);
+  if (ps->ev0) cudaEventDestroy(ps->ev0);
+  if (ps->ev1) cudaEventDestroy(ps->ev1);
+  delete ps;
+  ctx->poisson = nullptr;
+}
+
+int sf_poisson_get_field_internal(sf_ctx* ctx, int field, double* out) {
+  try {
+    SfPoisson* ps = poisson_get(ctx);
+    const size_t nn = (size_t)ctx->ni * ctx->nj;
+    const double* src = nullptr;
+    switch (field) {
+      case SF_FIELD_PHI: src = ps->phi; break;
+      case SF_FIELD_RHO: src = ps->rho; break;
+      case SF_FIELD_EFI: src = ps->efi; break;
+      case SF_FIELD_EFJ: src = ps->efj; break;
+      case SF_FIELD_NE: src = ps->ne; break;
+      default: SF_REQUIRE(false, SF_ERR_ARG, "unknown field selector");
+    }
+    SF_CUDA(cudaMemcpyAsync(out, src, 8 * nn, cudaMemcpyDeviceToHost, ctx->stream));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return SF_OK;
+  } catch (const sf::Error& e) {
+    ctx->err = e.what();
+    return e.code;
+  }
+}
+
+extern "C" {
+
+int sf_update_rho(sf_ctx* ctx) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx, SF_ERR_ARG, "null context");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  SfPoisson* ps = poisson_get(ctx);
+  const int nn = ctx->ni * ctx->nj;
+  SF_CUDA(cudaMemsetAsync(ps->rho, 0, 8 * (size_t)nn, ctx->stream));
+  for (SfSpecies* sp : ctx->species) {
+    if (sp->charge == 0) continue;
+    k_rho_add<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(nn, sp->nd, sp->charge, ps->rho);
+    ctx->launches++;
+  }
+  SF_CUDA(cudaGetLastError());
+  SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  ps->rho_set = true;
+  SF_API_END(ctx)
+}
+
+int sf_set_bc_values(sf_ctx* ctx, const double* bc) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx && bc, SF_ERR_ARG, "null argument");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  SfPoisson* ps = poisson_get(ctx);
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  std::copy(bc, bc + nn, ctx->bc_value.begin());
+  SF_CUDA(cudaMemcpyAsync(ps->bc, bc, 8 * nn, cudaMemcpyHostToDevice, ctx->stream));
+  SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  SF_API_END(ctx)
+}
+
+int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, double* phi, sf_solve_stats* stats) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx && prm, SF_ERR_ARG, "null argument");
+  SF_REQUIRE(prm->eps > 0 && prm->tol > 0 && prm->max_it > 0, SF_ERR_ARG, "bad solver parameters");
+  SF_REQUIRE(prm->linear || (prm->kTe0 > 0 && prm->n0 > 0), SF_ERR_ARG, "Boltzmann electrons need n0 > 0 and kTe0 > 0");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  SfPoisson* ps = poisson_get(ctx);
+  cudaStream_t s = ctx->stream;
+  const int nn = ctx->ni * ctx->nj;
+  if (rho) {
+    SF_CUDA(cudaMemcpyAsync(ps->rho, rho, 8 * (size_t)nn, cudaMemcpyHostToDevice, s));
+    ps->rho_set = true;
+  }
+  SF_REQUIRE(ps->rho_set, SF_ERR_STATE, "no charge density: pass rho or call sf_update_rho");
+  if (phi) SF_CUDA(cudaMemcpyAsync(ps->phi, phi, 8 * (size_t)nn, cudaMemcpyHostToDevice, s));
+  const int g = grid_for(nn, 256, ctx->num_sms * 8);
+  k_build_b0<<<g, 256, 0, s>>>(nn, ps->rho, ps->bc, ps->type0, 1.0 / prm->eps, ps->b0);
+  k_fix_phi<<<g, 256, 0, s>>>(nn, ps->phi, ps->bc, ps->type0);  // fixed rows exact from the start
+  ctx->launches += 2;
+  ps->prm = *prm;
+  ps->have_prm = true;
+  NlArgs a;
+  a.ni = ctx->ni;
+  a.nj = ctx->nj;
+  a.dx = ctx->dh[0];
+  a.dy = ctx->dh[1];
+  a.cx = 1.0 / (a.dx * a.dx);
+  a.cy = 1.0 / (a.dy * a.dy);
+  a.C_n0 = QE / prm->eps * prm->n0;
+  a.inv_kTe = prm->linear ? 0.0 : 1.0 / prm->kTe0;
+  a.phi0 = prm->phi0;
+  a.linear = prm->linear ? 1 : 0;
+  const int iters = prm->cycles > 0 ? prm->cycles : 3;
+  SF_CUDA(cudaEventRecord(ps->ev0, s));
+  double h[2];
+  double res = 0, res_inf = 0, res0 = -1;
+  int it = 0, vcount = 0;
+  bool conv = false, diverged = false;
+  for (it = 0; it <= prm->max_it; it++) {
+    k_nl_residual<<<ps->red_blocks, RB, 0, s>>>(a, ps->phi, ps->b0, ps->type0, ps->lv[0].r, ps->lv[0].P, ps->partial);
+    reduce(ctx, ps, ps->red, 1);
+    ctx->launches++;
+    SF_CUDA(cudaMemcpyAsync(h, ps->red, 16, cudaMemcpyDeviceToHost, s));
+    SF_CUDA(cudaStreamSynchronize(s));
+    res = std::sqrt(h[0]) / nn;
+    res_inf = h[1];
+    if (res0 < 0) res0 = res;
+    if (!std::isfinite(res)) {
+      diverged = true;
+      break;
+    }
+    if (res < prm->tol) {
+      conv = true;
+      break;
+    }
+    if (it == prm->max_it) break;
+    restrict_P(ctx, ps);
+    pcg(ctx, ps, iters);
+    vcount += iters;
+    k_update_phi<<<g, 256, 0, s>>>(nn, ps->phi, ps->cg_x);
+    ctx->launches++;
+  }
+  SF_CUDA(cudaEventRecord(ps->ev1, s));
+  SF_CUDA(cudaEventSynchronize(ps->ev1));
+  float ms = 0;
+  SF_CUDA(cudaEventElapsedTime(&ms, ps->ev0, ps->ev1));
+  SF_CUDA(cudaGetLastError());
+  if (phi) {
+    SF_CUDA(cudaMemcpyAsync(phi, ps->phi, 8 * (size_t)nn, cudaMemcpyDeviceToHost, s));
+    SF_CUDA(cudaStreamSynchronize(s));
+  }
+  if (stats) {
+    stats->newton_it = it;
+    stats->vcycles = vcount;
+    stats->residual = res;
+    stats->residual_inf = res_inf;
+    stats->initial_residual = res0;
+    stats->ms = ms;
+  }
+  SF_REQUIRE(!diverged, SF_ERR_DIVERGED, "Solver diverged (non-finite residual)");
+  SF_REQUIRE(conv, SF_ERR_NOT_CONVERGED, "Poisson solve did not reach the residual tolerance");
+  SF_API_END(ctx)
+}
+
+int sf_efield(sf_ctx* ctx, double* efi, double* efj) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx, SF_ERR_ARG, "null context");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  SfPoisson* ps = poisson_get(ctx);
+  const int nn = ctx->ni * ctx->nj;
+  k_efield<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+      ctx->ni, ctx->nj, 1.0 / ctx->dh[0], 1.0 / ctx->dh[1], ps->phi, ps->efi, ps->efj, ctx->E);
+  ctx->launches++;
+  SF_CUDA(cudaGetLastError());
+  if (efi) SF_CUDA(cudaMemcpyAsync(efi, ps->efi, 8 * (size_t)nn, cudaMemcpyDeviceToHost, ctx->stream));
+  if (efj) SF_CUDA(cudaMemcpyAsync(efj, ps->efj, 8 * (size_t)nn, cudaMemcpyDeviceToHost, ctx->stream));
+  SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->efield_set = true;
+  SF_API_END(ctx)
+}
+
+int sf_boltzmann(sf_ctx* ctx, double* ne) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx, SF_ERR_ARG, "null context");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  SfPoisson* ps = poisson_get(ctx);
+  SF_REQUIRE(ps->have_prm && !ps->prm.linear, SF_ERR_STATE, "no Boltzmann parameters: run sf_poisson_nl first");
+  const int nn = ctx->ni * ctx->nj;
+  k_boltzmann<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(nn, ps->phi, ps->prm.n0,
+                                                                           1.0 / ps->prm.kTe0, ps->prm.phi0, ps->ne);
+  ctx->launches++;
+  SF_CUDA(cudaGetLastError());
+  if (ne) SF_CUDA(cudaMemcpyAsync(ne, ps->ne, 8 * (size_t)nn, cudaMemcpyDeviceToHost, ctx->stream));
+  SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  SF_API_END(ctx)
+}
+
+}  // extern "C"

@@ -151,3 +151,61 @@ class KineticMaterial:
         self.d.check(self.d.lib.sf_get_surface_flux(self.d.ctx, self.sid, abi.ptr(flux),
                                                     abi.ptr(dep)))
         return flux[:2 * ns], dep[:2 * ns]
+
+
+class PoissonSolver:
+    """GPU nonlinear Poisson solver with Boltzmann electrons (pic/PoissonSolver.java).
+
+    Arguments follow the <solver type="poisson"> element: n0, Te0 (eV), phi0, eps_r,
+    tol (residual target, here on the FP64 nonlinear residual ||R||_2/N), max_it.
+    """
+
+    EPS0 = 8.85418782e-12
+
+    def __init__(self, domain: GpuDomain, n0=1e12, Te0=2.0, phi0=0.0, eps_r=1.0, tol=1e-6,
+                 max_it=60, cycles=1, linear=False):
+        self.d = domain
+        self.prm = abi.PoissonParams()
+        self.prm.n0, self.prm.kTe0, self.prm.phi0 = n0, Te0, phi0
+        self.prm.eps = self.EPS0 * eps_r
+        self.prm.tol = tol
+        self.prm.max_it = max_it
+        self.prm.cycles = cycles
+        self.prm.use_learned = 0
+        self.prm.linear = 1 if linear else 0
+
+    def update_rho(self):
+        """SolverModule.updateRho from the GPU-resident species densities."""
+        self.d.check(self.d.lib.sf_update_rho(self.d.ctx))
+
+    def set_bc_values(self, bc):
+        bc = np.ascontiguousarray(bc, np.float64)
+        self.d.check(self.d.lib.sf_set_bc_values(self.d.ctx, abi.ptr(bc)))
+
+    def solve(self, rho=None, phi=None, check=True):
+        """PoissonSolver.update(): returns (phi or None, stats dict)."""
+        st = abi.SolveStats()
+        rho_a = None if rho is None else np.ascontiguousarray(rho, np.float64)
+        phi_a = None if phi is None else np.array(phi, np.float64, copy=True)
+        rc = self.d.lib.sf_poisson_nl(self.d.ctx, C.byref(self.prm), abi.ptr(rho_a), abi.ptr(phi_a),
+                                      C.byref(st))
+        if check:
+            self.d.check(rc)
+        out = st.as_dict()
+        out["status"] = rc
+        return phi_a, out
+
+    def update_gradient_field(self, copy=False):
+        """PotentialSolver.updateGradientField: E = -grad(phi) on the device."""
+        if copy:
+            efi = np.zeros(self.d.ni * self.d.nj)
+            efj = np.zeros(self.d.ni * self.d.nj)
+            self.d.check(self.d.lib.sf_efield(self.d.ctx, abi.ptr(efi), abi.ptr(efj)))
+            return efi, efj
+        self.d.check(self.d.lib.sf_efield(self.d.ctx, None, None))
+        return None
+
+    def boltzmann(self):
+        ne = np.zeros(self.d.ni * self.d.nj)
+        self.d.check(self.d.lib.sf_boltzmann(self.d.ctx, abi.ptr(ne)))
+        return ne

@@ -140,3 +140,49 @@ def test_node_segments_box_rule():
     xlo, xhi = spec.seg_xy[:, 0].min() / 1e-3, spec.seg_xy[:, 0].max() / 1e-3
     assert i.min() >= np.floor(xlo) - 2 and i.max() <= np.ceil(xhi) + 2
     assert len(idx) > 0
+
+
+# ---- the oracle reproduces its committed golden fixtures -------------------------------
+import os  # noqa: E402
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_golden_java_random():
+    g = np.load(os.path.join(GOLDEN, "java_random.npz"))
+    assert np.array_equal(O.jrandom_doubles(0, 16), g["seed0"])
+    assert np.array_equal(O.jrandom_doubles(42, 16), g["seed42"])
+    assert np.array_equal(O.sample_maxw3d(7, 64, 1000.0), g["maxw3d_seed7"])
+
+
+def test_golden_push():
+    g = np.load(os.path.join(GOLDEN, "push_es_pic_81x41.npz"))
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    ion = W.IonSpecies()
+    m = _omesh(spec)
+    ptr, idx = O.node_segments(m, spec.seg_xy)
+    lc, vel = g["lc0"], g["vel0"]
+    P = np.zeros((lc.shape[0], 12))
+    P[:, 0:2] = lc * np.array(spec.dh)
+    P[:, 3:6] = vel
+    P[:, 6:8] = lc
+    P[:, 9] = ion.spwt
+    P[:, 10] = 1
+    segs = O.seg_table(spec.seg_xy, spec.seg_btype, O.SURF_ABSORB)
+    O.push(m, g["efi"], g["efj"], ion.charge, ion.mass, float(g["dt"]), segs, ptr, idx, P)
+    assert np.array_equal(P[:, 10].astype(np.int8), g["alive"])
+    assert np.array_equal(P[:, 6:8], g["lc1"])
+    assert np.array_equal(O.update_fields(m, O.node_volumes(m), P), g["den"])
+
+
+def test_golden_poisson_residual_and_field():
+    """The fixture potential satisfies the oracle operator at its FP64 floor, and its
+    field / electron density are reproduced."""
+    g = np.load(os.path.join(GOLDEN, "poisson_es_pic_81x41.npz"))
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    m = _omesh(spec)
+    r = O.poisson_residual(m, spec.bc_value, g["rho"], 1e12, 2.0, 0.0, 8.85418782e-12, g["phi"])
+    assert r / spec.nn < 1e-9
+    efi, efj = O.efield(m, g["phi"])
+    assert np.array_equal(efi, g["efi"]) and np.array_equal(efj, g["efj"])
+    assert np.array_equal(O.boltzmann(g["phi"], 1e12, 2.0, 0.0), g["ne"])

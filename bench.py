@@ -115,6 +115,39 @@ def setup_workload(n_particles, seed=0):
     return cfg, dom, km, efi, efj
 
 
+def electrode_potential(step, period=2000):
+    """Electrode potential of the learned-warm-start workload: -100 - 100 cos(2 pi t / T) V."""
+    return -100.0 - 100.0 * np.cos(2 * np.pi * step / period)
+
+
+def poisson_bench(cfg, dom, steps=20, tol=1e-6):
+    """Plain GPU Poisson-Boltzmann solve (FP64 Newton residual, FP32 MG-PCG inner) per step
+    with the electrode potential advancing one step of its 2000-step period each solve."""
+    from starfish_gb300.plugin import PoissonSolver
+    ps = PoissonSolver(dom, n0=cfg.n0, Te0=cfg.Te0, phi0=cfg.phi0, tol=tol, max_it=60, cycles=2)
+    ps.update_rho()
+    bc0 = cfg.mesh.bc_value.copy()
+    electrode = bc0 != 0
+    # warm up from a cold start at step 0
+    bc = bc0.copy()
+    bc[electrode] = electrode_potential(0)
+    ps.set_bc_values(bc)
+    _, st0 = ps.solve()
+    ms, its = [], []
+    for t in range(1, steps + 1):
+        bc[electrode] = electrode_potential(t * 10)
+        ps.set_bc_values(bc)
+        _, st = ps.solve()
+        ms.append(st["ms"])
+        its.append(st["newton_it"])
+    ps.update_gradient_field()
+    return {"metric": "Poisson ms/solve to ||R||_2/N < 1e-6 (FP64)", "plain_ms": float(np.mean(ms)),
+            "plain_ms_min": float(np.min(ms)), "newton_it_mean": float(np.mean(its)),
+            "cold_start_ms": st0["ms"], "cold_start_newton_it": st0["newton_it"], "solves": steps,
+            "electrode_step_per_solve": 10, "mesh": [cfg.mesh.ni, cfg.mesh.nj], "tol": tol,
+            "learned_ms": None}
+
+
 def cpu_baseline_sample(cfg, efi, efj, n_sample, threads, steps=1, seed=1):
     """The oracle port (reference algorithm, FP64 AoS) on a bounded sample of the workload."""
     from oracle import oracle as O
@@ -188,6 +221,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--particles", type=int, default=64 * 1024 * 1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--poisson-steps", type=int, default=20)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -309,9 +343,13 @@ def main():
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * nn,
                 "d2h_bytes_per_step": 8 * nn + 64},
     }
+    # ---- field solve on the same mesh: rho from the 64M-ion density, electrode potential
+    # varied sinusoidally (-100 - 100 cos(2 pi t / 2000) V), each solve warm-started from the
+    # previous potential and run to ||R||_2/N < 1e-6 in FP64 ----
+    line["poisson"] = poisson_bench(cfg, dom, steps=args.poisson_steps)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        n_sample = 4 * 1024 * 1024
+        n_sample = 16 * 1024 * 1024
         v, t = cpu_baseline_sample(cfg, efi, efj, n_sample, threads, steps=2)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{n_sample} particles of the 64M workload, 2 steps "

@@ -178,6 +178,16 @@ int sf_particles_sort(sf_ctx* ctx, int32_t sid);
 /* Removes all particles of a species. */
 int sf_particles_clear(sf_ctx* ctx, int32_t sid);
 
+/* Maxwellian boundary source on one straight segment (x1, y1, x2, y2), sampled on the
+ * device: MaxwellianSource.sampleParticle (sources/MaxwellianSource.java:93-125) with the
+ * particle count of Source.regenerate (core/source/Source.java:123-134), the 1e-6 dt
+ * push off the surface of Source.sampleKinetic (:167-198) and the -dt/2 velocity rewind
+ * of KineticMaterial.addParticle (KineticMaterial.java:776-796).  The segment normal
+ * (-dy, dx)/L gives the drift direction.  den: density (m^-3), temp (K), v_drift (m/s).
+ * *rem carries the fractional particle count between calls.  *n_added: particles added. */
+int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg_xy, double den, double v_drift,
+                         double temp, double dt, double* rem, int64_t* n_added);
+
 /* ---- fields ----------------------------------------------------------------- */
 /* Sets the electric field used by the push (DomainModule efi/efj, FP64 host -> FP32 device). */
 int sf_set_efield(sf_ctx* ctx, const double* efi, const double* efj);

@@ -113,6 +113,9 @@ EXPORTS = {
                                 C.POINTER(SolveStats)]),
     "sf_efield": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sf_boltzmann": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sf_source_maxwellian": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_double, C.c_double,
+                                       C.c_double, C.c_double, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_int64)]),
 }
 
 _lib = None

@@ -404,8 +404,12 @@ __global__ void k_cg_pupdate(int n, const double* __restrict__ sc, int first, co
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) p[u] = z[u] + be * p[u];
 }
 
-__global__ void k_update_phi(int n, double* __restrict__ x, const float* __restrict__ y) {
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) x[u] -= (double)y[u];
+// x -= y, each node's step limited to max_step (10 kTe): far from the solution an
+// undamped Newton step on the exponential can overshoot into overflow; near it the
+// steps are tiny and the limit never acts, so the converged potential is unchanged
+__global__ void k_update_phi(int n, double* __restrict__ x, const float* __restrict__ y, double max_step) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
+    x[u] -= fmin(fmax((double)y[u], -max_step), max_step);
 }
 
 __global__ void k_build_b0(int n, const double* __restrict__ rho, const double* __restrict__ bc,
@@ -793,7 +797,7 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
     restrict_P(ctx, ps);
     pcg(ctx, ps, iters);
     vcount += iters;
-    k_update_phi<<<g, 256, 0, s>>>(nn, ps->phi, ps->cg_x);
+    k_update_phi<<<g, 256, 0, s>>>(nn, ps->phi, ps->cg_x, prm->linear ? 1e300 : 10.0 * prm->kTe0);
     ctx->launches++;
   }
   SF_CUDA(cudaEventRecord(ps->ev1, s));

@@ -1,0 +1,120 @@
+// sf_source.cu -- particle sources sampled on the device.
+//
+// MaxwellianSource (sources/MaxwellianSource.java:93-125) run every step by
+// SourceModule.sampleSources (core/source/SourceModule.java:231-283): particles are drawn
+// uniformly along a straight boundary segment, with a drifting Maxwellian velocity from
+// the reference's 12-uniform sampler (Utils.SampleMaxw3D, core/common/Utils.java:27-57,
+// including its factor 1.2), rejected until v.n > 0, pushed 1e-6 dt off the surface
+// (Source.sampleKinetic, core/source/Source.java:167-198) and appended with the -dt/2
+// velocity rewind of KineticMaterial.addParticle (KineticMaterial.java:776-796).
+// Random numbers come from counter-based Philox streams keyed by (step, particle).
+#include <cmath>
+
+#include "sf_internal.h"
+
+using namespace sf;
+
+namespace {
+
+struct InjectArgs {
+  double x1, y1, x2, y2;
+  double nx, ny;         // segment normal (LinearSegment: (-dy, dx)/L)
+  double v_th, v_drift;  // Utils.computeVth(T, m), drift speed along the normal
+  double dt;
+  float qm_halfdt;       // (q/m) dt/2 for the rewind
+  uint64_t seed;
+  uint32_t step;
+  int64_t base;          // first free slot
+};
+
+__device__ inline double maxw1d_unit(Philox& r) {
+  // Utils.SampleMaxw1D(1): sqrt(1/2) * (sum of 12 uniforms - 6)
+  double s = 0.0;
+  for (int k = 0; k < 12; k++) s += r.uniform();
+  return 0.7071067811865476 * (s - 6.0);
+}
+
+__global__ void k_inject_maxwellian(MeshView m, ParticlesView P, InjectArgs a, int n, unsigned long long* counter) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  Philox rng(a.seed, RNG_INJECT, (uint64_t)k, a.step);
+  const double t = rng.uniform();  // Boundary.randomT on a single segment
+  double px = a.x1 + t * (a.x2 - a.x1), py = a.y1 + t * (a.y2 - a.y1);
+  double vx = 0, vy = 0, vz = 0;
+  for (int tries = 0; tries < 64; tries++) {
+    vx = (a.v_th * 1.2) * maxw1d_unit(rng) + a.nx * a.v_drift;
+    vy = (a.v_th * 1.2) * maxw1d_unit(rng) + a.ny * a.v_drift;
+    vz = (a.v_th * 1.2) * maxw1d_unit(rng);
+    (void)rng.uniform();  // part.dt = rnd * dt, overwritten by addParticle
+    if (a.nx * vx + a.ny * vy > 0) break;
+  }
+  px += vx * 1e-6 * a.dt;
+  py += vy * 1e-6 * a.dt;
+  double lx = (px - m.x0[0]) / m.dh[0], ly = (py - m.x0[1]) / m.dh[1];
+  if (!(lx >= 0 && ly >= 0 && lx <= m.ni - 1 && ly <= m.nj - 1)) return;  // outside every mesh
+  int i = (int)lx, j = (int)ly;
+  if (i > m.ni - 2) i = m.ni - 2;
+  if (j > m.nj - 2) j = m.nj - 2;
+  const float fx = (float)(lx - i), fy = (float)(ly - j);
+  const int u = j * m.ni + i;
+  const float2 e00 = m.E[u], e10 = m.E[u + 1], e11 = m.E[u + m.ni + 1], e01 = m.E[u + m.ni];
+  const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w11 = fx * fy, w01 = (1.f - fx) * fy;
+  const float ex = w00 * e00.x + w10 * e10.x + w11 * e11.x + w01 * e01.x;
+  const float ey = w00 * e00.y + w10 * e10.y + w11 * e11.y + w01 * e01.y;
+  const int64_t d = a.base + (int64_t)atomicAdd(counter, 1ULL);
+  P.cell[d] = pack_cell(i, j);
+  P.frac[d] = make_float2(fx, fy);
+  P.vxy[d] = make_float2((float)vx - a.qm_halfdt * ex, (float)vy - a.qm_halfdt * ey);
+  P.vz[d] = (float)vz;
+}
+
+}  // namespace
+
+extern "C" int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg, double den, double v_drift,
+                                    double temp, double dt, double* rem, int64_t* n_added) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(seg && rem && n_added, SF_ERR_ARG, "null argument");
+  SF_REQUIRE(den >= 0 && temp >= 0 && dt > 0, SF_ERR_ARG, "bad source parameters");
+  SF_REQUIRE(ctx->efield_set, SF_ERR_STATE, "electric field not set (the rewind gathers E)");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const double dx = seg[2] - seg[0], dy = seg[3] - seg[1];
+  const double len = std::sqrt(dx * dx + dy * dy);
+  SF_REQUIRE(len > 0, SF_ERR_ARG, "degenerate source segment");
+  // MaxwellianSource ctor (MaxwellianSource.java:60-80): mdot from den; Source.regenerate
+  const double v_mean = std::sqrt(8 * KB * temp / (PI * sp->mass));
+  const double mdot = den * len * (v_drift + v_mean / 4) * sp->mass;  // XY: area = length x 1 m
+  const double mp = (mdot * dt) / (sp->mass * sp->spwt) + *rem;
+  const int64_t num = (int64_t)mp;
+  *rem = mp - (double)num;
+  *n_added = 0;
+  if (num <= 0) return SF_OK;
+  SF_REQUIRE(sp->n + num <= sp->cap, SF_ERR_OOM, "species capacity exceeded by the source");
+  InjectArgs a;
+  a.x1 = seg[0];
+  a.y1 = seg[1];
+  a.x2 = seg[2];
+  a.y2 = seg[3];
+  a.nx = -dy / len;
+  a.ny = dx / len;
+  a.v_th = std::sqrt(2 * KB * temp / sp->mass);
+  a.v_drift = v_drift;
+  a.dt = dt;
+  a.qm_halfdt = (float)(sp->charge / sp->mass * 0.5 * dt);
+  a.seed = ctx->seed ^ (0x9E3779B97F4A7C15ULL * (uint64_t)(sid + 1));
+  a.step = sp->step;
+  a.base = sp->n;
+  unsigned long long* cnt = ctx->counters + 7;
+  SF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), ctx->stream));
+  k_inject_maxwellian<<<(int)((num + 255) / 256), 256, 0, ctx->stream>>>(ctx->mesh_view(), sp->cur, a, (int)num, cnt);
+  ctx->launches++;
+  SF_CUDA(cudaGetLastError());
+  unsigned long long added = 0;
+  SF_CUDA(cudaMemcpyAsync(&added, cnt, sizeof(added), cudaMemcpyDeviceToHost, ctx->stream));
+  SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  sp->n += (int64_t)added;
+  sp->cur.n = sp->n;
+  sp->sorted = false;
+  *n_added = (int64_t)added;
+  SF_API_END(ctx)
+}

@@ -85,6 +85,7 @@ class KineticMaterial:
                                                nd_back, C.byref(sid)))
         self.sid = sid.value
         self.mass, self.charge, self.spwt = mass, charge, spwt
+        self._src_rem = {}
 
     # KineticMaterial.addParticle(pos, vel) with the -dt/2 velocity rewind
     def add_particles(self, pos, vel, rewind=True, dt=0.0):
@@ -99,6 +100,18 @@ class KineticMaterial:
         vel = np.ascontiguousarray(vel, np.float64)
         self.d.check(self.d.lib.sf_particles_append_lc(self.d.ctx, self.sid, lc.shape[0],
                                                        abi.ptr(lc), abi.ptr(vel)))
+
+    def sample_maxwellian_source(self, seg_xy, den, v_drift, temp, dt):
+        """MaxwellianSource on one straight segment, sampled on the device; returns the
+        number of particles added (the fractional remainder is kept per source)."""
+        key = tuple(np.asarray(seg_xy, np.float64).reshape(-1))
+        rem = C.c_double(self._src_rem.get(key, 0.0))
+        seg = np.ascontiguousarray(seg_xy, np.float64).reshape(-1)
+        n = C.c_int64()
+        self.d.check(self.d.lib.sf_source_maxwellian(self.d.ctx, self.sid, abi.ptr(seg), den, v_drift,
+                                                     temp, dt, C.byref(rem), C.byref(n)))
+        self._src_rem[key] = rem.value
+        return n.value
 
     def set_surface(self, seg, model, vth=0.0, c_rest=1.0, c_accom=1.0):
         self.d.check(self.d.lib.sf_species_set_surface(self.d.ctx, self.sid, seg, model, vth,

@@ -142,8 +142,12 @@ def config1(n_particles=64 * 1024 * 1024) -> EsPicConfig:
     """2049x1025, dx = 0.05 mm, 64M preloaded ions.  dt is scaled with dx (2.5e-8 s)
     to keep config0's 3.5 cells of drift per step."""
     m = es_pic_mesh(2049, 1025, 5e-5, electrode_halfwidth=4.5e-3)
-    return EsPicConfig("es_pic_2049x1025_64M", m, IonSpecies(), dt=2.5e-8, steps=1000,
-                       n_particles=n_particles)
+    # macroparticle weight chosen so that the ions fill the gas region at config0's
+    # plasma density (1e12 m^-3, per metre of depth)
+    Lx, Ly = m.lengths()
+    gas_area = Lx * Ly - (2 * 4.5e-3) ** 2
+    ion = IonSpecies(spwt=1e12 * gas_area / max(n_particles, 1))
+    return EsPicConfig("es_pic_2049x1025_64M", m, ion, dt=2.5e-8, steps=1000, n_particles=n_particles)
 
 
 def uniform_maxwellian(mesh: MeshSpec, ion: IonSpecies, n: int, seed: int):

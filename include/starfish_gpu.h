@@ -261,6 +261,46 @@ int sf_efield(sf_ctx* ctx, double* efi, double* efj);
  * n_e = max(1, n0 exp((phi - phi0)/kTe)) into ne (ni*nj, may be NULL: device only). */
 int sf_boltzmann(sf_ctx* ctx, double* ne);
 
+/* ---- collisions ------------------------------------------------------------- */
+/* Cross-section models (interactions/Sigma.java:24-195, collisions/SigmaPlus.java:38-76) */
+#define SF_SIGMA_CONST 0    /* sigma = c0                                         */
+#define SF_SIGMA_INV 1      /* sigma = c0 / g                                     */
+#define SF_SIGMA_POLY 2     /* c0 + c1 g + c2 g^2 + c3 g^4 (the reference's g *= g) */
+#define SF_SIGMA_LN 3       /* sigma = (c0 + c1 ln g)^2                           */
+#define SF_SIGMA_BIRD463 4  /* VHS, Bird eq. 4.63                                 */
+typedef struct {
+  int32_t model;      /* SF_SIGMA_*                                              */
+  double c[4];        /* coefficients of CONST / INV / POLY / LN                 */
+  double diam;        /* BIRD463: molecular diameter of the species (Material.diam) */
+  double T_ref;       /* BIRD463: reference temperature (Material.ref_temp)       */
+  double omega;       /* BIRD463: viscosity-temperature index                     */
+  double vss_alpha;   /* scattering: 1 = VHS (isotropic), else VSS                */
+} sf_sigma;
+
+/* DSMC.perform for a same-species pair (collisions/DSMC.java:162-454): cell binning
+ * (a counting sort of the species), then per cell the NTC selection count
+ * nsel = (n1 w / Vc) n2 dt (sigma g)max / 2 + rem, random pairs accepted with
+ * sigma(g) g / (sigma g)max, and the elastic VHS/VSS scattering of ModelElastic.
+ * dt: frequency * dt of the reference.  sig_cr_max0: initial (sigma g)max of every cell
+ * (DSMC element sig_cr_max, default 1e-16).  *n_coll: collisions performed. */
+int sf_dsmc(sf_ctx* ctx, int32_t sid, const sf_sigma* sigma, double dt, double sig_cr_max0,
+            int64_t* n_coll);
+/* Per-cell collision sums accumulated by sf_dsmc ((ni-1)*(nj-1) each, j-major):
+ * count (col-count-sum) and weight (col-real-sum), DSMC.java:241-247. */
+int sf_dsmc_get_counts(sf_ctx* ctx, int32_t sid, double* count_sum, double* real_sum);
+/* Target (background) material of MCC: mass and node fields density, mean velocity and
+ * temperature (Material.getDen / getUAve.. / getT), ni*nj each; u, v, w may be NULL (0). */
+int sf_mcc_set_target(sf_ctx* ctx, double mass, const double* den, const double* u, const double* v,
+                      const double* w, const double* temp);
+/* MCC.perform (collisions/MCC.java:167-221) for a kinetic source species against the
+ * target: P = 1 - exp(-sigma(g) g dt n_t) with g from the target's mean velocity; on a
+ * collision a Maxwellian target particle is drawn (Material.sampleMaxwellianVelocity)
+ * and the source velocity is set by model SF_MCC_MEX (elastic, MCC.java:242-285) or
+ * SF_MCC_CEX (charge exchange, :287-297). */
+#define SF_MCC_MEX 0
+#define SF_MCC_CEX 1
+int sf_mcc(sf_ctx* ctx, int32_t sid, int32_t model, const sf_sigma* sigma, double dt, int64_t* n_coll);
+
 /* ---- measurement ---------------------------------------------------------- */
 /* The CUDA stream (cudaStream_t) all work of the context is issued on. */
 int sf_ctx_get_stream(sf_ctx* ctx, void** stream);

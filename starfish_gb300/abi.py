@@ -163,3 +163,21 @@ def build_node_segments(ni, nj, x0, dh, seg_xy):
     check(L.sf_build_node_segments(ni, nj, ptr(x0), ptr(dh), nseg, ptr(seg_xy), ptr(p), ptr(idx),
                                    C.byref(nnz)))
     return p, idx[:nnz.value]
+
+
+class Sigma(C.Structure):
+    _fields_ = [("model", C.c_int32), ("c", C.c_double * 4), ("diam", C.c_double),
+                ("T_ref", C.c_double), ("omega", C.c_double), ("vss_alpha", C.c_double)]
+
+
+SIGMA_CONST, SIGMA_INV, SIGMA_POLY, SIGMA_LN, SIGMA_BIRD463 = 0, 1, 2, 3, 4
+MCC_MEX, MCC_CEX = 0, 1
+EXPORTS.update({
+    "sf_dsmc": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Sigma), C.c_double, C.c_double,
+                          C.POINTER(C.c_int64)]),
+    "sf_dsmc_get_counts": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "sf_mcc_set_target": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p]),
+    "sf_mcc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(Sigma), C.c_double,
+                         C.POINTER(C.c_int64)]),
+})

@@ -1,0 +1,395 @@
+// sf_collide.cu -- DSMC (Bird NTC) and MCC collisions on cell-sorted particles.
+//
+// DSMC.perform(mesh) (collisions/DSMC.java:194-256) bins particles by cell every call;
+// here that binning is the species' counting sort, whose per-key offsets give each cell
+// a contiguous run of particles.  collideCell (:259-350) then runs per cell with the
+// reference's NTC count, remainder and (sigma g)max update; pair picks and acceptance use
+// counter-based Philox streams keyed by (cell, step), so results match the reference in
+// distribution (its global java.util.Random stream cannot be reproduced in parallel).
+// Velocities are FP32 as stored; the selection count and cell state are FP64.
+#include <cmath>
+
+#include "sf_internal.h"
+
+using namespace sf;
+
+namespace {
+
+struct SigmaDev {
+  int model;
+  float c[4];
+  float sigma0;    // BIRD463: pi d^2 for two equal diameters, 0.25 pi (d1+d2)^2
+  float kT2_mr;    // BIRD463: 2 k T_ref / m_r
+  float expo;      // omega - 1/2
+  float inv_gamma; // 1 / Gamma(5/2 - omega) (Bird's gamma, Utils.gamma)
+  float vss_inv;   // 0.5 (1/alpha1 + 1/alpha2)
+};
+
+// Sigma.eval (interactions/Sigma.java:121-195, SigmaPlus.java:54-76)
+__device__ inline float sigma_eval(const SigmaDev& s, float g) {
+  switch (s.model) {
+    case SF_SIGMA_CONST: return s.c[0];
+    case SF_SIGMA_INV: return g > 0.f ? s.c[0] / g : 0.f;
+    case SF_SIGMA_POLY: {
+      float v = s.c[0], gg = g;
+      for (int i = 1; i < 4; i++) {
+        v += s.c[i] * gg;
+        gg *= gg;
+      }
+      return v;
+    }
+    case SF_SIGMA_LN: {
+      if (!(g > 0.f)) return 0.f;
+      const float v = s.c[0] + s.c[1] * logf(g);
+      return v * v;
+    }
+    default:  // BIRD463
+      if (!(g > 0.f)) return 0.f;
+      return s.sigma0 * __powf(s.kT2_mr / (g * g), s.expo) * s.inv_gamma;
+  }
+}
+
+// ModelElastic post-collision relative velocity (DSMC.java:389-427), equal masses
+__device__ inline void elastic_vr(Philox& rng, float vss_inv, const float g[3], float g_mag, float vr[3]) {
+  if (fabsf(vss_inv - 1.f) < 1e-4f) {
+    const float B = 2.f * (float)rng.uniform() - 1.f;
+    const float A = sqrtf(fmaxf(1.f - B * B, 0.f));
+    vr[0] = B * g_mag;
+    const float C = 2.f * (float)PI * (float)rng.uniform();
+    float sC, cC;
+    __sincosf(C, &sC, &cC);
+    vr[1] = A * cC * g_mag;
+    vr[2] = A * sC * g_mag;
+  } else {
+    const float B = 2.f * __powf((float)rng.uniform(), vss_inv) - 1.f;
+    const float A = sqrtf(fmaxf(1.f - B * B, 0.f));
+    const float C = 2.f * (float)PI * (float)rng.uniform();
+    float SC, OC;
+    __sincosf(C, &SC, &OC);
+    const float D = sqrtf(g[1] * g[1] + g[2] * g[2]);
+    if (D > 1e-6f) {
+      vr[0] = B * g[0] + A * SC * D;
+      vr[1] = B * g[1] + A * (g_mag * g[2] * OC - g[0] * g[1] * SC) / D;
+      vr[2] = B * g[2] - A * (g_mag * g[1] * OC + g[0] * g[2] * SC) / D;
+    } else {
+      vr[0] = B * g[1];
+      vr[1] = A * OC * g[1];
+      vr[2] = A * SC * g[1];
+    }
+  }
+}
+
+// One thread per cell, the cell's pairs in sequence as in collideCell.
+__global__ void k_dsmc(MeshView m, ParticlesView P, const int* __restrict__ bins, int ntx, int nkeys,
+                       const double* __restrict__ cell_vol, double2* __restrict__ state, double2* __restrict__ counts,
+                       SigmaDev sg, double spwt, double dt, uint64_t seed, uint32_t step,
+                       unsigned long long* __restrict__ n_coll) {
+  for (int key = blockIdx.x * blockDim.x + threadIdx.x; key < nkeys; key += gridDim.x * blockDim.x) {
+    int i, j;
+    key_cell((uint32_t)key, ntx, i, j);
+    if (i >= m.ni - 1 || j >= m.nj - 1) continue;
+    const int c = j * (m.ni - 1) + i;
+    const int start = bins[key], np = bins[key + 1] - start;
+    double2 st = state[c];  // x: (sigma g)max, y: remainder
+    const double npd = (double)np;
+    // equal weights: Pab = Pba = 1, denominator Pab + (w2/w1) Pba = 2 (DSMC.java:276-286)
+    const double nsel_f = ((npd * spwt / cell_vol[c]) * npd * dt * st.x) / 2.0 + st.y;
+    int nsel = (int)nsel_f;
+    if (np < 2) continue;  // the reference returns before updating rem (:293-296)
+    st.y = nsel_f - nsel;
+    if ((double)nsel > npd * npd) {
+      nsel = (int)(npd * npd);
+      st.y = 0.0;
+    }
+    Philox rng(seed, RNG_DSMC, (uint64_t)c, step);
+    float smax_new = 0.f;
+    const float smax = (float)st.x;
+    int ncol = 0;
+    for (int k = 0; k < nsel; k++) {
+      const int p1 = min((int)(rng.uniform() * npd), np - 1);
+      int p2 = p1;
+      for (int tries = 0; tries < 64 && p2 == p1; tries++) p2 = min((int)(rng.uniform() * npd), np - 1);
+      if (p2 == p1) continue;
+      const int64_t a = start + p1, b = start + p2;
+      float2 va = P.vxy[a], vb = P.vxy[b];
+      float wa = P.vz[a], wb = P.vz[b];
+      const float g[3] = {va.x - vb.x, va.y - vb.y, wa - wb};
+      const float g_mag = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+      const float sigma_cr = g_mag * sigma_eval(sg, g_mag);
+      smax_new = fmaxf(smax_new, sigma_cr);
+      if ((float)rng.uniform() < sigma_cr / smax) {
+        // ModelElastic.perform with equal masses and weights (DSMC.java:373-415)
+        const float vc[3] = {0.5f * (va.x + vb.x), 0.5f * (va.y + vb.y), 0.5f * (wa + wb)};
+        float vr[3];
+        elastic_vr(rng, sg.vss_inv, g, g_mag, vr);
+        P.vxy[a] = make_float2(vc[0] + 0.5f * vr[0], vc[1] + 0.5f * vr[1]);
+        P.vz[a] = vc[2] + 0.5f * vr[2];
+        P.vxy[b] = make_float2(vc[0] - 0.5f * vr[0], vc[1] - 0.5f * vr[1]);
+        P.vz[b] = vc[2] - 0.5f * vr[2];
+        ncol++;
+      }
+    }
+    if (smax_new > 0.f) st.x = (double)smax_new;
+    state[c] = st;
+    if (ncol) {
+      double2 cs = counts[c];
+      cs.x += ncol;
+      cs.y += ncol * spwt;  // 0.5 (w1 + w2) per collision
+      counts[c] = cs;
+      atomicAdd(n_coll, (unsigned long long)ncol);
+    }
+  }
+}
+
+struct TargetView {
+  const float* den;
+  const float* u;
+  const float* v;
+  const float* w;
+  const float* T;
+  float mass;
+};
+
+__device__ inline float gather_node(const float* f, int ni, int i, int j, float fx, float fy) {
+  const int u = j * ni + i;
+  return (1.f - fx) * (1.f - fy) * f[u] + fx * (1.f - fy) * f[u + 1] + fx * fy * f[u + ni + 1] +
+         (1.f - fx) * fy * f[u + ni];
+}
+
+// MCC.perform(mesh) per particle (collisions/MCC.java:167-221)
+__global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, int model, float src_mass, float dt,
+                      uint64_t seed, uint32_t step, unsigned long long* __restrict__ n_coll) {
+  const float KBf = 1.3806503e-23f;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < P.n; p += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = P.cell[p];
+    if (c == DEAD) continue;
+    const int i = cell_i(c), j = cell_j(c);
+    const float2 f = P.frac[p];
+    const float den = gather_node(tg.den, m.ni, i, j, f.x, f.y);
+    if (den <= 0.f) continue;
+    const float tu = tg.u ? gather_node(tg.u, m.ni, i, j, f.x, f.y) : 0.f;
+    const float tv = tg.v ? gather_node(tg.v, m.ni, i, j, f.x, f.y) : 0.f;
+    const float tw = tg.w ? gather_node(tg.w, m.ni, i, j, f.x, f.y) : 0.f;
+    float2 vxy = P.vxy[p];
+    float vz = P.vz[p];
+    const float gx = tu - vxy.x, gy = tv - vxy.y, gz = tw - vz;
+    const float g = sqrtf(gx * gx + gy * gy + gz * gz);
+    const float Pc = 1.f - __expf(-sigma_eval(sg, g) * g * dt * den);
+    Philox rng(seed, RNG_MCC, (uint64_t)p, step);
+    if (Pc < (float)rng.uniform()) continue;
+    // Material.sampleMaxwellianVelocity (Material.java:880-896): mean + SampleMaxw3D(v_th)
+    float T = gather_node(tg.T, m.ni, i, j, f.x, f.y);
+    if (T < 0.f) T = 0.f;
+    const float vth = sqrtf(2.f * KBf * T / tg.mass);
+    float vt[3] = {tu, tv, tw};
+    for (int d = 0; d < 3; d++) {
+      float s = 0.f;
+      for (int k = 0; k < 12; k++) s += (float)rng.uniform();
+      vt[d] += (vth * 1.2f) * 0.70710678f * (s - 6.f);
+    }
+    if (model == SF_MCC_CEX) {
+      vxy = make_float2(vt[0], vt[1]);
+      vz = vt[2];
+    } else {
+      // ModelMEX (MCC.java:242-285): isotropic scattering in the centre-of-mass frame
+      const float rm1 = src_mass / (src_mass + tg.mass), rm2 = tg.mass / (src_mass + tg.mass);
+      const float gg[3] = {vxy.x - vt[0], vxy.y - vt[1], vz - vt[2]};
+      const float g_mag = sqrtf(gg[0] * gg[0] + gg[1] * gg[1] + gg[2] * gg[2]);
+      const float vc[3] = {rm1 * vxy.x + rm2 * vt[0], rm1 * vxy.y + rm2 * vt[1], rm1 * vz + rm2 * vt[2]};
+      const float B = 2.f * (float)rng.uniform() - 1.f;
+      const float A = sqrtf(fmaxf(1.f - B * B, 0.f));
+      const float C = 2.f * (float)PI * (float)rng.uniform();
+      float sC, cC;
+      __sincosf(C, &sC, &cC);
+      const float vr[3] = {B * g_mag, A * cC * g_mag, A * sC * g_mag};
+      vxy = make_float2(vc[0] + vr[0] * rm2, vc[1] + vr[1] * rm2);
+      vz = vc[2] + vr[2] * rm2;
+    }
+    P.vxy[p] = vxy;
+    P.vz[p] = vz;
+    atomicAdd(n_coll, 1ULL);
+  }
+}
+
+// Utils.gamma, Bird's approximation (core/common/Utils.java:218-236)
+double bird_gamma(double X) {
+  double A = 1., Y = X;
+  if (Y < 1.0) {
+    A = A / Y;
+  } else {
+    do {
+      Y = Y - 1;
+      if (Y >= 1.) A = A * Y;
+    } while (Y >= 1.);
+  }
+  return A * (1. - 0.5748646 * Y + 0.9512363 * Y * Y - 0.6998588 * Y * Y * Y + 0.4245549 * Y * Y * Y * Y -
+              0.1010678 * Y * Y * Y * Y * Y);
+}
+
+SigmaDev make_sigma(const sf_sigma* s, double m1, double m2) {
+  SF_REQUIRE(s, SF_ERR_ARG, "null sigma");
+  SF_REQUIRE(s->model >= SF_SIGMA_CONST && s->model <= SF_SIGMA_BIRD463, SF_ERR_ARG, "bad sigma model");
+  SigmaDev d{};
+  d.model = s->model;
+  for (int k = 0; k < 4; k++) d.c[k] = (float)s->c[k];
+  if (s->model == SF_SIGMA_BIRD463) {
+    SF_REQUIRE(s->diam > 0 && s->T_ref > 0, SF_ERR_ARG, "Bird 4.63 needs diam and T_ref");
+    // SigmaBird463.init (SigmaPlus.java:54-66) with mat1 == mat2
+    const double d_ref = s->diam + s->diam;
+    const double mr = m1 * m2 / (m1 + m2);
+    d.sigma0 = (float)(0.25 * PI * d_ref * d_ref);
+    d.kT2_mr = (float)(2.0 * KB * s->T_ref / mr);
+    d.expo = (float)(s->omega - 0.5);
+    d.inv_gamma = (float)(1.0 / bird_gamma(2.5 - s->omega));
+  }
+  const double a = s->vss_alpha > 0 ? s->vss_alpha : 1.0;
+  d.vss_inv = (float)(0.5 * (1.0 / a + 1.0 / a));
+  return d;
+}
+
+}  // namespace
+
+struct SfDsmcState {
+  double2* state = nullptr;   // per cell (sigma g)max, remainder
+  double2* counts = nullptr;  // per cell collision count, weight
+  double* cell_vol = nullptr;
+  bool init = false;
+};
+
+// per-context, per-species DSMC state; freed with the context through the destroy hook
+static SfDsmcState* dsmc_state(sf_ctx* ctx, int sid, double sig_cr_max0) {
+  if ((int)ctx->dsmc.size() <= sid) ctx->dsmc.resize(sid + 1, nullptr);
+  SfDsmcState*& st = ctx->dsmc[sid];
+  if (st) return st;
+  st = new SfDsmcState();
+  const int nc = ctx->ncells();
+  SF_CUDA(cudaMalloc(&st->state, sizeof(double2) * nc));
+  SF_CUDA(cudaMalloc(&st->counts, sizeof(double2) * nc));
+  SF_CUDA(cudaMalloc(&st->cell_vol, sizeof(double) * nc));
+  std::vector<double2> s0(nc, make_double2(sig_cr_max0, 0.0));
+  SF_CUDA(cudaMemcpy(st->state, s0.data(), sizeof(double2) * nc, cudaMemcpyHostToDevice));
+  SF_CUDA(cudaMemset(st->counts, 0, sizeof(double2) * nc));
+  // Mesh.cellVol = nodeVol(i + 1/2, j + 1/2) (core/domain/Mesh.java:1038-1040)
+  std::vector<double> cv(nc);
+  for (int j = 0; j < ctx->nj - 1; j++)
+    for (int i = 0; i < ctx->ni - 1; i++) {
+      const double area = ctx->dh[0] * ctx->dh[1];
+      double v = area;
+      if (ctx->domain == SF_DOMAIN_RZ) v = 2 * PI * area * (ctx->x0[0] + (i + 0.5) * ctx->dh[0]);
+      if (ctx->domain == SF_DOMAIN_ZR) v = 2 * PI * area * (ctx->x0[1] + (j + 0.5) * ctx->dh[1]);
+      cv[(size_t)j * (ctx->ni - 1) + i] = v;
+    }
+  SF_CUDA(cudaMemcpy(st->cell_vol, cv.data(), sizeof(double) * nc, cudaMemcpyHostToDevice));
+  st->init = true;
+  return st;
+}
+
+void sf_collide_destroy_internal(sf_ctx* ctx) {
+  for (SfDsmcState* st : ctx->dsmc) {
+    if (!st) continue;
+    cudaFree(st->state);
+    cudaFree(st->counts);
+    cudaFree(st->cell_vol);
+    delete st;
+  }
+  ctx->dsmc.clear();
+  if (ctx->mcc_target) {
+    cudaFree(ctx->mcc_target);
+    ctx->mcc_target = nullptr;
+  }
+}
+
+extern "C" {
+
+int sf_dsmc(sf_ctx* ctx, int32_t sid, const sf_sigma* sigma, double dt, double sig_cr_max0, int64_t* n_coll) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(dt > 0 && sig_cr_max0 > 0, SF_ERR_ARG, "dt and sig_cr_max must be positive");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const SigmaDev sg = make_sigma(sigma, sp->mass, sp->mass);
+  SfDsmcState* st = dsmc_state(ctx, sid, sig_cr_max0);
+  // DSMC.perform(mesh) bins particles by cell on every call: the counting sort
+  launch_sort(ctx, sp);
+  SF_CUDA(cudaMemsetAsync(ctx->counters + 6, 0, sizeof(unsigned long long), ctx->stream));
+  {
+    TimedScope ts(ctx, "dsmc");
+    k_dsmc<<<grid_for(ctx->nkeys, 128, ctx->num_sms * 16), 128, 0, ctx->stream>>>(
+        ctx->mesh_view(), sp->cur, ctx->bins, ctx->ntx, ctx->nkeys, st->cell_vol, st->state, st->counts, sg,
+        sp->spwt, dt, ctx->seed ^ 0xD5C0ULL, ctx->rng_epoch++, ctx->counters + 6);
+    ctx->launches++;
+  }
+  SF_CUDA(cudaGetLastError());
+  unsigned long long nc = 0;
+  SF_CUDA(cudaMemcpyAsync(&nc, ctx->counters + 6, sizeof(nc), cudaMemcpyDeviceToHost, ctx->stream));
+  SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  timer_collect(ctx);
+  if (n_coll) *n_coll = (int64_t)nc;
+  SF_API_END(ctx)
+}
+
+int sf_dsmc_get_counts(sf_ctx* ctx, int32_t sid, double* count_sum, double* real_sum) {
+  SF_API_BEGIN
+  get_species(ctx, sid);
+  SF_REQUIRE(sid < (int)ctx->dsmc.size() && ctx->dsmc[sid], SF_ERR_STATE, "no DSMC performed for this species");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const int nc = ctx->ncells();
+  std::vector<double2> h(nc);
+  SF_CUDA(cudaMemcpy(h.data(), ctx->dsmc[sid]->counts, sizeof(double2) * nc, cudaMemcpyDeviceToHost));
+  for (int c = 0; c < nc; c++) {
+    if (count_sum) count_sum[c] = h[c].x;
+    if (real_sum) real_sum[c] = h[c].y;
+  }
+  SF_API_END(ctx)
+}
+
+int sf_mcc_set_target(sf_ctx* ctx, double mass, const double* den, const double* u, const double* v, const double* w,
+                      const double* temp) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx && den && temp && mass > 0, SF_ERR_ARG, "target needs mass, density and temperature");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  if (!ctx->mcc_target) SF_CUDA(cudaMalloc(&ctx->mcc_target, sizeof(float) * 5 * nn));
+  std::vector<float> h(5 * nn, 0.f);
+  const double* src[5] = {den, u, v, w, temp};
+  for (int k = 0; k < 5; k++)
+    if (src[k])
+      for (size_t q = 0; q < nn; q++) h[k * nn + q] = (float)src[k][q];
+  SF_CUDA(cudaMemcpy(ctx->mcc_target, h.data(), sizeof(float) * 5 * nn, cudaMemcpyHostToDevice));
+  ctx->mcc_mass = mass;
+  SF_API_END(ctx)
+}
+
+int sf_mcc(sf_ctx* ctx, int32_t sid, int32_t model, const sf_sigma* sigma, double dt, int64_t* n_coll) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(ctx->mcc_target, SF_ERR_STATE, "no MCC target (sf_mcc_set_target)");
+  SF_REQUIRE(model == SF_MCC_MEX || model == SF_MCC_CEX, SF_ERR_ARG, "bad MCC model");
+  SF_REQUIRE(dt > 0, SF_ERR_ARG, "dt must be positive");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const SigmaDev sg = make_sigma(sigma, sp->mass, ctx->mcc_mass);
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  TargetView tg;
+  tg.den = ctx->mcc_target;
+  tg.u = ctx->mcc_target + nn;
+  tg.v = ctx->mcc_target + 2 * nn;
+  tg.w = ctx->mcc_target + 3 * nn;
+  tg.T = ctx->mcc_target + 4 * nn;
+  tg.mass = (float)ctx->mcc_mass;
+  SF_CUDA(cudaMemsetAsync(ctx->counters + 6, 0, sizeof(unsigned long long), ctx->stream));
+  if (sp->n > 0) {
+    TimedScope ts(ctx, "mcc");
+    k_mcc<<<grid_for(sp->n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
+        ctx->mesh_view(), sp->cur, tg, sg, model, (float)sp->mass, (float)dt, ctx->seed ^ 0x3CC0ULL, ctx->rng_epoch++,
+        ctx->counters + 6);
+    ctx->launches++;
+  }
+  SF_CUDA(cudaGetLastError());
+  unsigned long long nc = 0;
+  SF_CUDA(cudaMemcpyAsync(&nc, ctx->counters + 6, sizeof(nc), cudaMemcpyDeviceToHost, ctx->stream));
+  SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  timer_collect(ctx);
+  if (n_coll) *n_coll = (int64_t)nc;
+  SF_API_END(ctx)
+}
+
+}  // extern "C"

@@ -631,6 +631,7 @@ int sf_ctx_destroy(sf_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   sf_poisson_destroy_internal(ctx);
+  sf_collide_destroy_internal(ctx);
   for (SfSpecies* sp : ctx->species) {
     void* ptrs[] = {sp->cur.cell, sp->cur.frac, sp->cur.vxy, sp->cur.vz, sp->alt.cell, sp->alt.frac,
                     sp->alt.vxy, sp->alt.vz, sp->count, sp->mom, sp->nd, sp->uvw, sp->seg_model,

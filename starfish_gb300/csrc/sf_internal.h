@@ -179,7 +179,8 @@ struct SfSpecies {
   int pushes_since_sort = 1 << 30;
 };
 
-struct SfPoisson;  // sf_poisson.cu
+struct SfPoisson;    // sf_poisson.cu
+struct SfDsmcState;  // sf_collide.cu
 
 // CUDA-event timing of named kernels on the context stream
 struct SfTimer {
@@ -233,7 +234,11 @@ struct sf_ctx {
   double* dscratch = nullptr;              // ni*nj FP64 scratch (field transfers)
   std::vector<SfSpecies*> species;
   SfPoisson* poisson = nullptr;
+  std::vector<SfDsmcState*> dsmc;  // per species DSMC cell state
+  float* mcc_target = nullptr;     // MCC target density, u, v, w, T (5 * ni*nj)
+  double mcc_mass = 0;
   uint64_t seed = 0x5eed5eedULL;
+  uint32_t rng_epoch = 0;  // advanced by every stochastic call (sources, DSMC, MCC)
   int64_t launches = 0;   // kernels launched
   SfTimer timer;
 
@@ -243,6 +248,7 @@ struct sf_ctx {
 
 // helpers shared between translation units
 void sf_poisson_destroy_internal(sf_ctx* ctx);                       // sf_poisson.cu
+void sf_collide_destroy_internal(sf_ctx* ctx);                       // sf_collide.cu
 int sf_poisson_get_field_internal(sf_ctx* ctx, int field, double* out);  // sf_poisson.cu
 namespace sf {
 void launch_sort(sf_ctx* ctx, SfSpecies* sp);

@@ -102,7 +102,7 @@ extern "C" int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg,
   a.dt = dt;
   a.qm_halfdt = (float)(sp->charge / sp->mass * 0.5 * dt);
   a.seed = ctx->seed ^ (0x9E3779B97F4A7C15ULL * (uint64_t)(sid + 1));
-  a.step = sp->step;
+  a.step = ctx->rng_epoch++;
   a.base = sp->n;
   unsigned long long* cnt = ctx->counters + 7;
   SF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), ctx->stream));

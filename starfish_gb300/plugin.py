@@ -222,3 +222,53 @@ class PoissonSolver:
         ne = np.zeros(self.d.ni * self.d.nj)
         self.d.check(self.d.lib.sf_boltzmann(self.d.ctx, abi.ptr(ne)))
         return ne
+
+
+def _sigma(model, c=(0, 0, 0, 0), diam=0.0, T_ref=273.0, omega=0.5, vss_alpha=1.0):
+    s = abi.Sigma()
+    s.model = model
+    for k in range(4):
+        s.c[k] = float(c[k]) if k < len(c) else 0.0
+    s.diam, s.T_ref, s.omega, s.vss_alpha = diam, T_ref, omega, vss_alpha
+    return s
+
+
+class DSMC:
+    """GPU DSMC pair interaction (collisions/DSMC.java) for one kinetic species."""
+
+    def __init__(self, domain: GpuDomain, material: KineticMaterial, model=4, c=(0, 0, 0, 0), diam=0.0,
+                 T_ref=273.0, omega=0.5, vss_alpha=1.0, sig_cr_max=1e-16, frequency=1):
+        self.d, self.km = domain, material
+        self.sigma = _sigma(model, c, diam, T_ref, omega, vss_alpha)
+        self.sig_cr_max0 = sig_cr_max
+        self.frequency = frequency
+
+    def perform(self, dt):
+        n = C.c_int64()
+        self.d.check(self.d.lib.sf_dsmc(self.d.ctx, self.km.sid, C.byref(self.sigma), dt * self.frequency,
+                                        self.sig_cr_max0, C.byref(n)))
+        return n.value
+
+    def counts(self):
+        nc = (self.d.ni - 1) * (self.d.nj - 1)
+        cnt = np.zeros(nc)
+        real = np.zeros(nc)
+        self.d.check(self.d.lib.sf_dsmc_get_counts(self.d.ctx, self.km.sid, abi.ptr(cnt), abi.ptr(real)))
+        return cnt, real
+
+
+class MCC:
+    """GPU Monte Carlo collisions (collisions/MCC.java) of a kinetic species with a target."""
+
+    def __init__(self, domain: GpuDomain, material: KineticMaterial, target_mass, den, temp, u=None, v=None,
+                 w=None, model=0, sigma_model=0, c=(0, 0, 0, 0), diam=0.0, T_ref=273.0, omega=0.5):
+        self.d, self.km, self.model = domain, material, model
+        self.sigma = _sigma(sigma_model, c, diam, T_ref, omega)
+        arr = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (den, u, v, w, temp)]
+        self.d.check(self.d.lib.sf_mcc_set_target(self.d.ctx, target_mass, *[abi.ptr(a) for a in arr]))
+
+    def perform(self, dt):
+        n = C.c_int64()
+        self.d.check(self.d.lib.sf_mcc(self.d.ctx, self.km.sid, self.model, C.byref(self.sigma), dt,
+                                       C.byref(n)))
+        return n.value

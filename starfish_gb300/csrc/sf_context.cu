@@ -881,6 +881,10 @@ int sf_get_field(sf_ctx* ctx, int32_t field, int32_t sid, double* out) {
     if (rc != SF_OK) return rc;
     return SF_OK;
   }
+  if (field == SF_FIELD_NODE_VOL) {
+    std::copy(ctx->node_vol.begin(), ctx->node_vol.end(), out);
+    return SF_OK;
+  }
   SfSpecies* sp = get_species(ctx, sid);
   switch (field) {
     case SF_FIELD_ND:

@@ -83,7 +83,12 @@ extern "C" int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg,
   SF_REQUIRE(len > 0, SF_ERR_ARG, "degenerate source segment");
   // MaxwellianSource ctor (MaxwellianSource.java:60-80): mdot from den; Source.regenerate
   const double v_mean = std::sqrt(8 * KB * temp / (PI * sp->mass));
-  const double mdot = den * len * (v_drift + v_mean / 4) * sp->mass;  // XY: area = length x 1 m
+  // LinearSegment.area (core/boundaries/LinearSegment.java:51-76): length x 1 m in XY, the
+  // lateral area of the swept conical frustum pi (r1 + r2) L in RZ / ZR
+  double area = len;
+  if (ctx->domain == SF_DOMAIN_ZR) area = PI * (seg[1] + seg[3]) * len;
+  if (ctx->domain == SF_DOMAIN_RZ) area = PI * (seg[0] + seg[2]) * len;
+  const double mdot = den * area * (v_drift + v_mean / 4) * sp->mass;
   const double mp = (mdot * dt) / (sp->mass * sp->spwt) + *rem;
   const int64_t num = (int64_t)mp;
   *rem = mp - (double)num;

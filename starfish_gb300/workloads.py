@@ -193,3 +193,96 @@ def electrode_efield(mesh: MeshSpec, phi_e=-100.0, width=None):
     efi = -np.gradient(phi, dx, axis=1, edge_order=1)
     efj = -np.gradient(phi, dy, axis=0, edge_order=1)
     return phi.reshape(-1), efi.reshape(-1), efj.reshape(-1)
+
+
+# ---------------------------------------------------------------------------------------
+# axisymmetric DSMC jet (dat/examples/DSMC/jet shape)
+# ---------------------------------------------------------------------------------------
+@dataclass
+class JetConfig:
+    name: str
+    mesh: MeshSpec
+    mass: float
+    spwt: float
+    inlet: np.ndarray          # inlet segment (x1, y1, x2, y2) on the axis end
+    den: float
+    temp: float
+    v_drift: float
+    wall_temp: float
+    diam: float
+    T_ref: float
+    omega: float
+    dt: float
+    steps: int
+    n_particles: int
+
+
+def jet_mesh(ni=513, nj=257, Lz=0.5, Lr=0.25, r_inlet=5e-3) -> MeshSpec:
+    """ZR mesh: z along x (i), r along y (j).  The axis (r = 0) is a symmetry face; the
+    inlet face z = 0 (above the inlet), the outer radius and the far end are diffuse
+    walls given as boundary segments, whose normals point into the gas."""
+    nmax = max(ni, nj)
+    face = np.full((4, nmax), abi.DB_OPEN, np.int8)
+    face[abi.FACE_BOTTOM, :] = abi.DB_SYMMETRY
+    node_type = np.full(ni * nj, abi.NODE_OPEN, np.int8)
+    segs = np.array([
+        [0.0, Lr, 0.0, r_inlet],   # inlet plane above the opening, normal +z
+        [Lz, Lr, 0.0, Lr],         # outer cylinder, normal -r
+        [Lz, 0.0, Lz, Lr],         # far end, normal -z
+    ])
+    return MeshSpec(ni, nj, (0.0, 0.0), (Lz / (ni - 1), Lr / (nj - 1)), abi.DOMAIN_ZR, node_type, face,
+                    np.zeros(ni * nj), segs, np.full(3, abi.BT_DIRICHLET, np.int32))
+
+
+def config2(n_particles=16 * 1024 * 1024) -> JetConfig:
+    """Argon jet: inlet r < 5 mm at 1e22 m^-3, 300 K, 500 m/s; diffuse walls at 300 K; VHS
+    (d = 4.17e-10 m, omega = 0.81, T_ref = 273 K); dt = 1e-6 s."""
+    m = jet_mesh()
+    mass = 40 * AMU
+    # weight: the preloaded plume (jet_particles) holds n_particles macroparticles
+    spwt = _jet_content(m, 1e22, 5e-3) / n_particles
+    return JetConfig("dsmc_jet_513x257_zr", m, mass, spwt, np.array([0.0, 5e-3, 0.0, 0.0]), 1e22, 300.0,
+                     500.0, 300.0, 4.17e-10, 273.0, 0.81, 1e-6, 2000, n_particles)
+
+
+def _jet_density(z, r, n_inlet, r_inlet):
+    """Free-jet plume shape used to preload the domain: n_inlet r_in^2 / (r_in^2 + z^2 + r^2),
+    with a floor of 1e-4 n_inlet."""
+    return n_inlet * np.maximum(r_inlet ** 2 / (r_inlet ** 2 + z ** 2 + r ** 2), 1e-4)
+
+
+def _jet_content(m: MeshSpec, n_inlet, r_inlet, samples=400):
+    Lz, Lr = m.lengths()
+    z = (np.arange(samples) + 0.5) * Lz / samples
+    r = (np.arange(samples) + 0.5) * Lr / samples
+    Z, R = np.meshgrid(z, r)
+    dV = 2 * np.pi * R * (Lz / samples) * (Lr / samples)
+    return float((_jet_density(Z, R, n_inlet, r_inlet) * dV).sum())
+
+
+def jet_particles(cfg: JetConfig, n, seed):
+    """n macroparticles distributed like the plume (acceptance sampling in (z, r) with the
+    axisymmetric volume weight r), drifting Maxwellian velocities at the inlet temperature."""
+    rng = np.random.default_rng(seed)
+    Lz, Lr = cfg.mesh.lengths()
+    r_in = 5e-3
+    out = np.empty((n, 3))
+    got = 0
+    nmax = cfg.den
+    while got < n:
+        k = int((n - got) * 4) + 1024
+        z = rng.uniform(0, Lz, k)
+        r = Lr * np.sqrt(rng.uniform(0, 1, k))   # uniform in area of revolution (weight r)
+        acc = rng.uniform(0, 1, k) < _jet_density(z, r, nmax, r_in) / nmax
+        z, r = z[acc][: n - got], r[acc][: n - got]
+        out[got:got + z.size, 0] = z
+        out[got:got + z.size, 1] = r
+        got += z.size
+    out[:, 2] = 0.0
+    vth = np.sqrt(2 * KB * cfg.temp / cfg.mass)
+    vel = rng.normal(0.0, vth * 1.2 * np.sqrt(0.5), (n, 3))
+    # radial outflow of the plume
+    rr = np.sqrt(out[:, 0] ** 2 + out[:, 1] ** 2) + 1e-12
+    vel[:, 0] += cfg.v_drift * out[:, 0] / rr
+    vel[:, 1] += cfg.v_drift * out[:, 1] / rr
+    return out, vel

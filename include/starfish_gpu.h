@@ -205,6 +205,21 @@ int sf_get_field(sf_ctx* ctx, int32_t field, int32_t sid, double* out);
 #define SF_PUSH_STATS 1
 #define SF_PUSH_MOMENTS 2
 int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_stats* stats);
+/* sf_push_deposit without any device allocation; no counterpart in the reference.
+ * For hosts that must not have the library call cudaMalloc while they step (their own
+ * caching allocator already holds the device memory, or their device footprint is
+ * fixed at start-up): the push's per-call scratch -- slow-path queue, event counters,
+ * partial sums -- lives in a static __device__ array of the library instead of the
+ * context's buffers.  Same arguments, results and errors as sf_push_deposit, plus:
+ *  - the species may hold at most 2^21 (2,097,152) particle slots (live + removed
+ *    since the last sort); a larger species is rejected with SF_ERR_ARG;
+ *  - the first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) and caches it; make that first call before any stream
+ *    capture;
+ *  - every call, from every context on the device, shares the one array: calls whose
+ *    GPU work overlaps (other threads, other contexts' streams) race on it.  Calls
+ *    from one thread are safe, since each call waits for its own work to finish. */
+int sf_push_deposit_noalloc(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_stats* stats);
 /* Surface flux / mass deposit accumulated by the push since the last reset, per
  * segment and split over the segment ends exactly like the Field1D scatter of
  * Material.addSurfaceMomentum / addSurfaceMassDeposit (Material.java:759-796):

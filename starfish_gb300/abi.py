@@ -99,6 +99,8 @@ EXPORTS = {
     "sf_get_field": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
     "sf_push_deposit": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32,
                                   C.POINTER(PushStats)]),
+    "sf_push_deposit_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32,
+                                          C.POINTER(PushStats)]),
     "sf_get_surface_flux": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "sf_reset_surface_flux": (C.c_int, [C.c_void_p, C.c_int32]),
     "sf_ctx_get_stream": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),

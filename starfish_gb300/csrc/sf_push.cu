@@ -18,6 +18,8 @@
 //   k_finalize  int64 fixed-point counts -> FP64 density (and mean velocities).
 // The deposit is an integer sum, so node densities are bit-identical run to run.
 #include <climits>
+#include <mutex>
+#include <string>
 #include <cmath>
 
 #include "sf_internal.h"
@@ -807,22 +809,30 @@ __global__ void k_sum_partials(const double* part, int nblocks, double* out) {
   out[q] = s;
 }
 
-struct KernelCfg {
-  int blocks_per_sm = 0;
+// Per-call scratch of one push: the slow-path queue (one slot per particle), the event
+// counters, the per-block partial sums (stats_blocks x 8 doubles, the last row holds the
+// slow-path sums) and the 8-double output of k_sum_partials.
+struct PushScratch {
+  int* slow_idx;
+  unsigned long long* counters;
+  double* stats_partial;
+  int stats_blocks;
+  double* sums;
 };
 
 template <int DOM, bool STATS, bool MOM>
-void launch_push_t(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid) {
+void launch_push_t(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid, const PushScratch& sc) {
   k_push<DOM, STATS, MOM><<<grid, PB, 0, ctx->stream>>>(ctx->mesh_view(), sp->cur, a, sp->count, sp->mom,
-                                                      ctx->slow_idx, ctx->counters, ctx->stats_partial);
+                                                      sc.slow_idx, sc.counters, sc.stats_partial);
 }
 
 template <int DOM>
-void launch_push_dom(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid, bool stats, bool mom) {
-  if (stats && mom) launch_push_t<DOM, true, true>(ctx, sp, a, grid);
-  else if (stats) launch_push_t<DOM, true, false>(ctx, sp, a, grid);
-  else if (mom) launch_push_t<DOM, false, true>(ctx, sp, a, grid);
-  else launch_push_t<DOM, false, false>(ctx, sp, a, grid);
+void launch_push_dom(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid, bool stats, bool mom,
+                     const PushScratch& sc) {
+  if (stats && mom) launch_push_t<DOM, true, true>(ctx, sp, a, grid, sc);
+  else if (stats) launch_push_t<DOM, true, false>(ctx, sp, a, grid, sc);
+  else if (mom) launch_push_t<DOM, false, true>(ctx, sp, a, grid, sc);
+  else launch_push_t<DOM, false, false>(ctx, sp, a, grid, sc);
 }
 
 }  // namespace
@@ -838,12 +848,12 @@ void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments) {
 
 }  // namespace sf
 
-extern "C" int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_stats* stats) {
-  SF_API_BEGIN
-  SfSpecies* sp = get_species(ctx, sid);
-  SF_REQUIRE(dt > 0, SF_ERR_ARG, "dt must be positive");
-  SF_REQUIRE(ctx->efield_set, SF_ERR_STATE, "electric field not set (sf_set_efield or a Poisson solve)");
-  SF_CUDA(cudaSetDevice(ctx->device));
+namespace {
+
+// Body of sf_push_deposit and sf_push_deposit_noalloc: they differ only in where the
+// per-call scratch lives.  Allocates nothing.
+void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_push_stats* stats,
+                       const PushScratch& sc) {
   const bool want_stats = (flags & SF_PUSH_STATS) != 0;
   const bool mom = (flags & SF_PUSH_MOMENTS) != 0;
   // automatic cell sort every sort_interval pushes (the counter starts at the interval,
@@ -853,10 +863,10 @@ extern "C" int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flag
   cudaStream_t s = ctx->stream;
   SF_CUDA(cudaMemsetAsync(sp->count, 0, sizeof(unsigned long long) * nn, s));
   if (mom) SF_CUDA(cudaMemsetAsync(sp->mom, 0, sizeof(long long) * 3 * nn, s));
-  SF_CUDA(cudaMemsetAsync(ctx->counters, 0, sizeof(unsigned long long) * 8, s));
+  SF_CUDA(cudaMemsetAsync(sc.counters, 0, sizeof(unsigned long long) * 8, s));
   // stats_partial tail (after the per-block area) holds the slow-path sums
-  double* slow_stats = ctx->stats_partial + (size_t)8 * (ctx->stats_blocks - 1);
-  SF_CUDA(cudaMemsetAsync(ctx->stats_partial, 0, sizeof(double) * 8 * (size_t)ctx->stats_blocks, s));
+  double* slow_stats = sc.stats_partial + (size_t)8 * (sc.stats_blocks - 1);
+  SF_CUDA(cudaMemsetAsync(sc.stats_partial, 0, sizeof(double) * 8 * (size_t)sc.stats_blocks, s));
 
   PushArgs a;
   a.qm_dt = (float)(sp->charge / sp->mass * dt);
@@ -875,15 +885,15 @@ extern "C" int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flag
   a.step = sp->step;
 
   int tiles = (int)((sp->n + TILE - 1) / TILE);
-  int grid = std::max(1, std::min(tiles, ctx->stats_blocks - 1));
+  int grid = std::max(1, std::min(tiles, sc.stats_blocks - 1));
   if (sp->n > 0) {
     {
     TimedScope ts(ctx, "push");
     ctx->launches++;
     switch (ctx->domain) {
-      case SF_DOMAIN_XY: launch_push_dom<SF_DOMAIN_XY>(ctx, sp, a, grid, want_stats, mom); break;
-      case SF_DOMAIN_RZ: launch_push_dom<SF_DOMAIN_RZ>(ctx, sp, a, grid, want_stats, mom); break;
-      default: launch_push_dom<SF_DOMAIN_ZR>(ctx, sp, a, grid, want_stats, mom); break;
+      case SF_DOMAIN_XY: launch_push_dom<SF_DOMAIN_XY>(ctx, sp, a, grid, want_stats, mom, sc); break;
+      case SF_DOMAIN_RZ: launch_push_dom<SF_DOMAIN_RZ>(ctx, sp, a, grid, want_stats, mom, sc); break;
+      default: launch_push_dom<SF_DOMAIN_ZR>(ctx, sp, a, grid, want_stats, mom, sc); break;
     }
     }
     SF_CUDA(cudaGetLastError());
@@ -892,20 +902,20 @@ extern "C" int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flag
     sa.sv.param = sp->seg_param;
     sa.sv.flux = sp->flux;
     sa.sv.deposit = sp->deposit;
-    sa.counters = ctx->counters;
+    sa.counters = sc.counters;
     sa.stats_slow = slow_stats;
     const int sgrid = ctx->num_sms * 16;
     TimedScope ts(ctx, "push_slow");
     ctx->launches++;
     switch (ctx->domain) {
       case SF_DOMAIN_XY:
-        k_push_slow<SF_DOMAIN_XY><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, ctx->slow_idx, sp->count, sp->mom, mom);
+        k_push_slow<SF_DOMAIN_XY><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom);
         break;
       case SF_DOMAIN_RZ:
-        k_push_slow<SF_DOMAIN_RZ><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, ctx->slow_idx, sp->count, sp->mom, mom);
+        k_push_slow<SF_DOMAIN_RZ><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom);
         break;
       default:
-        k_push_slow<SF_DOMAIN_ZR><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, ctx->slow_idx, sp->count, sp->mom, mom);
+        k_push_slow<SF_DOMAIN_ZR><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom);
         break;
     }
     SF_CUDA(cudaGetLastError());
@@ -917,11 +927,11 @@ extern "C" int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flag
   SF_CUDA(cudaGetLastError());
   double* h = ctx->host_pinned;
   unsigned long long hc[4];
-  SF_CUDA(cudaMemcpyAsync(hc, ctx->counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  SF_CUDA(cudaMemcpyAsync(hc, sc.counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
   if (want_stats) {
-    k_sum_partials<<<1, 32, 0, s>>>(ctx->stats_partial, grid, ctx->dscratch);
+    k_sum_partials<<<1, 32, 0, s>>>(sc.stats_partial, grid, sc.sums);
     ctx->launches++;
-    SF_CUDA(cudaMemcpyAsync(h, ctx->dscratch, sizeof(double) * 5, cudaMemcpyDeviceToHost, s));
+    SF_CUDA(cudaMemcpyAsync(h, sc.sums, sizeof(double) * 5, cudaMemcpyDeviceToHost, s));
     SF_CUDA(cudaMemcpyAsync(h + 8, slow_stats, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));
   }
   SF_CUDA(cudaStreamSynchronize(s));
@@ -944,6 +954,82 @@ extern "C" int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flag
     stats->n_slow = (int64_t)hc[0];
     stats->n_bounce_limited = (int64_t)hc[2];
   }
+}
+
+// ---------------------------------------------------------------------------------
+// Push scratch that needs no allocation.
+//
+// Some hosts cannot let the library call cudaMalloc while they step the particles: a
+// host whose own caching allocator (PyTorch's, a JVM-side pool) has already reserved
+// the device memory, where a stray cudaMalloc can fail or force that allocator to give
+// its cache back, and services that fix their device footprint at start-up and treat
+// any later allocation as a fault.  For them, the per-call scratch of the push lives in
+// a file-scope __device__ array that is part of the loaded module, so it exists as soon
+// as the library is on the device.
+// ---------------------------------------------------------------------------------
+constexpr int64_t NOALLOC_MAX_PARTICLES = int64_t(1) << 21;  // slow-queue slots (8 MiB)
+constexpr int NOALLOC_MAX_STATS_BLOCKS = 4096;                // partial-sum rows (256 KiB)
+constexpr size_t NOALLOC_OFF_COUNTERS = 0;
+constexpr size_t NOALLOC_OFF_SUMS = 256;
+constexpr size_t NOALLOC_OFF_PARTIAL = 512;
+constexpr size_t NOALLOC_OFF_SLOW = NOALLOC_OFF_PARTIAL + sizeof(double) * 8 * NOALLOC_MAX_STATS_BLOCKS;
+constexpr size_t NOALLOC_BYTES = NOALLOC_OFF_SLOW + sizeof(int) * NOALLOC_MAX_PARTICLES;
+static_assert(NOALLOC_OFF_SLOW % 256 == 0, "scratch regions stay 256-byte aligned");
+
+static __device__ __align__(256) unsigned char g_push_scratch[NOALLOC_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_base[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_push_scratch on ctx->device, looked up once per device (the
+// device must be current).
+unsigned char* noalloc_scratch(sf_ctx* ctx) {
+  SF_REQUIRE(ctx->device >= 0 && ctx->device < NOALLOC_MAX_DEVICES, SF_ERR_ARG, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  unsigned char*& base = g_noalloc_base[ctx->device];
+  if (!base) {
+    void* p = nullptr;
+    const cudaError_t rc = cudaGetSymbolAddress(&p, g_push_scratch);
+    if (rc != cudaSuccess || !p)
+      throw Error(SF_ERR_CUDA, std::string("cudaGetSymbolAddress(push scratch) failed: ") + cudaGetErrorString(rc));
+    base = static_cast<unsigned char*>(p);
+  }
+  return base;
+}
+
+}  // namespace
+
+extern "C" int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_stats* stats) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(dt > 0, SF_ERR_ARG, "dt must be positive");
+  SF_REQUIRE(ctx->efield_set, SF_ERR_STATE, "electric field not set (sf_set_efield or a Poisson solve)");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const PushScratch sc{ctx->slow_idx, ctx->counters, ctx->stats_partial, ctx->stats_blocks, ctx->dscratch};
+  push_deposit_impl(ctx, sp, dt, flags, stats, sc);
+  SF_API_END(ctx)
+}
+
+extern "C" int sf_push_deposit_noalloc(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_stats* stats) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(dt > 0, SF_ERR_ARG, "dt must be positive");
+  SF_REQUIRE(ctx->efield_set, SF_ERR_STATE, "electric field not set (sf_set_efield or a Poisson solve)");
+  SF_REQUIRE(sp->n <= NOALLOC_MAX_PARTICLES, SF_ERR_ARG,
+             "sf_push_deposit_noalloc: species holds " + std::to_string(sp->n) + " particle slots, more than its " +
+                 std::to_string(NOALLOC_MAX_PARTICLES) + "-particle static scratch; use sf_push_deposit");
+  SF_REQUIRE(ctx->stats_blocks <= NOALLOC_MAX_STATS_BLOCKS, SF_ERR_ARG,
+             "sf_push_deposit_noalloc: device has too many SMs for the static partial-sum scratch");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  unsigned char* base = noalloc_scratch(ctx);
+  // counters and partial sums are cleared by push_deposit_impl on every call; the slow
+  // queue is written before it is read, so it may keep the previous call's contents
+  const PushScratch sc{reinterpret_cast<int*>(base + NOALLOC_OFF_SLOW),
+                       reinterpret_cast<unsigned long long*>(base + NOALLOC_OFF_COUNTERS),
+                       reinterpret_cast<double*>(base + NOALLOC_OFF_PARTIAL), ctx->stats_blocks,
+                       reinterpret_cast<double*>(base + NOALLOC_OFF_SUMS)};
+  push_deposit_impl(ctx, sp, dt, flags, stats, sc);
   SF_API_END(ctx)
 }
 

@@ -276,6 +276,29 @@ int sf_efield(sf_ctx* ctx, double* efi, double* efj);
  * n_e = max(1, n0 exp((phi - phi0)/kTe)) into ne (ni*nj, may be NULL: device only). */
 int sf_boltzmann(sf_ctx* ctx, double* ne);
 
+/* ---- learned warm start of the Poisson solve (no reference counterpart) -------- */
+/* A 4-level U-Net (base_channels 16 or 32, doubling per level; BF16 weights and
+ * activations, FP32 accumulation) on the mesh coarsened by `down` (1..8; (n-1)/down
+ * must be a multiple of 8 and >= 16 in both directions).  From the change of rho and of
+ * the Dirichlet values since the last converged solve (and the previous potential) it
+ * predicts the change of phi; sf_poisson_nl with use_learned = 1 and phi = NULL starts
+ * from phi_prev + prediction and still iterates to the same FP64 residual.  While
+ * training is on, every converged sf_poisson_nl adds one Adam step on the new pair. */
+int sf_unet_init(sf_ctx* ctx, int32_t base_channels, int32_t down, uint64_t seed);
+/* Training on/off, Adam learning rate, Adam steps per converged solve. */
+int sf_unet_set_training(sf_ctx* ctx, int32_t on, double lr, int32_t iters_per_sample);
+/* Last training loss (MSE of the scaled change), pairs trained on, device ms spent
+ * training (any pointer may be NULL). */
+int sf_unet_stats(sf_ctx* ctx, double* last_loss, int64_t* samples, double* train_ms);
+/* Gradient checking: runs the network on x (Hn*Wn*16 floats, NHWC, Hn = (nj-1)/down,
+ * Wn = (ni-1)/down) into pred (Hn*Wn); with dpred given, back-propagates it and writes
+ * the parameter gradients into grads, flattened per layer (conv weight [co][ky][kx][ci],
+ * conv bias, ..., head weight, head bias; encoder convs first, then decoder, then head).
+ * *nparams receives the parameter count (x may be NULL to query it only). */
+int sf_unet_debug(sf_ctx* ctx, const float* x, const float* dpred, float* pred, float* grads, int64_t* nparams);
+/* Reads (get) and/or replaces (set) the FP32 master parameters, same flattening. */
+int sf_unet_params(sf_ctx* ctx, float* get, const float* set);
+
 /* ---- collisions ------------------------------------------------------------- */
 /* Cross-section models (interactions/Sigma.java:24-195, collisions/SigmaPlus.java:38-76) */
 #define SF_SIGMA_CONST 0    /* sigma = c0                                         */

@@ -630,6 +630,7 @@ int sf_ctx_destroy(sf_ctx* ctx) {
   if (!ctx) return SF_OK;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  sf_unet_destroy_internal(ctx);
   sf_poisson_destroy_internal(ctx);
   sf_collide_destroy_internal(ctx);
   for (SfSpecies* sp : ctx->species) {

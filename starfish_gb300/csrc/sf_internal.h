@@ -181,6 +181,7 @@ struct SfSpecies {
 
 struct SfPoisson;    // sf_poisson.cu
 struct SfDsmcState;  // sf_collide.cu
+struct SfUnet;       // sf_unet.cu
 
 // CUDA-event timing of named kernels on the context stream
 struct SfTimer {
@@ -234,6 +235,7 @@ struct sf_ctx {
   double* dscratch = nullptr;              // ni*nj FP64 scratch (field transfers)
   std::vector<SfSpecies*> species;
   SfPoisson* poisson = nullptr;
+  SfUnet* unet = nullptr;          // learned warm start of the Poisson solve
   std::vector<SfDsmcState*> dsmc;  // per species DSMC cell state
   float* mcc_target = nullptr;     // MCC target density, u, v, w, T (5 * ni*nj)
   double mcc_mass = 0;
@@ -250,6 +252,13 @@ struct sf_ctx {
 void sf_poisson_destroy_internal(sf_ctx* ctx);                       // sf_poisson.cu
 void sf_collide_destroy_internal(sf_ctx* ctx);                       // sf_collide.cu
 int sf_poisson_get_field_internal(sf_ctx* ctx, int field, double* out);  // sf_poisson.cu
+void sf_unet_destroy_internal(sf_ctx* ctx);                          // sf_unet.cu
+// Poisson hooks of the learned warm start (sf_unet.cu): phi <- phi_prev + prediction
+// before a solve (false when the network cannot predict yet), and after a converged
+// solve one training step on the new (d rho, d bc) -> d phi pair.
+bool sf_unet_warm_start(sf_ctx* ctx, double* phi, const double* rho, const double* bc, const uint8_t* type);
+void sf_unet_after_solve(sf_ctx* ctx, const double* phi, const double* rho, const double* bc,
+                         const uint8_t* type, double eps);
 namespace sf {
 void launch_sort(sf_ctx* ctx, SfSpecies* sp);
 void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments);

@@ -772,6 +772,9 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
   a.linear = prm->linear ? 1 : 0;
   const int iters = prm->cycles > 0 ? prm->cycles : 3;
   SF_CUDA(cudaEventRecord(ps->ev0, s));
+  // learned warm start: phi <- phi_prev + U-Net prediction of the change (inside the
+  // timed region; the solve below still has to reach the same residual)
+  if (prm->use_learned && !phi && ctx->unet) sf_unet_warm_start(ctx, ps->phi, ps->rho, ps->bc, ps->type0);
   double h[2];
   double res = 0, res_inf = 0, res0 = -1;
   int it = 0, vcount = 0;
@@ -805,6 +808,9 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
   float ms = 0;
   SF_CUDA(cudaEventElapsedTime(&ms, ps->ev0, ps->ev1));
   SF_CUDA(cudaGetLastError());
+  // every converged solve is a training pair for the warm-start network (outside the
+  // timed region; its cost is reported by sf_unet_stats)
+  if (conv && ctx->unet) sf_unet_after_solve(ctx, ps->phi, ps->rho, ps->bc, ps->type0, prm->eps);
   if (phi) {
     SF_CUDA(cudaMemcpyAsync(phi, ps->phi, 8 * (size_t)nn, cudaMemcpyDeviceToHost, s));
     SF_CUDA(cudaStreamSynchronize(s));

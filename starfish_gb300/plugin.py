@@ -223,6 +223,65 @@ class PoissonSolver:
         self.d.check(self.d.lib.sf_boltzmann(self.d.ctx, abi.ptr(ne)))
         return ne
 
+    def use_learned(self, on=True):
+        """Start each solve from the learned warm start (LearnedWarmStart must exist)."""
+        self.prm.use_learned = 1 if on else 0
+
+
+class LearnedWarmStart:
+    """The U-Net warm start of the Poisson solve (no reference counterpart).
+
+    Created on a domain, it learns from every converged solve of that domain while
+    training is on; PoissonSolver.use_learned() makes the solves start from its
+    prediction.  base: channels of the first level (16 or 32); down: coarsening of the
+    network grid relative to the mesh.
+    """
+
+    def __init__(self, domain: GpuDomain, base=32, down=4, seed=0, lr=1e-3, iters_per_sample=1):
+        self.d = domain
+        self.d.check(self.d.lib.sf_unet_init(self.d.ctx, base, down, seed))
+        self.Hn, self.Wn = (domain.nj - 1) // down, (domain.ni - 1) // down
+        self.train(True, lr, iters_per_sample)
+
+    def train(self, on=True, lr=1e-3, iters_per_sample=1):
+        self.d.check(self.d.lib.sf_unet_set_training(self.d.ctx, int(on), float(lr),
+                                                     int(iters_per_sample)))
+
+    def stats(self):
+        loss, n, ms = C.c_double(), C.c_int64(), C.c_double()
+        self.d.check(self.d.lib.sf_unet_stats(self.d.ctx, C.byref(loss), C.byref(n), C.byref(ms)))
+        return {"loss": loss.value, "samples": n.value, "train_ms": ms.value}
+
+    def nparams(self):
+        n = C.c_int64()
+        self.d.check(self.d.lib.sf_unet_debug(self.d.ctx, None, None, None, None, C.byref(n)))
+        return n.value
+
+    def params(self, set_to=None):
+        n = self.nparams()
+        if set_to is not None:
+            p = np.ascontiguousarray(set_to, np.float32)
+            assert p.size == n
+            self.d.check(self.d.lib.sf_unet_params(self.d.ctx, None, abi.ptr(p)))
+            return p
+        out = np.zeros(n, np.float32)
+        self.d.check(self.d.lib.sf_unet_params(self.d.ctx, abi.ptr(out), None))
+        return out
+
+    def forward_backward(self, x, dpred=None):
+        """Network output for x (Hn, Wn, 16) and, with dpred, the parameter gradients."""
+        x = np.ascontiguousarray(x, np.float32)
+        assert x.shape == (self.Hn, self.Wn, 16)
+        pred = np.zeros((self.Hn, self.Wn), np.float32)
+        grads = None
+        n = C.c_int64()
+        if dpred is not None:
+            dpred = np.ascontiguousarray(dpred, np.float32)
+            grads = np.zeros(self.nparams(), np.float32)
+        self.d.check(self.d.lib.sf_unet_debug(self.d.ctx, abi.ptr(x), abi.ptr(dpred), abi.ptr(pred),
+                                              abi.ptr(grads), C.byref(n)))
+        return pred, grads
+
 
 def _sigma(model, c=(0, 0, 0, 0), diam=0.0, T_ref=273.0, omega=0.5, vss_alpha=1.0):
     s = abi.Sigma()

@@ -1,0 +1,259 @@
+"""The learned Poisson warm start: U-Net kernels against a PyTorch CPU reference of the
+same network, and what the trained network gains over the plain warm start.
+
+Gradient check: the library's parameters are loaded into a torch model of the same
+architecture (3x3 convs + ReLU, 2x2 average pooling, nearest upsampling, concatenated
+skips, 1x1 FP32 head), evaluated in float64, that rounds inputs, conv weights, every
+stored activation and every stored activation gradient to BF16 where the GPU stores
+them.  On dyadic values no FP32 sum rounds, so the two must agree exactly; on random
+values they agree to BF16 level (tolerances in each test).
+
+Gain: on the 81x41 electrode mesh the electrode potential follows a sinusoid and rho a
+slow modulation; after online training on 300 solves, each of the next solves is run
+twice from the same previous potential -- with the learned warm start and plain -- and
+both must reach the same residual; the learned start must lower the initial residual.
+"""
+import numpy as np
+import pytest
+
+from starfish_gb300 import abi
+from starfish_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _bf16(t):
+    return t.to(torch.bfloat16).to(t.dtype)
+
+
+class RoundBF16(torch.autograd.Function):
+    """An activation the GPU stores in BF16: its value and its gradient are both rounded."""
+
+    @staticmethod
+    def forward(ctx, x):
+        return _bf16(x)
+
+    @staticmethod
+    def backward(ctx, g):
+        return _bf16(g)
+
+
+class RoundBF16Weight(torch.autograd.Function):
+    """The BF16 copy of an FP32 master weight: rounded value, FP32 gradient."""
+
+    @staticmethod
+    def forward(ctx, x):
+        return _bf16(x)
+
+    @staticmethod
+    def backward(ctx, g):
+        return g
+
+
+def unet_reference(params, x, base, levels=4):
+    """Forward pass of the library's U-Net in torch; params: list of leaf tensors in the
+    library's flattening (conv w [co][ky][kx][ci], conv b, ..., head w, head b)."""
+    import torch.nn.functional as F
+    C = [base << l for l in range(levels)]
+    it = iter(params)
+
+    def conv(h):
+        w = next(it)  # (co, 3, 3, ci)
+        b = next(it)
+        wt = RoundBF16Weight.apply(w).permute(0, 3, 1, 2)
+        return RoundBF16.apply(F.relu(F.conv2d(h, wt, b, padding=1)))
+
+    h = RoundBF16.apply(x)
+    skips = []
+    for l in range(levels):
+        h = conv(h)
+        h = conv(h)
+        if l < levels - 1:
+            skips.append(h)
+            h = RoundBF16.apply(F.avg_pool2d(h, 2))
+    for k in range(levels - 1):
+        skip = skips[levels - 2 - k]
+        up = F.interpolate(h, scale_factor=2, mode="nearest")
+        h = RoundBF16.apply(torch.cat([up, skip], dim=1))
+        h = conv(h)
+        h = conv(h)
+    hw = next(it)
+    hb = next(it)
+    return (h * hw.view(1, -1, 1, 1)).sum(dim=1)[0] + hb[0]
+
+
+def _param_shapes(base, levels=4, cin=16):
+    C = [base << l for l in range(levels)]
+    shapes = []
+    c = cin
+    for l in range(levels):
+        shapes += [(C[l], 3, 3, c), (C[l],), (C[l], 3, 3, C[l]), (C[l],)]
+        c = C[l]
+    for l in range(levels - 2, -1, -1):
+        shapes += [(C[l], 3, 3, C[l + 1] + C[l]), (C[l],), (C[l], 3, 3, C[l]), (C[l],)]
+    shapes += [(C[0],), (1,)]
+    return shapes
+
+
+def _split(flat, shapes):
+    out, off = [], 0
+    for s in shapes:
+        n = int(np.prod(s))
+        out.append(flat[off:off + n].reshape(s))
+        off += n
+    assert off == flat.size
+    return out
+
+
+def _compare(net, base, p, x, dpred):
+    """GPU forward + backward against the float64 torch reference; returns the forward
+    relative error and per-tensor (relative error, cosine) of the parameter gradients."""
+    shapes = _param_shapes(base)
+    net.params(set_to=p)
+    assert np.array_equal(net.params(), p)
+    pred, grads = net.forward_backward(x, dpred)
+    # float64 reference: CPU fp32 convolutions may take reduced-precision library paths
+    tp = [torch.tensor(a.astype(np.float64), requires_grad=True) for a in _split(p, shapes)]
+    xt = torch.tensor(x.astype(np.float64)).permute(2, 0, 1).unsqueeze(0)
+    out = unet_reference(tp, xt, base)
+    ref = out.detach().numpy()
+    err = np.linalg.norm(pred - ref) / np.linalg.norm(ref)
+    (out * torch.tensor(dpred.astype(np.float64))).sum().backward()
+    res = []
+    for a, t in zip(_split(grads, shapes), tp):
+        a = a.reshape(-1)
+        b = t.grad.numpy().reshape(-1)
+        nb = np.linalg.norm(b)
+        res.append((np.linalg.norm(a - b) / max(nb, 1e-30), float(a @ b / max(np.linalg.norm(a) * nb, 1e-30))))
+    return err, res
+
+
+def _net(base):
+    from starfish_gb300.plugin import GpuDomain, LearnedWarmStart
+    dom = GpuDomain(W.es_pic_mesh(65, 33, 1e-3))  # network grid 32 x 64
+    return dom, LearnedWarmStart(dom, base=base, down=1, seed=5)
+
+
+@pytest.mark.parametrize("base", [16, 32])
+def test_unet_exact_on_dyadic_values(gpulib, base):
+    """Sparse +-1 weights (about two nonzero taps per output, so magnitudes stay level),
+    integer biases, inputs and output gradients, head weights 1: every value is a small
+    multiple of 1/64, no FP32 product or sum rounds, and each stored BF16 value is rounded
+    from the same exact number on both sides, so the GPU must match the reference exactly
+    and any index or data-flow error shows as a mismatch.  (The same values give identical
+    FP32 and FP64 reference results.)"""
+    dom, net = _net(base)
+    try:
+        shapes = _param_shapes(base)
+        rng = np.random.default_rng(base + 1)
+        parts = []
+        for sh in shapes[:-2]:
+            if len(sh) == 4:
+                nz = rng.random(sh) < 2.0 / (9 * sh[3])
+                parts.append(np.where(nz, rng.choice([-1.0, 1.0], sh), 0.0))
+            else:
+                parts.append(rng.integers(-1, 2, sh).astype(np.float64))
+        parts += [np.ones(shapes[-2]), np.zeros(1)]
+        p = np.concatenate([a.reshape(-1) for a in parts]).astype(np.float32)
+        x = rng.integers(-4, 5, (net.Hn, net.Wn, 16)).astype(np.float32)
+        dpred = rng.integers(-3, 4, (net.Hn, net.Wn)).astype(np.float32)
+        err, res = _compare(net, base, p, x, dpred)
+        assert err <= 1e-7, f"forward relative error {err:.3g}"
+        bad = [f"tensor {k} {shapes[k]}: rel {r:.3g}" for k, (r, c) in enumerate(res) if not r <= 1e-7]
+        assert not bad, "; ".join(bad)
+    finally:
+        dom.close()
+
+
+def test_unet_matches_torch_random(gpulib):
+    """Random weights (the library's He initialisation), biases and inputs.  Every BF16
+    store turns summation-order differences into occasional one-ulp flips that propagate:
+    the same rounding-emulated network evaluated on the CPU in FP32 instead of FP64
+    differs by ~5e-3 in the forward and by up to 16 % (cosine down to 0.988) in single
+    gradient tensors, and tensor-core accumulation is a third order.  So this is a
+    BF16-level bound -- forward 2e-2 relative L2, gradients cosine >= 0.95 and relative
+    L2 <= 0.35 -- and exactness is left to the dyadic test."""
+    base = 32
+    dom, net = _net(base)
+    try:
+        shapes = _param_shapes(base)
+        rng = np.random.default_rng(7)
+        parts = _split(net.params().copy(), shapes)
+        for k in range(1, len(parts) - 2, 2):
+            parts[k][:] = rng.normal(0, 0.05, parts[k].shape)
+        parts[-2][:] = rng.normal(0, 0.3, parts[-2].shape)
+        parts[-1][:] = 0.1
+        p = np.concatenate([a.reshape(-1) for a in parts]).astype(np.float32)
+        x = rng.normal(0, 1, (net.Hn, net.Wn, 16)).astype(np.float32)
+        dpred = rng.normal(0, 1, (net.Hn, net.Wn)).astype(np.float32)
+        err, res = _compare(net, base, p, x, dpred)
+        assert err < 2e-2, f"forward relative error {err:.3g}"
+        bad = [f"tensor {k} {shapes[k]}: rel {r:.3g} cos {c:.4f}" for k, (r, c) in enumerate(res)
+               if not (r <= 0.35 and c >= 0.95)]
+        assert not bad, f"forward error {err:.3g}; " + "; ".join(bad)
+    finally:
+        dom.close()
+
+
+def _rho(spec, t, rng):
+    """Quasi-neutral ion charge with a slow central modulation and 1 % noise."""
+    x = np.arange(spec.ni) * spec.dh[0]
+    y = np.arange(spec.nj) * spec.dh[1]
+    X, Y = np.meshgrid(x, y)
+    Lx, Ly = spec.lengths()
+    blob = np.exp(-((X - 0.3 * Lx) ** 2 + (Y - 0.5 * Ly) ** 2) / (2 * (0.15 * Ly) ** 2))
+    n = 1e12 * (1 + 0.3 * np.sin(2 * np.pi * t / 150.0) * blob) * (1 + 0.01 * rng.standard_normal(X.shape))
+    return (abi_QE * n).reshape(-1)
+
+
+abi_QE = 1.60217646e-19
+
+
+def test_learned_warm_start_gain(gpulib):
+    from starfish_gb300.plugin import GpuDomain, LearnedWarmStart, PoissonSolver
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    electrode = spec.bc_value != 0
+    dom = GpuDomain(spec)
+    try:
+        ps = PoissonSolver(dom, n0=1e12, Te0=2.0, tol=1e-6, max_it=60, cycles=2)
+        net = LearnedWarmStart(dom, base=16, down=1, seed=1, lr=2e-3, iters_per_sample=4)
+        rng = np.random.default_rng(0)
+        bc = spec.bc_value.copy()
+        period = 400
+        n_train, n_test = 300, 40
+        for t in range(n_train):
+            bc[electrode] = -100 - 100 * np.cos(2 * np.pi * t / period)
+            ps.set_bc_values(bc)
+            ps.solve(rho=_rho(spec, t, rng))
+        st = net.stats()
+        assert st["samples"] == n_train - 1
+        net.train(False)
+        ps_l, ps_p = [], []
+        for t in range(n_train, n_train + n_test):
+            phi_prev = dom.get_field(abi.FIELD_PHI)
+            rho = _rho(spec, t, rng)
+            bc[electrode] = -100 - 100 * np.cos(2 * np.pi * t / period)
+            ps.set_bc_values(bc)
+            ps.use_learned(True)
+            _, sl = ps.solve(rho=rho)
+            phi_l = dom.get_field(abi.FIELD_PHI)
+            ps.use_learned(False)
+            phi_p, sp = ps.solve(rho=rho, phi=phi_prev)
+            assert sl["residual"] < 1e-6 and sp["residual"] < 1e-6
+            # both converge to the same potential (within what the residual allows)
+            assert np.max(np.abs(phi_l - phi_p)) < 1e-6 * np.max(np.abs(phi_p))
+            ps_l.append(sl)
+            ps_p.append(sp)
+        r_l = np.mean([s["initial_residual"] for s in ps_l])
+        r_p = np.mean([s["initial_residual"] for s in ps_p])
+        it_l = np.mean([s["newton_it"] for s in ps_l])
+        it_p = np.mean([s["newton_it"] for s in ps_p])
+        print(f"\nlearned warm start: initial residual {r_l:.3g} vs plain {r_p:.3g} "
+              f"({r_p / r_l:.1f}x lower); Newton iterations {it_l:.2f} vs {it_p:.2f}; "
+              f"training loss {st['loss']:.3g}")
+        assert r_l < 0.5 * r_p
+        assert it_l <= it_p
+    finally:
+        dom.close()

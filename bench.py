@@ -135,7 +135,7 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
     spec = cfg.mesh
     Lx, Ly = spec.lengths()
     inlet = np.array([spec.x0[0], spec.x0[1] + Ly, spec.x0[0], spec.x0[1]])
-    ps = PoissonSolver(dom, n0=cfg.n0, Te0=cfg.Te0, phi0=cfg.phi0, tol=tol, max_it=60, cycles=2)
+    ps = PoissonSolver(dom, n0=cfg.n0, Te0=cfg.Te0, phi0=cfg.phi0, tol=tol, max_it=60, cycles=4)
     net = LearnedWarmStart(dom, base=base, down=down, seed=0, lr=1e-3, iters_per_sample=1)
     electrode = spec.bc_value != 0
     bc = spec.bc_value.copy()

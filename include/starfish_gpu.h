@@ -237,7 +237,7 @@ typedef struct {
   double eps;       /* permittivity, Constants.EPS0 * eps_r                             */
   double tol;       /* target FP64 residual ||R||_2 / N (LinearSolverGS metric, :111-125) */
   int32_t max_it;   /* cap on Newton / refinement iterations                            */
-  int32_t cycles;   /* multigrid V-cycles per Newton iteration (inner FP32 solve)       */
+  int32_t cycles;   /* PCG iterations (one V-cycle each) per Newton step; <= 0: 4       */
   int32_t use_learned; /* 1: start from the learned predictor when it is trained       */
   int32_t linear;   /* 1: linear Poisson (no electron term), PoissonSolver linear_mode  */
 } sf_poisson_params;

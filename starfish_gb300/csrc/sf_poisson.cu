@@ -116,6 +116,7 @@ __device__ __forceinline__ float prolong_value(const float* yc, int i, int j, in
 // ------------------------------------------------------------------------------------
 // global-memory level kernels
 // ------------------------------------------------------------------------------------
+// one colour of a red-black Gauss-Seidel sweep: nodes with (i + j) & 1 == color
 __global__ void k_smooth(LevelView L, int color) {
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -171,10 +172,16 @@ __device__ void cta_smooth(float* y, const float* r, const float* P, const uint8
   for (int s = 0; s < sweeps; s++)
     for (int c = 0; c < 2; c++) {
       const int color = rb ? c : 1 - c;
-      for (int u = threadIdx.x; u < n; u += blockDim.x) {
-        const int j = u / ni, i = u - j * ni;
-        if (((i + j) & 1) != color) continue;
-        y[u] = gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy);
+      if (ni & 1) {
+        // odd row length: the colour (i + j) & 1 of node u = j ni + i is u & 1
+        for (int u = 2 * threadIdx.x + color; u < n; u += 2 * blockDim.x)
+          y[u] = gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy);
+      } else {
+        for (int u = threadIdx.x; u < n; u += blockDim.x) {
+          const int j = u / ni, i = u - j * ni;
+          if (((i + j) & 1) != color) continue;
+          y[u] = gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy);
+        }
       }
       __syncthreads();
     }
@@ -254,6 +261,7 @@ struct NlArgs {
   double C_n0;            // (e/eps) n0
   double inv_kTe, phi0;
   int linear;
+  int fp64_exp;  // 0: Boltzmann exponential in FP32 (with an error bound), 1: FP64
 };
 
 constexpr int RB = 256;
@@ -282,16 +290,49 @@ __device__ inline void block_sum2(double a, double b, double* part, bool max2) {
   }
 }
 
+// per block: sum of a, max of b, max of c -> part[3 * block + {0, 1, 2}]
+__device__ inline void block_sum_max_max(double a, double b, double c, double* part) {
+  __shared__ double sh[3][RB / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b = fmax(b, __shfl_down_sync(0xffffffffu, b, o));
+    c = fmax(c, __shfl_down_sync(0xffffffffu, c, o));
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sh[0][wid] = a;
+    sh[1][wid] = b;
+    sh[2][wid] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0, y = 0, z = 0;
+    for (int w = 0; w < RB / 32; w++) {
+      x += sh[0][w];
+      y = fmax(y, sh[1][w]);
+      z = fmax(z, sh[2][w]);
+    }
+    part[3 * blockIdx.x] = x;
+    part[3 * blockIdx.x + 1] = y;
+    part[3 * blockIdx.x + 2] = z;
+  }
+}
+
 // F = A x - b0 - (e n0/eps) exp((x - phi0)/kTe) on interior rows, x - bc on fixed rows,
 // the one-sided gradient on open-face rows (b = 0 there, as Solver.java:322-338 sets);
 // P = d(exp term)/dx.  F (open-face rows scaled by 1/h for the symmetric inner system)
-// and P go to the FP32 level 0; per block sum F^2 and max |F| of the unscaled F.
+// and P go to the FP32 level 0; per block sum F^2, max |F| of the unscaled F and the
+// largest error bound of an FP32 exponential.
+// The Laplacian is FP64 (its terms cancel to ~1e-14 of their size at the tolerance);
+// the Boltzmann term is small next to them and its exponential is taken in FP32 unless
+// a.fp64_exp: its relative error is at most |arg| 2^-24 (rounding of the argument) plus
+// 2^-22, and the host switches to FP64 when that bound could reach the tolerance.
 __global__ void __launch_bounds__(RB) k_nl_residual(NlArgs a, const double* __restrict__ x,
                                                     const double* __restrict__ b0, const uint8_t* __restrict__ type,
                                                     float* __restrict__ F32, float* __restrict__ P32,
                                                     double* __restrict__ partial) {
   const int n = a.ni * a.nj;
-  double s2 = 0.0, smax = 0.0;
+  double s2 = 0.0, smax = 0.0, emax = 0.0;
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
     const uint8_t t = type[u];
     const double xc = x[u];
@@ -306,7 +347,13 @@ __global__ void __launch_bounds__(RB) k_nl_residual(NlArgs a, const double* __re
         const double Ax = a.cx * (x[u - 1] + x[u + 1] - 2.0 * xc) + a.cy * (x[u - a.ni] + x[u + a.ni] - 2.0 * xc);
         double ex = 0.0;
         if (!a.linear) {
-          ex = a.C_n0 * exp((xc - a.phi0) * a.inv_kTe);
+          const double arg = (xc - a.phi0) * a.inv_kTe;
+          if (a.fp64_exp || arg > 80.0) {
+            ex = a.C_n0 * exp(arg);
+          } else {
+            ex = a.C_n0 * (double)expf((float)arg);
+            emax = fmax(emax, ex * (fabs(arg) * 5.9604645e-8 + 2.3841858e-7));
+          }
           P = ex * a.inv_kTe;
         }
         F = Fs = Ax - (b0[u] + ex);
@@ -317,7 +364,34 @@ __global__ void __launch_bounds__(RB) k_nl_residual(NlArgs a, const double* __re
     s2 += F * F;
     smax = fmax(smax, fabs(F));
   }
-  block_sum2(s2, smax, partial, true);
+  block_sum_max_max(s2, smax, emax, partial);
+}
+
+__global__ void k_reduce_partials3(const double* partial, int nb, double* out) {
+  __shared__ double sa[256], sb[256], sc[256];
+  double a = 0, b = 0, c = 0;
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+    a += partial[3 * k];
+    b = fmax(b, partial[3 * k + 1]);
+    c = fmax(c, partial[3 * k + 2]);
+  }
+  sa[threadIdx.x] = a;
+  sb[threadIdx.x] = b;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sa[threadIdx.x] += sa[threadIdx.x + w];
+      sb[threadIdx.x] = fmax(sb[threadIdx.x], sb[threadIdx.x + w]);
+      sc[threadIdx.x] = fmax(sc[threadIdx.x], sc[threadIdx.x + w]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[0] = sa[0];
+    out[1] = sb[0];
+    out[2] = sc[0];
+  }
 }
 
 __global__ void k_reduce_partials(const double* partial, int nb, double* out, int max2) {
@@ -351,13 +425,13 @@ enum { SC_RZ = 0, SC_PQ = 1, SC_ALPHA = 2, SC_BETA = 3, SC_RED = 4 };
 __global__ void __launch_bounds__(RB) k_cg_matvec(LevelView L, const float* __restrict__ p, float* __restrict__ q,
                                                   double* __restrict__ partial) {
   const int n = L.ni * L.nj;
-  double s = 0.0;
+  float s = 0.f;  // a thread sums a few dozen products; blocks and the grid sum in FP64
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
     const float qu = apply_J(L.type[u], p, L.P[u], u, L.ni, L.cx, L.cy);
     q[u] = qu;
-    s += (double)p[u] * (double)qu;
+    s = fmaf(p[u], qu, s);
   }
-  block_sum2(s, 0.0, partial, false);
+  block_sum2((double)s, 0.0, partial, false);
 }
 
 // x += alpha p, r -= alpha q, zo = z
@@ -374,13 +448,13 @@ __global__ void k_cg_axpy(int n, const double* __restrict__ sc, const float* __r
 // partial sums of r.z and r.(z - zo)
 __global__ void __launch_bounds__(RB) k_cg_dots(int n, const float* __restrict__ r, const float* __restrict__ z,
                                                 const float* __restrict__ zo, double* __restrict__ partial) {
-  double a = 0.0, b = 0.0;
+  float a = 0.f, b = 0.f;  // per-thread FP32, blocks and the grid in FP64
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
-    const double ru = r[u], zu = z[u];
-    a += ru * zu;
-    b += ru * (zu - (double)zo[u]);
+    const float ru = r[u], zu = z[u];
+    a = fmaf(ru, zu, a);
+    b = fmaf(ru, zu - zo[u], b);
   }
-  block_sum2(a, b, partial, false);
+  block_sum2((double)a, (double)b, partial, false);
 }
 
 // scalar updates of the CG recurrence (one thread)
@@ -478,6 +552,12 @@ struct SfPoisson {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   sf_poisson_params prm{};
   bool have_prm = false;
+  bool fp64_exp = false;  // a previous solve needed the FP64 exponential: start there
+  // the inner work of one Newton step (restrict P, PCG, update) as a CUDA graph
+  cudaGraphExec_t step_graph = nullptr;
+  int graph_iters = -1;
+  double graph_max_step = 0;
+  int64_t graph_launches = 0;
 };
 
 static void* dalloc(SfPoisson* ps, size_t bytes) {
@@ -510,8 +590,8 @@ static SfPoisson* poisson_get(sf_ctx* ctx) {
   ps->cg_zo = (float*)dalloc(ps, 4 * nn);
   ps->type0 = (uint8_t*)dalloc(ps, nn);
   ps->red_blocks = ctx->num_sms * 4;
-  ps->partial = (double*)dalloc(ps, 16 * (size_t)ps->red_blocks);
-  ps->red = (double*)dalloc(ps, 16);
+  ps->partial = (double*)dalloc(ps, 24 * (size_t)ps->red_blocks);
+  ps->red = (double*)dalloc(ps, 24);
   ps->sc = (double*)dalloc(ps, 8 * 8);
   SF_CUDA(cudaMemsetAsync(ps->phi, 0, 8 * nn, ctx->stream));
   SF_CUDA(cudaMemsetAsync(ps->rho, 0, 8 * nn, ctx->stream));
@@ -607,18 +687,24 @@ static void restrict_P(sf_ctx* ctx, SfPoisson* ps) {
 }
 
 // z = M^-1 r: one V(nu1,nu2)-cycle on level 0 from zero, r = lv[0].r, z -> lv[0].y
+// nu red-black sweeps on a level; first = the colour updated first in each sweep
+static void smooth(sf_ctx* ctx, const LevelView& L, int nu, int first) {
+  const dim3 blk(32, 8);
+  const dim3 g((L.ni / 2 + 1 + blk.x - 1) / blk.x, (L.nj + blk.y - 1) / blk.y);
+  for (int k = 0; k < nu; k++) {
+    k_smooth<<<g, blk, 0, ctx->stream>>>(L, first);
+    k_smooth<<<g, blk, 0, ctx->stream>>>(L, 1 - first);
+    ctx->launches += 2;
+  }
+}
+
 static void vcycle(sf_ctx* ctx, SfPoisson* ps, int nu1, int nu2) {
   cudaStream_t s = ctx->stream;
   const dim3 blk(32, 8);
   if (ps->cs > 0) SF_CUDA(cudaMemsetAsync(ps->lv[0].y, 0, 4 * (size_t)ps->lv[0].ni * ps->lv[0].nj, s));
   for (int l = 0; l < ps->cs; l++) {
     const LevelView& L = ps->lv[l];
-    const dim3 gs((L.ni / 2 + 1 + blk.x - 1) / blk.x, (L.nj + blk.y - 1) / blk.y);
-    for (int k = 0; k < nu1; k++) {
-      k_smooth<<<gs, blk, 0, s>>>(L, 0);
-      k_smooth<<<gs, blk, 0, s>>>(L, 1);
-      ctx->launches += 2;
-    }
+    smooth(ctx, L, nu1, 0);
     k_resid<<<grid2(L.ni, L.nj, blk), blk, 0, s>>>(L);
     k_restrict<<<grid2(ps->lv[l + 1].ni, ps->lv[l + 1].nj, blk), blk, 0, s>>>(L, ps->lv[l + 1]);
     ctx->launches += 2;
@@ -629,12 +715,7 @@ static void vcycle(sf_ctx* ctx, SfPoisson* ps, int nu1, int nu2) {
     const LevelView& L = ps->lv[l];
     k_prolong<<<grid2(L.ni, L.nj, blk), blk, 0, s>>>(ps->lv[l + 1], L);
     ctx->launches++;
-    const dim3 gs((L.ni / 2 + 1 + blk.x - 1) / blk.x, (L.nj + blk.y - 1) / blk.y);
-    for (int k = 0; k < nu2; k++) {
-      k_smooth<<<gs, blk, 0, s>>>(L, 1);
-      k_smooth<<<gs, blk, 0, s>>>(L, 0);
-      ctx->launches += 2;
-    }
+    smooth(ctx, L, nu2, 1);
   }
 }
 
@@ -674,12 +755,50 @@ static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters) {
   }
 }
 
+// The inner work of one Newton step -- restriction of P, `iters` PCG iterations with
+// their V-cycles, phi -= correction -- is ~70 launches of mostly small kernels; it is
+// captured once as a CUDA graph and replayed, re-captured when its parameters change.
+static void newton_step(sf_ctx* ctx, SfPoisson* ps, int iters, double max_step) {
+  cudaStream_t s = ctx->stream;
+  const int nn = ps->ni * ps->nj;
+  if (!ps->step_graph || ps->graph_iters != iters || ps->graph_max_step != max_step) {
+    if (ps->step_graph) {
+      SF_CUDA(cudaGraphExecDestroy(ps->step_graph));
+      ps->step_graph = nullptr;
+    }
+    const int64_t l0 = ctx->launches;
+    cudaGraph_t graph = nullptr;
+    SF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      restrict_P(ctx, ps);
+      pcg(ctx, ps, iters);
+      k_update_phi<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, s>>>(nn, ps->phi, ps->cg_x, max_step);
+      ctx->launches++;
+    } catch (...) {
+      cudaStreamEndCapture(s, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    SF_CUDA(cudaStreamEndCapture(s, &graph));
+    const cudaError_t e = cudaGraphInstantiate(&ps->step_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    SF_CUDA(e);
+    ps->graph_iters = iters;
+    ps->graph_max_step = max_step;
+    ps->graph_launches = ctx->launches - l0;
+    ctx->launches = l0;
+  }
+  SF_CUDA(cudaGraphLaunch(ps->step_graph, s));
+  ctx->launches += ps->graph_launches;
+}
+
 void sf_poisson_destroy_internal(sf_ctx* ctx) {
   SfPoisson* ps = ctx->poisson;
   if (!ps) return;
   for (void* p : ps->allocs) cudaFree(p);
   if (ps->ev0) cudaEventDestroy(ps->ev0);
   if (ps->ev1) cudaEventDestroy(ps->ev1);
+  if (ps->step_graph) cudaGraphExecDestroy(ps->step_graph);
   delete ps;
   ctx->poisson = nullptr;
 }
@@ -770,21 +889,29 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
   a.inv_kTe = prm->linear ? 0.0 : 1.0 / prm->kTe0;
   a.phi0 = prm->phi0;
   a.linear = prm->linear ? 1 : 0;
-  const int iters = prm->cycles > 0 ? prm->cycles : 3;
+  a.fp64_exp = ps->fp64_exp ? 1 : 0;
+  const int iters = prm->cycles > 0 ? prm->cycles : 4;
   SF_CUDA(cudaEventRecord(ps->ev0, s));
   // learned warm start: phi <- phi_prev + U-Net prediction of the change (inside the
   // timed region; the solve below still has to reach the same residual)
   if (prm->use_learned && !phi && ctx->unet) sf_unet_warm_start(ctx, ps->phi, ps->rho, ps->bc, ps->type0);
-  double h[2];
+  double h[3];
   double res = 0, res_inf = 0, res0 = -1;
   int it = 0, vcount = 0;
   bool conv = false, diverged = false;
   for (it = 0; it <= prm->max_it; it++) {
     k_nl_residual<<<ps->red_blocks, RB, 0, s>>>(a, ps->phi, ps->b0, ps->type0, ps->lv[0].r, ps->lv[0].P, ps->partial);
-    reduce(ctx, ps, ps->red, 1);
-    ctx->launches++;
-    SF_CUDA(cudaMemcpyAsync(h, ps->red, 16, cudaMemcpyDeviceToHost, s));
+    k_reduce_partials3<<<1, 256, 0, s>>>(ps->partial, ps->red_blocks, ps->red);
+    ctx->launches += 2;
+    SF_CUDA(cudaMemcpyAsync(h, ps->red, 24, cudaMemcpyDeviceToHost, s));
     SF_CUDA(cudaStreamSynchronize(s));
+    // FP32 exponential error bound against the tolerance: its worst node contributes at
+    // most h[2] / sqrt(nn) to ||R||_2 / N; past 1 % of tol the solve continues in FP64
+    if (!a.fp64_exp && h[2] / std::sqrt((double)nn) > 0.01 * prm->tol) {
+      a.fp64_exp = 1;
+      it--;
+      continue;
+    }
     res = std::sqrt(h[0]) / nn;
     res_inf = h[1];
     if (res0 < 0) res0 = res;
@@ -797,12 +924,10 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
       break;
     }
     if (it == prm->max_it) break;
-    restrict_P(ctx, ps);
-    pcg(ctx, ps, iters);
+    newton_step(ctx, ps, iters, prm->linear ? 1e300 : 10.0 * prm->kTe0);
     vcount += iters;
-    k_update_phi<<<g, 256, 0, s>>>(nn, ps->phi, ps->cg_x, prm->linear ? 1e300 : 10.0 * prm->kTe0);
-    ctx->launches++;
   }
+  ps->fp64_exp = a.fp64_exp != 0;
   SF_CUDA(cudaEventRecord(ps->ev1, s));
   SF_CUDA(cudaEventSynchronize(ps->ev1));
   float ms = 0;

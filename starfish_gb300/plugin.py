@@ -176,7 +176,7 @@ class PoissonSolver:
     EPS0 = 8.85418782e-12
 
     def __init__(self, domain: GpuDomain, n0=1e12, Te0=2.0, phi0=0.0, eps_r=1.0, tol=1e-6,
-                 max_it=60, cycles=1, linear=False):
+                 max_it=60, cycles=4, linear=False):
         self.d = domain
         self.prm = abi.PoissonParams()
         self.prm.n0, self.prm.kTe0, self.prm.phi0 = n0, Te0, phi0

@@ -22,7 +22,7 @@ class EsPicSimulation:
         cap = capacity or max(4 * cfg.n_particles, 1 << 20)
         self.ions = KineticMaterial(self.dom, ion.mass, ion.charge, ion.spwt, capacity=cap)
         self.solver = PoissonSolver(self.dom, n0=cfg.n0, Te0=cfg.Te0, phi0=cfg.phi0, tol=poisson_tol,
-                                    max_it=60, cycles=2)
+                                    max_it=60, cycles=4)
         Lx, Ly = cfg.mesh.lengths()
         x0, y0 = cfg.mesh.x0
         # inlet on the x = x0 face, drifting into +x: segment from top to bottom so that the

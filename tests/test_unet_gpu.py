@@ -217,7 +217,7 @@ def test_learned_warm_start_gain(gpulib):
     electrode = spec.bc_value != 0
     dom = GpuDomain(spec)
     try:
-        ps = PoissonSolver(dom, n0=1e12, Te0=2.0, tol=1e-6, max_it=60, cycles=2)
+        ps = PoissonSolver(dom, n0=1e12, Te0=2.0, tol=1e-6, max_it=60)
         net = LearnedWarmStart(dom, base=16, down=1, seed=1, lr=2e-3, iters_per_sample=4)
         rng = np.random.default_rng(0)
         bc = spec.bc_value.copy()

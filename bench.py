@@ -121,7 +121,7 @@ def electrode_potential(step, period=2000):
 
 
 def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_every=10, tol=1e-6,
-                          base=32, down=4):
+                          base=32, down=8, keep_training_every=0):
     """Learned-warm-start workload on the 2049x1025 mesh: the full ES-PIC step (Maxwellian
     inlet at x = 0, push + scatter of the ions, rho, Poisson-Boltzmann solve, E) with the
     electrode potential following -100 - 100 cos(2 pi t / 2000) V.  The U-Net trains online
@@ -129,7 +129,9 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
     and, every `compare_every` steps, the same solve is repeated plain (from the same
     previous potential), so both are timed on identical inputs and reach the same FP64
     residual ||R||_2/N < tol.  Solve times are CUDA-event device times of sf_poisson_nl
-    (the learned one includes the network's inference)."""
+    (the learned one includes the network's inference and the residual of the previous
+    potential it is checked against).  keep_training_every > 0 keeps training online
+    after the training phase on one pair every that many solves (outside the timing)."""
     from starfish_gb300 import abi
     from starfish_gb300.plugin import LearnedWarmStart, PoissonSolver
     spec = cfg.mesh
@@ -150,7 +152,10 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
         km.update_fields(cfg.dt, stats=False)
         ps.update_rho()
         if t == train_steps:
-            net.train(False)
+            if keep_training_every > 0:
+                net.train(True, lr=1e-3, every=keep_training_every)
+            else:
+                net.train(False)
             ps.use_learned(True)
         compare = t >= train_steps and (t - train_steps) % compare_every == 0
         phi_prev = dom.get_field(abi.FIELD_PHI) if compare else None
@@ -183,7 +188,9 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
             "cold_start_ms": cold["ms"], "cold_start_newton_it": cold["newton_it"],
             "training": {"solves": ns["samples"], "ms_per_solve": ns["train_ms"] / max(ns["samples"], 1),
                          "final_loss": ns["loss"], "network": f"U-Net 4 levels, base {base}, "
-                         f"grid {net.Wn}x{net.Hn} (mesh / {down}), BF16 mma.sync, Adam lr 1e-3"},
+                         f"grid {net.Wn}x{net.Hn} (mesh / {down}), BF16 mma.sync, Adam lr 1e-3",
+                         "keep_training_every": keep_training_every},
+            "predictions_used": ns["used"], "predictions_rejected": ns["rejected"],
             "steps": steps, "train_steps": train_steps, "electrode": "-100 - 100 cos(2 pi t / 2000) V",
             "mesh": [spec.ni, spec.nj], "tol": tol, "particles_end": km.get_np(), "wall_s": wall}
 

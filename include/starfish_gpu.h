@@ -282,14 +282,19 @@ int sf_boltzmann(sf_ctx* ctx, double* ne);
  * must be a multiple of 8 and >= 16 in both directions).  From the change of rho and of
  * the Dirichlet values since the last converged solve (and the previous potential) it
  * predicts the change of phi; sf_poisson_nl with use_learned = 1 and phi = NULL starts
- * from phi_prev + prediction and still iterates to the same FP64 residual.  While
- * training is on, every converged sf_poisson_nl adds one Adam step on the new pair. */
+ * from phi_prev + prediction when that start has the lower FP64 residual, and still
+ * iterates to the same tolerance.  While training is on, converged sf_poisson_nl calls
+ * add Adam steps on the new pairs. */
 int sf_unet_init(sf_ctx* ctx, int32_t base_channels, int32_t down, uint64_t seed);
-/* Training on/off, Adam learning rate, Adam steps per converged solve. */
-int sf_unet_set_training(sf_ctx* ctx, int32_t on, double lr, int32_t iters_per_sample);
+/* Training on/off, Adam learning rate, Adam steps per training pair, and the thinning
+ * of online training: one training pair every `every` converged solves. */
+int sf_unet_set_training(sf_ctx* ctx, int32_t on, double lr, int32_t iters_per_sample, int32_t every);
 /* Last training loss (MSE of the scaled change), pairs trained on, device ms spent
- * training (any pointer may be NULL). */
-int sf_unet_stats(sf_ctx* ctx, double* last_loss, int64_t* samples, double* train_ms);
+ * training, predictions used as the start of a solve and predictions rejected because
+ * their FP64 residual was not below that of the previous potential (any pointer may be
+ * NULL). */
+int sf_unet_stats(sf_ctx* ctx, double* last_loss, int64_t* samples, double* train_ms, int64_t* used,
+                  int64_t* rejected);
 /* Gradient checking: runs the network on x (Hn*Wn*16 floats, NHWC, Hn = (nj-1)/down,
  * Wn = (ni-1)/down) into pred (Hn*Wn); with dpred given, back-propagates it and writes
  * the parameter gradients into grads, flattened per layer (conv weight [co][ky][kx][ci],

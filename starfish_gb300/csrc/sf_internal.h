@@ -259,6 +259,8 @@ void sf_unet_destroy_internal(sf_ctx* ctx);                          // sf_unet.
 bool sf_unet_warm_start(sf_ctx* ctx, double* phi, const double* rho, const double* bc, const uint8_t* type);
 void sf_unet_after_solve(sf_ctx* ctx, const double* phi, const double* rho, const double* bc,
                          const uint8_t* type, double eps);
+// the prediction made the start worse: phi <- phi_prev (counted as rejected)
+void sf_unet_reject(sf_ctx* ctx, double* phi);
 namespace sf {
 void launch_sort(sf_ctx* ctx, SfSpecies* sp);
 void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments);

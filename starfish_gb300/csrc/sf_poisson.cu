@@ -892,28 +892,53 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
   a.fp64_exp = ps->fp64_exp ? 1 : 0;
   const int iters = prm->cycles > 0 ? prm->cycles : 4;
   SF_CUDA(cudaEventRecord(ps->ev0, s));
-  // learned warm start: phi <- phi_prev + U-Net prediction of the change (inside the
-  // timed region; the solve below still has to reach the same residual)
-  if (prm->use_learned && !phi && ctx->unet) sf_unet_warm_start(ctx, ps->phi, ps->rho, ps->bc, ps->type0);
   double h[3];
+  // FP64 residual of the current phi into level 0 (F, P) and its norms.  The FP32
+  // exponential's error bound is checked against the tolerance: its worst node adds at
+  // most h[2] / sqrt(nn) to ||R||_2 / N; past 1 % of tol the solve continues in FP64.
+  auto residual = [&](double* r2, double* rinf) {
+    for (;;) {
+      k_nl_residual<<<ps->red_blocks, RB, 0, s>>>(a, ps->phi, ps->b0, ps->type0, ps->lv[0].r, ps->lv[0].P,
+                                                  ps->partial);
+      k_reduce_partials3<<<1, 256, 0, s>>>(ps->partial, ps->red_blocks, ps->red);
+      ctx->launches += 2;
+      SF_CUDA(cudaMemcpyAsync(h, ps->red, 24, cudaMemcpyDeviceToHost, s));
+      SF_CUDA(cudaStreamSynchronize(s));
+      if (!a.fp64_exp && h[2] / std::sqrt((double)nn) > 0.01 * prm->tol) {
+        a.fp64_exp = 1;
+        continue;
+      }
+      *r2 = std::sqrt(h[0]) / nn;
+      *rinf = h[1];
+      return;
+    }
+  };
+  // learned warm start (inside the timed region): phi <- phi_prev + U-Net prediction of
+  // the change, kept only if its FP64 residual is below that of phi_prev itself
   double res = 0, res_inf = 0, res0 = -1;
+  if (prm->use_learned && !phi && ctx->unet) {
+    double r_prev, rinf_prev;
+    residual(&r_prev, &rinf_prev);
+    if (sf_unet_warm_start(ctx, ps->phi, ps->rho, ps->bc, ps->type0)) {
+      residual(&res, &res_inf);
+      if (!(res < r_prev)) {
+        // back to the previous potential, with this solve's Dirichlet values (the inner
+        // system is symmetric only while the fixed rows are exact)
+        sf_unet_reject(ctx, ps->phi);
+        k_fix_phi<<<g, 256, 0, s>>>(nn, ps->phi, ps->bc, ps->type0);
+        ctx->launches++;
+        residual(&res, &res_inf);
+      }
+    } else {
+      res = r_prev;
+      res_inf = rinf_prev;
+    }
+    res0 = res;
+  }
   int it = 0, vcount = 0;
   bool conv = false, diverged = false;
   for (it = 0; it <= prm->max_it; it++) {
-    k_nl_residual<<<ps->red_blocks, RB, 0, s>>>(a, ps->phi, ps->b0, ps->type0, ps->lv[0].r, ps->lv[0].P, ps->partial);
-    k_reduce_partials3<<<1, 256, 0, s>>>(ps->partial, ps->red_blocks, ps->red);
-    ctx->launches += 2;
-    SF_CUDA(cudaMemcpyAsync(h, ps->red, 24, cudaMemcpyDeviceToHost, s));
-    SF_CUDA(cudaStreamSynchronize(s));
-    // FP32 exponential error bound against the tolerance: its worst node contributes at
-    // most h[2] / sqrt(nn) to ||R||_2 / N; past 1 % of tol the solve continues in FP64
-    if (!a.fp64_exp && h[2] / std::sqrt((double)nn) > 0.01 * prm->tol) {
-      a.fp64_exp = 1;
-      it--;
-      continue;
-    }
-    res = std::sqrt(h[0]) / nn;
-    res_inf = h[1];
+    if (it > 0 || res0 < 0) residual(&res, &res_inf);
     if (res0 < 0) res0 = res;
     if (!std::isfinite(res)) {
       diverged = true;

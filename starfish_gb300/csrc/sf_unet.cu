@@ -482,6 +482,9 @@ struct SfUnet {
   float *pred = nullptr, *target = nullptr, *gpred = nullptr, *loss = nullptr;
   std::vector<void*> allocs;
   int64_t samples = 0, steps = 0;
+  int64_t pairs = 0;               // converged pairs seen while training
+  int train_every = 1;             // one training step every train_every pairs
+  int64_t used = 0, rejected = 0;  // predictions kept / rejected by the solve
   double last_loss = 0;
   float lr = 1e-3f;
   int iters_per_sample = 1;
@@ -818,7 +821,7 @@ void sf_unet_after_solve(sf_ctx* ctx, const double* phi, const double* rho, cons
   cudaStream_t s = ctx->stream;
   const double L = std::min((ctx->ni - 1) * ctx->dh[0], (ctx->nj - 1) * ctx->dh[1]) / 4;
   u->k_rho = L * L / eps;
-  if (u->have_prev && u->training) {
+  if (u->have_prev && u->training && (u->pairs++ % u->train_every) == 0) {
     cudaEvent_t e0, e1;
     SF_CUDA(cudaEventCreate(&e0));
     SF_CUDA(cudaEventCreate(&e1));
@@ -867,7 +870,16 @@ bool sf_unet_warm_start(sf_ctx* ctx, double* phi, const double* rho, const doubl
   unet_forward(ctx, u);
   k_unet_apply<<<ew_grid(ctx, (size_t)ctx->ni * ctx->nj), 256, 0, s>>>(a, u->sigma, u->pred, type, u->phi_prev, phi);
   ctx->launches++;
+  u->used++;
   return true;
+}
+
+void sf_unet_reject(sf_ctx* ctx, double* phi) {
+  SfUnet* u = ctx->unet;
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  SF_CUDA(cudaMemcpyAsync(phi, u->phi_prev, 8 * nn, cudaMemcpyDeviceToDevice, ctx->stream));
+  u->used--;
+  u->rejected++;
 }
 
 extern "C" {
@@ -898,22 +910,26 @@ int sf_unet_init(sf_ctx* ctx, int32_t base_channels, int32_t down, uint64_t seed
   SF_API_END(ctx)
 }
 
-int sf_unet_set_training(sf_ctx* ctx, int32_t on, double lr, int32_t iters_per_sample) {
+int sf_unet_set_training(sf_ctx* ctx, int32_t on, double lr, int32_t iters_per_sample, int32_t every) {
   SF_API_BEGIN
   SF_REQUIRE(ctx && ctx->unet, SF_ERR_STATE, "no U-Net (sf_unet_init)");
-  SF_REQUIRE(lr > 0 && iters_per_sample >= 1, SF_ERR_ARG, "bad training parameters");
+  SF_REQUIRE(lr > 0 && iters_per_sample >= 1 && every >= 1, SF_ERR_ARG, "bad training parameters");
   ctx->unet->training = on != 0;
   ctx->unet->lr = (float)lr;
   ctx->unet->iters_per_sample = iters_per_sample;
+  ctx->unet->train_every = every;
   SF_API_END(ctx)
 }
 
-int sf_unet_stats(sf_ctx* ctx, double* last_loss, int64_t* samples, double* train_ms) {
+int sf_unet_stats(sf_ctx* ctx, double* last_loss, int64_t* samples, double* train_ms, int64_t* used,
+                  int64_t* rejected) {
   SF_API_BEGIN
   SF_REQUIRE(ctx && ctx->unet, SF_ERR_STATE, "no U-Net (sf_unet_init)");
   if (last_loss) *last_loss = ctx->unet->last_loss;
   if (samples) *samples = ctx->unet->samples;
   if (train_ms) *train_ms = ctx->unet->train_ms;
+  if (used) *used = ctx->unet->used;
+  if (rejected) *rejected = ctx->unet->rejected;
   SF_API_END(ctx)
 }
 

@@ -243,14 +243,18 @@ class LearnedWarmStart:
         self.Hn, self.Wn = (domain.nj - 1) // down, (domain.ni - 1) // down
         self.train(True, lr, iters_per_sample)
 
-    def train(self, on=True, lr=1e-3, iters_per_sample=1):
+    def train(self, on=True, lr=1e-3, iters_per_sample=1, every=1):
+        """Online training on/off; one training pair every `every` converged solves."""
         self.d.check(self.d.lib.sf_unet_set_training(self.d.ctx, int(on), float(lr),
-                                                     int(iters_per_sample)))
+                                                     int(iters_per_sample), int(every)))
 
     def stats(self):
         loss, n, ms = C.c_double(), C.c_int64(), C.c_double()
-        self.d.check(self.d.lib.sf_unet_stats(self.d.ctx, C.byref(loss), C.byref(n), C.byref(ms)))
-        return {"loss": loss.value, "samples": n.value, "train_ms": ms.value}
+        used, rej = C.c_int64(), C.c_int64()
+        self.d.check(self.d.lib.sf_unet_stats(self.d.ctx, C.byref(loss), C.byref(n), C.byref(ms),
+                                              C.byref(used), C.byref(rej)))
+        return {"loss": loss.value, "samples": n.value, "train_ms": ms.value, "used": used.value,
+                "rejected": rej.value}
 
     def nparams(self):
         n = C.c_int64()

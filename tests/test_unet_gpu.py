@@ -257,3 +257,40 @@ def test_learned_warm_start_gain(gpulib):
         assert it_l <= it_p
     finally:
         dom.close()
+
+
+def test_rejected_prediction_still_converges(gpulib):
+    """A prediction worse than the previous potential is rejected (phi reverts to the
+    previous solution) and the solve converges from there to the same potential."""
+    from starfish_gb300.plugin import GpuDomain, LearnedWarmStart, PoissonSolver
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    electrode = spec.bc_value != 0
+    dom = GpuDomain(spec)
+    try:
+        ps = PoissonSolver(dom, n0=1e12, Te0=2.0, tol=1e-6, max_it=60)
+        net = LearnedWarmStart(dom, base=16, down=1, seed=1)
+        rng = np.random.default_rng(3)
+        bc = spec.bc_value.copy()
+        for t in range(3):
+            bc[electrode] = -100.0 - t
+            ps.set_bc_values(bc)
+            ps.solve(rho=_rho(spec, t, rng))
+        net.train(False)
+        p = net.params()
+        net.params(set_to=(rng.normal(0, 1.0, p.size)).astype(np.float32))  # garbage network
+        phi_prev = dom.get_field(abi.FIELD_PHI)
+        bc[electrode] = -103.0
+        ps.set_bc_values(bc)
+        rho = _rho(spec, 3, rng)
+        ps.use_learned(True)
+        _, sl = ps.solve(rho=rho)
+        st = net.stats()
+        assert st["rejected"] == 1 and st["used"] == 0
+        phi_l = dom.get_field(abi.FIELD_PHI)
+        ps.use_learned(False)
+        phi_p, sp = ps.solve(rho=rho, phi=phi_prev)
+        assert sl["residual"] < 1e-6, sl
+        assert sl["newton_it"] == sp["newton_it"], (sl, sp)
+        assert np.max(np.abs(phi_l - phi_p)) < 1e-6 * np.max(np.abs(phi_p))
+    finally:
+        dom.close()

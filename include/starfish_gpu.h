@@ -90,6 +90,18 @@ typedef struct sf_ctx sf_ctx;
 #define SF_FIELD_EFI 12    /* electric field components (DomainModule efi/efj)         */
 #define SF_FIELD_EFJ 13
 #define SF_FIELD_NE 14     /* Boltzmann electron density                               */
+/* sampled gas properties of a species (KineticMaterial.computeFields), after
+ * sf_samples_compute: nd-ave, u/v/w-ave, T, t1, t2, t3, p, mpc */
+#define SF_FIELD_ND_AVE 20
+#define SF_FIELD_U_AVE 21
+#define SF_FIELD_V_AVE 22
+#define SF_FIELD_W_AVE 23
+#define SF_FIELD_T 24
+#define SF_FIELD_T1 25
+#define SF_FIELD_T2 26
+#define SF_FIELD_T3 27
+#define SF_FIELD_P 28
+#define SF_FIELD_MPC 29
 
 /* ---- mesh --------------------------------------------------------------------- */
 typedef struct {
@@ -204,7 +216,17 @@ int sf_get_field(sf_ctx* ctx, int32_t field, int32_t sid, double* out);
  * deposits the u/v/w moments.  stats may be NULL. */
 #define SF_PUSH_STATS 1
 #define SF_PUSH_MOMENTS 2
+#define SF_PUSH_SAMPLE 4   /* also KineticMaterial.updateSamples after the push (implies MOMENTS) */
 int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_stats* stats);
+/* Velocity sampling (KineticMaterial.updateGasProperties, KineticMaterial.java:1553-1671).
+ * sf_samples_clear (clearSamples, :1509-1530) zeroes the running sums; its first call sets
+ * up the species' sampling buffers (allocates).  Each sf_push_deposit with SF_PUSH_SAMPLE
+ * then adds the post-push scatter of w, w v, w v^2 and the macroparticles per cell
+ * (updateSamples, :1570-1595).  sf_samples_compute (computeFields, :1606-1671) derives
+ * the SF_FIELD_ND_AVE..SF_FIELD_MPC fields; T_init is used where nothing was sampled
+ * (Material init_vals.T).  *num_samples (may be NULL) receives the sample count. */
+int sf_samples_clear(sf_ctx* ctx, int32_t sid);
+int sf_samples_compute(sf_ctx* ctx, int32_t sid, double T_init, int64_t* num_samples);
 /* sf_push_deposit without any device allocation; no counterpart in the reference.
  * For hosts that must not have the library call cudaMalloc while they step (their own
  * caching allocator already holds the device memory, or their device footprint is

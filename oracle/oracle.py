@@ -81,6 +81,8 @@ def _declare(L):
     L.orc_push.restype = C.c_int
     L.orc_update_fields.argtypes = [C.c_int, C.c_int, d, d, C.c_int, i8, i8, d, C.c_int, d,
                                     C.c_double, d, vp, vp, vp]
+    L.orc_update_samples.argtypes = [C.c_int, C.c_int, d, d, C.c_int, i8, i8, C.c_int, d, d]
+    L.orc_compute_fields.argtypes = [C.c_int, d, C.c_int, d, C.c_double, C.c_double, d]
     L.orc_add_particles.argtypes = [C.c_int, C.c_int, d, d, C.c_int, i8, i8, d, d, C.c_double,
                                     C.c_double, C.c_double, C.c_int, d]
     L.orc_maxwellian_source.argtypes = [C.c_int64, d, C.c_double, C.c_double, C.c_double,
@@ -237,6 +239,25 @@ def update_fields(m: OMesh, node_vol, parts, nd_back=0.0, moments=False):
     lib().orc_update_fields(*m.args(), _f64(node_vol), parts.shape[0], parts.reshape(-1), nd_back,
                             den, *(None if a is None else a.ctypes.data for a in (U, V, W)))
     return (den, U, V, W) if moments else den
+
+
+def update_samples(m: OMesh, parts, sums=None):
+    """KineticMaterial.updateSamples: adds one sample to the 8 running sums (8, ni*nj)."""
+    nu = m.ni * m.nj
+    if sums is None:
+        sums = np.zeros((8, nu))
+    lib().orc_update_samples(*m.args(), parts.shape[0], parts.reshape(-1), sums.reshape(-1))
+    return sums
+
+
+def compute_fields(sums, num_samples, node_vol, mass, T_init):
+    """KineticMaterial.computeFields: dict of the 10 sampled gas fields."""
+    nu = sums.shape[1]
+    out = np.zeros((10, nu))
+    lib().orc_compute_fields(nu, sums.reshape(-1), int(num_samples), _f64(node_vol), mass, T_init,
+                             out.reshape(-1))
+    names = ["nd-ave", "u-ave", "v-ave", "w-ave", "T", "t1", "t2", "t3", "p", "mpc"]
+    return {k: out[i] for i, k in enumerate(names)}
 
 
 def add_particles(m: OMesh, efi, efj, q, mass, dt, parts):

@@ -1112,6 +1112,63 @@ void orc_update_fields(int ni, int nj, const double* x0, const double* dh, int d
     for (int u = 0; u < nu; u++) den[u] += nd_back;
 }
 
+// KineticMaterial.updateSamples (KineticMaterial.java:1570-1595): adds the scatter of
+// mpw, mpw v and mpw v^2 of every live particle to the running sums, and 1 per particle
+// to the cell counter at ((int) lc0, (int) lc1).  sums: 8 node fields (count, u, v, w,
+// uu, vv, ww, mpc), j-major.
+void orc_update_samples(int ni, int nj, const double* x0, const double* dh, int domain,
+                        const int8_t* node_type, const int8_t* face_type, int n, const double* parts,
+                        double* sums) {
+  Mesh m = make_mesh(ni, nj, x0, dh, domain, node_type, face_type);
+  const size_t nu = (size_t)ni * nj;
+  const Particle* P = reinterpret_cast<const Particle*>(parts);
+  for (int p = 0; p < n; p++) {
+    if (P[p].alive == 0) continue;
+    const double w = P[p].mpw;
+    const double* v = P[p].vel;
+    const double a = P[p].lc[0], b = P[p].lc[1];
+    scatter(m, sums + 1 * nu, a, b, w * v[0]);
+    scatter(m, sums + 2 * nu, a, b, w * v[1]);
+    scatter(m, sums + 3 * nu, a, b, w * v[2]);
+    scatter(m, sums + 4 * nu, a, b, w * v[0] * v[0]);
+    scatter(m, sums + 5 * nu, a, b, w * v[1] * v[1]);
+    scatter(m, sums + 6 * nu, a, b, w * v[2] * v[2]);
+    scatter(m, sums + 0 * nu, a, b, w);
+    sums[7 * nu + (size_t)((int)b) * ni + (int)a] += 1;
+  }
+}
+
+// KineticMaterial.computeFields (KineticMaterial.java:1606-1671) from the running sums:
+// out = 10 node fields nd-ave, u-ave, v-ave, w-ave, T, T1, T2, T3, p, mpc.
+void orc_compute_fields(int nu, const double* sums, int num_samples, const double* node_volume, double mass,
+                        double T_init, double* out) {
+  const double f = mass / KB;
+  for (int u = 0; u < nu; u++) {
+    const double count = sums[u];
+    double T = T_init, T1 = T_init, T2 = T_init, T3 = T_init;
+    if (count > 0) {
+      const double U = sums[1 * nu + u] / count, V = sums[2 * nu + u] / count, W = sums[3 * nu + u] / count;
+      const double uu = sums[4 * nu + u] / count - U * U;
+      const double vv = sums[5 * nu + u] / count - V * V;
+      const double ww = sums[6 * nu + u] / count - W * W;
+      T = (uu + vv + ww) * f / 3.0;
+      T1 = uu * f;
+      T2 = vv * f;
+      T3 = ww * f;
+    }
+    // Field2D.mult(1/num_samples) then scaleByVol; divideByField gives 0 where count is 0
+    const double nd = count * (1.0 / num_samples) / node_volume[u];
+    out[0 * nu + u] = nd;
+    for (int d = 0; d < 3; d++) out[(1 + d) * nu + u] = count != 0 ? sums[(1 + d) * nu + u] / count : 0.0;
+    out[4 * nu + u] = T;
+    out[5 * nu + u] = T1;
+    out[6 * nu + u] = T2;
+    out[7 * nu + u] = T3;
+    out[8 * nu + u] = nd * KB * T;
+    out[9 * nu + u] = sums[7 * nu + u] * (1.0 / num_samples);
+  }
+}
+
 // KineticMaterial.addParticle(md, part) (KineticMaterial.java:776-802) for XY/B=0:
 // lc from pos, clamp to the mesh, rewind the velocity by -dt/2 with E at lc.
 void orc_add_particles(int ni, int nj, const double* x0, const double* dh, int domain,

@@ -26,7 +26,9 @@ BT_DIRICHLET, BT_OPEN, BT_SINK, BT_VIRTUAL = 0, 1, 2, 3
 SURF_PASS, SURF_ABSORB, SURF_NONE, SURF_SPECULAR, SURF_DIFFUSE = -1, 0, 1, 2, 3
 FIELD_ND, FIELD_U, FIELD_V, FIELD_W, FIELD_COUNT, FIELD_NODE_VOL = 0, 1, 2, 3, 4, 5
 FIELD_PHI, FIELD_RHO, FIELD_EFI, FIELD_EFJ, FIELD_NE = 10, 11, 12, 13, 14
-PUSH_STATS, PUSH_MOMENTS = 1, 2
+PUSH_STATS, PUSH_MOMENTS, PUSH_SAMPLE = 1, 2, 4
+FIELD_ND_AVE, FIELD_U_AVE, FIELD_V_AVE, FIELD_W_AVE, FIELD_T = 20, 21, 22, 23, 24
+FIELD_T1, FIELD_T2, FIELD_T3, FIELD_P, FIELD_MPC = 25, 26, 27, 28, 29
 
 _STATUS = {1: "SF_ERR_ARG", 2: "SF_ERR_CUDA", 3: "SF_ERR_NOT_CONVERGED", 4: "SF_ERR_DIVERGED",
            5: "SF_ERR_TIMEOUT", 6: "SF_ERR_OOM", 7: "SF_ERR_STATE"}
@@ -191,4 +193,8 @@ EXPORTS.update({
     "sf_unet_debug": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                 C.POINTER(C.c_int64)]),
     "sf_unet_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+})
+EXPORTS.update({
+    "sf_samples_clear": (C.c_int, [C.c_void_p, C.c_int32]),
+    "sf_samples_compute": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_int64)]),
 })

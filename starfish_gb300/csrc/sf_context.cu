@@ -634,9 +634,10 @@ int sf_ctx_destroy(sf_ctx* ctx) {
   sf_poisson_destroy_internal(ctx);
   sf_collide_destroy_internal(ctx);
   for (SfSpecies* sp : ctx->species) {
-    void* ptrs[] = {sp->cur.cell, sp->cur.frac, sp->cur.vxy, sp->cur.vz, sp->alt.cell, sp->alt.frac,
-                    sp->alt.vxy, sp->alt.vz, sp->count, sp->mom, sp->nd, sp->uvw, sp->seg_model,
-                    sp->seg_param, sp->flux, sp->deposit};
+    void* ptrs[] = {sp->cur.cell, sp->cur.frac, sp->cur.vxy,  sp->cur.vz,     sp->alt.cell,  sp->alt.frac,
+                    sp->alt.vxy,  sp->alt.vz,   sp->count,    sp->mom,        sp->nd,        sp->uvw,
+                    sp->seg_model, sp->seg_param, sp->flux,   sp->deposit,    sp->smp.mom2,  sp->smp.mpc,
+                    sp->samp,     sp->gas};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     delete sp;
@@ -877,7 +878,7 @@ int sf_get_field(sf_ctx* ctx, int32_t field, int32_t sid, double* out) {
   SF_REQUIRE(ctx && out, SF_ERR_ARG, "null argument");
   SF_CUDA(cudaSetDevice(ctx->device));
   size_t nn = (size_t)ctx->ni * ctx->nj;
-  if (field >= SF_FIELD_PHI) {
+  if (field >= SF_FIELD_PHI && field <= SF_FIELD_NE) {
     int rc = sf_poisson_get_field_internal(ctx, field, out);
     if (rc != SF_OK) return rc;
     return SF_OK;
@@ -909,7 +910,10 @@ int sf_get_field(sf_ctx* ctx, int32_t field, int32_t sid, double* out) {
       break;
     }
     default:
-      SF_REQUIRE(false, SF_ERR_ARG, "unknown field selector");
+      SF_REQUIRE(field >= SF_FIELD_ND_AVE && field <= SF_FIELD_MPC, SF_ERR_ARG, "unknown field selector");
+      SF_REQUIRE(sp->gas, SF_ERR_STATE, "no sampled moments (sf_samples_clear, SF_PUSH_SAMPLE, sf_samples_compute)");
+      SF_CUDA(cudaMemcpyAsync(out, sp->gas + (size_t)(field - SF_FIELD_ND_AVE) * nn, sizeof(double) * nn,
+                              cudaMemcpyDeviceToHost, ctx->stream));
   }
   SF_CUDA(cudaStreamSynchronize(ctx->stream));
   SF_API_END(ctx)

@@ -43,6 +43,8 @@ constexpr double FLT_EPS_REF = 1e-7;     // Constants.FLT_EPS
 constexpr double DEP_SCALE = 2147483648.0;
 // Moment fixed point: S * v * 2^16 per (m/s).
 constexpr double MOM_SCALE = 65536.0;
+// Second-moment fixed point (velocity sampling): S * v^2 * 2^4 per (m/s)^2.
+constexpr double MOM2_SCALE = 16.0;
 
 // Segment end points x1, y1, x2, y2 (16-byte aligned for vector loads).
 struct alignas(16) Seg4 {
@@ -158,6 +160,13 @@ enum : uint32_t { RNG_SURFACE = 1, RNG_DSMC = 2, RNG_MCC = 3, RNG_INJECT = 4 };
 // ---------------------------------------------------------------------------------
 // Host-side context
 // ---------------------------------------------------------------------------------
+// Per-step deposits of the velocity sampling (KineticMaterial.updateSamples): second
+// moments and macroparticles per cell; null when the species is not sampled.
+struct SampleView {
+  unsigned long long* mom2;  // 3*ni*nj, S v^2 MOM2_SCALE
+  unsigned* mpc;             // ni*nj, particles per cell at the cell's lower-left node
+};
+
 struct SfSpecies {
   double charge = 0, mass = 1, spwt = 1, nd_back = 0;
   int64_t cap = 0;
@@ -177,6 +186,11 @@ struct SfSpecies {
   uint32_t step = 0;          // pushes done (RNG counter)
   int sort_interval = 16;     // automatic sort every N pushes (0 = never)
   int pushes_since_sort = 1 << 30;
+  // velocity sampling (allocated by sf_samples_clear)
+  SampleView smp{nullptr, nullptr};
+  double* samp = nullptr;   // 8*ni*nj running sums: count, u, v, w, uu, vv, ww, mpc
+  double* gas = nullptr;    // 10*ni*nj: nd-ave, u/v/w-ave, T, T1, T2, T3, p, mpc
+  int64_t num_samples = 0;
 };
 
 struct SfPoisson;    // sf_poisson.cu

@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushAr
                                               unsigned long long* __restrict__ count,
                                               long long* __restrict__ mom, int* __restrict__ slow_idx,
                                               unsigned long long* __restrict__ counters,
-                                              double* __restrict__ stats_partial) {
+                                              double* __restrict__ stats_partial, SampleView smp) {
   __shared__ unsigned acc_lo[SBOX];
   __shared__ unsigned acc_hi[SBOX];
   __shared__ int sred[4][PB / 32];
@@ -287,6 +287,9 @@ __global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushAr
 #pragma unroll
       for (int k = 0; k < PPT; k++) {
         // scatter skip rule at the far mesh edges (lc >= n-1 is not scattered)
+        // macroparticles per cell at (int) lc (KineticMaterial.updateSamples)
+        if (MOM && dep[k] && smp.mpc)
+          atomicAdd(&smp.mpc[(pj[k] + (pfy[k] >= 1.f)) * m.ni + pi[k] + (pfx[k] >= 1.f)], 1u);
         const bool d = dep[k] && !((pfx[k] >= 1.f && pi[k] == m.ni - 2) || (pfy[k] >= 1.f && pj[k] == m.nj - 2));
         if (!d) continue;
         float wx, wy;
@@ -303,6 +306,13 @@ __global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushAr
             for (int dd = 0; dd < 3; dd++)
               atomicAdd((unsigned long long*)&mom[dd * nn + base + off[cc]],
                         (unsigned long long)__float2ll_rn(s[cc] * pv[k][dd] * 65536.0f));
+          if (smp.mom2)
+#pragma unroll
+            for (int cc = 0; cc < 4; cc++)
+#pragma unroll
+              for (int dd = 0; dd < 3; dd++)
+                atomicAdd(&smp.mom2[dd * nn + base + off[cc]],
+                          __float2ull_rn(s[cc] * pv[k][dd] * pv[k][dd] * (float)MOM2_SCALE));
         }
         if (use_smem) {
           const int l = (pj[k] - jmin) * bw + (pi[k] - imin);
@@ -588,8 +598,10 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
 // fixed point and edge rule as the fused kernel.
 template <int DOM>
 __device__ inline void deposit_global_t(const MeshView& m, unsigned long long* count, long long* mom, int mom_on,
-                                        int i, int j, float fx, float fy, float wx, float wy, float vx, float vy,
-                                        float vz, size_t nn) {
+                                        const SampleView& smp, int i, int j, float fx, float fy, float wx, float wy,
+                                        float vx, float vy, float vz, size_t nn) {
+  // macroparticles per cell at (int) lc (KineticMaterial.updateSamples), before the skip
+  if (mom_on && smp.mpc) atomicAdd(&smp.mpc[(size_t)(j + (fy >= 1.f)) * m.ni + i + (fx >= 1.f)], 1u);
   if ((fx >= 1.f && i == m.ni - 2) || (fy >= 1.f && j == m.nj - 2)) return;  // scatter skip rule
   const size_t u = (size_t)j * m.ni + i;
   const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
@@ -601,6 +613,10 @@ __device__ inline void deposit_global_t(const MeshView& m, unsigned long long* c
       for (int dd = 0; dd < 3; dd++)
         atomicAdd((unsigned long long*)&mom[dd * nn + u + off[cc]],
                   (unsigned long long)__float2ll_rn(s[cc] * vv[dd] * 65536.0f));
+    if (smp.mom2)
+      for (int cc = 0; cc < 4; cc++)
+        for (int dd = 0; dd < 3; dd++)
+          atomicAdd(&smp.mom2[dd * nn + u + off[cc]], __float2ull_rn(s[cc] * vv[dd] * vv[dd] * (float)MOM2_SCALE));
   }
 }
 #define deposit_global deposit_global_t<DOM>
@@ -647,7 +663,7 @@ template <int DOM>
 __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, PushArgs a, SlowArgs sg,
                                                    const int* __restrict__ slow_idx,
                                                    unsigned long long* __restrict__ count,
-                                                   long long* __restrict__ mom, int mom_on) {
+                                                   long long* __restrict__ mom, int mom_on, SampleView smp) {
   // Totals, counters and (for small geometries) per-segment surface sums are first
   // accumulated per block in shared memory and flushed once at the end: the exact
   // path's particles hit the same few segments, so global atomics would serialise.
@@ -698,7 +714,7 @@ __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, 
           atomicAdd(&sa.stats_slow[4], (double)sqrtf(v.x * v.x + v.y * v.y + vz * vz));
           float wx, wy;
           scatter_weights<DOM>(nfx, nfy, i2, j2, a, wx, wy);
-          deposit_global(m, count, mom, mom_on, i2, j2, nfx, nfy, wx, wy, v.x, v.y, vz, nn);
+          deposit_global(m, count, mom, mom_on, smp, i2, j2, nfx, nfy, wx, wy, v.x, v.y, vz, nn);
           continue;
         }
         if (m.all_delete) {
@@ -771,7 +787,7 @@ __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, 
     atomicAdd(&sa.stats_slow[4], sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]));
     float wx, wy;
     scatter_weights<DOM>(fx, fy, i, j, a, wx, wy);
-    deposit_global(m, count, mom, mom_on, i, j, fx, fy, wx, wy, (float)vel[0], (float)vel[1], (float)vel[2], nn);
+    deposit_global(m, count, mom, mom_on, smp, i, j, fx, fy, wx, wy, (float)vel[0], (float)vel[1], (float)vel[2], nn);
   }
   __syncthreads();
   for (int q = threadIdx.x; q < 6; q += blockDim.x)
@@ -800,6 +816,54 @@ __global__ void k_finalize(int nn, const unsigned long long* __restrict__ count,
   }
 }
 
+// running sums of the velocity sampling (KineticMaterial.updateSamples,
+// KineticMaterial.java:1570-1595): count, u, v, w, uu, vv, ww (scattered w S v^k, in
+// weight units) and mpc.  The per-step values are exact integer sums, added in step
+// order, so the sums are reproducible.
+__global__ void k_sample_accum(int nn, const unsigned long long* __restrict__ count, const long long* __restrict__ mom,
+                               const unsigned long long* __restrict__ mom2, const unsigned* __restrict__ mpc,
+                               double spwt, double* __restrict__ samp) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x) {
+    samp[u] += (double)count[u] * (spwt / DEP_SCALE);
+    for (int d = 0; d < 3; d++) {
+      samp[(size_t)(1 + d) * nn + u] += (double)mom[(size_t)d * nn + u] * (spwt / MOM_SCALE);
+      samp[(size_t)(4 + d) * nn + u] += (double)mom2[(size_t)d * nn + u] * (spwt / MOM2_SCALE);
+    }
+    samp[(size_t)7 * nn + u] += (double)mpc[u];
+  }
+}
+
+// KineticMaterial.computeFields (KineticMaterial.java:1606-1671): temperatures from the
+// sampled moments (the initial temperature where nothing was sampled), averaged density
+// (count / samples / node volume), mean velocities, pressure n k T, particles per cell
+__global__ void k_gas_fields(int nn, const double* __restrict__ samp, double inv_samples, const double* __restrict__ vol,
+                             double m_over_k, double T_init, double* __restrict__ gas) {
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x) {
+    const double c = samp[u];
+    double T = T_init, T1 = T_init, T2 = T_init, T3 = T_init, U[3] = {0, 0, 0};
+    if (c > 0) {
+      double uu[3];
+      for (int d = 0; d < 3; d++) {
+        U[d] = samp[(size_t)(1 + d) * nn + u] / c;
+        uu[d] = samp[(size_t)(4 + d) * nn + u] / c - U[d] * U[d];
+      }
+      T = (uu[0] + uu[1] + uu[2]) * m_over_k / 3.0;
+      T1 = uu[0] * m_over_k;
+      T2 = uu[1] * m_over_k;
+      T3 = uu[2] * m_over_k;
+    }
+    const double nd = c * inv_samples / vol[u];
+    gas[u] = nd;
+    for (int d = 0; d < 3; d++) gas[(size_t)(1 + d) * nn + u] = U[d];
+    gas[(size_t)4 * nn + u] = T;
+    gas[(size_t)5 * nn + u] = T1;
+    gas[(size_t)6 * nn + u] = T2;
+    gas[(size_t)7 * nn + u] = T3;
+    gas[(size_t)8 * nn + u] = nd * KB * T;
+    gas[(size_t)9 * nn + u] = samp[(size_t)7 * nn + u] * inv_samples;
+  }
+}
+
 __global__ void k_sum_partials(const double* part, int nblocks, double* out) {
   // deterministic sum of per-block partials; one thread per quantity
   int q = threadIdx.x;
@@ -821,18 +885,19 @@ struct PushScratch {
 };
 
 template <int DOM, bool STATS, bool MOM>
-void launch_push_t(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid, const PushScratch& sc) {
+void launch_push_t(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid, const PushScratch& sc,
+                   const SampleView& smp) {
   k_push<DOM, STATS, MOM><<<grid, PB, 0, ctx->stream>>>(ctx->mesh_view(), sp->cur, a, sp->count, sp->mom,
-                                                      sc.slow_idx, sc.counters, sc.stats_partial);
+                                                      sc.slow_idx, sc.counters, sc.stats_partial, smp);
 }
 
 template <int DOM>
 void launch_push_dom(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid, bool stats, bool mom,
-                     const PushScratch& sc) {
-  if (stats && mom) launch_push_t<DOM, true, true>(ctx, sp, a, grid, sc);
-  else if (stats) launch_push_t<DOM, true, false>(ctx, sp, a, grid, sc);
-  else if (mom) launch_push_t<DOM, false, true>(ctx, sp, a, grid, sc);
-  else launch_push_t<DOM, false, false>(ctx, sp, a, grid, sc);
+                     const PushScratch& sc, const SampleView& smp) {
+  if (stats && mom) launch_push_t<DOM, true, true>(ctx, sp, a, grid, sc, smp);
+  else if (stats) launch_push_t<DOM, true, false>(ctx, sp, a, grid, sc, smp);
+  else if (mom) launch_push_t<DOM, false, true>(ctx, sp, a, grid, sc, smp);
+  else launch_push_t<DOM, false, false>(ctx, sp, a, grid, sc, smp);
 }
 
 }  // namespace
@@ -855,7 +920,10 @@ namespace {
 void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_push_stats* stats,
                        const PushScratch& sc) {
   const bool want_stats = (flags & SF_PUSH_STATS) != 0;
-  const bool mom = (flags & SF_PUSH_MOMENTS) != 0;
+  const bool sample = (flags & SF_PUSH_SAMPLE) != 0;
+  const bool mom = sample || (flags & SF_PUSH_MOMENTS) != 0;
+  SF_REQUIRE(!sample || sp->samp, SF_ERR_STATE, "velocity sampling not set up (sf_samples_clear)");
+  const SampleView smp = sample ? sp->smp : SampleView{nullptr, nullptr};
   // automatic cell sort every sort_interval pushes (the counter starts at the interval,
   // so the first push of a species sorts)
   if (sp->sort_interval > 0 && sp->pushes_since_sort >= sp->sort_interval) launch_sort(ctx, sp);
@@ -863,6 +931,10 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   cudaStream_t s = ctx->stream;
   SF_CUDA(cudaMemsetAsync(sp->count, 0, sizeof(unsigned long long) * nn, s));
   if (mom) SF_CUDA(cudaMemsetAsync(sp->mom, 0, sizeof(long long) * 3 * nn, s));
+  if (sample) {
+    SF_CUDA(cudaMemsetAsync(smp.mom2, 0, sizeof(unsigned long long) * 3 * nn, s));
+    SF_CUDA(cudaMemsetAsync(smp.mpc, 0, sizeof(unsigned) * nn, s));
+  }
   SF_CUDA(cudaMemsetAsync(sc.counters, 0, sizeof(unsigned long long) * 8, s));
   // stats_partial tail (after the per-block area) holds the slow-path sums
   double* slow_stats = sc.stats_partial + (size_t)8 * (sc.stats_blocks - 1);
@@ -891,9 +963,9 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
     TimedScope ts(ctx, "push");
     ctx->launches++;
     switch (ctx->domain) {
-      case SF_DOMAIN_XY: launch_push_dom<SF_DOMAIN_XY>(ctx, sp, a, grid, want_stats, mom, sc); break;
-      case SF_DOMAIN_RZ: launch_push_dom<SF_DOMAIN_RZ>(ctx, sp, a, grid, want_stats, mom, sc); break;
-      default: launch_push_dom<SF_DOMAIN_ZR>(ctx, sp, a, grid, want_stats, mom, sc); break;
+      case SF_DOMAIN_XY: launch_push_dom<SF_DOMAIN_XY>(ctx, sp, a, grid, want_stats, mom, sc, smp); break;
+      case SF_DOMAIN_RZ: launch_push_dom<SF_DOMAIN_RZ>(ctx, sp, a, grid, want_stats, mom, sc, smp); break;
+      default: launch_push_dom<SF_DOMAIN_ZR>(ctx, sp, a, grid, want_stats, mom, sc, smp); break;
     }
     }
     SF_CUDA(cudaGetLastError());
@@ -909,13 +981,16 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
     ctx->launches++;
     switch (ctx->domain) {
       case SF_DOMAIN_XY:
-        k_push_slow<SF_DOMAIN_XY><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom);
+        k_push_slow<SF_DOMAIN_XY><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom,
+                                                        smp);
         break;
       case SF_DOMAIN_RZ:
-        k_push_slow<SF_DOMAIN_RZ><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom);
+        k_push_slow<SF_DOMAIN_RZ><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom,
+                                                        smp);
         break;
       default:
-        k_push_slow<SF_DOMAIN_ZR><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom);
+        k_push_slow<SF_DOMAIN_ZR><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom,
+                                                        smp);
         break;
     }
     SF_CUDA(cudaGetLastError());
@@ -923,6 +998,14 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   {
     TimedScope ts(ctx, "finalize");
     launch_finalize(ctx, sp, mom);
+  }
+  if (sample) {
+    // KineticMaterial.updateSamples: this step's deposits into the running sums
+    TimedScope ts(ctx, "sample");
+    k_sample_accum<<<grid_for((int64_t)nn, 256, ctx->num_sms * 8), 256, 0, s>>>(
+        (int)nn, sp->count, sp->mom, smp.mom2, smp.mpc, sp->spwt, sp->samp);
+    ctx->launches++;
+    sp->num_samples++;
   }
   SF_CUDA(cudaGetLastError());
   double* h = ctx->host_pinned;
@@ -1038,5 +1121,41 @@ extern "C" int sf_species_set_sort_interval(sf_ctx* ctx, int32_t sid, int32_t in
   SfSpecies* sp = get_species(ctx, sid);
   SF_REQUIRE(interval >= 0, SF_ERR_ARG, "interval must be >= 0");
   sp->sort_interval = interval;
+  SF_API_END(ctx)
+}
+
+// KineticMaterial.clearSamples (KineticMaterial.java:1509-1530); the first call sets up
+// the sampling buffers of the species (8 + 10 FP64 node fields and the per-step deposits)
+extern "C" int sf_samples_clear(sf_ctx* ctx, int32_t sid) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  if (!sp->samp) {
+    SF_CUDA(cudaMalloc(&sp->smp.mom2, sizeof(unsigned long long) * 3 * nn));
+    SF_CUDA(cudaMalloc(&sp->smp.mpc, sizeof(unsigned) * nn));
+    SF_CUDA(cudaMalloc(&sp->gas, sizeof(double) * 10 * nn));
+    SF_CUDA(cudaMalloc(&sp->samp, sizeof(double) * 8 * nn));
+    SF_CUDA(cudaMemsetAsync(sp->gas, 0, sizeof(double) * 10 * nn, ctx->stream));
+  }
+  SF_CUDA(cudaMemsetAsync(sp->samp, 0, sizeof(double) * 8 * nn, ctx->stream));
+  SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  sp->num_samples = 0;
+  SF_API_END(ctx)
+}
+
+extern "C" int sf_samples_compute(sf_ctx* ctx, int32_t sid, double T_init, int64_t* num_samples) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(sp->samp, SF_ERR_STATE, "velocity sampling not set up (sf_samples_clear)");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const int nn = ctx->ni * ctx->nj;
+  const double inv = sp->num_samples > 0 ? 1.0 / (double)sp->num_samples : 0.0;
+  k_gas_fields<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(nn, sp->samp, inv, ctx->d_node_vol,
+                                                                              sp->mass / KB, T_init, sp->gas);
+  ctx->launches++;
+  SF_CUDA(cudaGetLastError());
+  SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (num_samples) *num_samples = sp->num_samples;
   SF_API_END(ctx)
 }

@@ -126,13 +126,30 @@ class KineticMaterial:
     def clear(self):
         self.d.check(self.d.lib.sf_particles_clear(self.d.ctx, self.sid))
 
-    # KineticMaterial.updateFields(): push + scatter
-    def update_fields(self, dt, stats=True, moments=False):
+    # KineticMaterial.updateFields(): push + scatter (+ updateSamples with sample=True)
+    def update_fields(self, dt, stats=True, moments=False, sample=False):
         st = abi.PushStats()
-        flags = (abi.PUSH_STATS if stats else 0) | (abi.PUSH_MOMENTS if moments else 0)
+        flags = ((abi.PUSH_STATS if stats else 0) | (abi.PUSH_MOMENTS if moments else 0) |
+                 (abi.PUSH_SAMPLE if sample else 0))
         self.d.check(self.d.lib.sf_push_deposit(self.d.ctx, self.sid, float(dt), flags,
                                                 C.byref(st)))
         return st.as_dict()
+
+    def clear_samples(self):
+        """KineticMaterial.clearSamples (sets up the sampling buffers on first use)."""
+        self.d.check(self.d.lib.sf_samples_clear(self.d.ctx, self.sid))
+
+    GAS_FIELDS = {"nd-ave": abi.FIELD_ND_AVE, "u-ave": abi.FIELD_U_AVE, "v-ave": abi.FIELD_V_AVE,
+                  "w-ave": abi.FIELD_W_AVE, "T": abi.FIELD_T, "t1": abi.FIELD_T1, "t2": abi.FIELD_T2,
+                  "t3": abi.FIELD_T3, "p": abi.FIELD_P, "mpc": abi.FIELD_MPC}
+
+    def compute_fields(self, T_init=273.15):
+        """KineticMaterial.computeFields: dict of the sampled gas fields (ni*nj each)."""
+        n = C.c_int64()
+        self.d.check(self.d.lib.sf_samples_compute(self.d.ctx, self.sid, float(T_init), C.byref(n)))
+        out = {k: self.d.get_field(f, self.sid) for k, f in self.GAS_FIELDS.items()}
+        out["num_samples"] = n.value
+        return out
 
     def get_np(self):
         n = C.c_int64()

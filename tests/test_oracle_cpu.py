@@ -186,3 +186,48 @@ def test_golden_poisson_residual_and_field():
     efi, efj = O.efield(m, g["phi"])
     assert np.array_equal(efi, g["efi"]) and np.array_equal(efj, g["efj"])
     assert np.array_equal(O.boltzmann(g["phi"], 1e12, 2.0, 0.0), g["ne"])
+
+
+def test_oracle_samples_known_answers():
+    """updateSamples / computeFields: one particle scatters its weight bilinearly, has
+    zero spread (T = 0 where sampled, T_init elsewhere) and counts once in its cell; a
+    Maxwellian sample gives back its temperature."""
+    spec = W.es_pic_mesh(11, 11, 1e-3)
+    m = O.OMesh(spec.ni, spec.nj, spec.x0, spec.dh, spec.domain, spec.node_type, spec.face_type)
+    P = np.zeros((1, 12))
+    P[0, 6:8] = (2.25, 3.5)
+    P[0, 3:6] = (100.0, -50.0, 10.0)
+    P[0, 9] = 2.0
+    P[0, 10] = 1
+    sums = O.update_samples(m, P)
+    sums = O.update_samples(m, P, sums)   # two samples of the same state
+    ni = spec.ni
+    c = sums[0].reshape(spec.nj, ni)
+    assert c[3, 2] == pytest.approx(2 * 2.0 * 0.75 * 0.5)
+    assert c[3, 3] == pytest.approx(2 * 2.0 * 0.25 * 0.5)
+    assert c[4, 3] == pytest.approx(2 * 2.0 * 0.25 * 0.5)
+    assert c[4, 2] == pytest.approx(2 * 2.0 * 0.75 * 0.5)
+    assert sums[7].reshape(spec.nj, ni)[3, 2] == 2 and sums[7].sum() == 2
+    vol = O.node_volumes(m)
+    f = O.compute_fields(sums, 2, vol, 16 * 1.66053886e-27, 300.0)
+    sampled = sums[0] > 0
+    assert np.allclose(f["T"][sampled], 0.0, atol=1e-9)
+    assert np.all(f["T"][~sampled] == 300.0)
+    assert np.allclose(f["u-ave"][sampled], 100.0) and np.allclose(f["v-ave"][sampled], -50.0)
+    assert f["mpc"].reshape(spec.nj, ni)[3, 2] == 1.0
+    assert np.allclose(f["nd-ave"], sums[0] / 2 / vol)
+    # Maxwellian at 500 K: T from the sampled second moments
+    rng = np.random.default_rng(5)
+    n = 200_000
+    mass = 16 * 1.66053886e-27
+    Q = np.zeros((n, 12))
+    Q[:, 6] = rng.uniform(1, 9, n)
+    Q[:, 7] = rng.uniform(1, 9, n)
+    Q[:, 3:6] = rng.normal(0, np.sqrt(1.3806503e-23 * 500 / mass), (n, 3)) + [700.0, 0, 0]
+    Q[:, 9] = 1.0
+    Q[:, 10] = 1
+    g = O.compute_fields(O.update_samples(m, Q), 1, vol, mass, 300.0)
+    inner = (np.arange(spec.nj)[:, None] >= 2) & (np.arange(spec.nj)[:, None] <= 8) & \
+            (np.arange(ni)[None, :] >= 2) & (np.arange(ni)[None, :] <= 8)
+    assert np.mean(g["T"].reshape(spec.nj, ni)[inner]) == pytest.approx(500.0, rel=0.02)
+    assert np.mean(g["u-ave"].reshape(spec.nj, ni)[inner]) == pytest.approx(700.0, rel=0.02)

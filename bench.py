@@ -195,6 +195,78 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
             "mesh": [spec.ni, spec.nj], "tol": tol, "particles_end": km.get_np(), "wall_s": wall}
 
 
+def dsmc_jet_bench(steps=20, warmup=3, n_particles=16 * 1024 * 1024, seed=0):
+    """The DSMC expanding-jet workload: Argon on the 513x257 axisymmetric (ZR) mesh, inlet
+    r < 5 mm at 1e22 m^-3 / 300 K / 500 m/s sampled on the device every step, diffuse
+    walls at 300 K, VHS NTC collisions (Bird 4.63 cross-section) per cell, 16M preloaded
+    macroparticles.  One step = inlet source + push (with wall hits) + DSMC (counting
+    sort into cells + NTC).  Throughput in particle-steps/s over device-resident
+    particles; k_dsmc's roofline from 28 B per particle (velocity read + write, cell) plus
+    16 B per cell of per-cell state."""
+    import torch
+    from starfish_gb300 import abi
+    from starfish_gb300 import workloads as W
+    from starfish_gb300.plugin import DSMC, GpuDomain, KineticMaterial
+    cfg = W.config2(n_particles)
+    spec = cfg.mesh
+    dom = GpuDomain(spec, device=0)
+    try:
+        dom.set_efield(np.zeros(spec.nn), np.zeros(spec.nn))
+        km = KineticMaterial(dom, cfg.mass, 0.0, cfg.spwt, capacity=int(n_particles * 1.3) + 4096)
+        vth = np.sqrt(2 * W.KB * cfg.wall_temp / cfg.mass)
+        for sidx in range(spec.seg_xy.shape[0]):
+            km.set_surface(sidx, abi.SURF_DIFFUSE, vth=vth, c_rest=1.0, c_accom=1.0)
+        chunk = 4 * 1024 * 1024
+        for c0 in range(0, n_particles, chunk):
+            pos, vel = W.jet_particles(cfg, min(chunk, n_particles - c0), seed + c0)
+            km.add_particles(pos, vel, rewind=False, dt=cfg.dt)
+        ds = DSMC(dom, km, model=abi.SIGMA_BIRD463, diam=cfg.diam, T_ref=cfg.T_ref, omega=cfg.omega)
+
+        def step():
+            km.sample_maxwellian_source(cfg.inlet, cfg.den, cfg.v_drift, cfg.temp, cfg.dt)
+            np0 = km.get_np()
+            km.update_fields(cfg.dt, stats=False)
+            nc = ds.perform(cfg.dt)
+            return np0, nc
+
+        for _ in range(max(warmup, 3)):
+            step()
+        ext = torch.cuda.ExternalStream(dom.stream())
+        dom.timing(True)
+        dom.timing_reset()
+        l0 = dom.launches()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        psteps, colls = 0, 0
+        e0.record(ext)
+        for _ in range(steps):
+            np0, nc = step()
+            psteps += np0
+            colls += nc
+        e1.record(ext)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        launches = dom.launches() - l0
+        k = {name: dom.kernel_time(name) for name in ("push", "push_slow", "sort", "finalize", "dsmc")}
+        dom.timing(False)
+        avg_np = psteps / steps
+        nc_cells = (spec.ni - 1) * (spec.nj - 1)
+        dsmc_ms = k["dsmc"][0] / max(k["dsmc"][1], 1)
+        alg = 28.0 * avg_np + 16.0 * nc_cells
+        peak, peak_kind = measured_peaks()
+        return {"metric": "particle-steps/s (source + push + DSMC)", "value": psteps / (ms / 1e3),
+                "unit": "particle-steps/s", "ms_per_step": ms / steps, "steps": steps,
+                "workload": cfg.name, "mesh": [spec.ni, spec.nj], "particles_avg": avg_np,
+                "collisions_per_step": colls / steps, "dt_s": cfg.dt,
+                "kernel_ms": {n: v[0] / max(v[1], 1) for n, v in k.items()},
+                "roofline_dsmc": {"bound": "hbm", "achieved": alg / (dsmc_ms / 1e3) / 1e9, "peak": peak,
+                                  "unit": "GB/s", "frac": alg / (dsmc_ms / 1e3) / 1e9 / peak,
+                                  "peak_kind": peak_kind, "alg_bytes_per_launch": alg},
+                "gpu_launches": launches}
+    finally:
+        dom.close()
+
+
 def cpu_baseline_sample(cfg, efi, efj, n_sample, threads, steps=1, seed=1):
     """The oracle port (reference algorithm, FP64 AoS) on a bounded sample of the workload."""
     from oracle import oracle as O
@@ -269,6 +341,7 @@ def main():
     ap.add_argument("--particles", type=int, default=64 * 1024 * 1024)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--poisson-steps", type=int, default=2000)
+    ap.add_argument("--dsmc-steps", type=int, default=20)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -395,6 +468,8 @@ def main():
     if args.poisson_steps > 0:
         line["poisson"] = learned_poisson_bench(cfg, dom, km, steps=args.poisson_steps,
                                                 train_steps=min(500, args.poisson_steps // 4))
+    if args.dsmc_steps > 0:
+        line["dsmc"] = dsmc_jet_bench(steps=args.dsmc_steps)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n_sample = 16 * 1024 * 1024

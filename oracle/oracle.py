@@ -85,7 +85,7 @@ def _declare(L):
     L.orc_compute_fields.argtypes = [C.c_int, d, C.c_int, d, C.c_double, C.c_double, d]
     L.orc_add_particles.argtypes = [C.c_int, C.c_int, d, d, C.c_int, i8, i8, d, d, C.c_double,
                                     C.c_double, C.c_double, C.c_int, d]
-    L.orc_maxwellian_source.argtypes = [C.c_int64, d, C.c_double, C.c_double, C.c_double,
+    L.orc_maxwellian_source.argtypes = [C.c_int64, C.c_int, d, C.c_double, C.c_double, C.c_double,
                                         C.c_double, C.c_double, C.c_double, d, C.c_int, d]
     L.orc_maxwellian_source.restype = C.c_int
     L.orc_dsmc.argtypes = [C.c_int, C.c_int, d, C.c_int, d, C.c_double, C.c_double, C.c_double,
@@ -265,11 +265,11 @@ def add_particles(m: OMesh, efi, efj, q, mass, dt, parts):
                             parts.reshape(-1))
 
 
-def maxwellian_source(seed, seg_xy, den, v_drift, temp, mass, spwt, dt, rem=0.0, cap=1 << 20):
+def maxwellian_source(seed, seg_xy, den, v_drift, temp, mass, spwt, dt, rem=0.0, cap=1 << 20, domain=0):
     r = np.array([rem], np.float64)
     parts = np.zeros((cap, 12))
-    n = lib().orc_maxwellian_source(int(seed), _f64(seg_xy), den, v_drift, temp, mass, spwt, dt,
-                                    r, cap, parts.reshape(-1))
+    n = lib().orc_maxwellian_source(int(seed), int(domain), _f64(seg_xy), den, v_drift, temp, mass, spwt,
+                                    dt, r, cap, parts.reshape(-1))
     return parts[:n].copy(), float(r[0])
 
 

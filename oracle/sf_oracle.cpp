@@ -1192,7 +1192,16 @@ void orc_add_particles(int ni, int nj, const double* x0, const double* dh, int d
 // MaxwellianSource.sampleParticle + Source.regenerate/sampleKinetic for a straight inlet
 // segment (MaxwellianSource.java:93-125; Source.java:123-198).  Writes up to cap particles
 // (pos, vel, mpw; lc/dt unset: call orc_add_particles next).  rem: in/out remainder.
-int orc_maxwellian_source(int64_t seed, const double* seg_xy, double den, double v_drift,
+// Spline.randomT on an axisymmetric mesh (core/boundaries/Spline.java:582-641): t such
+// that the frustum area of [0, t] is the fraction f of the segment's; the root of
+// t (2 r1 + t (r2 - r1)) / (r1 + r2) = f (the reference finds it by secant steps).
+static double frustum_t(double f, double r1, double r2) {
+  const double S = r1 + r2;
+  if (!(S > 0.0) || f <= 0.0) return f;
+  return f * S / (r1 + std::sqrt(r1 * r1 + (r2 - r1) * f * S));
+}
+
+int orc_maxwellian_source(int64_t seed, int domain, const double* seg_xy, double den, double v_drift,
                           double temp, double mass, double spwt, double dt, double* rem, int cap,
                           double* parts) {
   JRandom r;
@@ -1203,7 +1212,10 @@ int orc_maxwellian_source(int64_t seed, const double* seg_xy, double den, double
   seg_init(s);
   double len = std::sqrt((x2[0] - x1[0]) * (x2[0] - x1[0]) + (x2[1] - x1[1]) * (x2[1] - x1[1]));
   double v_mean = std::sqrt(8 * KB * temp / (PI * mass));
-  double A = len;  // XY area per unit depth (LinearSegment.area, LinearSegment.java:51-54)
+  // LinearSegment.area (LinearSegment.java:51-76): length x 1 m in XY, the lateral area
+  // pi (r1 + r2) L of the swept frustum in RZ / ZR
+  const double r1 = domain == DOM_RZ ? x1[0] : x1[1], r2 = domain == DOM_RZ ? x2[0] : x2[1];
+  double A = domain == DOM_XY ? len : PI * (r1 + r2) * len;
   double mdot = den * A * (v_drift + v_mean / 4) * mass;
   double v_th = std::sqrt(2 * KB * temp / mass);
   double mp = (mdot * dt) / (mass * spwt) + *rem;
@@ -1213,6 +1225,7 @@ int orc_maxwellian_source(int64_t seed, const double* seg_xy, double den, double
   Particle* P = reinterpret_cast<Particle*>(parts);
   for (int k = 0; k < num && out < cap; k++) {
     double t = r.nextDouble();  // Boundary.randomT for a single linear segment
+    if (domain != DOM_XY) t = frustum_t(t, r1, r2);
     Particle& p = P[out];
     memset(&p, 0, sizeof(Particle));
     p.pos[0] = x1[0] + t * (x2[0] - x1[0]);

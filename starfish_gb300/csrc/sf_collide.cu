@@ -79,64 +79,105 @@ __device__ inline void elastic_vr(Philox& rng, float vss_inv, const float g[3], 
   }
 }
 
-// One thread per cell, the cell's pairs in sequence as in collideCell.
-__global__ void k_dsmc(MeshView m, ParticlesView P, const int* __restrict__ bins, int ntx, int nkeys,
-                       const double* __restrict__ cell_vol, double2* __restrict__ state, double2* __restrict__ counts,
-                       SigmaDev sg, double spwt, double dt, uint64_t seed, uint32_t step,
-                       unsigned long long* __restrict__ n_coll) {
-  for (int key = blockIdx.x * blockDim.x + threadIdx.x; key < nkeys; key += gridDim.x * blockDim.x) {
+__device__ inline unsigned gcd_u(unsigned a, unsigned b) {
+  while (b) {
+    const unsigned t = a % b;
+    a = b;
+    b = t;
+  }
+  return a;
+}
+
+// DSMC.collideCell (DSMC.java:259-350) with one warp per cell.  Warps take cells from a
+// work counter (the cells of a jet hold from a few to thousands of particles).  The NTC
+// selection count and the acceptance sigma g / (sigma g)max are the reference's; the
+// nsel candidate pairs are drawn in rounds of up to 32 disjoint pairs, one per lane: a
+// round uses the cell's particles s + k t (mod np), k < 2 m, with random s and a random
+// stride t coprime to np, so its 2 m particles are distinct and the pairs can collide
+// in parallel.  Each pair is two distinct random particles of the cell, as in the
+// reference; only pairs within one round cannot share a particle.
+__global__ void __launch_bounds__(128) k_dsmc(MeshView m, ParticlesView P, const int* __restrict__ bins, int ntx,
+                                              int nkeys, const double* __restrict__ cell_vol,
+                                              double2* __restrict__ state, double2* __restrict__ counts,
+                                              SigmaDev sg, double spwt, double dt, uint64_t seed, uint32_t step,
+                                              unsigned long long* __restrict__ n_coll, unsigned* __restrict__ work) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int key = 0;
+    if (lane == 0) key = (int)atomicAdd(work, 1u);
+    key = __shfl_sync(FULL, key, 0);
+    if (key >= nkeys) break;
     int i, j;
     key_cell((uint32_t)key, ntx, i, j);
     if (i >= m.ni - 1 || j >= m.nj - 1) continue;
     const int c = j * (m.ni - 1) + i;
     const int start = bins[key], np = bins[key + 1] - start;
+    if (np < 2) continue;  // the reference returns before updating rem (:293-296)
     double2 st = state[c];  // x: (sigma g)max, y: remainder
     const double npd = (double)np;
     // equal weights: Pab = Pba = 1, denominator Pab + (w2/w1) Pba = 2 (DSMC.java:276-286)
     const double nsel_f = ((npd * spwt / cell_vol[c]) * npd * dt * st.x) / 2.0 + st.y;
     int nsel = (int)nsel_f;
-    if (np < 2) continue;  // the reference returns before updating rem (:293-296)
     st.y = nsel_f - nsel;
     if ((double)nsel > npd * npd) {
       nsel = (int)(npd * npd);
       st.y = 0.0;
     }
-    Philox rng(seed, RNG_DSMC, (uint64_t)c, step);
+    Philox rng(seed, RNG_DSMC, (uint64_t)c * 32u + (uint64_t)lane, step);
     float smax_new = 0.f;
     const float smax = (float)st.x;
     int ncol = 0;
-    for (int k = 0; k < nsel; k++) {
-      const int p1 = min((int)(rng.uniform() * npd), np - 1);
-      int p2 = p1;
-      for (int tries = 0; tries < 64 && p2 == p1; tries++) p2 = min((int)(rng.uniform() * npd), np - 1);
-      if (p2 == p1) continue;
-      const int64_t a = start + p1, b = start + p2;
-      float2 va = P.vxy[a], vb = P.vxy[b];
-      float wa = P.vz[a], wb = P.vz[b];
-      const float g[3] = {va.x - vb.x, va.y - vb.y, wa - wb};
-      const float g_mag = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-      const float sigma_cr = g_mag * sigma_eval(sg, g_mag);
-      smax_new = fmaxf(smax_new, sigma_cr);
-      if ((float)rng.uniform() < sigma_cr / smax) {
-        // ModelElastic.perform with equal masses and weights (DSMC.java:373-415)
-        const float vc[3] = {0.5f * (va.x + vb.x), 0.5f * (va.y + vb.y), 0.5f * (wa + wb)};
-        float vr[3];
-        elastic_vr(rng, sg.vss_inv, g, g_mag, vr);
-        P.vxy[a] = make_float2(vc[0] + 0.5f * vr[0], vc[1] + 0.5f * vr[1]);
-        P.vz[a] = vc[2] + 0.5f * vr[2];
-        P.vxy[b] = make_float2(vc[0] - 0.5f * vr[0], vc[1] - 0.5f * vr[1]);
-        P.vz[b] = vc[2] - 0.5f * vr[2];
-        ncol++;
+    const int per_round = min(32, np / 2);
+    for (int k0 = 0; k0 < nsel; k0 += per_round) {
+      const int mr = min(per_round, nsel - k0);
+      unsigned s0 = 0, t0 = 1;
+      if (lane == 0) {
+        s0 = (unsigned)min((int)(rng.uniform() * npd), np - 1);
+        t0 = 1u + (unsigned)min((int)(rng.uniform() * (npd - 1.0)), np - 2);
+        for (int tries = 0; tries < 64 && gcd_u(t0, (unsigned)np) != 1u; tries++) t0 = t0 % (unsigned)(np - 1) + 1u;
+        if (gcd_u(t0, (unsigned)np) != 1u) t0 = 1u;
       }
+      s0 = __shfl_sync(FULL, s0, 0);
+      t0 = __shfl_sync(FULL, t0, 0);
+      if (lane < mr) {
+        const int p1 = (int)((s0 + (uint64_t)(2 * lane) * t0) % (uint64_t)np);
+        const int p2 = (int)((s0 + (uint64_t)(2 * lane + 1) * t0) % (uint64_t)np);
+        const int64_t a = start + p1, b = start + p2;
+        const float2 va = P.vxy[a], vb = P.vxy[b];
+        const float wa = P.vz[a], wb = P.vz[b];
+        const float g[3] = {va.x - vb.x, va.y - vb.y, wa - wb};
+        const float g_mag = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+        const float sigma_cr = g_mag * sigma_eval(sg, g_mag);
+        smax_new = fmaxf(smax_new, sigma_cr);
+        if ((float)rng.uniform() < sigma_cr / smax) {
+          // ModelElastic.perform with equal masses and weights (DSMC.java:373-415)
+          const float vc[3] = {0.5f * (va.x + vb.x), 0.5f * (va.y + vb.y), 0.5f * (wa + wb)};
+          float vr[3];
+          elastic_vr(rng, sg.vss_inv, g, g_mag, vr);
+          P.vxy[a] = make_float2(vc[0] + 0.5f * vr[0], vc[1] + 0.5f * vr[1]);
+          P.vz[a] = vc[2] + 0.5f * vr[2];
+          P.vxy[b] = make_float2(vc[0] - 0.5f * vr[0], vc[1] - 0.5f * vr[1]);
+          P.vz[b] = vc[2] - 0.5f * vr[2];
+          ncol++;
+        }
+      }
+      __syncwarp();  // this round's velocities are visible to the next round's lanes
     }
-    if (smax_new > 0.f) st.x = (double)smax_new;
-    state[c] = st;
-    if (ncol) {
-      double2 cs = counts[c];
-      cs.x += ncol;
-      cs.y += ncol * spwt;  // 0.5 (w1 + w2) per collision
-      counts[c] = cs;
-      atomicAdd(n_coll, (unsigned long long)ncol);
+    for (int o = 16; o > 0; o >>= 1) {
+      smax_new = fmaxf(smax_new, __shfl_xor_sync(FULL, smax_new, o));
+      ncol += __shfl_xor_sync(FULL, ncol, o);
+    }
+    if (lane == 0) {
+      if (smax_new > 0.f) st.x = (double)smax_new;
+      state[c] = st;
+      if (ncol) {
+        double2 cs = counts[c];
+        cs.x += ncol;
+        cs.y += ncol * spwt;  // 0.5 (w1 + w2) per collision
+        counts[c] = cs;
+        atomicAdd(n_coll, (unsigned long long)ncol);
+      }
     }
   }
 }
@@ -310,12 +351,14 @@ int sf_dsmc(sf_ctx* ctx, int32_t sid, const sf_sigma* sigma, double dt, double s
   SfDsmcState* st = dsmc_state(ctx, sid, sig_cr_max0);
   // DSMC.perform(mesh) bins particles by cell on every call: the counting sort
   launch_sort(ctx, sp);
-  SF_CUDA(cudaMemsetAsync(ctx->counters + 6, 0, sizeof(unsigned long long), ctx->stream));
+  // counters[6]: collisions; counters[5] (as unsigned): the warps' cell work counter
+  SF_CUDA(cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), ctx->stream));
   {
     TimedScope ts(ctx, "dsmc");
-    k_dsmc<<<grid_for(ctx->nkeys, 128, ctx->num_sms * 16), 128, 0, ctx->stream>>>(
+    k_dsmc<<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(
         ctx->mesh_view(), sp->cur, ctx->bins, ctx->ntx, ctx->nkeys, st->cell_vol, st->state, st->counts, sg,
-        sp->spwt, dt, ctx->seed ^ 0xD5C0ULL, ctx->rng_epoch++, ctx->counters + 6);
+        sp->spwt, dt, ctx->seed ^ 0xD5C0ULL, ctx->rng_epoch++, ctx->counters + 6,
+        reinterpret_cast<unsigned*>(ctx->counters + 5));
     ctx->launches++;
   }
   SF_CUDA(cudaGetLastError());

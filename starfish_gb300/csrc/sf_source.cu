@@ -25,7 +25,19 @@ struct InjectArgs {
   uint64_t seed;
   uint32_t step;
   int64_t base;          // first free slot
+  int axi;               // RZ / ZR: positions uniform in the swept (frustum) area
+  double r1, r2;         // radii of the segment ends
 };
+
+// Spline.randomT on an axisymmetric mesh (core/boundaries/Spline.java:582-641) picks t so
+// that the frustum area swept by [0, t] is the fraction f of the segment's area:
+// t (2 r1 + t (r2 - r1)) / (r1 + r2) = f.  The reference solves it by secant steps to
+// 1e-6; this is the root of the same quadratic in a cancellation-free form.
+__device__ inline double frustum_t(double f, double r1, double r2) {
+  const double S = r1 + r2;
+  if (!(S > 0.0) || f <= 0.0) return f;
+  return f * S / (r1 + sqrt(r1 * r1 + (r2 - r1) * f * S));
+}
 
 __device__ inline double maxw1d_unit(Philox& r) {
   // Utils.SampleMaxw1D(1): sqrt(1/2) * (sum of 12 uniforms - 6)
@@ -38,7 +50,8 @@ __global__ void k_inject_maxwellian(MeshView m, ParticlesView P, InjectArgs a, i
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   Philox rng(a.seed, RNG_INJECT, (uint64_t)k, a.step);
-  const double t = rng.uniform();  // Boundary.randomT on a single segment
+  double t = rng.uniform();  // Boundary.randomT on a single segment
+  if (a.axi) t = frustum_t(t, a.r1, a.r2);
   double px = a.x1 + t * (a.x2 - a.x1), py = a.y1 + t * (a.y2 - a.y1);
   double vx = 0, vy = 0, vz = 0;
   for (int tries = 0; tries < 64; tries++) {
@@ -109,6 +122,9 @@ extern "C" int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg,
   a.seed = ctx->seed ^ (0x9E3779B97F4A7C15ULL * (uint64_t)(sid + 1));
   a.step = ctx->rng_epoch++;
   a.base = sp->n;
+  a.axi = ctx->domain != SF_DOMAIN_XY;
+  a.r1 = ctx->domain == SF_DOMAIN_RZ ? seg[0] : seg[1];
+  a.r2 = ctx->domain == SF_DOMAIN_RZ ? seg[2] : seg[3];
   unsigned long long* cnt = ctx->counters + 7;
   SF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), ctx->stream));
   k_inject_maxwellian<<<(int)((num + 255) / 256), 256, 0, ctx->stream>>>(ctx->mesh_view(), sp->cur, a, (int)num, cnt);

@@ -261,27 +261,27 @@ def _jet_content(m: MeshSpec, n_inlet, r_inlet, samples=400):
 
 
 def jet_particles(cfg: JetConfig, n, seed):
-    """n macroparticles distributed like the plume (acceptance sampling in (z, r) with the
-    axisymmetric volume weight r), drifting Maxwellian velocities at the inlet temperature."""
+    """n macroparticles distributed like the plume: each mesh cell receives a share of
+    n proportional to its content (plume density at the cell centre x the cell's volume of
+    revolution), positions uniform in z and in area of revolution (r^2) inside the cell;
+    drifting Maxwellian velocities at the inlet temperature, radial outflow from the inlet."""
     rng = np.random.default_rng(seed)
-    Lz, Lr = cfg.mesh.lengths()
-    r_in = 5e-3
+    m = cfg.mesh
+    dz, dr = m.dh
+    z0 = np.arange(m.ni - 1) * dz
+    r0 = np.arange(m.nj - 1) * dr
+    Z, R = np.meshgrid(z0 + 0.5 * dz, r0 + 0.5 * dr)
+    vol = np.pi * ((R + 0.5 * dr) ** 2 - (R - 0.5 * dr) ** 2) * dz
+    w = (_jet_density(Z, R, cfg.den, 5e-3) * vol).ravel()
+    cells = rng.choice(w.size, size=n, p=w / w.sum())
+    ci, cj = cells % (m.ni - 1), cells // (m.ni - 1)
     out = np.empty((n, 3))
-    got = 0
-    nmax = cfg.den
-    while got < n:
-        k = int((n - got) * 4) + 1024
-        z = rng.uniform(0, Lz, k)
-        r = Lr * np.sqrt(rng.uniform(0, 1, k))   # uniform in area of revolution (weight r)
-        acc = rng.uniform(0, 1, k) < _jet_density(z, r, nmax, r_in) / nmax
-        z, r = z[acc][: n - got], r[acc][: n - got]
-        out[got:got + z.size, 0] = z
-        out[got:got + z.size, 1] = r
-        got += z.size
+    out[:, 0] = z0[ci] + dz * rng.uniform(0, 1, n)
+    ra, rb = r0[cj], r0[cj] + dr
+    out[:, 1] = np.sqrt(ra ** 2 + (rb ** 2 - ra ** 2) * rng.uniform(0, 1, n))
     out[:, 2] = 0.0
     vth = np.sqrt(2 * KB * cfg.temp / cfg.mass)
     vel = rng.normal(0.0, vth * 1.2 * np.sqrt(0.5), (n, 3))
-    # radial outflow of the plume
     rr = np.sqrt(out[:, 0] ** 2 + out[:, 1] ** 2) + 1e-12
     vel[:, 0] += cfg.v_drift * out[:, 0] / rr
     vel[:, 1] += cfg.v_drift * out[:, 1] / rr

@@ -231,3 +231,22 @@ def test_oracle_samples_known_answers():
             (np.arange(ni)[None, :] >= 2) & (np.arange(ni)[None, :] <= 8)
     assert np.mean(g["T"].reshape(spec.nj, ni)[inner]) == pytest.approx(500.0, rel=0.02)
     assert np.mean(g["u-ave"].reshape(spec.nj, ni)[inner]) == pytest.approx(700.0, rel=0.02)
+
+
+def test_oracle_axisymmetric_source_area_weighted():
+    """Spline.randomT on an axisymmetric mesh: positions uniform in the swept area, so on a
+    radial inlet r in [0, R] the radius has density 2 r / R^2 (mean 2R/3, median R/sqrt 2),
+    and the flux uses the frustum area pi (r1 + r2) L."""
+    R = 5e-3
+    seg = np.array([0.0, R, 0.0, 0.0])
+    mass = 40 * 1.66053886e-27
+    parts, _ = O.maxwellian_source(7, seg, 1e22, 500.0, 300.0, mass, 1e9, 1e-6, cap=1 << 20,
+                                   domain=2)
+    r = parts[:, 1]
+    assert parts.shape[0] > 100_000
+    assert np.mean(r) == pytest.approx(2 * R / 3, rel=5e-3)
+    assert np.median(r) == pytest.approx(R / np.sqrt(2), rel=5e-3)
+    # expected count from the frustum area (here a disc of radius R)
+    v_mean = np.sqrt(8 * 1.3806503e-23 * 300.0 / (np.pi * mass))
+    expect = 1e22 * np.pi * R * R * (500.0 + v_mean / 4) * 1e-6 / 1e9
+    assert parts.shape[0] == int(expect)

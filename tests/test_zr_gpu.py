@@ -101,3 +101,26 @@ def test_zr_push_with_diffuse_walls(gpulib):
     gspeed = np.linalg.norm(gvel, axis=1)
     assert hit.sum() > 100
     assert gspeed[hit].mean() == pytest.approx(2 * vth / np.sqrt(np.pi), rel=0.1)
+
+
+def test_zr_source_area_weighted(gpulib):
+    """Device Maxwellian source on the axisymmetric jet mesh: the particle count uses the
+    frustum area pi (r1 + r2) L, and positions are uniform in the swept area (Spline.randomT
+    on RZ/ZR meshes), so on the inlet r in [0, R] the radius has density 2 r / R^2."""
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    spec = W.jet_mesh()
+    R, mass, spwt = 5e-3, 40 * 1.66053886e-27, 1e9
+    dom = GpuDomain(spec)
+    try:
+        dom.set_efield(np.zeros(spec.nn), np.zeros(spec.nn))
+        km = KineticMaterial(dom, mass, 0.0, spwt, capacity=1 << 20)
+        n = km.sample_maxwellian_source(np.array([0.0, R, 0.0, 0.0]), 1e22, 500.0, 300.0, 1e-6)
+        v_mean = np.sqrt(8 * 1.3806503e-23 * 300.0 / (np.pi * mass))
+        assert n == int(1e22 * np.pi * R * R * (500.0 + v_mean / 4) * 1e-6 / spwt)
+        lc, vel = km.download()
+        r = lc[:, 1] * spec.dh[1]
+        assert np.mean(r) == pytest.approx(2 * R / 3, rel=5e-3)
+        assert np.median(r) == pytest.approx(R / np.sqrt(2), rel=5e-3)
+        assert np.all(vel[:, 0] > 0)  # v . n > 0 on the inlet (normal +z)
+    finally:
+        dom.close()

@@ -79,6 +79,31 @@ __device__ inline void elastic_vr(Philox& rng, float vss_inv, const float g[3], 
   }
 }
 
+constexpr int DSMC_HEAVY_NSEL = 1024;    // candidate pairs beyond which a cell gets a CTA
+constexpr int DSMC_HEAVY_THREADS = 512;
+
+// One candidate pair (a, b) of collideCell: sigma g, the NTC acceptance against the
+// cell's (sigma g)max, and ModelElastic.perform with equal masses and weights
+// (DSMC.java:373-415).  Returns whether the pair collided.
+__device__ inline bool collide_pair(ParticlesView& P, int64_t a, int64_t b, const SigmaDev& sg, float smax, Philox& rng,
+                                    float& smax_new) {
+  const float2 va = P.vxy[a], vb = P.vxy[b];
+  const float wa = P.vz[a], wb = P.vz[b];
+  const float g[3] = {va.x - vb.x, va.y - vb.y, wa - wb};
+  const float g_mag = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+  const float sigma_cr = g_mag * sigma_eval(sg, g_mag);
+  smax_new = fmaxf(smax_new, sigma_cr);
+  if (!((float)rng.uniform() < sigma_cr / smax)) return false;
+  const float vc[3] = {0.5f * (va.x + vb.x), 0.5f * (va.y + vb.y), 0.5f * (wa + wb)};
+  float vr[3];
+  elastic_vr(rng, sg.vss_inv, g, g_mag, vr);
+  P.vxy[a] = make_float2(vc[0] + 0.5f * vr[0], vc[1] + 0.5f * vr[1]);
+  P.vz[a] = vc[2] + 0.5f * vr[2];
+  P.vxy[b] = make_float2(vc[0] - 0.5f * vr[0], vc[1] - 0.5f * vr[1]);
+  P.vz[b] = vc[2] - 0.5f * vr[2];
+  return true;
+}
+
 __device__ inline unsigned gcd_u(unsigned a, unsigned b) {
   while (b) {
     const unsigned t = a % b;
@@ -88,8 +113,9 @@ __device__ inline unsigned gcd_u(unsigned a, unsigned b) {
   return a;
 }
 
-// DSMC.collideCell (DSMC.java:259-350) with one warp per cell.  Warps take cells from a
-// work counter (the cells of a jet hold from a few to thousands of particles).  The NTC
+// DSMC.collideCell (DSMC.java:259-350) with one warp per cell, warps striding over the
+// cells; cells with more than DSMC_HEAVY_NSEL candidate pairs (dense cells of a jet hold
+// thousands of particles) are listed for k_dsmc_heavy instead.  The NTC
 // selection count and the acceptance sigma g / (sigma g)max are the reference's; the
 // nsel candidate pairs are drawn in rounds of up to 32 disjoint pairs, one per lane: a
 // round uses the cell's particles s + k t (mod np), k < 2 m, with random s and a random
@@ -100,14 +126,12 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, ParticlesView P, const
                                               int nkeys, const double* __restrict__ cell_vol,
                                               double2* __restrict__ state, double2* __restrict__ counts,
                                               SigmaDev sg, double spwt, double dt, uint64_t seed, uint32_t step,
-                                              unsigned long long* __restrict__ n_coll, unsigned* __restrict__ work) {
+                                              unsigned long long* __restrict__ n_coll, int* __restrict__ heavy,
+                                              unsigned* __restrict__ n_heavy, int heavy_cap) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  for (;;) {
-    int key = 0;
-    if (lane == 0) key = (int)atomicAdd(work, 1u);
-    key = __shfl_sync(FULL, key, 0);
-    if (key >= nkeys) break;
+  const int warps = (int)(gridDim.x * blockDim.x) >> 5;
+  for (int key = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); key < nkeys; key += warps) {
     int i, j;
     key_cell((uint32_t)key, ntx, i, j);
     if (i >= m.ni - 1 || j >= m.nj - 1) continue;
@@ -119,6 +143,16 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, ParticlesView P, const
     // equal weights: Pab = Pba = 1, denominator Pab + (w2/w1) Pba = 2 (DSMC.java:276-286)
     const double nsel_f = ((npd * spwt / cell_vol[c]) * npd * dt * st.x) / 2.0 + st.y;
     int nsel = (int)nsel_f;
+    if (nsel > DSMC_HEAVY_NSEL && np >= 128) {
+      // many rounds: hand the cell to a whole CTA (k_dsmc_heavy), which recomputes nsel
+      int slot = 0;
+      if (lane == 0) slot = (int)atomicAdd(n_heavy, 1u);
+      slot = __shfl_sync(FULL, slot, 0);
+      if (slot < heavy_cap) {
+        if (lane == 0) heavy[slot] = key;
+        continue;
+      }
+    }
     st.y = nsel_f - nsel;
     if ((double)nsel > npd * npd) {
       nsel = (int)(npd * npd);
@@ -143,24 +177,7 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, ParticlesView P, const
       if (lane < mr) {
         const int p1 = (int)((s0 + (uint64_t)(2 * lane) * t0) % (uint64_t)np);
         const int p2 = (int)((s0 + (uint64_t)(2 * lane + 1) * t0) % (uint64_t)np);
-        const int64_t a = start + p1, b = start + p2;
-        const float2 va = P.vxy[a], vb = P.vxy[b];
-        const float wa = P.vz[a], wb = P.vz[b];
-        const float g[3] = {va.x - vb.x, va.y - vb.y, wa - wb};
-        const float g_mag = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-        const float sigma_cr = g_mag * sigma_eval(sg, g_mag);
-        smax_new = fmaxf(smax_new, sigma_cr);
-        if ((float)rng.uniform() < sigma_cr / smax) {
-          // ModelElastic.perform with equal masses and weights (DSMC.java:373-415)
-          const float vc[3] = {0.5f * (va.x + vb.x), 0.5f * (va.y + vb.y), 0.5f * (wa + wb)};
-          float vr[3];
-          elastic_vr(rng, sg.vss_inv, g, g_mag, vr);
-          P.vxy[a] = make_float2(vc[0] + 0.5f * vr[0], vc[1] + 0.5f * vr[1]);
-          P.vz[a] = vc[2] + 0.5f * vr[2];
-          P.vxy[b] = make_float2(vc[0] - 0.5f * vr[0], vc[1] - 0.5f * vr[1]);
-          P.vz[b] = vc[2] - 0.5f * vr[2];
-          ncol++;
-        }
+        if (collide_pair(P, start + p1, start + p2, sg, smax, rng, smax_new)) ncol++;
       }
       __syncwarp();  // this round's velocities are visible to the next round's lanes
     }
@@ -175,6 +192,90 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, ParticlesView P, const
         double2 cs = counts[c];
         cs.x += ncol;
         cs.y += ncol * spwt;  // 0.5 (w1 + w2) per collision
+        counts[c] = cs;
+        atomicAdd(n_coll, (unsigned long long)ncol);
+      }
+    }
+  }
+}
+
+// The cells handed over by k_dsmc, one CTA of DSMC_HEAVY_THREADS per cell: rounds of up
+// to DSMC_HEAVY_THREADS disjoint pairs (same selection as k_dsmc), the CTA synchronising
+// between rounds.
+__global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(
+    MeshView m, ParticlesView P, const int* __restrict__ bins, int ntx, const double* __restrict__ cell_vol,
+    double2* __restrict__ state, double2* __restrict__ counts, SigmaDev sg, double spwt, double dt, uint64_t seed,
+    uint32_t step, unsigned long long* __restrict__ n_coll, const int* __restrict__ heavy,
+    const unsigned* __restrict__ n_heavy, int heavy_cap, unsigned* __restrict__ work) {
+  __shared__ int s_idx;
+  __shared__ unsigned s_s0, s_t0;
+  __shared__ float s_max[DSMC_HEAVY_THREADS / 32];
+  __shared__ int s_n[DSMC_HEAVY_THREADS / 32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int nh = min((int)*n_heavy, heavy_cap);
+  for (;;) {
+    if (tid == 0) s_idx = (int)atomicAdd(work, 1u);
+    __syncthreads();
+    const int idx = s_idx;
+    __syncthreads();
+    if (idx >= nh) break;
+    const int key = heavy[idx];
+    int i, j;
+    key_cell((uint32_t)key, ntx, i, j);
+    const int c = j * (m.ni - 1) + i;
+    const int start = bins[key], np = bins[key + 1] - start;
+    double2 st = state[c];
+    const double npd = (double)np;
+    const double nsel_f = ((npd * spwt / cell_vol[c]) * npd * dt * st.x) / 2.0 + st.y;
+    int nsel = (int)nsel_f;
+    st.y = nsel_f - nsel;
+    if ((double)nsel > npd * npd) {
+      nsel = (int)(npd * npd);
+      st.y = 0.0;
+    }
+    Philox rng(seed, RNG_DSMC_HEAVY, (uint64_t)c * DSMC_HEAVY_THREADS + (uint64_t)tid, step);
+    float smax_new = 0.f;
+    const float smax = (float)st.x;
+    int ncol = 0;
+    const int per_round = min(DSMC_HEAVY_THREADS, np / 2);
+    for (int k0 = 0; k0 < nsel; k0 += per_round) {
+      const int mr = min(per_round, nsel - k0);
+      if (tid == 0) {
+        unsigned s0 = (unsigned)min((int)(rng.uniform() * npd), np - 1);
+        unsigned t0 = 1u + (unsigned)min((int)(rng.uniform() * (npd - 1.0)), np - 2);
+        for (int tries = 0; tries < 64 && gcd_u(t0, (unsigned)np) != 1u; tries++) t0 = t0 % (unsigned)(np - 1) + 1u;
+        if (gcd_u(t0, (unsigned)np) != 1u) t0 = 1u;
+        s_s0 = s0;
+        s_t0 = t0;
+      }
+      __syncthreads();
+      if (tid < mr) {
+        const int p1 = (int)((s_s0 + (uint64_t)(2 * tid) * s_t0) % (uint64_t)np);
+        const int p2 = (int)((s_s0 + (uint64_t)(2 * tid + 1) * s_t0) % (uint64_t)np);
+        if (collide_pair(P, start + p1, start + p2, sg, smax, rng, smax_new)) ncol++;
+      }
+      __syncthreads();  // velocities and s_s0 / s_t0 of this round are done with
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      smax_new = fmaxf(smax_new, __shfl_xor_sync(0xffffffffu, smax_new, o));
+      ncol += __shfl_xor_sync(0xffffffffu, ncol, o);
+    }
+    if (lane == 0) {
+      s_max[wid] = smax_new;
+      s_n[wid] = ncol;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int w = 1; w < DSMC_HEAVY_THREADS / 32; w++) {
+        smax_new = fmaxf(smax_new, s_max[w]);
+        ncol += s_n[w];
+      }
+      if (smax_new > 0.f) st.x = (double)smax_new;
+      state[c] = st;
+      if (ncol) {
+        double2 cs = counts[c];
+        cs.x += ncol;
+        cs.y += ncol * spwt;
         counts[c] = cs;
         atomicAdd(n_coll, (unsigned long long)ncol);
       }
@@ -351,15 +452,22 @@ int sf_dsmc(sf_ctx* ctx, int32_t sid, const sf_sigma* sigma, double dt, double s
   SfDsmcState* st = dsmc_state(ctx, sid, sig_cr_max0);
   // DSMC.perform(mesh) bins particles by cell on every call: the counting sort
   launch_sort(ctx, sp);
-  // counters[6]: collisions; counters[5] (as unsigned): the warps' cell work counter
-  SF_CUDA(cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), ctx->stream));
+  // counters[6]: collisions; as unsigned: [3] the number of heavy cells, [4] the
+  // heavy-cell work counter.  The heavy-cell list lives
+  // in bins_tmp (the sort's write cursors, free once the particles are binned).
+  SF_CUDA(cudaMemsetAsync(ctx->counters + 3, 0, 4 * sizeof(unsigned long long), ctx->stream));
+  unsigned* n_heavy = reinterpret_cast<unsigned*>(ctx->counters + 3);
+  const uint32_t epoch = ctx->rng_epoch++;
+  const uint64_t seed = ctx->seed ^ 0xD5C0ULL;
   {
     TimedScope ts(ctx, "dsmc");
     k_dsmc<<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(
         ctx->mesh_view(), sp->cur, ctx->bins, ctx->ntx, ctx->nkeys, st->cell_vol, st->state, st->counts, sg,
-        sp->spwt, dt, ctx->seed ^ 0xD5C0ULL, ctx->rng_epoch++, ctx->counters + 6,
-        reinterpret_cast<unsigned*>(ctx->counters + 5));
-    ctx->launches++;
+        sp->spwt, dt, seed, epoch, ctx->counters + 6, ctx->bins_tmp, n_heavy, ctx->nkeys);
+    k_dsmc_heavy<<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(
+        ctx->mesh_view(), sp->cur, ctx->bins, ctx->ntx, st->cell_vol, st->state, st->counts, sg, sp->spwt, dt, seed,
+        epoch, ctx->counters + 6, ctx->bins_tmp, n_heavy, ctx->nkeys, reinterpret_cast<unsigned*>(ctx->counters + 4));
+    ctx->launches += 2;
   }
   SF_CUDA(cudaGetLastError());
   unsigned long long nc = 0;

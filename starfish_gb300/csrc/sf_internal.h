@@ -153,7 +153,7 @@ struct Philox {
 };
 
 // RNG stream identifiers
-enum : uint32_t { RNG_SURFACE = 1, RNG_DSMC = 2, RNG_MCC = 3, RNG_INJECT = 4 };
+enum : uint32_t { RNG_SURFACE = 1, RNG_DSMC = 2, RNG_MCC = 3, RNG_INJECT = 4, RNG_DSMC_HEAVY = 5 };
 
 }  // namespace sf
 

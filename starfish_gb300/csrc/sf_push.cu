@@ -102,7 +102,7 @@ struct Kahan {
 // global atomic per touched node.  Tiles whose box does not fit (unsorted input) fall
 // back to 64-bit global atomics per corner.
 template <int DOM, bool STATS, bool MOM>
-__global__ void __launch_bounds__(PB) k_push(MeshView m, ParticlesView P, PushArgs a,
+__global__ void __launch_bounds__(PB, 4) k_push(MeshView m, ParticlesView P, PushArgs a,
                                               unsigned long long* __restrict__ count,
                                               long long* __restrict__ mom, int* __restrict__ slow_idx,
                                               unsigned long long* __restrict__ counters,
@@ -621,6 +621,39 @@ __device__ inline void deposit_global_t(const MeshView& m, unsigned long long* c
 }
 #define deposit_global deposit_global_t<DOM>
 
+// The fast path's FP32 move of a particle in cell (i, j) at fraction f with the updated
+// velocity nv: the new position (gx, gy) in cells relative to node (i, j), not yet
+// reduced to a cell, and for RZ / ZR the velocity rotated into the new (z, r) plane
+// (rotateToRZ / rotateToZR, KineticMaterial.java:424-462, relative to the cell radius).
+template <int DOM>
+__device__ __forceinline__ void move_fp32(int i, int j, float2 f, const PushArgs& a, float& gx, float& gy,
+                                          float nv[3]) {
+  if (DOM == SF_DOMAIN_XY) {
+    gx = f.x + nv[0] * a.dt_dx;
+    gy = f.y + nv[1] * a.dt_dy;
+  } else if (DOM == SF_DOMAIN_ZR) {
+    gx = f.x + nv[0] * a.dt_dx;
+    const float rj = a.r0y + (float)j * a.dy;
+    const float A = nv[2] * a.dt, dl = f.y * a.dy + nv[1] * a.dt;
+    const float B = rj + dl, R = sqrtf(A * A + B * B), den = R + rj;
+    gy = (den > 0.f ? (A * A + dl * (2.f * rj + dl)) / den : 0.f) / a.dy;
+    const float cs = R > 0.f ? B / R : 1.f, sn = R > 0.f ? A / R : 0.f;
+    const float v1 = nv[1], v2 = nv[2];
+    nv[1] = cs * v1 + sn * v2;
+    nv[2] = -sn * v1 + cs * v2;
+  } else {
+    gy = f.y + nv[1] * a.dt_dy;
+    const float ri = a.r0x + (float)i * a.dx;
+    const float A = nv[2] * a.dt, dl = f.x * a.dx + nv[0] * a.dt;
+    const float B = ri + dl, R = sqrtf(A * A + B * B), den = R + ri;
+    gx = (den > 0.f ? (A * A + dl * (2.f * ri + dl)) / den : 0.f) / a.dx;
+    const float cs = R > 0.f ? B / R : 1.f, sn = R > 0.f ? A / R : 0.f;
+    const float v1 = nv[0], v2 = nv[2];
+    nv[0] = cs * v1 + sn * v2;
+    nv[2] = -sn * v1 + cs * v2;
+  }
+}
+
 // Conservative FP32 test of a move from (i + fx, j + fy) to (i + gx, j + gy) in cells:
 // false means the path cannot meet any DIRICHLET/SINK segment listed on the nodes of
 // its box (the candidate set of KineticMaterial.ProcessBoundary, :480-515), so the
@@ -684,17 +717,22 @@ __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, 
     sa.sv.deposit = s_seg + 2 * SMALL_NSEG;
   }
   const size_t nn = (size_t)m.ni * m.nj;
+  // per-thread totals of the particles finished here (one shared atomic per warp at the
+  // end instead of six per particle on the same few addresses)
+  double lst[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  unsigned long long ldone = 0;
   for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; t < nslow;
        t += (unsigned long long)gridDim.x * blockDim.x) {
     const int64_t p = slow_idx[t];
     const uint32_t c = P.cell[p];
     const float2 f = P.frac[p];
     const float2 v = P.vxy[p];
-    if (DOM == SF_DOMAIN_XY) {
-      // FP32 pre-filter: a particle whose path certainly misses every candidate segment
-      // and stays in the mesh finishes exactly like the fast path
+    {
+      // FP32 pre-filter: a particle whose (logical, straight) path certainly misses every
+      // candidate segment and stays in the mesh finishes exactly like the fast path
       const int i = cell_i(c), j = cell_j(c);
-      const float gx = f.x + v.x * a.dt_dx, gy = f.y + v.y * a.dt_dy;
+      float gx, gy, nv[3] = {v.x, v.y, P.vz[p]};
+      move_fp32<DOM>(i, j, f, a, gx, gy, nv);
       if (!may_hit_fp32(m, i, j, f.x, f.y, gx, gy)) {
         float fdi = floorf(gx), fdj = floorf(gy);
         float nfx = gx - fdi, nfy = gy - fdj;
@@ -703,18 +741,21 @@ __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, 
         const int i2 = i + (int)fdi, j2 = j + (int)fdj;
         const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
         if (inside) {
-          const float vz = P.vz[p];
           P.cell[p] = pack_cell(i2, j2);
           P.frac[p] = make_float2(nfx, nfy);
-          atomicAdd(&sa.counters[3], 1ULL);
-          atomicAdd(&sa.stats_slow[0], 1.0);
-          atomicAdd(&sa.stats_slow[1], (double)v.x);
-          atomicAdd(&sa.stats_slow[2], (double)v.y);
-          atomicAdd(&sa.stats_slow[3], (double)vz);
-          atomicAdd(&sa.stats_slow[4], (double)sqrtf(v.x * v.x + v.y * v.y + vz * vz));
+          if (DOM != SF_DOMAIN_XY) {  // the rotation changed the velocity
+            P.vxy[p] = make_float2(nv[0], nv[1]);
+            P.vz[p] = nv[2];
+          }
+          ldone++;
+          lst[0] += 1.0;
+          lst[1] += (double)nv[0];
+          lst[2] += (double)nv[1];
+          lst[3] += (double)nv[2];
+          lst[4] += (double)sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
           float wx, wy;
           scatter_weights<DOM>(nfx, nfy, i2, j2, a, wx, wy);
-          deposit_global(m, count, mom, mom_on, smp, i2, j2, nfx, nfy, wx, wy, v.x, v.y, vz, nn);
+          deposit_global(m, count, mom, mom_on, smp, i2, j2, nfx, nfy, wx, wy, nv[0], nv[1], nv[2], nn);
           continue;
         }
         if (m.all_delete) {
@@ -780,14 +821,23 @@ __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, 
     P.frac[p] = make_float2(fx, fy);
     P.vxy[p] = make_float2((float)vel[0], (float)vel[1]);
     P.vz[p] = (float)vel[2];
-    atomicAdd(&sa.stats_slow[0], 1.0);
-    atomicAdd(&sa.stats_slow[1], vel[0]);
-    atomicAdd(&sa.stats_slow[2], vel[1]);
-    atomicAdd(&sa.stats_slow[3], vel[2]);
-    atomicAdd(&sa.stats_slow[4], sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]));
+    lst[0] += 1.0;
+    lst[1] += vel[0];
+    lst[2] += vel[1];
+    lst[3] += vel[2];
+    lst[4] += sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
     float wx, wy;
     scatter_weights<DOM>(fx, fy, i, j, a, wx, wy);
     deposit_global(m, count, mom, mom_on, smp, i, j, fx, fy, wx, wy, (float)vel[0], (float)vel[1], (float)vel[2], nn);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    for (int q = 0; q < 5; q++) lst[q] += __shfl_down_sync(0xffffffffu, lst[q], o);
+    ldone += __shfl_down_sync(0xffffffffu, ldone, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    for (int q = 0; q < 5; q++)
+      if (lst[q] != 0.0) atomicAdd(&s_stats[q], lst[q]);
+    if (ldone) atomicAdd(&s_cnt[3], ldone);
   }
   __syncthreads();
   for (int q = threadIdx.x; q < 6; q += blockDim.x)
@@ -864,13 +914,15 @@ __global__ void k_gas_fields(int nn, const double* __restrict__ samp, double inv
   }
 }
 
+// deterministic sum of the per-block partials: one warp per quantity, lanes take fixed
+// strided subsets and a fixed shuffle tree combines them
 __global__ void k_sum_partials(const double* part, int nblocks, double* out) {
-  // deterministic sum of per-block partials; one thread per quantity
-  int q = threadIdx.x;
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (q >= 5) return;
   double s = 0;
-  for (int b = 0; b < nblocks; b++) s += part[(size_t)b * 8 + q];
-  out[q] = s;
+  for (int b = lane; b < nblocks; b += 32) s += part[(size_t)b * 8 + q];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) out[q] = s;
 }
 
 // Per-call scratch of one push: the slow-path queue (one slot per particle), the event
@@ -1012,7 +1064,7 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   unsigned long long hc[4];
   SF_CUDA(cudaMemcpyAsync(hc, sc.counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
   if (want_stats) {
-    k_sum_partials<<<1, 32, 0, s>>>(sc.stats_partial, grid, sc.sums);
+    k_sum_partials<<<1, 160, 0, s>>>(sc.stats_partial, grid, sc.sums);
     ctx->launches++;
     SF_CUDA(cudaMemcpyAsync(h, sc.sums, sizeof(double) * 5, cudaMemcpyDeviceToHost, s));
     SF_CUDA(cudaMemcpyAsync(h + 8, slow_stats, sizeof(double) * 6, cudaMemcpyDeviceToHost, s));

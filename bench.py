@@ -267,6 +267,71 @@ def dsmc_jet_bench(steps=20, warmup=3, n_particles=16 * 1024 * 1024, seed=0):
         dom.close()
 
 
+def batch_bench(n_instances=256, steps=16, warmup=10, threads=16, dt=5e-7):
+    """The batched-instances workload: 256 independent 81x41-type ES-PIC cases (mesh sizes
+    log-uniform from 33x17 to 257x129 nodes, 1e4..2e6 preloaded ions each, electrode at
+    -200..-20 V, O+ inlet, seeds 0..255) advanced together by sf_batch_step: batched
+    sources + one push launch over all instances (replayed as one CUDA graph), then every
+    instance's rho, Poisson-Boltzmann solve to 1e-6 and E, overlapping from `threads` host
+    threads.  The warm-up steps include the autotuner's trials.  Throughput: live
+    particles of all instances x steps / wall time of the steps."""
+    from starfish_gb300 import workloads as W
+    from starfish_gb300.plugin import GpuBatch, GpuDomain, KineticMaterial, PoissonSolver
+    cases = W.config4(n_instances)
+    doms, kms, solvers = [], [], []
+    t_setup = time.perf_counter()
+    for c in cases:
+        spec, ion = c.mesh, c.ion
+        dom = GpuDomain(spec, device=0)
+        ps = PoissonSolver(dom, n0=1e12, Te0=2.0, tol=1e-6, max_it=60)
+        ps.solve(rho=np.zeros(spec.nn), phi=np.zeros(spec.nn))
+        ps.update_gradient_field()
+        Lx, Ly = spec.lengths()
+        v_mean = np.sqrt(8 * W.KB * ion.temp / (np.pi * ion.mass))
+        inject = 1e12 * Ly * (ion.v_drift + v_mean / 4) * dt / ion.spwt
+        # removed slots stay until the sort every 16 steps
+        km = KineticMaterial(dom, ion.mass, ion.charge, ion.spwt,
+                             capacity=int(1.3 * c.n_particles + 24 * inject) + 8192)
+        pos, vel = W.uniform_maxwellian(spec, ion, c.n_particles, c.seed)
+        km.add_particles(pos, vel, rewind=True, dt=dt)
+        doms.append(dom)
+        kms.append(km)
+        solvers.append(ps)
+    batch = GpuBatch(doms, kms, threads=threads)
+    try:
+        for i, c in enumerate(cases):
+            Lx, Ly = c.mesh.lengths()
+            batch.set_source(i, [0.0, Ly, 0.0, 0.0], c.ion.den, c.ion.v_drift, c.ion.temp)
+        t_setup = time.perf_counter() - t_setup
+        for _ in range(warmup):
+            batch.step(dt, solvers[0])
+        psteps, dev_ms, solve_sum, solve_max, newton = 0, 0.0, 0.0, 0.0, 0.0
+        live = sum(km.get_np() for km in kms)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            psteps += live
+            st = batch.step(dt, solvers[0])
+            live = st["particles"]
+            dev_ms += st["device_phase_ms"]
+            solve_sum += st["solve_ms_sum"]
+            solve_max = max(solve_max, st["solve_ms_max"])
+            newton += st["newton_it_mean"]
+        wall = time.perf_counter() - t0
+        sizes = [c.mesh.nn for c in cases]
+        return {"metric": "particle-steps/s over all instances (source + push + scatter + Poisson + E)",
+                "value": psteps / wall, "unit": "particle-steps/s", "ms_per_step": 1e3 * wall / steps,
+                "steps": steps, "warmup": warmup, "instances": n_instances,
+                "particles_live_end": live, "mesh_nodes": [min(sizes), max(sizes)],
+                "device_phase_ms": dev_ms / steps, "solve_ms_sum_per_step": solve_sum / steps,
+                "solve_ms_max": solve_max, "newton_it_mean": newton / steps,
+                "host_threads": threads, "tuning": batch.tuning(), "setup_s": t_setup,
+                "timing": "wall clock of sf_batch_step (host threads and graph launches included)"}
+    finally:
+        batch.close()
+        for d in doms:
+            d.close()
+
+
 def cpu_baseline_sample(cfg, efi, efj, n_sample, threads, steps=1, seed=1):
     """The oracle port (reference algorithm, FP64 AoS) on a bounded sample of the workload."""
     from oracle import oracle as O
@@ -342,6 +407,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--poisson-steps", type=int, default=2000)
     ap.add_argument("--dsmc-steps", type=int, default=20)
+    ap.add_argument("--batch-steps", type=int, default=16)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -470,6 +536,8 @@ def main():
                                                 train_steps=min(500, args.poisson_steps // 4))
     if args.dsmc_steps > 0:
         line["dsmc"] = dsmc_jet_bench(steps=args.dsmc_steps)
+    if args.batch_steps > 0:
+        line["batch"] = batch_bench(steps=args.batch_steps)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n_sample = 16 * 1024 * 1024

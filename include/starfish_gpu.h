@@ -326,6 +326,36 @@ int sf_unet_debug(sf_ctx* ctx, const float* x, const float* dpred, float* pred, 
 /* Reads (get) and/or replaces (set) the FP32 master parameters, same flattening. */
 int sf_unet_params(sf_ctx* ctx, float* get, const float* set);
 
+/* ---- batches of independent instances (no reference counterpart) --------------- */
+/* Many independent cases (contexts of different mesh sizes and particle counts, one
+ * kinetic species each, XY meshes) advanced together.  One sf_batch_step does, for all
+ * instances: the Maxwellian inlet sources, the push + scatter (one launch over every
+ * instance's particles, the device phase replayed as one CUDA graph), then per instance
+ * rho, the Poisson-Boltzmann solve and E, issued from `threads` host threads so that the
+ * instances' solves overlap on the GPU.  Instances are cell-sorted every 16 steps.  The
+ * first steps tune the push launch shape and the PCG iterations per Newton step per
+ * mesh-size bucket (sf_batch_tuning).  The contexts stay owned by the caller and must
+ * not be used by other calls while a batch step runs; between steps their usual entry
+ * points work. */
+typedef struct sf_batch sf_batch;
+typedef struct {
+  int64_t particles;         /* live particles over all instances after the step          */
+  double device_phase_ms;    /* sources + push + deposit of all instances (CUDA events)    */
+  double solve_ms_sum;       /* device time of the instances' Poisson solves, summed       */
+  double solve_ms_max;       /* ... and the longest one                                    */
+  double newton_it_mean;     /* Newton steps per solve                                     */
+  int32_t capacity_overflow; /* a source hit an instance's capacity (step returns SF_ERR_OOM) */
+} sf_batch_stats;
+int sf_batch_create(sf_ctx** ctxs, const int32_t* sids, int32_t n, int32_t threads, sf_batch** out);
+int sf_batch_destroy(sf_batch* b);
+const char* sf_batch_last_error(const sf_batch* b);
+/* MaxwellianSource on a straight segment for instance i (as sf_source_maxwellian). */
+int sf_batch_set_source(sf_batch* b, int32_t i, const double* seg, double den, double v_drift, double temp);
+int sf_batch_step(sf_batch* b, double dt, const sf_poisson_params* prm, sf_batch_stats* stats);
+/* Chosen push blocks per SM and exact-path blocks per SM (-1 while tuning), and PCG
+ * iterations per Newton step for meshes of < 4096, < 16384 and more nodes (-1 while tuning). */
+int sf_batch_tuning(const sf_batch* b, int32_t* blocks_per_sm, int32_t* slow_blocks, int32_t* cycles_by_bucket);
+
 /* ---- collisions ------------------------------------------------------------- */
 /* Cross-section models (interactions/Sigma.java:24-195, collisions/SigmaPlus.java:38-76) */
 #define SF_SIGMA_CONST 0    /* sigma = c0                                         */

@@ -198,3 +198,22 @@ EXPORTS.update({
     "sf_samples_clear": (C.c_int, [C.c_void_p, C.c_int32]),
     "sf_samples_compute": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_int64)]),
 })
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("particles", C.c_int64), ("device_phase_ms", C.c_double), ("solve_ms_sum", C.c_double),
+                ("solve_ms_max", C.c_double), ("newton_it_mean", C.c_double), ("capacity_overflow", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+EXPORTS.update({
+    "sf_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.c_int32, C.c_int32,
+                                  C.POINTER(C.c_void_p)]),
+    "sf_batch_destroy": (C.c_int, [C.c_void_p]),
+    "sf_batch_last_error": (C.c_char_p, [C.c_void_p]),
+    "sf_batch_set_source": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_double, C.c_double, C.c_double]),
+    "sf_batch_step": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(PoissonParams), C.POINTER(BatchStats)]),
+    "sf_batch_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p]),
+})

@@ -409,8 +409,8 @@ static SfDsmcState* dsmc_state(sf_ctx* ctx, int sid, double sig_cr_max0) {
   SF_CUDA(cudaMalloc(&st->counts, sizeof(double2) * nc));
   SF_CUDA(cudaMalloc(&st->cell_vol, sizeof(double) * nc));
   std::vector<double2> s0(nc, make_double2(sig_cr_max0, 0.0));
-  SF_CUDA(cudaMemcpy(st->state, s0.data(), sizeof(double2) * nc, cudaMemcpyHostToDevice));
-  SF_CUDA(cudaMemset(st->counts, 0, sizeof(double2) * nc));
+  copy_wait(st->state, s0.data(), sizeof(double2) * nc, cudaMemcpyHostToDevice, ctx->stream);
+  zero_wait(st->counts, sizeof(double2) * nc, ctx->stream);
   // Mesh.cellVol = nodeVol(i + 1/2, j + 1/2) (core/domain/Mesh.java:1038-1040)
   std::vector<double> cv(nc);
   for (int j = 0; j < ctx->nj - 1; j++)
@@ -421,7 +421,7 @@ static SfDsmcState* dsmc_state(sf_ctx* ctx, int sid, double sig_cr_max0) {
       if (ctx->domain == SF_DOMAIN_ZR) v = 2 * PI * area * (ctx->x0[1] + (j + 0.5) * ctx->dh[1]);
       cv[(size_t)j * (ctx->ni - 1) + i] = v;
     }
-  SF_CUDA(cudaMemcpy(st->cell_vol, cv.data(), sizeof(double) * nc, cudaMemcpyHostToDevice));
+  copy_wait(st->cell_vol, cv.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, ctx->stream);
   st->init = true;
   return st;
 }
@@ -485,7 +485,7 @@ int sf_dsmc_get_counts(sf_ctx* ctx, int32_t sid, double* count_sum, double* real
   SF_CUDA(cudaSetDevice(ctx->device));
   const int nc = ctx->ncells();
   std::vector<double2> h(nc);
-  SF_CUDA(cudaMemcpy(h.data(), ctx->dsmc[sid]->counts, sizeof(double2) * nc, cudaMemcpyDeviceToHost));
+  copy_wait(h.data(), ctx->dsmc[sid]->counts, sizeof(double2) * nc, cudaMemcpyDeviceToHost, ctx->stream);
   for (int c = 0; c < nc; c++) {
     if (count_sum) count_sum[c] = h[c].x;
     if (real_sum) real_sum[c] = h[c].y;
@@ -505,7 +505,7 @@ int sf_mcc_set_target(sf_ctx* ctx, double mass, const double* den, const double*
   for (int k = 0; k < 5; k++)
     if (src[k])
       for (size_t q = 0; q < nn; q++) h[k * nn + q] = (float)src[k][q];
-  SF_CUDA(cudaMemcpy(ctx->mcc_target, h.data(), sizeof(float) * 5 * nn, cudaMemcpyHostToDevice));
+  copy_wait(ctx->mcc_target, h.data(), sizeof(float) * 5 * nn, cudaMemcpyHostToDevice, ctx->stream);
   ctx->mcc_mass = mass;
   SF_API_END(ctx)
 }

@@ -478,12 +478,9 @@ void launch_sort(sf_ctx* ctx, SfSpecies* sp) {
                             cudaMemcpyDeviceToDevice, ctx->stream));
     ParticlesView dst = sp->alt;
     dst.n = sp->n;
-    static bool attr_set = false;
-    if (!attr_set) {
-      SF_CUDA(cudaFuncSetAttribute(k_sort_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)SORT_SCATTER_SMEM));
-      attr_set = true;
-    }
+    // per device and the same for every context (set-up threads may sort concurrently)
+    SF_CUDA(cudaFuncSetAttribute(k_sort_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SORT_SCATTER_SMEM));
     const int gs = grid_for((sp->n + SORT_CHUNK - 1) / SORT_CHUNK, 1, ctx->num_sms * 2);
     k_sort_scatter<<<gs, SORT_B, SORT_SCATTER_SMEM, ctx->stream>>>(sp->cur, dst, ctx->ntx, ctx->bins_tmp);
     SF_CUDA(cudaGetLastError());
@@ -584,22 +581,22 @@ int sf_ctx_create(const sf_mesh_desc* md, int device, sf_ctx** out) {
     SF_CUDA(cudaMalloc(&ctx->E, sizeof(float2) * nn));
     SF_CUDA(cudaMemsetAsync(ctx->E, 0, sizeof(float2) * nn, ctx->stream));
     SF_CUDA(cudaMalloc(&ctx->seg_dist, nn));
-    SF_CUDA(cudaMemcpy(ctx->seg_dist, sd.data(), nn, cudaMemcpyHostToDevice));
+    copy_wait(ctx->seg_dist, sd.data(), nn, cudaMemcpyHostToDevice, ctx->stream);
     SF_CUDA(cudaMalloc(&ctx->node_seg_ptr, sizeof(int) * (nn + 1)));
-    SF_CUDA(cudaMemcpy(ctx->node_seg_ptr, ptr.data(), sizeof(int) * (nn + 1), cudaMemcpyHostToDevice));
+    copy_wait(ctx->node_seg_ptr, ptr.data(), sizeof(int) * (nn + 1), cudaMemcpyHostToDevice, ctx->stream);
     SF_CUDA(cudaMalloc(&ctx->node_seg_idx, sizeof(int) * std::max<size_t>(idx.size(), 1)));
     if (!idx.empty())
-      SF_CUDA(cudaMemcpy(ctx->node_seg_idx, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice));
+      copy_wait(ctx->node_seg_idx, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, ctx->stream);
     SF_CUDA(cudaMalloc(&ctx->d_seg_xy, sizeof(Seg4) * std::max(ctx->nseg, 1)));
     SF_CUDA(cudaMalloc(&ctx->d_seg_btype, sizeof(int) * std::max(ctx->nseg, 1)));
     if (ctx->nseg > 0) {
-      SF_CUDA(cudaMemcpy(ctx->d_seg_xy, ctx->seg_xy.data(), sizeof(Seg4) * ctx->nseg, cudaMemcpyHostToDevice));
-      SF_CUDA(cudaMemcpy(ctx->d_seg_btype, ctx->seg_btype.data(), sizeof(int) * ctx->nseg, cudaMemcpyHostToDevice));
+      copy_wait(ctx->d_seg_xy, ctx->seg_xy.data(), sizeof(Seg4) * ctx->nseg, cudaMemcpyHostToDevice, ctx->stream);
+      copy_wait(ctx->d_seg_btype, ctx->seg_btype.data(), sizeof(int) * ctx->nseg, cudaMemcpyHostToDevice, ctx->stream);
     }
     SF_CUDA(cudaMalloc(&ctx->d_face_type, 4 * (size_t)ctx->nmax));
-    SF_CUDA(cudaMemcpy(ctx->d_face_type, ctx->face_type.data(), 4 * (size_t)ctx->nmax, cudaMemcpyHostToDevice));
+    copy_wait(ctx->d_face_type, ctx->face_type.data(), 4 * (size_t)ctx->nmax, cudaMemcpyHostToDevice, ctx->stream);
     SF_CUDA(cudaMalloc(&ctx->d_node_vol, sizeof(double) * nn));
-    SF_CUDA(cudaMemcpy(ctx->d_node_vol, ctx->node_vol.data(), sizeof(double) * nn, cudaMemcpyHostToDevice));
+    copy_wait(ctx->d_node_vol, ctx->node_vol.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->stream);
     SF_CUDA(cudaMalloc(&ctx->counters, sizeof(unsigned long long) * 8));
     ctx->stats_blocks = ctx->num_sms * 8;
     SF_CUDA(cudaMalloc(&ctx->stats_partial, sizeof(double) * 8 * (size_t)ctx->stats_blocks));
@@ -691,9 +688,9 @@ int sf_species_add(sf_ctx* ctx, double charge, double mass, double spwt, int64_t
   std::vector<int> model(ns, SF_SURF_ABSORB);
   std::vector<float4> param(ns, make_float4(0, 1, 1, 0));
   SF_CUDA(cudaMalloc(&sp->seg_model, sizeof(int) * ns));
-  SF_CUDA(cudaMemcpy(sp->seg_model, model.data(), sizeof(int) * ns, cudaMemcpyHostToDevice));
+  copy_wait(sp->seg_model, model.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, ctx->stream);
   SF_CUDA(cudaMalloc(&sp->seg_param, sizeof(float4) * ns));
-  SF_CUDA(cudaMemcpy(sp->seg_param, param.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice));
+  copy_wait(sp->seg_param, param.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, ctx->stream);
   SF_CUDA(cudaMalloc(&sp->flux, sizeof(double) * 2 * ns));
   SF_CUDA(cudaMalloc(&sp->deposit, sizeof(double) * 2 * ns));
   SF_CUDA(cudaMemsetAsync(sp->flux, 0, sizeof(double) * 2 * ns, ctx->stream));
@@ -712,8 +709,8 @@ int sf_species_set_surface(sf_ctx* ctx, int32_t sid, int32_t seg, int32_t model,
   SF_REQUIRE(model >= SF_SURF_PASS && model <= SF_SURF_DIFFUSE, SF_ERR_ARG, "bad surface model");
   SF_REQUIRE(model != SF_SURF_DIFFUSE || vth > 0, SF_ERR_ARG, "DIFFUSE needs vth > 0");
   float4 p = make_float4((float)vth, (float)c_rest, (float)c_accom, 0.f);
-  SF_CUDA(cudaMemcpy(sp->seg_model + seg, &model, sizeof(int), cudaMemcpyHostToDevice));
-  SF_CUDA(cudaMemcpy(sp->seg_param + seg, &p, sizeof(float4), cudaMemcpyHostToDevice));
+  copy_wait(sp->seg_model + seg, &model, sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+  copy_wait(sp->seg_param + seg, &p, sizeof(float4), cudaMemcpyHostToDevice, ctx->stream);
   SF_API_END(ctx)
 }
 
@@ -1040,9 +1037,9 @@ int sf_get_surface_flux(sf_ctx* ctx, int32_t sid, double* flux, double* deposit)
   SfSpecies* sp = get_species(ctx, sid);
   SF_CUDA(cudaSetDevice(ctx->device));
   if (ctx->nseg > 0) {
-    if (flux) SF_CUDA(cudaMemcpy(flux, sp->flux, sizeof(double) * 2 * ctx->nseg, cudaMemcpyDeviceToHost));
+    if (flux) copy_wait(flux, sp->flux, sizeof(double) * 2 * ctx->nseg, cudaMemcpyDeviceToHost, ctx->stream);
     if (deposit)
-      SF_CUDA(cudaMemcpy(deposit, sp->deposit, sizeof(double) * 2 * ctx->nseg, cudaMemcpyDeviceToHost));
+      copy_wait(deposit, sp->deposit, sizeof(double) * 2 * ctx->nseg, cudaMemcpyDeviceToHost, ctx->stream);
   }
   SF_API_END(ctx)
 }
@@ -1052,8 +1049,8 @@ int sf_reset_surface_flux(sf_ctx* ctx, int32_t sid) {
   SfSpecies* sp = get_species(ctx, sid);
   SF_CUDA(cudaSetDevice(ctx->device));
   int ns = std::max(ctx->nseg, 1);
-  SF_CUDA(cudaMemset(sp->flux, 0, sizeof(double) * 2 * ns));
-  SF_CUDA(cudaMemset(sp->deposit, 0, sizeof(double) * 2 * ns));
+  zero_wait(sp->flux, sizeof(double) * 2 * ns, ctx->stream);
+  zero_wait(sp->deposit, sizeof(double) * 2 * ns, ctx->stream);
   SF_API_END(ctx)
 }
 

@@ -101,6 +101,26 @@ struct ParticlesView {
   int64_t n;  // slots in use
 };
 
+// Per-launch arguments of the push (sf_push.cu) and of its exact surface path.
+struct PushArgs {
+  float qm_dt;        // (q/m) dt
+  float dt_dx, dt_dy; // dt/dx, dt/dy
+  float dt;
+  float dx, dy;
+  float r0x, r0y;     // mesh origin (radius origin for RZ / ZR)
+  double dt64;
+  double qm;          // q/m
+  double charge, spwt;
+  uint64_t seed;
+  uint32_t step;
+};
+
+struct SlowArgs {
+  SurfaceView sv;
+  unsigned long long* counters;
+  double* stats_slow;   // 5 sums + boundary charge
+};
+
 // ---------------------------------------------------------------------------------
 // Philox4x32-10 counter-based RNG (Salmon, Moraes, Dror, Shaw, "Parallel random
 // numbers: as easy as 1, 2, 3", SC'11).  Streams are keyed by (seed, purpose) and
@@ -192,6 +212,48 @@ struct SfSpecies {
   double* gas = nullptr;    // 10*ni*nj: nd-ave, u/v/w-ave, T, T1, T2, T3, p, mpc
   int64_t num_samples = 0;
 };
+
+// One instance of a batch (sf_batch.cu): everything the batched kernels need to push,
+// inject and deposit for it without host values, so that a batch step is one CUDA graph.
+// Particle counts live on the device (sf_batch's n_dev); P.n is not used.
+struct BatchInst {
+  sf::MeshView m;
+  sf::ParticlesView P;
+  sf::PushArgs a;                  // a.step is advanced on the device after every push
+  sf::SlowArgs sa;                 // counters and slow-path sums of the instance's context
+  unsigned long long* count;   // species deposit (fixed point)
+  int* slow_idx;
+  double* nd;
+  const double* vol;
+  double w_scale, nd_back;
+  // Maxwellian inlet (MaxwellianSource on one segment); src_on = 0: no source
+  double sx1, sy1, sx2, sy2, snx, sny, v_th, v_drift, src_dt, mp_step;
+  float qm_halfdt;
+  int src_on;
+  uint64_t src_seed;
+  int64_t cap;
+};
+
+// Device state of a batch step shared by the batched kernels
+struct BatchDev {
+  BatchInst* insts;
+  int n;
+  int64_t* n_dev;      // slots in use per instance
+  int64_t* dead_dev;   // removed slots among them (until the next sort)
+  double* rem_dev;     // source remainders
+  int64_t* num_dev;    // particles to inject this step
+  int64_t* base_dev;   // first slot of this step's injection
+  unsigned long long* added_dev;
+  int64_t* tile_start; // n + 1: prefix of push tiles over the instances
+  int64_t* chunk_start;  // n + 1: prefix of slow-queue chunks over the instances
+  uint32_t* step_dev;  // batch step counter (RNG epoch of the sources)
+  int* overflow;       // set when a source hit an instance's capacity
+};
+namespace sf {
+// batched phases of one step, all on `stream` (sf_push.cu, sf_source.cu)
+void batch_inject(const BatchDev& b, cudaStream_t stream, int num_sms);
+void batch_push(const BatchDev& b, cudaStream_t stream, int num_sms, int blocks_per_sm, int slow_blocks_per_sm);
+}  // namespace sf
 
 struct SfPoisson;    // sf_poisson.cu
 struct SfDsmcState;  // sf_collide.cu
@@ -294,6 +356,18 @@ inline int grid_for(int64_t n, int block, int max_blocks) {
   if (g > max_blocks) g = max_blocks;
   if (g < 1) g = 1;
   return (int)g;
+}
+// Set-up copies and fills.  Every stream here is created with cudaStreamNonBlocking, and
+// the plain cudaMemcpy / cudaMemset run on the legacy stream, which such streams do not
+// wait for: a plain zero fill issued before an async copy could land after it.  These
+// run on the owning stream and return once it is done, so host buffers may go at once.
+inline void copy_wait(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
+  SF_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, s));
+  SF_CUDA(cudaStreamSynchronize(s));
+}
+inline void zero_wait(void* p, size_t bytes, cudaStream_t s) {
+  SF_CUDA(cudaMemsetAsync(p, 0, bytes, s));
+  SF_CUDA(cudaStreamSynchronize(s));
 }
 }  // namespace sf
 

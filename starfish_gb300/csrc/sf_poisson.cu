@@ -33,6 +33,7 @@ namespace {
 enum : uint8_t { NC_INTERIOR = 0, NC_FIXED = 1, NC_NLEFT = 2, NC_NRIGHT = 3, NC_NBOTTOM = 4, NC_NTOP = 5 };
 
 constexpr int COARSE_NODES = 8600;  // a level this small and everything below run in one CTA
+constexpr size_t COARSE_SMEM_MAX = 220 * 1024;  // dynamic shared memory bound of the coarse V-cycle
 constexpr int MAX_LEVELS = 16;
 
 struct LevelView {
@@ -52,6 +53,7 @@ struct CoarseDesc {  // levels [0, n) of the single-CTA solve; level 0 is read f
   int off[MAX_LEVELS];  // node offset of each level in the shared arrays
   int total;
   int coarsest_sweeps;
+  float omega;  // SOR factor of the coarsest level
 };
 
 __host__ __device__ inline uint8_t node_class(bool fixed, int i, int j, int ni, int nj) {
@@ -167,7 +169,7 @@ __global__ void k_restrict_P(LevelView F, LevelView Cl) {
 // rb: red then black (pre-smoothing); otherwise black then red (post-smoothing), so the
 // V-cycle is a symmetric preconditioner
 __device__ void cta_smooth(float* y, const float* r, const float* P, const uint8_t* ty, int ni, int nj, float cx,
-                           float cy, int sweeps, bool rb) {
+                           float cy, int sweeps, bool rb, float omega = 1.f) {
   const int n = ni * nj;
   for (int s = 0; s < sweeps; s++)
     for (int c = 0; c < 2; c++) {
@@ -175,12 +177,12 @@ __device__ void cta_smooth(float* y, const float* r, const float* P, const uint8
       if (ni & 1) {
         // odd row length: the colour (i + j) & 1 of node u = j ni + i is u & 1
         for (int u = 2 * threadIdx.x + color; u < n; u += 2 * blockDim.x)
-          y[u] = gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy);
+          y[u] += omega * (gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy) - y[u]);
       } else {
         for (int u = threadIdx.x; u < n; u += blockDim.x) {
           const int j = u / ni, i = u - j * ni;
           if (((i + j) & 1) != color) continue;
-          y[u] = gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy);
+          y[u] += omega * (gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy) - y[u]);
         }
       }
       __syncthreads();
@@ -229,12 +231,14 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseDesc D, LevelView 
     }
     __syncthreads();
   }
-  // coarsest: symmetric sweep pairs
+  // coarsest: symmetric pairs of red-black SOR sweeps with the optimal Laplacian omega
+  // (a coarsest grid of tens of nodes per side, left when n - 1 has an odd factor,
+  // needs it: plain Gauss-Seidel would barely reduce its error)
   {
     const int l = D.n - 1, o = D.off[l];
     for (int s = 0; s < D.coarsest_sweeps; s++) {
-      cta_smooth(Y + o, R + o, PP + o, TY + o, D.ni[l], D.nj[l], D.cx[l], D.cy[l], 1, true);
-      cta_smooth(Y + o, R + o, PP + o, TY + o, D.ni[l], D.nj[l], D.cx[l], D.cy[l], 1, false);
+      cta_smooth(Y + o, R + o, PP + o, TY + o, D.ni[l], D.nj[l], D.cx[l], D.cy[l], 1, true, D.omega);
+      cta_smooth(Y + o, R + o, PP + o, TY + o, D.ni[l], D.nj[l], D.cx[l], D.cy[l], 1, false, D.omega);
     }
   }
   // ascend
@@ -471,11 +475,13 @@ __global__ void k_cg_scalars(double* sc, int stage) {
   }
 }
 
-// p = z + beta p  (beta = 0 for the first direction)
+// p = z + beta p; the first direction is z itself (p holds no value yet: not even its
+// product with 0 may be formed, it could be a NaN pattern)
 __global__ void k_cg_pupdate(int n, const double* __restrict__ sc, int first, const float* __restrict__ z,
                              float* __restrict__ p) {
   const float be = first ? 0.f : (float)sc[SC_BETA];
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) p[u] = z[u] + be * p[u];
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
+    p[u] = first ? z[u] : z[u] + be * p[u];
 }
 
 // x -= y, each node's step limited to max_step (10 kTe): far from the solution an
@@ -560,10 +566,13 @@ struct SfPoisson {
   int64_t graph_launches = 0;
 };
 
-static void* dalloc(SfPoisson* ps, size_t bytes) {
+// zeroed: the first solve without a host phi starts from phi = 0, and no buffer holds
+// stale bit patterns from earlier allocations
+static void* dalloc(sf_ctx* ctx, SfPoisson* ps, size_t bytes) {
   void* p = nullptr;
   SF_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
   ps->allocs.push_back(p);
+  zero_wait(p, std::max<size_t>(bytes, 16), ctx->stream);
   return p;
 }
 
@@ -577,22 +586,22 @@ static SfPoisson* poisson_get(sf_ctx* ctx) {
   const size_t nn = (size_t)ni * nj;
   ps->ni = ni;
   ps->nj = nj;
-  ps->phi = (double*)dalloc(ps, 8 * nn);
-  ps->b0 = (double*)dalloc(ps, 8 * nn);
-  ps->rho = (double*)dalloc(ps, 8 * nn);
-  ps->bc = (double*)dalloc(ps, 8 * nn);
-  ps->ne = (double*)dalloc(ps, 8 * nn);
-  ps->efi = (double*)dalloc(ps, 8 * nn);
-  ps->efj = (double*)dalloc(ps, 8 * nn);
-  ps->cg_x = (float*)dalloc(ps, 4 * nn);
-  ps->cg_p = (float*)dalloc(ps, 4 * nn);
-  ps->cg_q = (float*)dalloc(ps, 4 * nn);
-  ps->cg_zo = (float*)dalloc(ps, 4 * nn);
-  ps->type0 = (uint8_t*)dalloc(ps, nn);
+  ps->phi = (double*)dalloc(ctx, ps, 8 * nn);
+  ps->b0 = (double*)dalloc(ctx, ps, 8 * nn);
+  ps->rho = (double*)dalloc(ctx, ps, 8 * nn);
+  ps->bc = (double*)dalloc(ctx, ps, 8 * nn);
+  ps->ne = (double*)dalloc(ctx, ps, 8 * nn);
+  ps->efi = (double*)dalloc(ctx, ps, 8 * nn);
+  ps->efj = (double*)dalloc(ctx, ps, 8 * nn);
+  ps->cg_x = (float*)dalloc(ctx, ps, 4 * nn);
+  ps->cg_p = (float*)dalloc(ctx, ps, 4 * nn);
+  ps->cg_q = (float*)dalloc(ctx, ps, 4 * nn);
+  ps->cg_zo = (float*)dalloc(ctx, ps, 4 * nn);
+  ps->type0 = (uint8_t*)dalloc(ctx, ps, nn);
   ps->red_blocks = ctx->num_sms * 4;
-  ps->partial = (double*)dalloc(ps, 24 * (size_t)ps->red_blocks);
-  ps->red = (double*)dalloc(ps, 24);
-  ps->sc = (double*)dalloc(ps, 8 * 8);
+  ps->partial = (double*)dalloc(ctx, ps, 24 * (size_t)ps->red_blocks);
+  ps->red = (double*)dalloc(ctx, ps, 24);
+  ps->sc = (double*)dalloc(ctx, ps, 8 * 8);
   SF_CUDA(cudaMemsetAsync(ps->phi, 0, 8 * nn, ctx->stream));
   SF_CUDA(cudaMemsetAsync(ps->rho, 0, 8 * nn, ctx->stream));
   SF_CUDA(cudaMemcpyAsync(ps->bc, ctx->bc_value.data(), 8 * nn, cudaMemcpyHostToDevice, ctx->stream));
@@ -616,14 +625,14 @@ static SfPoisson* poisson_get(sf_ctx* ctx) {
     L.cx = (float)(1.0 / (ldx * ldx));
     L.cy = (float)(1.0 / (ldy * ldy));
     const size_t n = (size_t)lni * lnj;
-    L.y = (float*)dalloc(ps, 4 * n);
-    L.r = (float*)dalloc(ps, 4 * n);
-    L.P = (float*)dalloc(ps, 4 * n);
-    L.t = (float*)dalloc(ps, 4 * n);
+    L.y = (float*)dalloc(ctx, ps, 4 * n);
+    L.r = (float*)dalloc(ctx, ps, 4 * n);
+    L.P = (float*)dalloc(ctx, ps, 4 * n);
+    L.t = (float*)dalloc(ctx, ps, 4 * n);
     if (l == 0) {
       L.type = ps->type0;
     } else {
-      uint8_t* ty = (uint8_t*)dalloc(ps, n);
+      uint8_t* ty = (uint8_t*)dalloc(ctx, ps, n);
       SF_CUDA(cudaMemcpyAsync(ty, types[l].data(), n, cudaMemcpyHostToDevice, ctx->stream));
       L.type = ty;
     }
@@ -666,10 +675,14 @@ static SfPoisson* poisson_get(sf_ctx* ctx) {
   D.total = off;
   const LevelView& Lc = ps->lv[nl - 1];
   D.coarsest_sweeps = std::min(200, std::max(10, std::max(Lc.ni, Lc.nj)));
+  D.omega = (float)(2.0 / (1.0 + std::sin(PI / std::max(Lc.ni, Lc.nj))));
   ps->coarse_smem = (size_t)D.total * (4 * sizeof(float) + 1) + 16;
-  SF_REQUIRE(ps->coarse_smem <= 220 * 1024, SF_ERR_ARG,
+  SF_REQUIRE(ps->coarse_smem <= COARSE_SMEM_MAX, SF_ERR_ARG,
              "mesh not coarsenable to a level that fits in shared memory (use (2^k)m+1 nodes per direction)");
-  SF_CUDA(cudaFuncSetAttribute(k_coarse_vcycle, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps->coarse_smem));
+  // the limit is a property of the kernel on the device, shared by every context: always
+  // the same bound, so that a context with a smaller coarse end cannot lower it under the
+  // launches (and captured graphs) of another
+  SF_CUDA(cudaFuncSetAttribute(k_coarse_vcycle, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)COARSE_SMEM_MAX));
   SF_CUDA(cudaEventCreate(&ps->ev0));
   SF_CUDA(cudaEventCreate(&ps->ev1));
   SF_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -33,18 +33,6 @@ constexpr int PPT = 4;             // particles per thread per tile
 constexpr int TILE = PB * PPT;     // particles per block tile
 constexpr int SBOX = 4096;         // shared-memory deposit box (nodes)
 
-struct PushArgs {
-  float qm_dt;        // (q/m) dt
-  float dt_dx, dt_dy; // dt/dx, dt/dy
-  float dt;
-  float dx, dy;
-  float r0x, r0y;     // mesh origin (radius origin for RZ / ZR)
-  double dt64;
-  double qm;          // q/m
-  double charge, spwt;
-  uint64_t seed;
-  uint32_t step;
-};
 
 __device__ __forceinline__ unsigned quant(float w) {
   // S in [0,1] -> round(S * 2^31); S = 1 gives 2^31 which fits in 32 bits
@@ -101,6 +89,242 @@ struct Kahan {
 // atomics cannot overflow (<= 1024 particles per tile), then flushed with one 64-bit
 // global atomic per touched node.  Tiles whose box does not fit (unsorted input) fall
 // back to 64-bit global atomics per corner.
+// One tile (TILE particles from t0) of the fused push + deposit: load, push, fast-path
+// test, enqueue of slow candidates, shared-memory deposit of the tile's box and its
+// flush.  Shared by k_push (one mesh) and k_push_batch (many instances).
+template <int DOM, bool STATS, bool MOM>
+__device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView& P, const PushArgs& a, int64_t t0,
+                                          unsigned long long* __restrict__ count, long long* __restrict__ mom,
+                                          int* __restrict__ slow_idx, unsigned long long* __restrict__ counters,
+                                          const SampleView& smp, unsigned* acc_lo, unsigned* acc_hi,
+                                          int (*sred)[PB / 32], Kahan& st_px, Kahan& st_py, Kahan& st_pz, Kahan& st_e,
+                                          unsigned& st_n) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned FULL = 0xffffffffu;
+  const size_t nn = (size_t)m.ni * m.nj;
+  int pi[PPT], pj[PPT];
+  float pfx[PPT], pfy[PPT];
+  float pv[PPT][3];
+  bool dep[PPT];
+  int imin = INT_MAX, imax = -1, jmin = INT_MAX, jmax = -1;
+  // load phase: all of the thread's particles are requested before any is used, so
+  // each warp keeps PPT independent streams of loads in flight (streaming hints keep
+  // L2 for the field and the deposit grid)
+  uint32_t lcell[PPT];
+  float2 lfrac[PPT], lvxy[PPT];
+  float lvz[PPT];
+#pragma unroll
+  for (int k = 0; k < PPT; k++) {
+    const int64_t p = t0 + k * PB + threadIdx.x;
+    lcell[k] = DEAD;
+    lvz[k] = 0.f;
+    if (p < P.n) {
+      lcell[k] = __ldcs(&P.cell[p]);
+      lfrac[k] = __ldcs(&P.frac[p]);
+      lvxy[k] = __ldcs(&P.vxy[p]);
+      if (DOM != SF_DOMAIN_XY || STATS || MOM) lvz[k] = __ldcs(&P.vz[p]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < PPT; k++) {
+    const int64_t p = t0 + k * PB + threadIdx.x;
+    dep[k] = false;
+    pi[k] = pj[k] = 0;
+    pfx[k] = pfy[k] = 0.f;
+    int status = 0;  // 1 finished here, 2 exact path, 3 removed at a domain face
+    if (p < P.n) {
+      const uint32_t c = lcell[k];
+      if (c != DEAD) {
+        const int i = cell_i(c), j = cell_j(c);
+        const float2 f = lfrac[k];
+        float2 v = lvxy[k];
+        // velocity update (KineticMaterial.java:336-346); B = 0
+        const float2 e = gather_E(m, i, j, f.x, f.y);
+        v.x += a.qm_dt * e.x;
+        v.y += a.qm_dt * e.y;
+        float vz = lvz[k];
+        // move in logical coordinates (x += v dt; XtoL)
+        float nfx, nfy, nvx = v.x, nvy = v.y, nvz = vz;
+        if (DOM == SF_DOMAIN_XY) {
+          nfx = f.x + v.x * a.dt_dx;
+          nfy = f.y + v.y * a.dt_dy;
+        } else if (DOM == SF_DOMAIN_ZR) {
+          // rotateToZR (KineticMaterial.java:444-462) relative to the cell radius rj
+          nfx = f.x + v.x * a.dt_dx;
+          const float rj = a.r0y + (float)j * a.dy;
+          const float A = vz * a.dt;
+          const float dl = f.y * a.dy + v.y * a.dt;
+          const float B = rj + dl;
+          const float R = sqrtf(A * A + B * B);
+          const float den = R + rj;
+          const float rrel = den > 0.f ? (A * A + dl * (2.f * rj + dl)) / den : 0.f;
+          nfy = rrel / a.dy;
+          const float cs = R > 0.f ? B / R : 1.f, sn = R > 0.f ? A / R : 0.f;
+          nvy = cs * v.y + sn * vz;
+          nvz = -sn * v.y + cs * vz;
+        } else {
+          // rotateToRZ (KineticMaterial.java:424-442), radius along x
+          nfy = f.y + v.y * a.dt_dy;
+          const float ri = a.r0x + (float)i * a.dx;
+          const float A = vz * a.dt;
+          const float dl = f.x * a.dx + v.x * a.dt;
+          const float B = ri + dl;
+          const float R = sqrtf(A * A + B * B);
+          const float den = R + ri;
+          const float rrel = den > 0.f ? (A * A + dl * (2.f * ri + dl)) / den : 0.f;
+          nfx = rrel / a.dx;
+          const float cs = R > 0.f ? B / R : 1.f, sn = R > 0.f ? A / R : 0.f;
+          nvx = cs * v.x + sn * vz;
+          nvz = -sn * v.x + cs * vz;
+        }
+        float fdi = floorf(nfx), fdj = floorf(nfy);
+        nfx -= fdi;
+        nfy -= fdj;
+        if (nfx >= 1.f) { nfx -= 1.f; fdi += 1.f; }
+        if (nfy >= 1.f) { nfy -= 1.f; fdj += 1.f; }
+        const int di = (int)fdi, dj = (int)fdj;
+        const int i2 = i + di, j2 = j + dj;
+        const int span = max(abs(di), abs(dj)) + 1;
+        const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
+        const bool clear = (int)__ldg(&m.seg_dist[j * m.ni + i]) > span;
+        if (inside && clear) {
+          __stcs(&P.cell[p], pack_cell(i2, j2));
+          __stcs(&P.frac[p], make_float2(nfx, nfy));
+          __stcs(&P.vxy[p], make_float2(nvx, nvy));
+          if (DOM != SF_DOMAIN_XY) __stcs(&P.vz[p], nvz);
+          status = 1;
+          dep[k] = true;
+          pi[k] = i2;
+          pj[k] = j2;
+          pfx[k] = nfx;
+          pfy[k] = nfy;
+          pv[k][0] = nvx;
+          pv[k][1] = nvy;
+          pv[k][2] = nvz;
+          imin = min(imin, i2);
+          imax = max(imax, i2);
+          jmin = min(jmin, j2);
+          jmax = max(jmax, j2);
+          if (STATS) {
+            st_n++;
+            st_px.add(nvx);
+            st_py.add(nvy);
+            st_pz.add(nvz);
+            st_e.add(sqrtf(nvx * nvx + nvy * nvy + nvz * nvz));
+          }
+        } else if (!inside && clear && m.all_delete) {
+          // no candidate segment on the way and every domain face removes particles
+          // (KineticMaterial.java:614-746: OPEN/DIRICHLET/... return false)
+          P.cell[p] = DEAD;
+          status = 3;
+        } else {
+          // exact path later: keep the old position, store the updated velocity
+          P.vxy[p] = v;
+          status = 2;
+        }
+      }
+    }
+    const unsigned ms = __ballot_sync(FULL, status == 2);
+    if (ms) {
+      const int leader = __ffs(ms) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(ms));
+      base = __shfl_sync(FULL, base, leader);
+      if (status == 2) slow_idx[base + __popc(ms & ((1u << lane) - 1u))] = (int)p;
+    }
+    const unsigned md = __ballot_sync(FULL, status == 3);
+    if (md && lane == __ffs(md) - 1) atomicAdd(&counters[1], (unsigned long long)__popc(md));
+  }
+  // ---- block bounding box of this tile's deposits ----
+  imin = __reduce_min_sync(FULL, imin);
+  jmin = __reduce_min_sync(FULL, jmin);
+  imax = __reduce_max_sync(FULL, imax);
+  jmax = __reduce_max_sync(FULL, jmax);
+  if (lane == 0) {
+    sred[0][wid] = imin;
+    sred[1][wid] = jmin;
+    sred[2][wid] = imax;
+    sred[3][wid] = jmax;
+  }
+  __syncthreads();
+  imin = sred[0][0];
+  jmin = sred[1][0];
+  imax = sred[2][0];
+  jmax = sred[3][0];
+#pragma unroll
+  for (int w = 1; w < PB / 32; w++) {
+    imin = min(imin, sred[0][w]);
+    jmin = min(jmin, sred[1][w]);
+    imax = max(imax, sred[2][w]);
+    jmax = max(jmax, sred[3][w]);
+  }
+  const int bw = imax - imin + 2, bh = jmax - jmin + 2;
+  const bool any = imax >= 0;
+  const bool use_smem = any && (bw * bh <= SBOX);
+  if (use_smem) {
+    for (int q = threadIdx.x; q < bw * bh; q += PB) {
+      acc_lo[q] = 0u;
+      acc_hi[q] = 0u;
+    }
+  }
+  __syncthreads();
+  if (any) {
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+      // scatter skip rule at the far mesh edges (lc >= n-1 is not scattered)
+      // macroparticles per cell at (int) lc (KineticMaterial.updateSamples)
+      if (MOM && dep[k] && smp.mpc)
+        atomicAdd(&smp.mpc[(pj[k] + (pfy[k] >= 1.f)) * m.ni + pi[k] + (pfx[k] >= 1.f)], 1u);
+      const bool d = dep[k] && !((pfx[k] >= 1.f && pi[k] == m.ni - 2) || (pfy[k] >= 1.f && pj[k] == m.nj - 2));
+      if (!d) continue;
+      float wx, wy;
+      scatter_weights<DOM>(pfx[k], pfy[k], pi[k], pj[k], a, wx, wy);
+      const unsigned q[4] = {quant((1.f - wx) * (1.f - wy)), quant(wx * (1.f - wy)), quant(wx * wy),
+                             quant((1.f - wx) * wy)};
+      if (MOM) {
+        const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
+        const int base = pj[k] * m.ni + pi[k];
+        const int off[4] = {0, 1, m.ni + 1, m.ni};
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++)
+#pragma unroll
+          for (int dd = 0; dd < 3; dd++)
+            atomicAdd((unsigned long long*)&mom[dd * nn + base + off[cc]],
+                      (unsigned long long)__float2ll_rn(s[cc] * pv[k][dd] * 65536.0f));
+        if (smp.mom2)
+#pragma unroll
+          for (int cc = 0; cc < 4; cc++)
+#pragma unroll
+            for (int dd = 0; dd < 3; dd++)
+              atomicAdd(&smp.mom2[dd * nn + base + off[cc]],
+                        __float2ull_rn(s[cc] * pv[k][dd] * pv[k][dd] * (float)MOM2_SCALE));
+      }
+      if (use_smem) {
+        const int l = (pj[k] - jmin) * bw + (pi[k] - imin);
+        const int off[4] = {0, 1, bw + 1, bw};
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++) {
+          atomicAdd(&acc_lo[l + off[cc]], q[cc] & 0xFFFFu);
+          atomicAdd(&acc_hi[l + off[cc]], q[cc] >> 16);
+        }
+      } else {
+        const size_t u = (size_t)pj[k] * m.ni + pi[k];
+        const size_t off[4] = {0, 1, (size_t)m.ni + 1, (size_t)m.ni};
+#pragma unroll
+        for (int cc = 0; cc < 4; cc++) atomicAdd(&count[u + off[cc]], (unsigned long long)q[cc]);
+      }
+    }
+  }
+  __syncthreads();
+  if (use_smem) {
+    for (int q = threadIdx.x; q < bw * bh; q += PB) {
+      const unsigned long long v = ((unsigned long long)acc_hi[q] << 16) + acc_lo[q];
+      if (v) atomicAdd(&count[(size_t)(jmin + q / bw) * m.ni + imin + q % bw], v);
+    }
+  }
+  __syncthreads();
+}
+
 template <int DOM, bool STATS, bool MOM>
 __global__ void __launch_bounds__(PB, 4) k_push(MeshView m, ParticlesView P, PushArgs a,
                                               unsigned long long* __restrict__ count,
@@ -117,227 +341,8 @@ __global__ void __launch_bounds__(PB, 4) k_push(MeshView m, ParticlesView P, Pus
   unsigned st_n = 0;
 
   for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < P.n; t0 += (int64_t)gridDim.x * TILE) {
-    int pi[PPT], pj[PPT];
-    float pfx[PPT], pfy[PPT];
-    float pv[PPT][3];
-    bool dep[PPT];
-    int imin = INT_MAX, imax = -1, jmin = INT_MAX, jmax = -1;
-    // load phase: all of the thread's particles are requested before any is used, so
-    // each warp keeps PPT independent streams of loads in flight (streaming hints keep
-    // L2 for the field and the deposit grid)
-    uint32_t lcell[PPT];
-    float2 lfrac[PPT], lvxy[PPT];
-    float lvz[PPT];
-#pragma unroll
-    for (int k = 0; k < PPT; k++) {
-      const int64_t p = t0 + k * PB + threadIdx.x;
-      lcell[k] = DEAD;
-      lvz[k] = 0.f;
-      if (p < P.n) {
-        lcell[k] = __ldcs(&P.cell[p]);
-        lfrac[k] = __ldcs(&P.frac[p]);
-        lvxy[k] = __ldcs(&P.vxy[p]);
-        if (DOM != SF_DOMAIN_XY || STATS || MOM) lvz[k] = __ldcs(&P.vz[p]);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < PPT; k++) {
-      const int64_t p = t0 + k * PB + threadIdx.x;
-      dep[k] = false;
-      pi[k] = pj[k] = 0;
-      pfx[k] = pfy[k] = 0.f;
-      int status = 0;  // 1 finished here, 2 exact path, 3 removed at a domain face
-      if (p < P.n) {
-        const uint32_t c = lcell[k];
-        if (c != DEAD) {
-          const int i = cell_i(c), j = cell_j(c);
-          const float2 f = lfrac[k];
-          float2 v = lvxy[k];
-          // velocity update (KineticMaterial.java:336-346); B = 0
-          const float2 e = gather_E(m, i, j, f.x, f.y);
-          v.x += a.qm_dt * e.x;
-          v.y += a.qm_dt * e.y;
-          float vz = lvz[k];
-          // move in logical coordinates (x += v dt; XtoL)
-          float nfx, nfy, nvx = v.x, nvy = v.y, nvz = vz;
-          if (DOM == SF_DOMAIN_XY) {
-            nfx = f.x + v.x * a.dt_dx;
-            nfy = f.y + v.y * a.dt_dy;
-          } else if (DOM == SF_DOMAIN_ZR) {
-            // rotateToZR (KineticMaterial.java:444-462) relative to the cell radius rj
-            nfx = f.x + v.x * a.dt_dx;
-            const float rj = a.r0y + (float)j * a.dy;
-            const float A = vz * a.dt;
-            const float dl = f.y * a.dy + v.y * a.dt;
-            const float B = rj + dl;
-            const float R = sqrtf(A * A + B * B);
-            const float den = R + rj;
-            const float rrel = den > 0.f ? (A * A + dl * (2.f * rj + dl)) / den : 0.f;
-            nfy = rrel / a.dy;
-            const float cs = R > 0.f ? B / R : 1.f, sn = R > 0.f ? A / R : 0.f;
-            nvy = cs * v.y + sn * vz;
-            nvz = -sn * v.y + cs * vz;
-          } else {
-            // rotateToRZ (KineticMaterial.java:424-442), radius along x
-            nfy = f.y + v.y * a.dt_dy;
-            const float ri = a.r0x + (float)i * a.dx;
-            const float A = vz * a.dt;
-            const float dl = f.x * a.dx + v.x * a.dt;
-            const float B = ri + dl;
-            const float R = sqrtf(A * A + B * B);
-            const float den = R + ri;
-            const float rrel = den > 0.f ? (A * A + dl * (2.f * ri + dl)) / den : 0.f;
-            nfx = rrel / a.dx;
-            const float cs = R > 0.f ? B / R : 1.f, sn = R > 0.f ? A / R : 0.f;
-            nvx = cs * v.x + sn * vz;
-            nvz = -sn * v.x + cs * vz;
-          }
-          float fdi = floorf(nfx), fdj = floorf(nfy);
-          nfx -= fdi;
-          nfy -= fdj;
-          if (nfx >= 1.f) { nfx -= 1.f; fdi += 1.f; }
-          if (nfy >= 1.f) { nfy -= 1.f; fdj += 1.f; }
-          const int di = (int)fdi, dj = (int)fdj;
-          const int i2 = i + di, j2 = j + dj;
-          const int span = max(abs(di), abs(dj)) + 1;
-          const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
-          const bool clear = (int)__ldg(&m.seg_dist[j * m.ni + i]) > span;
-          if (inside && clear) {
-            __stcs(&P.cell[p], pack_cell(i2, j2));
-            __stcs(&P.frac[p], make_float2(nfx, nfy));
-            __stcs(&P.vxy[p], make_float2(nvx, nvy));
-            if (DOM != SF_DOMAIN_XY) __stcs(&P.vz[p], nvz);
-            status = 1;
-            dep[k] = true;
-            pi[k] = i2;
-            pj[k] = j2;
-            pfx[k] = nfx;
-            pfy[k] = nfy;
-            pv[k][0] = nvx;
-            pv[k][1] = nvy;
-            pv[k][2] = nvz;
-            imin = min(imin, i2);
-            imax = max(imax, i2);
-            jmin = min(jmin, j2);
-            jmax = max(jmax, j2);
-            if (STATS) {
-              st_n++;
-              st_px.add(nvx);
-              st_py.add(nvy);
-              st_pz.add(nvz);
-              st_e.add(sqrtf(nvx * nvx + nvy * nvy + nvz * nvz));
-            }
-          } else if (!inside && clear && m.all_delete) {
-            // no candidate segment on the way and every domain face removes particles
-            // (KineticMaterial.java:614-746: OPEN/DIRICHLET/... return false)
-            P.cell[p] = DEAD;
-            status = 3;
-          } else {
-            // exact path later: keep the old position, store the updated velocity
-            P.vxy[p] = v;
-            status = 2;
-          }
-        }
-      }
-      const unsigned ms = __ballot_sync(FULL, status == 2);
-      if (ms) {
-        const int leader = __ffs(ms) - 1;
-        unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(ms));
-        base = __shfl_sync(FULL, base, leader);
-        if (status == 2) slow_idx[base + __popc(ms & ((1u << lane) - 1u))] = (int)p;
-      }
-      const unsigned md = __ballot_sync(FULL, status == 3);
-      if (md && lane == __ffs(md) - 1) atomicAdd(&counters[1], (unsigned long long)__popc(md));
-    }
-    // ---- block bounding box of this tile's deposits ----
-    imin = __reduce_min_sync(FULL, imin);
-    jmin = __reduce_min_sync(FULL, jmin);
-    imax = __reduce_max_sync(FULL, imax);
-    jmax = __reduce_max_sync(FULL, jmax);
-    if (lane == 0) {
-      sred[0][wid] = imin;
-      sred[1][wid] = jmin;
-      sred[2][wid] = imax;
-      sred[3][wid] = jmax;
-    }
-    __syncthreads();
-    imin = sred[0][0];
-    jmin = sred[1][0];
-    imax = sred[2][0];
-    jmax = sred[3][0];
-#pragma unroll
-    for (int w = 1; w < PB / 32; w++) {
-      imin = min(imin, sred[0][w]);
-      jmin = min(jmin, sred[1][w]);
-      imax = max(imax, sred[2][w]);
-      jmax = max(jmax, sred[3][w]);
-    }
-    const int bw = imax - imin + 2, bh = jmax - jmin + 2;
-    const bool any = imax >= 0;
-    const bool use_smem = any && (bw * bh <= SBOX);
-    if (use_smem) {
-      for (int q = threadIdx.x; q < bw * bh; q += PB) {
-        acc_lo[q] = 0u;
-        acc_hi[q] = 0u;
-      }
-    }
-    __syncthreads();
-    if (any) {
-#pragma unroll
-      for (int k = 0; k < PPT; k++) {
-        // scatter skip rule at the far mesh edges (lc >= n-1 is not scattered)
-        // macroparticles per cell at (int) lc (KineticMaterial.updateSamples)
-        if (MOM && dep[k] && smp.mpc)
-          atomicAdd(&smp.mpc[(pj[k] + (pfy[k] >= 1.f)) * m.ni + pi[k] + (pfx[k] >= 1.f)], 1u);
-        const bool d = dep[k] && !((pfx[k] >= 1.f && pi[k] == m.ni - 2) || (pfy[k] >= 1.f && pj[k] == m.nj - 2));
-        if (!d) continue;
-        float wx, wy;
-        scatter_weights<DOM>(pfx[k], pfy[k], pi[k], pj[k], a, wx, wy);
-        const unsigned q[4] = {quant((1.f - wx) * (1.f - wy)), quant(wx * (1.f - wy)), quant(wx * wy),
-                               quant((1.f - wx) * wy)};
-        if (MOM) {
-          const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
-          const int base = pj[k] * m.ni + pi[k];
-          const int off[4] = {0, 1, m.ni + 1, m.ni};
-#pragma unroll
-          for (int cc = 0; cc < 4; cc++)
-#pragma unroll
-            for (int dd = 0; dd < 3; dd++)
-              atomicAdd((unsigned long long*)&mom[dd * nn + base + off[cc]],
-                        (unsigned long long)__float2ll_rn(s[cc] * pv[k][dd] * 65536.0f));
-          if (smp.mom2)
-#pragma unroll
-            for (int cc = 0; cc < 4; cc++)
-#pragma unroll
-              for (int dd = 0; dd < 3; dd++)
-                atomicAdd(&smp.mom2[dd * nn + base + off[cc]],
-                          __float2ull_rn(s[cc] * pv[k][dd] * pv[k][dd] * (float)MOM2_SCALE));
-        }
-        if (use_smem) {
-          const int l = (pj[k] - jmin) * bw + (pi[k] - imin);
-          const int off[4] = {0, 1, bw + 1, bw};
-#pragma unroll
-          for (int cc = 0; cc < 4; cc++) {
-            atomicAdd(&acc_lo[l + off[cc]], q[cc] & 0xFFFFu);
-            atomicAdd(&acc_hi[l + off[cc]], q[cc] >> 16);
-          }
-        } else {
-          const size_t u = (size_t)pj[k] * m.ni + pi[k];
-          const size_t off[4] = {0, 1, (size_t)m.ni + 1, (size_t)m.ni};
-#pragma unroll
-          for (int cc = 0; cc < 4; cc++) atomicAdd(&count[u + off[cc]], (unsigned long long)q[cc]);
-        }
-      }
-    }
-    __syncthreads();
-    if (use_smem) {
-      for (int q = threadIdx.x; q < bw * bh; q += PB) {
-        const unsigned long long v = ((unsigned long long)acc_hi[q] << 16) + acc_lo[q];
-        if (v) atomicAdd(&count[(size_t)(jmin + q / bw) * m.ni + imin + q % bw], v);
-      }
-    }
-    __syncthreads();
+    push_tile<DOM, STATS, MOM>(m, P, a, t0, count, mom, slow_idx, counters, smp, acc_lo, acc_hi, sred, st_px, st_py,
+                               st_pz, st_e, st_n);
   }
   if (STATS) {
     // block reduction of the per-thread sums (FP64 from here on)
@@ -409,11 +414,6 @@ __device__ double sample_maxw_speed(Philox& r, double v_th) {
   return v;
 }
 
-struct SlowArgs {
-  SurfaceView sv;
-  unsigned long long* counters;
-  double* stats_slow;   // 5 sums + boundary charge
-};
 
 // Visits the DIRICHLET/SINK segments that KineticMaterial.ProcessBoundary collects for
 // the node box [i_min..i_max] x [j_min..j_max] (KineticMaterial.java:480-515); f(s)
@@ -692,11 +692,14 @@ __device__ bool may_hit_fp32(const MeshView& m, int i, int j, float fx, float fy
   return hit;
 }
 
+// The exact path over the slow-queue entries t_first, t_first + t_stride, ... below t_end
+// (every thread of the block calls it; totals are flushed to the instance at the end).
 template <int DOM>
-__global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, PushArgs a, SlowArgs sg,
-                                                   const int* __restrict__ slow_idx,
-                                                   unsigned long long* __restrict__ count,
-                                                   long long* __restrict__ mom, int mom_on, SampleView smp) {
+__device__ __forceinline__ void push_slow_body(const MeshView& m, const ParticlesView& P, const PushArgs& a,
+                                               const SlowArgs& sg, const int* __restrict__ slow_idx,
+                                               unsigned long long* __restrict__ count, long long* __restrict__ mom,
+                                               int mom_on, const SampleView& smp, unsigned long long t_first,
+                                               unsigned long long t_end, unsigned long long t_stride) {
   // Totals, counters and (for small geometries) per-segment surface sums are first
   // accumulated per block in shared memory and flushed once at the end: the exact
   // path's particles hit the same few segments, so global atomics would serialise.
@@ -704,11 +707,11 @@ __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, 
   __shared__ double s_seg[4 * SMALL_NSEG];
   __shared__ unsigned long long s_cnt[4];
   const bool seg_local = m.nseg <= SMALL_NSEG;
+  __syncthreads();  // a block calling this again: the previous call's flush has read everything
   for (int q = threadIdx.x; q < 8; q += blockDim.x) s_stats[q] = 0.0;
   for (int q = threadIdx.x; q < 4 * SMALL_NSEG; q += blockDim.x) s_seg[q] = 0.0;
   if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0ULL;
   __syncthreads();
-  const unsigned long long nslow = sg.counters[0];
   SlowArgs sa = sg;
   sa.stats_slow = s_stats;
   sa.counters = s_cnt;
@@ -721,8 +724,7 @@ __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, 
   // end instead of six per particle on the same few addresses)
   double lst[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   unsigned long long ldone = 0;
-  for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; t < nslow;
-       t += (unsigned long long)gridDim.x * blockDim.x) {
+  for (unsigned long long t = t_first; t < t_end; t += t_stride) {
     const int64_t p = slow_idx[t];
     const uint32_t c = P.cell[p];
     const float2 f = P.frac[p];
@@ -851,6 +853,16 @@ __global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, 
     }
 }
 
+template <int DOM>
+__global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, PushArgs a, SlowArgs sg,
+                                                   const int* __restrict__ slow_idx,
+                                                   unsigned long long* __restrict__ count,
+                                                   long long* __restrict__ mom, int mom_on, SampleView smp) {
+  push_slow_body<DOM>(m, P, a, sg, slow_idx, count, mom, mom_on, smp,
+                     (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x, sg.counters[0],
+                     (unsigned long long)gridDim.x * blockDim.x);
+}
+
 // int64 fixed point -> density (Field2D.scaleByVol, Field2D.java:418-431) and mean
 // velocities (Field2D.divideByField, :403-414)
 __global__ void k_finalize(int nn, const unsigned long long* __restrict__ count, const long long* __restrict__ mom,
@@ -936,6 +948,137 @@ struct PushScratch {
   double* sums;
 };
 
+// ---------------------------------------------------------------------------------
+// batched push over the instances of a batch (one launch for all instances)
+// ---------------------------------------------------------------------------------
+// instance holding global tile gt: tile_start[i] <= gt < tile_start[i + 1]
+__device__ __forceinline__ int batch_find(const int64_t* __restrict__ tile_start, int n, int64_t gt) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (tile_start[mid] <= gt) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Exclusive prefix of val(0..n-1) into out[0..n] (out[n] = total) by one block whose size
+// is a multiple of 32; val(i) is called once per i.
+template <typename F>
+__device__ void block_exclusive_prefix(int n, F val, int64_t* __restrict__ out) {
+  __shared__ int64_t wsum[32];
+  __shared__ int64_t carry;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const int64_t v = i < n ? val(i) : 0;
+    int64_t x = v;  // inclusive prefix within the warp
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int64_t w = lane < nwarps ? wsum[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[lane] = w;  // inclusive prefix of the warp totals
+    }
+    __syncthreads();
+    const int64_t before = carry + (warp > 0 ? wsum[warp - 1] : 0) + x - v;
+    if (i < n) out[i] = before;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = before + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
+// slots in use after this step's injection, and the prefix of push tiles (one block)
+__global__ void __launch_bounds__(1024) k_batch_begin(BatchDev b) {
+  block_exclusive_prefix(
+      b.n,
+      [&](int i) {
+        const int64_t nd = b.base_dev[i] + (int64_t)b.added_dev[i];
+        b.n_dev[i] = nd;
+        return (nd + TILE - 1) / TILE;
+      },
+      b.tile_start);
+}
+
+// the slow queues of all instances cut into chunks of SLOW_CHUNK entries: prefix of the
+// chunk counts (one block, after the batched fast push filled the queues)
+constexpr int SLOW_CHUNK = 512;
+__global__ void __launch_bounds__(1024) k_slow_plan(BatchDev b) {
+  block_exclusive_prefix(
+      b.n, [&](int i) { return (int64_t)((b.insts[i].sa.counters[0] + SLOW_CHUNK - 1) / SLOW_CHUNK); },
+      b.chunk_start);
+}
+
+// per instance: zero the deposit, the push counters and the slow-path sums
+__global__ void k_batch_zero(BatchDev b) {
+  const BatchInst& I = b.insts[blockIdx.y];
+  const int nn = I.m.ni * I.m.nj;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x) I.count[u] = 0ULL;
+  if (blockIdx.x == 0 && threadIdx.x < 8) {
+    if (threadIdx.x < 4) I.sa.counters[threadIdx.x] = 0ULL;
+    I.sa.stats_slow[threadIdx.x] = 0.0;
+  }
+}
+
+template <int DOM>
+__global__ void __launch_bounds__(PB, 4) k_push_batch(BatchDev b) {
+  __shared__ unsigned acc_lo[SBOX];
+  __shared__ unsigned acc_hi[SBOX];
+  __shared__ int sred[4][PB / 32];
+  Kahan st_px, st_py, st_pz, st_e;
+  unsigned st_n = 0;
+  const int64_t total = b.tile_start[b.n];
+  for (int64_t gt = blockIdx.x; gt < total; gt += gridDim.x) {
+    const int i = batch_find(b.tile_start, b.n, gt);
+    const BatchInst& I = b.insts[i];
+    ParticlesView P = I.P;
+    P.n = b.n_dev[i];
+    push_tile<DOM, false, false>(I.m, P, I.a, (gt - b.tile_start[i]) * TILE, I.count, nullptr, I.slow_idx,
+                                 I.sa.counters, SampleView{nullptr, nullptr}, acc_lo, acc_hi, sred, st_px, st_py,
+                                 st_pz, st_e, st_n);
+  }
+}
+
+// The exact path over the chunks of all instances' slow queues: every block takes chunks
+// in turn, so an instance with a long queue is spread over the whole GPU.
+template <int DOM>
+__global__ void __launch_bounds__(128) k_push_slow_batch(BatchDev b) {
+  const int64_t total = b.chunk_start[b.n];
+  for (int64_t c = blockIdx.x; c < total; c += gridDim.x) {
+    const int i = batch_find(b.chunk_start, b.n, c);
+    const BatchInst& I = b.insts[i];
+    const unsigned long long t0 = (unsigned long long)(c - b.chunk_start[i]) * SLOW_CHUNK;
+    const unsigned long long t1 = min(t0 + (unsigned long long)SLOW_CHUNK, I.sa.counters[0]);
+    push_slow_body<DOM>(I.m, I.P, I.a, I.sa, I.slow_idx, I.count, nullptr, 0, SampleView{nullptr, nullptr},
+                        t0 + threadIdx.x, t1, blockDim.x);
+  }
+}
+
+// nd = count w / V + nd_back per instance; removed slots counted; the instance's push
+// step (its surface RNG epoch) and the batch step advanced
+__global__ void k_finalize_batch(BatchDev b) {
+  BatchInst& I = b.insts[blockIdx.y];
+  const int nn = I.m.ni * I.m.nj;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x)
+    I.nd[u] = (double)I.count[u] * I.w_scale / I.vol[u] + I.nd_back;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    b.dead_dev[blockIdx.y] += (int64_t)I.sa.counters[1];
+    I.a.step++;
+    if (blockIdx.y == 0) atomicAdd(b.step_dev, 1u);
+  }
+}
+
 template <int DOM, bool STATS, bool MOM>
 void launch_push_t(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid, const PushScratch& sc,
                    const SampleView& smp) {
@@ -955,6 +1098,16 @@ void launch_push_dom(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid, bo
 }  // namespace
 
 namespace sf {
+
+void batch_push(const BatchDev& b, cudaStream_t stream, int num_sms, int blocks_per_sm, int slow_blocks_per_sm) {
+  k_batch_begin<<<1, 1024, 0, stream>>>(b);
+  k_batch_zero<<<dim3(8, b.n), 256, 0, stream>>>(b);
+  k_push_batch<SF_DOMAIN_XY><<<num_sms * blocks_per_sm, PB, 0, stream>>>(b);
+  k_slow_plan<<<1, 1024, 0, stream>>>(b);
+  k_push_slow_batch<SF_DOMAIN_XY><<<num_sms * slow_blocks_per_sm, 128, 0, stream>>>(b);
+  k_finalize_batch<<<dim3(4, b.n), 256, 0, stream>>>(b);
+  SF_CUDA(cudaGetLastError());
+}
 
 void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments) {
   int nn = ctx->ni * ctx->nj;

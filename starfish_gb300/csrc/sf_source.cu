@@ -8,6 +8,7 @@
 // (Source.sampleKinetic, core/source/Source.java:167-198) and appended with the -dt/2
 // velocity rewind of KineticMaterial.addParticle (KineticMaterial.java:776-796).
 // Random numbers come from counter-based Philox streams keyed by (step, particle).
+#include <algorithm>
 #include <cmath>
 
 #include "sf_internal.h"
@@ -46,9 +47,9 @@ __device__ inline double maxw1d_unit(Philox& r) {
   return 0.7071067811865476 * (s - 6.0);
 }
 
-__global__ void k_inject_maxwellian(MeshView m, ParticlesView P, InjectArgs a, int n, unsigned long long* counter) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
+// Particle k of this step's injection on the segment of a; appended at a.base + slot.
+__device__ __forceinline__ void inject_one(const MeshView& m, const ParticlesView& P, const InjectArgs& a, int64_t k,
+                                           unsigned long long* counter) {
   Philox rng(a.seed, RNG_INJECT, (uint64_t)k, a.step);
   double t = rng.uniform();  // Boundary.randomT on a single segment
   if (a.axi) t = frustum_t(t, a.r1, a.r2);
@@ -81,7 +82,68 @@ __global__ void k_inject_maxwellian(MeshView m, ParticlesView P, InjectArgs a, i
   P.vz[d] = (float)vz;
 }
 
+__global__ void k_inject_maxwellian(MeshView m, ParticlesView P, InjectArgs a, int n, unsigned long long* counter) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) inject_one(m, P, a, k, counter);
+}
+
+// ---- batched sources (one launch for all instances of a batch) -------------------
+// per instance: this step's count from the flux and the remainder (Source.regenerate),
+// clamped to the capacity
+__global__ void k_inject_prepare(BatchDev b) {
+  for (int i = threadIdx.x; i < b.n; i += blockDim.x) {
+    const BatchInst& I = b.insts[i];
+    const int64_t base = b.n_dev[i];
+    int64_t num = 0;
+    if (I.src_on) {
+      const double mp = I.mp_step + b.rem_dev[i];
+      num = (int64_t)mp;
+      b.rem_dev[i] = mp - (double)num;
+      if (base + num > I.cap) {
+        num = I.cap > base ? I.cap - base : 0;
+        atomicExch(b.overflow, 1);
+      }
+    }
+    b.num_dev[i] = num;
+    b.base_dev[i] = base;
+    b.added_dev[i] = 0ULL;
+  }
+}
+
+__global__ void k_inject_batch(BatchDev b) {
+  const int i = blockIdx.y;
+  const BatchInst& I = b.insts[i];
+  const int64_t num = b.num_dev[i];
+  if (num <= 0) return;
+  InjectArgs a;
+  a.x1 = I.sx1;
+  a.y1 = I.sy1;
+  a.x2 = I.sx2;
+  a.y2 = I.sy2;
+  a.nx = I.snx;
+  a.ny = I.sny;
+  a.v_th = I.v_th;
+  a.v_drift = I.v_drift;
+  a.dt = I.src_dt;
+  a.qm_halfdt = I.qm_halfdt;
+  a.seed = I.src_seed;
+  a.step = *b.step_dev;
+  a.base = b.base_dev[i];
+  a.axi = 0;
+  a.r1 = a.r2 = 0.0;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < num; k += (int64_t)gridDim.x * blockDim.x)
+    inject_one(I.m, I.P, a, k, &b.added_dev[i]);
+}
+
 }  // namespace
+
+namespace sf {
+void batch_inject(const BatchDev& b, cudaStream_t stream, int num_sms) {
+  k_inject_prepare<<<1, 256, 0, stream>>>(b);
+  k_inject_batch<<<dim3(std::max(1, num_sms / 8), b.n), 256, 0, stream>>>(b);
+  SF_CUDA(cudaGetLastError());
+}
+}  // namespace sf
 
 extern "C" int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg, double den, double v_drift,
                                     double temp, double dt, double* rem, int64_t* n_added) {

@@ -481,6 +481,7 @@ struct SfUnet {
   std::vector<UAct> dec;        // 2 per decoder level
   float *pred = nullptr, *target = nullptr, *gpred = nullptr, *loss = nullptr;
   std::vector<void*> allocs;
+  cudaStream_t stream = nullptr;  // the context's stream (set-up copies and fills)
   int64_t samples = 0, steps = 0;
   int64_t pairs = 0;               // converged pairs seen while training
   int train_every = 1;             // one training step every train_every pairs
@@ -504,7 +505,7 @@ struct SfUnet {
 static void* ualloc(SfUnet* u, size_t bytes) {
   void* p = nullptr;
   SF_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
-  SF_CUDA(cudaMemset(p, 0, std::max<size_t>(bytes, 16)));
+  zero_wait(p, std::max<size_t>(bytes, 16), u->stream);
   u->allocs.push_back(p);
   return p;
 }
@@ -538,7 +539,7 @@ static UConv make_conv(SfUnet* u, int cin, int cout, std::mt19937& rng) {
   c.vb = (float*)ualloc(u, 4 * cout);
   c.w16 = (bf16*)ualloc(u, 2 * c.nw);
   c.wflip = (bf16*)ualloc(u, 2 * c.nw);
-  SF_CUDA(cudaMemcpy(c.w, h.data(), 4 * c.nw, cudaMemcpyHostToDevice));
+  copy_wait(c.w, h.data(), 4 * c.nw, cudaMemcpyHostToDevice, u->stream);
   return c;
 }
 
@@ -611,7 +612,7 @@ static void unet_build(sf_ctx* ctx, SfUnet* u, uint64_t seed) {
   u->vhw = (float*)ualloc(u, 4 * C[0]);
   u->mhb = (float*)ualloc(u, 4);
   u->vhb = (float*)ualloc(u, 4);
-  SF_CUDA(cudaMemcpy(u->hw, hw.data(), 4 * C[0], cudaMemcpyHostToDevice));
+  copy_wait(u->hw, hw.data(), 4 * C[0], cudaMemcpyHostToDevice, u->stream);
   // activations
   u->x = make_act(u, u->Hn, u->Wn, 16);
   int H = u->Hn, W = u->Wn;
@@ -893,6 +894,7 @@ int sf_unet_init(sf_ctx* ctx, int32_t base_channels, int32_t down, uint64_t seed
   sf_unet_destroy_internal(ctx);
   SfUnet* u = new SfUnet();
   ctx->unet = u;
+  u->stream = ctx->stream;
   u->base = base_channels;
   u->down = down;
   u->Wn = (ctx->ni - 1) / down;
@@ -981,8 +983,8 @@ int sf_unet_params(sf_ctx* ctx, float* get, const float* set) {
   SfUnet* u = ctx->unet;
   int64_t off = 0;
   auto io = [&](float* d, size_t n) {
-    if (get) SF_CUDA(cudaMemcpy(get + off, d, 4 * n, cudaMemcpyDeviceToHost));
-    if (set) SF_CUDA(cudaMemcpy(d, set + off, 4 * n, cudaMemcpyHostToDevice));
+    if (get) copy_wait(get + off, d, 4 * n, cudaMemcpyDeviceToHost, ctx->stream);
+    if (set) copy_wait(d, set + off, 4 * n, cudaMemcpyHostToDevice, ctx->stream);
     off += (int64_t)n;
   };
   for (auto& c : u->convs) {

@@ -352,3 +352,52 @@ class MCC:
         self.d.check(self.d.lib.sf_mcc(self.d.ctx, self.km.sid, self.model, C.byref(self.sigma), dt,
                                        C.byref(n)))
         return n.value
+
+
+class GpuBatch:
+    """Independent instances advanced together (sf_batch_*): each instance is a GpuDomain
+    with one KineticMaterial; a step runs every instance's source, push + scatter (one
+    batched device phase) and Poisson solve + E (overlapping on the GPU)."""
+
+    def __init__(self, domains, materials, threads=8):
+        self.domains, self.materials = list(domains), list(materials)
+        self.lib = abi.load()
+        n = len(self.domains)
+        ctxs = (C.c_void_p * n)(*[d.ctx.value for d in self.domains])
+        sids = np.ascontiguousarray([m.sid for m in self.materials], np.int32)
+        h = C.c_void_p()
+        rc = self.lib.sf_batch_create(ctxs, abi.ptr(sids), n, int(threads), C.byref(h))
+        abi.check(rc, None)
+        self.b = h
+        self._sids = sids
+
+    def check(self, rc):
+        if rc != abi.SF_OK:
+            raise abi.SfError(rc, (self.lib.sf_batch_last_error(self.b) or b"").decode())
+
+    def set_source(self, i, seg_xy, den, v_drift, temp):
+        seg = np.ascontiguousarray(seg_xy, np.float64).reshape(-1)
+        self.check(self.lib.sf_batch_set_source(self.b, int(i), abi.ptr(seg), den, v_drift, temp))
+
+    def step(self, dt, solver: "PoissonSolver"):
+        st = abi.BatchStats()
+        self.check(self.lib.sf_batch_step(self.b, float(dt), C.byref(solver.prm), C.byref(st)))
+        return st.as_dict()
+
+    def tuning(self):
+        bps, sb = C.c_int32(), C.c_int32()
+        cyc = np.zeros(3, np.int32)
+        self.check(self.lib.sf_batch_tuning(self.b, C.byref(bps), C.byref(sb), abi.ptr(cyc)))
+        return {"push_blocks_per_sm": bps.value, "slow_blocks_per_sm": sb.value,
+                "pcg_iterations_by_bucket": cyc.tolist()}
+
+    def close(self):
+        if self.b:
+            self.lib.sf_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -286,3 +286,37 @@ def jet_particles(cfg: JetConfig, n, seed):
     vel[:, 0] += cfg.v_drift * out[:, 0] / rr
     vel[:, 1] += cfg.v_drift * out[:, 1] / rr
     return out, vel
+
+
+# ---------------------------------------------------------------------------------------
+# batched uneven instances (config-0-type cases of many sizes)
+# ---------------------------------------------------------------------------------------
+@dataclass
+class BatchCase:
+    mesh: MeshSpec
+    ion: IonSpecies
+    n_particles: int
+    phi_electrode: float
+    seed: int
+
+
+def config4(n_instances=256, seed=0, max_particles=2_000_000, min_particles=10_000):
+    """Independent 81x41-type ES-PIC cases: mesh sizes log-uniform from 33x17 to 257x129
+    nodes (rounded to 16k + 1 nodes per direction so that multigrid coarsens them), dx = 1
+    mm, centred electrode box at a potential uniform in [-200, -20] V, preloaded ion counts
+    log-uniform in [1e4, 2e6] at the 1e12 m^-3 plasma density, O+ inlet on the x = 0 face,
+    seeds 0..n-1."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for k in range(n_instances):
+        e = rng.uniform(0.0, 3.0)
+        ni = int(16 * round(2 * 2 ** e)) + 1
+        nj = (ni - 1) // 2 + 1
+        phi = rng.uniform(-200.0, -20.0)
+        m = es_pic_mesh(ni, nj, 1e-3, electrode_halfwidth=4.5e-3, phi_electrode=phi)
+        n = int(round(np.exp(rng.uniform(np.log(min_particles), np.log(max_particles)))))
+        Lx, Ly = m.lengths()
+        gas_area = Lx * Ly - (2 * 4.5e-3) ** 2
+        ion = IonSpecies(spwt=1e12 * gas_area / n)
+        cases.append(BatchCase(m, ion, n, phi, k))
+    return cases

@@ -76,3 +76,33 @@ def test_bad_arguments_rejected(lib):
     d = spec.desc()
     d.ni = 2
     assert lib.sf_ctx_create(C.byref(d), 0, C.byref(h)) == abi.SF_ERR_ARG
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every ctypes structure has the size and field offsets that the C compiler gives the
+    header's struct of the same name (a shorter Python struct would let the library write
+    past its end)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = [(abi.MeshDesc, "sf_mesh_desc"), (abi.PushStats, "sf_push_stats"),
+             (abi.PoissonParams, "sf_poisson_params"), (abi.SolveStats, "sf_solve_stats"),
+             (abi.Sigma, "sf_sigma"), (abi.BatchStats, "sf_batch_stats")]
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "starfish_gpu.h"', "int main(void) {"]
+    expect = []
+    for cls, cname in pairs:
+        lines.append(f'  printf("%zu\\n", sizeof({cname}));')
+        expect.append(C.sizeof(cls))
+        for f in cls._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({cname}, {f[0]}));')
+            expect.append(getattr(cls, f[0]).offset)
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == expect

@@ -124,3 +124,34 @@ def test_poisson_large_mesh_residual(gpulib):
     R = lap - (-rho.reshape(nj, ni) / EPS0 + QE / EPS0 * 1e12 * np.exp(P / 2.0))
     R[fixed] = (P - spec.bc_value.reshape(nj, ni))[fixed]
     assert np.sqrt((R ** 2).sum()) / spec.nn < 1e-6
+
+
+def test_solves_independent_of_other_contexts(gpulib):
+    """Two contexts in one process: A (81x41, large single-CTA coarse end), then B
+    (33x17, small coarse end), then A solves again with another PCG iteration count, so
+    its Newton step is captured anew after B was set up.  Each context's result must not
+    depend on the other's existence: A's potential equals that of A alone, bit for bit."""
+    from starfish_gb300.plugin import GpuDomain, PoissonSolver
+    big, small = W.es_pic_mesh(81, 41, 1e-3), W.es_pic_mesh(33, 17, 1e-3)
+    rho_b, rho_s = ion_rho(big, 1), ion_rho(small, 2)
+
+    def solve(dom, spec, rho, cycles):
+        ps = PoissonSolver(dom, n0=1e12, Te0=2.0, tol=1e-6, max_it=60, cycles=cycles)
+        return ps.solve(rho=rho, phi=np.zeros(spec.nn))
+
+    alone = GpuDomain(big)
+    try:
+        ref4, _ = solve(alone, big, rho_b, 4)
+        ref3, _ = solve(alone, big, rho_b, 3)
+    finally:
+        alone.close()
+    a, b = GpuDomain(big), GpuDomain(small)
+    try:
+        p4, _ = solve(a, big, rho_b, 4)
+        _, sb = solve(b, small, rho_s, 4)
+        p3, st = solve(a, big, rho_b, 3)
+        assert sb["status"] == 0 and st["status"] == 0
+        assert np.array_equal(p4, ref4) and np.array_equal(p3, ref3)
+    finally:
+        a.close()
+        b.close()

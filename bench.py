@@ -267,7 +267,7 @@ def dsmc_jet_bench(steps=20, warmup=3, n_particles=16 * 1024 * 1024, seed=0):
         dom.close()
 
 
-def batch_bench(n_instances=256, steps=16, warmup=10, threads=16, dt=5e-7):
+def batch_bench(n_instances=256, steps=16, warmup=10, threads=16, dt=5e-7, unbatched_steps=3):
     """The batched-instances workload: 256 independent 81x41-type ES-PIC cases (mesh sizes
     log-uniform from 33x17 to 257x129 nodes, 1e4..2e6 preloaded ions each, electrode at
     -200..-20 V, O+ inlet, seeds 0..255) advanced together by sf_batch_step: batched
@@ -317,6 +317,30 @@ def batch_bench(n_instances=256, steps=16, warmup=10, threads=16, dt=5e-7):
             solve_max = max(solve_max, st["solve_ms_max"])
             newton += st["newton_it_mean"]
         wall = time.perf_counter() - t0
+        tuning = batch.tuning()
+        batch.close()
+        # the same instances afterwards, one at a time through the per-instance entry
+        # points (source, push + scatter, rho, Poisson with the tuned PCG iterations, E)
+        ps_u, wall_u = 0, 0.0
+        if unbatched_steps > 0:
+            for c, ps in zip(cases, solvers):
+                nn = c.mesh.nn
+                ps.prm.cycles = tuning["pcg_iterations_by_bucket"][0 if nn < 4096 else (1 if nn < 16384 else 2)]
+            live_u = sum(km.get_np() for km in kms)
+            t1 = time.perf_counter()
+            for _ in range(unbatched_steps):
+                ps_u += live_u
+                live_u = 0
+                for c, km, ps in zip(cases, kms, solvers):
+                    Ly = c.mesh.lengths()[1]
+                    km.sample_maxwellian_source(np.array([0.0, Ly, 0.0, 0.0]), c.ion.den, c.ion.v_drift,
+                                                c.ion.temp, dt)
+                    km.update_fields(dt, stats=False)
+                    ps.update_rho()
+                    ps.solve()
+                    ps.update_gradient_field()
+                    live_u += km.get_np()
+            wall_u = time.perf_counter() - t1
         sizes = [c.mesh.nn for c in cases]
         return {"metric": "particle-steps/s over all instances (source + push + scatter + Poisson + E)",
                 "value": psteps / wall, "unit": "particle-steps/s", "ms_per_step": 1e3 * wall / steps,
@@ -324,8 +348,13 @@ def batch_bench(n_instances=256, steps=16, warmup=10, threads=16, dt=5e-7):
                 "particles_live_end": live, "mesh_nodes": [min(sizes), max(sizes)],
                 "device_phase_ms": dev_ms / steps, "solve_ms_sum_per_step": solve_sum / steps,
                 "solve_ms_max": solve_max, "newton_it_mean": newton / steps,
-                "host_threads": threads, "tuning": batch.tuning(), "setup_s": t_setup,
-                "timing": "wall clock of sf_batch_step (host threads and graph launches included)"}
+                "host_threads": threads, "tuning": tuning, "setup_s": t_setup,
+                "timing": "wall clock of sf_batch_step (host threads and graph launches included)",
+                "unbatched": None if unbatched_steps <= 0 else {
+                    "value": ps_u / wall_u, "ms_per_step": 1e3 * wall_u / unbatched_steps,
+                    "steps": unbatched_steps,
+                    "how": "the same contexts after the batched steps, each instance stepped in turn "
+                           "from one host thread through the per-instance entry points"}}
     finally:
         batch.close()
         for d in doms:

@@ -394,7 +394,28 @@ int sf_mcc_set_target(sf_ctx* ctx, double mass, const double* den, const double*
  * SF_MCC_CEX (charge exchange, :287-297). */
 #define SF_MCC_MEX 0
 #define SF_MCC_CEX 1
+#define SF_MCC_IONIZATION 2
 int sf_mcc(sf_ctx* ctx, int32_t sid, int32_t model, const sf_sigma* sigma, double dt, int64_t* n_coll);
+/* MCC.perform with ModelIonization (MCC.java:304-356): electrons (species sid) against the
+ * neutral target.  On a collision the electron loses ionization_energy (eV) and keeps a
+ * uniform random share of the rest, with an isotropic direction; a second electron with
+ * the same speed (the reference draws its speed from the first share too) is appended to
+ * sid, and (int)(spwt_sid / spwt_product + rnd) ions of product_sid, Maxwellian at the
+ * target temperature (100 K where it is <= 0), at the same place.  New particles get the
+ * -dt/2 rewind of addParticle.  The created product weight is summed into the delta-N
+ * field (sf_mcc_get_sums); the caller removes it from its target density (the
+ * reference's KineticMaterial.deleteMass).  Products past a species' capacity are
+ * dropped and the call returns SF_ERR_OOM.  *n_electrons / *n_ions: created. */
+int sf_mcc_ionization(sf_ctx* ctx, int32_t sid, int32_t product_sid, const sf_sigma* sigma,
+                      double ionization_energy, double dt, int64_t* n_coll, int64_t* n_electrons,
+                      int64_t* n_ions);
+/* Sums accumulated by every MCC call since the target was set or the last reset, ni*nj
+ * node fields each (any pointer may be NULL): S, the target's energy term mpw (E1 - E2) /
+ * (dt V) with E = 0.5 m |v| as in MCC.java:204-210, scattered like Field2D.scatter;
+ * count_sum and real_sum (collisions and collided weight at node (int) lc, MCC.java:
+ * 213-218); delta_n (product weight created by ionization at node (int) lc). */
+int sf_mcc_get_sums(sf_ctx* ctx, double* S, double* count_sum, double* real_sum, double* delta_n,
+                    int32_t reset);
 
 /* ---- measurement ---------------------------------------------------------- */
 /* The CUDA stream (cudaStream_t) all work of the context is issued on. */

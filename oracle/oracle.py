@@ -94,6 +94,11 @@ def _declare(L):
     L.orc_mcc.argtypes = [C.c_int, C.c_int, d, d, C.c_int, i8, i8, C.c_int, d, C.c_double,
                           C.c_double, d, d, d, d, d, C.c_double, C.c_double, C.c_int, C.c_int64]
     L.orc_mcc.restype = C.c_long
+    L.orc_mcc_ex.argtypes = [C.c_int, C.c_int, d, d, C.c_int, i8, i8, C.c_int, d, C.c_double,
+                             C.c_double, d, d, d, d, d, C.c_double, C.c_double, C.c_int, C.c_int64,
+                             C.c_double, C.c_double, C.c_double, C.c_double, d, d, d, d, C.c_long,
+                             d, C.POINTER(C.c_long), d, C.POINTER(C.c_long)]
+    L.orc_mcc_ex.restype = C.c_long
 
 
 def _f64(a):
@@ -284,6 +289,27 @@ def mcc(m: OMesh, parts, src_mass, tgt_mass, tden, tu, tv, tw, tT, sigma, dt, mo
     return lib().orc_mcc(*m.args(), parts.shape[0], parts.reshape(-1), src_mass, tgt_mass,
                          _f64(tden), _f64(tu), _f64(tv), _f64(tw), _f64(tT), sigma, dt,
                          int(model), int(seed))
+
+
+def mcc_ex(m: OMesh, parts, src_mass, tgt_mass, tden, tu, tv, tw, tT, sigma, dt, model, seed,
+           src_spwt=1.0, e_ion=0.0, prod_mass=1.0, prod_spwt=1.0, max_new=0):
+    """MCC with every model (2 = ionization) and its outputs: a dict with the collision
+    count, the S / count_sum / real_sum / delta_n node fields and the created electrons and
+    ions (12-double particles, velocities before the addParticle rewind)."""
+    nn = m.ni * m.nj
+    out = {k: np.zeros(nn) for k in ("S", "count_sum", "real_sum", "delta_n")}
+    new_e = np.zeros((max(max_new, 1), 12))
+    new_i = np.zeros((max(max_new, 1), 12))
+    ne, ni = C.c_long(), C.c_long()
+    out["cols"] = lib().orc_mcc_ex(*m.args(), parts.shape[0], parts.reshape(-1), src_mass, tgt_mass,
+                                   _f64(tden), _f64(tu), _f64(tv), _f64(tw), _f64(tT), sigma, dt, int(model),
+                                   int(seed), src_spwt, e_ion, prod_mass, prod_spwt, out["S"], out["count_sum"],
+                                   out["real_sum"], out["delta_n"], int(max_new), new_e.reshape(-1), C.byref(ne),
+                                   new_i.reshape(-1), C.byref(ni))
+    out["n_new_e"], out["n_new_i"] = ne.value, ni.value
+    out["new_e"] = new_e[:min(ne.value, max_new)]
+    out["new_i"] = new_i[:min(ni.value, max_new)]
+    return out
 
 
 def jrandom_doubles(seed, n):

@@ -1344,16 +1344,24 @@ long orc_dsmc(int ni, int nj, const double* cell_vol, int n, double* parts, doub
 // --- MCC (collisions/MCC.java:167-285): MEX (elastic) or CEX against a Maxwellian
 // target described by node fields (den, u, v, w, T).  Constant cross-section sigma
 // (SigmaConst, Sigma.java:121-126).  model: 0 = MEX, 1 = CEX.  Returns collisions.
-long orc_mcc(int ni, int nj, const double* x0, const double* dh, int domain,
-             const int8_t* node_type, const int8_t* face_type, int n, double* parts,
-             double src_mass, double tgt_mass, const double* tden, const double* tu,
-             const double* tv, const double* tw, const double* tT, double sigma, double dt,
-             int model, int64_t seed) {
+// MCC.perform(mesh) (collisions/MCC.java:167-221) with the models MEX (:242-285), CEX
+// (:287-297) and ionization (:304-356), in the reference's order of random draws.  The
+// optional outputs are ni*nj node fields accumulated in place (S, count_sum, real_sum,
+// delta_n) and the particles ionization creates (12 doubles each, velocities before the
+// addParticle rewind, which needs E and is left to the caller).
+long orc_mcc_ex(int ni, int nj, const double* x0, const double* dh, int domain, const int8_t* node_type,
+                const int8_t* face_type, int n, double* parts, double src_mass, double tgt_mass, const double* tden,
+                const double* tu, const double* tv, const double* tw, const double* tT, double sigma, double dt,
+                int model, int64_t seed, double src_spwt, double e_ion, double prod_mass, double prod_spwt,
+                double* S, double* count_sum, double* real_sum, double* delta_n, long max_new, double* new_e,
+                long* n_new_e, double* new_i, long* n_new_i) {
   Mesh m = make_mesh(ni, nj, x0, dh, domain, node_type, face_type);
   JRandom rnd;
   rnd.set_seed(seed);
   Particle* P = reinterpret_cast<Particle*>(parts);
-  long cols = 0;
+  Particle* NE = reinterpret_cast<Particle*>(new_e);
+  Particle* NI = reinterpret_cast<Particle*>(new_i);
+  long cols = 0, ne = 0, nion = 0;
   for (int p = 0; p < n; p++) {
     Particle& a = P[p];
     if (a.alive == 0) continue;
@@ -1373,7 +1381,42 @@ long orc_mcc(int ni, int nj, const double* x0, const double* dh, int domain,
     double vm[3];
     sample_maxw_3d(rnd, v_th, vm);
     for (int i = 0; i < 3; i++) vt[i] += vm[i];
-    if (model == 1) {
+    const double E1 = 0.5 * src_mass * std::sqrt(a.vel[0] * a.vel[0] + a.vel[1] * a.vel[1] + a.vel[2] * a.vel[2]);
+    if (model == 2) {
+      double e1 = 0.5 * src_mass * (a.vel[0] * a.vel[0] + a.vel[1] * a.vel[1] + a.vel[2] * a.vel[2]) / QE;
+      double e2 = e1 - e_ion;
+      if (e2 >= 0) {
+        double e2a = rnd.nextDouble() * e2;
+        double speed2a = std::sqrt(e2a * QE * 2 / src_mass);
+        isotropic_vel(rnd, speed2a, a.vel);
+        double Tt = gather(m, tT, a.lc);  // getTempCollection().eval(pos, 300) inside the mesh
+        if (Tt <= 0) Tt = 100;
+        double v2b[3];
+        isotropic_vel(rnd, speed2a, v2b);  // the reference's speed2a, not speed2b
+        if (NE && ne < max_new) {
+          Particle q = a;
+          for (int i = 0; i < 3; i++) q.vel[i] = v2b[i];
+          NE[ne] = q;
+        }
+        ne++;
+        int mp_gen = (int)(src_spwt / prod_spwt + rnd.nextDouble());
+        if (mp_gen > 0) {
+          double vth_i = std::sqrt(2 * KB * Tt / prod_mass);
+          for (int k = 0; k < mp_gen; k++) {
+            double v3[3];
+            sample_maxw_3d(rnd, vth_i, v3);
+            if (NI && nion < max_new) {
+              Particle q = a;
+              for (int i = 0; i < 3; i++) q.vel[i] = v3[i];
+              q.mpw = prod_spwt;
+              NI[nion] = q;
+            }
+            nion++;
+          }
+          if (delta_n) delta_n[(int)a.lc[1] * ni + (int)a.lc[0]] += prod_spwt * mp_gen;
+        }
+      }
+    } else if (model == 1) {
       for (int i = 0; i < 3; i++) a.vel[i] = vt[i];
     } else {
       double rm1 = src_mass / (src_mass + tgt_mass), rm2 = tgt_mass / (src_mass + tgt_mass);
@@ -1389,9 +1432,26 @@ long orc_mcc(int ni, int nj, const double* x0, const double* dh, int domain,
       vr[2] = A * std::sin(C) * g_mag;
       for (int i = 0; i < 3; i++) a.vel[i] = vc[i] + vr[i] * rm2;
     }
+    // target energy term and collision counts (MCC.java:204-218)
+    const double E2 = 0.5 * src_mass * std::sqrt(a.vel[0] * a.vel[0] + a.vel[1] * a.vel[1] + a.vel[2] * a.vel[2]);
+    if (S) scatter(m, S, a.lc[0], a.lc[1], a.mpw * (E1 - E2) / (dt * node_vol(m, a.lc[0], a.lc[1])));
+    const int u = (int)a.lc[1] * ni + (int)a.lc[0];
+    if (count_sum) count_sum[u] += 1;
+    if (real_sum) real_sum[u] += a.mpw;
     cols++;
   }
+  if (n_new_e) *n_new_e = ne;
+  if (n_new_i) *n_new_i = nion;
   return cols;
+}
+
+long orc_mcc(int ni, int nj, const double* x0, const double* dh, int domain, const int8_t* node_type,
+             const int8_t* face_type, int n, double* parts, double src_mass, double tgt_mass, const double* tden,
+             const double* tu, const double* tv, const double* tw, const double* tT, double sigma, double dt,
+             int model, int64_t seed) {
+  return orc_mcc_ex(ni, nj, x0, dh, domain, node_type, face_type, n, parts, src_mass, tgt_mass, tden, tu, tv, tw, tT,
+                    sigma, dt, model, seed, 1.0, 0.0, 1.0, 1.0, nullptr, nullptr, nullptr, nullptr, 0, nullptr,
+                    nullptr, nullptr, nullptr);
 }
 
 }  // extern "C"

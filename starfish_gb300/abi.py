@@ -175,7 +175,7 @@ class Sigma(C.Structure):
 
 
 SIGMA_CONST, SIGMA_INV, SIGMA_POLY, SIGMA_LN, SIGMA_BIRD463 = 0, 1, 2, 3, 4
-MCC_MEX, MCC_CEX = 0, 1
+MCC_MEX, MCC_CEX, MCC_IONIZATION = 0, 1, 2
 EXPORTS.update({
     "sf_dsmc": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Sigma), C.c_double, C.c_double,
                           C.POINTER(C.c_int64)]),
@@ -184,6 +184,10 @@ EXPORTS.update({
                                     C.c_void_p, C.c_void_p]),
     "sf_mcc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(Sigma), C.c_double,
                          C.POINTER(C.c_int64)]),
+    "sf_mcc_ionization": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(Sigma), C.c_double,
+                                    C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                    C.POINTER(C.c_int64)]),
+    "sf_mcc_get_sums": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]),
 })
 EXPORTS.update({
     "sf_unet_init": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64]),

@@ -330,6 +330,15 @@ int sf_batch_destroy(sf_batch* b) {
   if (!b) return SF_OK;
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
+  // the contexts go on from where the batch left them: their push steps (surface RNG
+  // epochs) were advanced on the device (the particle counts already follow every step)
+  if (b->table_ready) {
+    std::vector<BatchInst> cur(b->n);
+    if (cudaMemcpyAsync(cur.data(), b->d.insts, sizeof(BatchInst) * b->n, cudaMemcpyDeviceToHost, b->stream) ==
+            cudaSuccess &&
+        cudaStreamSynchronize(b->stream) == cudaSuccess)
+      for (int i = 0; i < b->n; i++) b->ctx[i]->species[b->sid[i]]->step = cur[i].a.step;  // checked at create
+  }
   for (auto& g : b->graph)
     if (g) cudaGraphExecDestroy(g);
   for (void* p : b->allocs) cudaFree(p);

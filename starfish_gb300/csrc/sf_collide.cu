@@ -298,9 +298,99 @@ __device__ inline float gather_node(const float* f, int ni, int i, int j, float 
          (1.f - fx) * fy * f[u + ni];
 }
 
+// Per-collision sums of MCC.perform (MCC.java:198-219) and the products of
+// ModelIonization (:304-356).  Every pointer may be null (not accumulated).
+struct MccExtra {
+  double* S;          // ni*nj: target energy term mpw (E1 - E2) / (dt V), Field2D.scatter
+  double* count_sum;  // ni*nj at node (int) lc: collisions
+  double* real_sum;   // ni*nj at node (int) lc: collided weight
+  double* dn;         // ni*nj at node (int) lc: product weight created (target delta-N)
+  double spwt;        // source weight (uniform)
+  double dt;
+  // ionization (model SF_MCC_IONIZATION)
+  double e_ion;       // eV
+  double prod_mass, prod_spwt, spwt_ratio;  // spwt_ratio = source spwt / product spwt
+  float qm_halfdt_src, qm_halfdt_prod;      // (q/m) dt/2 of the addParticle rewind
+  ParticlesView Pe;   // source species: new electrons from slot Pe.n
+  ParticlesView Pi;   // product species: new ions from slot Pi.n
+  int64_t cap_e, cap_i;
+};
+
+// Mesh.nodeVol at a fractional position (Mesh.java:961-1020) on a single mesh: the
+// control volume [i0 -/+ 1/2] x [j0 -/+ 1/2] clipped to the mesh (Mesh.controlVolumeLCs;
+// the corner moves next to INSULATOR nodes do not apply on MCC meshes without them).
+__device__ double node_vol_at(const MeshView& m, double i0, double j0) {
+  const double wi = fmin(i0 + 0.5, (double)(m.ni - 1)) - fmax(i0 - 0.5, 0.0);
+  const double wj = fmin(j0 + 0.5, (double)(m.nj - 1)) - fmax(j0 - 0.5, 0.0);
+  const double area = wi * m.dh[0] * wj * m.dh[1];
+  if (m.domain == SF_DOMAIN_XY) return area;
+  double r;
+  if (m.domain == SF_DOMAIN_RZ) {
+    double ir = i0;
+    if (i0 == 0.0) ir = 0.25;
+    else if (i0 == m.ni - 1) ir = i0 - 0.25;
+    r = m.x0[0] + ir * m.dh[0];
+  } else {
+    double jr = j0;
+    if (j0 == 0.0) jr = 0.25;
+    else if (j0 == m.nj - 1) jr = j0 - 0.25;
+    r = m.x0[1] + jr * m.dh[1];
+  }
+  return 2.0 * PI * area * r;
+}
+
+// Field2D.scatter (Field2D.java:244-295) with the Ruyten RZ / ZR weights, FP64 atomics
+__device__ void scatter_fp64(const MeshView& m, double* f, double fi, double fj, double val) {
+  const int i = (int)fi, j = (int)fj;
+  if (i < 0 || j < 0 || i >= m.ni - 1 || j >= m.nj - 1) return;
+  double di = fi - i, dj = fj - j;
+  if (m.domain == SF_DOMAIN_RZ) {
+    const double rp = m.x0[0] + (i + 1) * m.dh[0], rm = m.x0[0] + i * m.dh[0], r = m.x0[0] + fi * m.dh[0];
+    di = 1 - (0.5 * (rp - r) * (2 * rp + 3 * rm - r) / (rp * rp - rm * rm));
+  } else if (m.domain == SF_DOMAIN_ZR) {
+    const double rp = m.x0[1] + (j + 1) * m.dh[1], rm = m.x0[1] + j * m.dh[1], r = m.x0[1] + fj * m.dh[1];
+    dj = 1 - (0.5 * (rp - r) * (2 * rp + 3 * rm - r) / (rp * rp - rm * rm));
+  }
+  const int u = j * m.ni + i;
+  atomicAdd(&f[u], (1 - di) * (1 - dj) * val);
+  atomicAdd(&f[u + 1], di * (1 - dj) * val);
+  atomicAdd(&f[u + m.ni + 1], di * dj * val);
+  atomicAdd(&f[u + m.ni], (1 - di) * dj * val);
+}
+
+// Utils.isotropicVel (core/common/Utils.java:121-136)
+__device__ inline void isotropic_vel(Philox& r, double mag, double v[3]) {
+  const double theta = 2 * PI * r.uniform();
+  const double R = -1.0 + 2 * r.uniform();
+  const double a = sqrt(fmax(1 - R * R, 0.0));
+  const double am = fabs(mag);
+  v[0] = cos(theta) * a * am;
+  v[1] = sin(theta) * a * am;
+  v[2] = R * am;
+}
+
+// KineticMaterial.addParticle (KineticMaterial.java:776-796): the new particle at the
+// source particle's place with the -dt/2 velocity rewind; false past the capacity
+__device__ bool mcc_append(const MeshView& m, const ParticlesView& Q, int64_t cap, unsigned long long* ctr, uint32_t cell,
+                           float2 f, const double v[3], float qm_halfdt) {
+  const int64_t d = Q.n + (int64_t)atomicAdd(ctr, 1ULL);
+  if (d >= cap) return false;
+  const int i = cell_i(cell), j = cell_j(cell);
+  const int u = j * m.ni + i;
+  const float w00 = (1.f - f.x) * (1.f - f.y), w10 = f.x * (1.f - f.y), w11 = f.x * f.y, w01 = (1.f - f.x) * f.y;
+  const float2 e00 = m.E[u], e10 = m.E[u + 1], e11 = m.E[u + m.ni + 1], e01 = m.E[u + m.ni];
+  const float2 e = make_float2(w00 * e00.x + w10 * e10.x + w11 * e11.x + w01 * e01.x,
+                               w00 * e00.y + w10 * e10.y + w11 * e11.y + w01 * e01.y);
+  Q.cell[d] = cell;
+  Q.frac[d] = f;
+  Q.vxy[d] = make_float2((float)v[0] - qm_halfdt * e.x, (float)v[1] - qm_halfdt * e.y);
+  Q.vz[d] = (float)v[2];
+  return true;
+}
+
 // MCC.perform(mesh) per particle (collisions/MCC.java:167-221)
 __global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, int model, float src_mass, float dt,
-                      uint64_t seed, uint32_t step, unsigned long long* __restrict__ n_coll) {
+                      uint64_t seed, uint32_t step, unsigned long long* __restrict__ cnt, MccExtra ex) {
   const float KBf = 1.3806503e-23f;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < P.n; p += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t c = P.cell[p];
@@ -329,7 +419,45 @@ __global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, i
       for (int k = 0; k < 12; k++) s += (float)rng.uniform();
       vt[d] += (vth * 1.2f) * 0.70710678f * (s - 6.f);
     }
-    if (model == SF_MCC_CEX) {
+    // pre-collision "energy" 0.5 m |v| (Vec.mag3, as in MCC.java:204)
+    const double E1 = 0.5 * (double)src_mass * sqrt((double)vxy.x * vxy.x + (double)vxy.y * vxy.y + (double)vz * vz);
+    if (model == SF_MCC_IONIZATION) {
+      // ModelIonization (MCC.java:304-356): the source electron keeps a random share of
+      // the energy left after ionization; a second electron (with the same speed, as in
+      // the reference) and (int)(spwt_src / spwt_prod + rnd) product ions at the neutral
+      // temperature are added where the collision happened
+      const double e1 = 0.5 * (double)src_mass * ((double)vxy.x * vxy.x + (double)vxy.y * vxy.y + (double)vz * vz) / QE;
+      const double e2 = e1 - ex.e_ion;
+      if (e2 >= 0) {
+        const double e2a = rng.uniform() * e2;
+        const double speed2a = sqrt(e2a * QE * 2 / (double)src_mass);
+        double vs[3], v2b[3];
+        isotropic_vel(rng, speed2a, vs);
+        vxy = make_float2((float)vs[0], (float)vs[1]);
+        vz = (float)vs[2];
+        double Tt = (double)gather_node(tg.T, m.ni, i, j, f.x, f.y);
+        if (Tt <= 0) Tt = 100;
+        isotropic_vel(rng, speed2a, v2b);
+        if (!mcc_append(m, ex.Pe, ex.cap_e, &cnt[1], c, f, v2b, ex.qm_halfdt_src)) atomicAdd(&cnt[3], 1ULL);
+        const int mp_gen = (int)(ex.spwt_ratio + rng.uniform());
+        if (mp_gen > 0) {
+          const double v_th = sqrt(2 * KB * Tt / ex.prod_mass);
+          for (int k = 0; k < mp_gen; k++) {
+            double v3[3];
+            for (int d = 0; d < 3; d++) {
+              double s = 0.0;
+              for (int q = 0; q < 12; q++) s += rng.uniform();
+              v3[d] = (v_th * 1.2) * 0.7071067811865476 * (s - 6.0);  // Utils.SampleMaxw3D
+            }
+            if (!mcc_append(m, ex.Pi, ex.cap_i, &cnt[2], c, f, v3, ex.qm_halfdt_prod)) atomicAdd(&cnt[3], 1ULL);
+          }
+          if (ex.dn) {
+            const int ii = i + (f.x >= 1.f), jj = j + (f.y >= 1.f);
+            atomicAdd(&ex.dn[jj * m.ni + ii], ex.prod_spwt * mp_gen);
+          }
+        }
+      }
+    } else if (model == SF_MCC_CEX) {
       vxy = make_float2(vt[0], vt[1]);
       vz = vt[2];
     } else {
@@ -349,7 +477,17 @@ __global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, i
     }
     P.vxy[p] = vxy;
     P.vz[p] = vz;
-    atomicAdd(n_coll, 1ULL);
+    atomicAdd(&cnt[0], 1ULL);
+    const double li = i + (double)f.x, lj = j + (double)f.y;
+    if (ex.S) {
+      const double E2 = 0.5 * (double)src_mass * sqrt((double)vxy.x * vxy.x + (double)vxy.y * vxy.y + (double)vz * vz);
+      scatter_fp64(m, ex.S, li, lj, ex.spwt * (E1 - E2) / (ex.dt * node_vol_at(m, li, lj)));
+    }
+    if (ex.count_sum) {
+      const int u = (j + (f.y >= 1.f)) * m.ni + i + (f.x >= 1.f);
+      atomicAdd(&ex.count_sum[u], 1.0);
+      atomicAdd(&ex.real_sum[u], ex.spwt);
+    }
   }
 }
 
@@ -439,6 +577,14 @@ void sf_collide_destroy_internal(sf_ctx* ctx) {
     cudaFree(ctx->mcc_target);
     ctx->mcc_target = nullptr;
   }
+  if (ctx->mcc_sums) {
+    cudaFree(ctx->mcc_sums);
+    ctx->mcc_sums = nullptr;
+  }
+  if (ctx->mcc_cnt) {
+    cudaFree(ctx->mcc_cnt);
+    ctx->mcc_cnt = nullptr;
+  }
 }
 
 extern "C" {
@@ -500,6 +646,11 @@ int sf_mcc_set_target(sf_ctx* ctx, double mass, const double* den, const double*
   SF_CUDA(cudaSetDevice(ctx->device));
   const size_t nn = (size_t)ctx->ni * ctx->nj;
   if (!ctx->mcc_target) SF_CUDA(cudaMalloc(&ctx->mcc_target, sizeof(float) * 5 * nn));
+  if (!ctx->mcc_sums) {
+    SF_CUDA(cudaMalloc(&ctx->mcc_sums, sizeof(double) * 4 * nn));
+    zero_wait(ctx->mcc_sums, sizeof(double) * 4 * nn, ctx->stream);
+  }
+  if (!ctx->mcc_cnt) SF_CUDA(cudaMalloc(&ctx->mcc_cnt, sizeof(unsigned long long) * 4));
   std::vector<float> h(5 * nn, 0.f);
   const double* src[5] = {den, u, v, w, temp};
   for (int k = 0; k < 5; k++)
@@ -510,11 +661,13 @@ int sf_mcc_set_target(sf_ctx* ctx, double mass, const double* den, const double*
   SF_API_END(ctx)
 }
 
-int sf_mcc(sf_ctx* ctx, int32_t sid, int32_t model, const sf_sigma* sigma, double dt, int64_t* n_coll) {
-  SF_API_BEGIN
-  SfSpecies* sp = get_species(ctx, sid);
+namespace {
+
+// One MCC.perform: the kernel over the source species, then the counts; the new
+// electrons and ions (ionization) extend their species' slot ranges.
+void mcc_run(sf_ctx* ctx, SfSpecies* sp, int model, const sf_sigma* sigma, double dt, SfSpecies* prod, double e_ion,
+             unsigned long long out[3]) {
   SF_REQUIRE(ctx->mcc_target, SF_ERR_STATE, "no MCC target (sf_mcc_set_target)");
-  SF_REQUIRE(model == SF_MCC_MEX || model == SF_MCC_CEX, SF_ERR_ARG, "bad MCC model");
   SF_REQUIRE(dt > 0, SF_ERR_ARG, "dt must be positive");
   SF_CUDA(cudaSetDevice(ctx->device));
   const SigmaDev sg = make_sigma(sigma, sp->mass, ctx->mcc_mass);
@@ -526,20 +679,92 @@ int sf_mcc(sf_ctx* ctx, int32_t sid, int32_t model, const sf_sigma* sigma, doubl
   tg.w = ctx->mcc_target + 3 * nn;
   tg.T = ctx->mcc_target + 4 * nn;
   tg.mass = (float)ctx->mcc_mass;
-  SF_CUDA(cudaMemsetAsync(ctx->counters + 6, 0, sizeof(unsigned long long), ctx->stream));
+  MccExtra ex{};
+  ex.S = ctx->mcc_sums;
+  ex.count_sum = ctx->mcc_sums + nn;
+  ex.real_sum = ctx->mcc_sums + 2 * nn;
+  ex.dn = ctx->mcc_sums + 3 * nn;
+  ex.spwt = sp->spwt;
+  ex.dt = dt;
+  ex.Pe = sp->cur;
+  ex.cap_e = sp->cap;
+  if (prod) {
+    ex.e_ion = e_ion;
+    ex.prod_mass = prod->mass;
+    ex.prod_spwt = prod->spwt;
+    ex.spwt_ratio = sp->spwt / prod->spwt;
+    ex.qm_halfdt_src = (float)(sp->charge / sp->mass * 0.5 * dt);
+    ex.qm_halfdt_prod = (float)(prod->charge / prod->mass * 0.5 * dt);
+    ex.Pi = prod->cur;
+    ex.cap_i = prod->cap;
+  }
+  SF_CUDA(cudaMemsetAsync(ctx->mcc_cnt, 0, sizeof(unsigned long long) * 4, ctx->stream));
   if (sp->n > 0) {
     TimedScope ts(ctx, "mcc");
     k_mcc<<<grid_for(sp->n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
         ctx->mesh_view(), sp->cur, tg, sg, model, (float)sp->mass, (float)dt, ctx->seed ^ 0x3CC0ULL, ctx->rng_epoch++,
-        ctx->counters + 6);
+        ctx->mcc_cnt, ex);
     ctx->launches++;
   }
   SF_CUDA(cudaGetLastError());
-  unsigned long long nc = 0;
-  SF_CUDA(cudaMemcpyAsync(&nc, ctx->counters + 6, sizeof(nc), cudaMemcpyDeviceToHost, ctx->stream));
+  unsigned long long h[4] = {0, 0, 0, 0};
+  SF_CUDA(cudaMemcpyAsync(h, ctx->mcc_cnt, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
   SF_CUDA(cudaStreamSynchronize(ctx->stream));
   timer_collect(ctx);
-  if (n_coll) *n_coll = (int64_t)nc;
+  if (prod) {
+    const int64_t ne = std::min<int64_t>((int64_t)h[1], sp->cap - sp->n);
+    const int64_t ni = std::min<int64_t>((int64_t)h[2], prod->cap - prod->n);
+    sp->n += ne;
+    sp->cur.n = sp->n;
+    prod->n += ni;
+    prod->cur.n = prod->n;
+    if (ne > 0) sp->sorted = false;
+    if (ni > 0) prod->sorted = false;
+  }
+  out[0] = h[0];
+  out[1] = h[1];
+  out[2] = h[2];
+  SF_REQUIRE(h[3] == 0, SF_ERR_OOM, "MCC ionization products exceeded a species' capacity (the excess was dropped)");
+}
+
+}  // namespace
+
+int sf_mcc(sf_ctx* ctx, int32_t sid, int32_t model, const sf_sigma* sigma, double dt, int64_t* n_coll) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(model == SF_MCC_MEX || model == SF_MCC_CEX, SF_ERR_ARG,
+             "bad MCC model (ionization: sf_mcc_ionization)");
+  unsigned long long h[3];
+  mcc_run(ctx, sp, model, sigma, dt, nullptr, 0.0, h);
+  if (n_coll) *n_coll = (int64_t)h[0];
+  SF_API_END(ctx)
+}
+
+int sf_mcc_ionization(sf_ctx* ctx, int32_t sid, int32_t product_sid, const sf_sigma* sigma, double ionization_energy,
+                      double dt, int64_t* n_coll, int64_t* n_electrons, int64_t* n_ions) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SfSpecies* prod = get_species(ctx, product_sid);
+  SF_REQUIRE(product_sid != sid, SF_ERR_ARG, "the product (ion) species must differ from the source (electrons)");
+  SF_REQUIRE(ionization_energy >= 0, SF_ERR_ARG, "ionization energy must be >= 0 eV");
+  unsigned long long h[3];
+  mcc_run(ctx, sp, SF_MCC_IONIZATION, sigma, dt, prod, ionization_energy, h);
+  if (n_coll) *n_coll = (int64_t)h[0];
+  if (n_electrons) *n_electrons = (int64_t)h[1];
+  if (n_ions) *n_ions = (int64_t)h[2];
+  SF_API_END(ctx)
+}
+
+int sf_mcc_get_sums(sf_ctx* ctx, double* S, double* count_sum, double* real_sum, double* delta_n, int32_t reset) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx, SF_ERR_ARG, "null context");
+  SF_REQUIRE(ctx->mcc_sums, SF_ERR_STATE, "no MCC target (sf_mcc_set_target)");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  double* out[4] = {S, count_sum, real_sum, delta_n};
+  for (int k = 0; k < 4; k++)
+    if (out[k]) copy_wait(out[k], ctx->mcc_sums + k * nn, sizeof(double) * nn, cudaMemcpyDeviceToHost, ctx->stream);
+  if (reset) zero_wait(ctx->mcc_sums, sizeof(double) * 4 * nn, ctx->stream);
   SF_API_END(ctx)
 }
 

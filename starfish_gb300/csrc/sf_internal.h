@@ -315,6 +315,8 @@ struct sf_ctx {
   std::vector<SfDsmcState*> dsmc;  // per species DSMC cell state
   float* mcc_target = nullptr;     // MCC target density, u, v, w, T (5 * ni*nj)
   double mcc_mass = 0;
+  double* mcc_sums = nullptr;      // MCC S, count sum, weight sum, delta-N (4 * ni*nj)
+  unsigned long long* mcc_cnt = nullptr;  // collisions, new electrons, new ions (3)
   uint64_t seed = 0x5eed5eedULL;
   uint32_t rng_epoch = 0;  // advanced by every stochastic call (sources, DSMC, MCC)
   int64_t launches = 0;   // kernels launched

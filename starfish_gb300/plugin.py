@@ -347,11 +347,30 @@ class MCC:
         arr = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (den, u, v, w, temp)]
         self.d.check(self.d.lib.sf_mcc_set_target(self.d.ctx, target_mass, *[abi.ptr(a) for a in arr]))
 
-    def perform(self, dt):
+    def perform(self, dt, product: "KineticMaterial" = None, ionization_energy=None):
+        """MCC.perform: the number of collisions.  With model MCC_IONIZATION, `product` is
+        the ion species and `ionization_energy` the target's (eV); the return value is then
+        (collisions, new electrons, new ions)."""
         n = C.c_int64()
+        if self.model == abi.MCC_IONIZATION:
+            if product is None or ionization_energy is None:
+                raise ValueError("ionization needs the product species and the ionization energy")
+            ne, ni = C.c_int64(), C.c_int64()
+            self.d.check(self.d.lib.sf_mcc_ionization(self.d.ctx, self.km.sid, product.sid, C.byref(self.sigma),
+                                                      float(ionization_energy), dt, C.byref(n), C.byref(ne),
+                                                      C.byref(ni)))
+            return n.value, ne.value, ni.value
         self.d.check(self.d.lib.sf_mcc(self.d.ctx, self.km.sid, self.model, C.byref(self.sigma), dt,
                                        C.byref(n)))
         return n.value
+
+    def sums(self, reset=False):
+        """S (target energy term), count_sum, real_sum and delta_n node fields (ni*nj)."""
+        nn = self.d.ni * self.d.nj
+        out = {k: np.zeros(nn) for k in ("S", "count_sum", "real_sum", "delta_n")}
+        self.d.check(self.d.lib.sf_mcc_get_sums(self.d.ctx, abi.ptr(out["S"]), abi.ptr(out["count_sum"]),
+                                                abi.ptr(out["real_sum"]), abi.ptr(out["delta_n"]), int(reset)))
+        return out
 
 
 class GpuBatch:

@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from starfish_gb300 import abi
 from starfish_gb300 import workloads as W
 
 
@@ -250,3 +251,78 @@ def test_oracle_axisymmetric_source_area_weighted():
     v_mean = np.sqrt(8 * 1.3806503e-23 * 300.0 / (np.pi * mass))
     expect = 1e22 * np.pi * R * R * (500.0 + v_mean / 4) * 1e-6 / 1e9
     assert parts.shape[0] == int(expect)
+
+
+def _ionization_case(n=4000, seed=5, eV=50.0):
+    """Electrons of one energy, isotropic, uniform in a 21x21 XY box; a neutral target."""
+    spec = W.es_pic_mesh(21, 21, 1e-3, walls=abi.DB_SYMMETRY, electrode_halfwidth=1e-12)
+    spec.node_type[:] = abi.NODE_OPEN
+    me = 9.10938e-31
+    rng = np.random.default_rng(seed)
+    lc = rng.uniform(0.5, 19.5, (n, 2))  # control volumes of full size
+    d = rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    vel = d * np.sqrt(2 * eV * 1.60217646e-19 / me)
+    P = np.zeros((n, 12))
+    P[:, 0:2] = spec.x0 + lc * spec.dh
+    P[:, 3:6] = vel
+    P[:, 6:8] = lc
+    P[:, 9] = 2.5e6
+    P[:, 10] = 1
+    return spec, me, P
+
+
+def test_oracle_mcc_ionization_known_answers():
+    """ModelIonization (MCC.java:304-356) in the oracle: with a dense target every electron
+    collides; each collided electron makes one more electron of the same speed (the
+    reference's speed2a), keeps at most e - e_ion, and (int)(2.5 + rnd) ions are made per
+    collision; delta_n, count_sum and real_sum add up exactly; S holds the energy term."""
+    spec, me, P = _ionization_case()
+    m = _omesh(spec)
+    nn = spec.nn
+    z = np.zeros(nn)
+    den, T = np.full(nn, 1e26), np.full(nn, 300.0)
+    e_ion, mi, spwt_i = 15.76, 40 * 1.66053886e-27, 1e6
+    e0 = 0.5 * me * (P[:, 3:6] ** 2).sum(1) / 1.60217646e-19
+    v0 = P[:, 3:6].copy()
+    out = O.mcc_ex(m, P, me, mi, den, z, z, z, T, 1e-20, 5e-8, 2, 7, src_spwt=2.5e6, e_ion=e_ion,
+                   prod_mass=mi, prod_spwt=spwt_i, max_new=20000)
+    n = P.shape[0]
+    assert out["cols"] == n and out["n_new_e"] == n
+    e1 = 0.5 * me * (P[:, 3:6] ** 2).sum(1) / 1.60217646e-19
+    assert np.all(e1 <= e0 - e_ion + 1e-9)
+    assert abs(e1.mean() / ((e0 - e_ion).mean() / 2) - 1) < 0.05
+    s_src = np.linalg.norm(P[:, 3:6], axis=1)
+    s_new = np.linalg.norm(out["new_e"][:, 3:6], axis=1)
+    assert np.allclose(s_new, s_src, rtol=1e-12)
+    assert np.array_equal(out["new_e"][:, 6:8], P[:, 6:8])
+    ratio = out["n_new_i"] / out["cols"]
+    assert 2.4 < ratio < 2.6
+    assert out["delta_n"].sum() == pytest.approx(spwt_i * out["n_new_i"], rel=1e-12)
+    assert out["count_sum"].sum() == out["cols"]
+    assert out["real_sum"].sum() == pytest.approx(2.5e6 * out["cols"], rel=1e-12)
+    # interior particles only touch nodes with the full control volume dx*dy (XY depth 1):
+    # the scattered S sums to sum mpw (E1 - E2) / (dt dx dy) with E = 0.5 m |v|
+    interior = np.all((P[:, 6:8] >= 0.5) & (P[:, 6:8] <= 19.5), axis=1)
+    assert interior.all()
+    dE = 0.5 * me * (np.linalg.norm(v0, axis=1) - s_src)
+    assert out["S"].sum() == pytest.approx((2.5e6 * dE / (5e-8 * 1e-6)).sum(), rel=1e-9)
+    # ions: Maxwellian at 300 K with the sampler's 1.2 factor
+    vi = out["new_i"][:, 3:6]
+    sig = 1.2 * np.sqrt(2 * 1.3806503e-23 * 300 / mi) / np.sqrt(2)
+    assert abs(vi.std() / sig - 1) < 0.05
+
+
+def test_oracle_mcc_ex_matches_plain_for_mex_cex():
+    """The extended entry point draws the same random numbers for MEX and CEX."""
+    spec, me, P = _ionization_case(n=2000, seed=9)
+    m = _omesh(spec)
+    nn = spec.nn
+    z = np.zeros(nn)
+    den, T = np.full(nn, 1e20), np.full(nn, 300.0)
+    for model in (0, 1):
+        A, B = P.copy(), P.copy()
+        ca = O.mcc(m, A, me, 40 * 1.66e-27, den, z, z, z, T, 1e-20, 5e-8, model, 3)
+        out = O.mcc_ex(m, B, me, 40 * 1.66e-27, den, z, z, z, T, 1e-20, 5e-8, model, 3)
+        assert ca == out["cols"] > 0
+        assert np.array_equal(A, B)

@@ -126,6 +126,7 @@ struct sf_batch {
   double cyc_ms[N_BUCKETS][3] = {};
   int cyc_n[N_BUCKETS][3] = {};
   std::unique_ptr<Pool> pool;
+  sf::BatchPoisson* bp = nullptr;  // batched field phase (created at the first step that uses it)
   std::string err;
   // source parameters per instance (den, v_drift, temp, seg) for the step's dt
   struct Src {
@@ -341,6 +342,8 @@ int sf_batch_destroy(sf_batch* b) {
   }
   for (auto& g : b->graph)
     if (g) cudaGraphExecDestroy(g);
+  sf::batch_poisson_destroy(b->bp);
+  b->bp = nullptr;
   for (void* p : b->allocs) cudaFree(p);
   if (b->ev_dev) cudaEventDestroy(b->ev_dev);
   if (b->ev0) cudaEventDestroy(b->ev0);
@@ -428,10 +431,35 @@ int sf_batch_step(sf_batch* b, double dt, const sf_poisson_params* prm, sf_batch
     SF_CUDA(cudaGraphLaunch(graph_for(b, shape), b->stream));
     SF_CUDA(cudaEventRecord(b->ev1, b->stream));
     SF_CUDA(cudaEventRecord(b->ev_dev, b->stream));
-    // field phase: per instance rho, Poisson, E on the instance streams
+    // field phase: rho, Poisson, E of every instance
     const int tuning_step = (int)(b->steps % (3 * TRIAL_STEPS)) / TRIAL_STEPS;  // cycles choice under trial
     std::vector<double> solve_ms(b->n, 0.0);
     std::vector<int> newton(b->n, 0);
+    double field_sum = 0, field_max = 0;
+    if (!prm->use_learned) {
+      // one launch per stage for all instances on the batch stream (after the device phase)
+      if (!b->bp) b->bp = batch_poisson_create(b->ctx.data(), b->n, b->num_sms, b->stream);
+      std::vector<int> iters(b->n), status(b->n);
+      std::vector<sf_solve_stats> ss(b->n);
+      for (int i = 0; i < b->n; i++) {
+        const int bk = bucket_of(b->ctx[i]);
+        iters[i] = b->cycles[bk] > 0 ? b->cycles[bk] : CYCLE_CHOICES[tuning_step];
+      }
+      const float ms = batch_poisson_step(b->bp, *prm, iters.data(), ss.data(), status.data());
+      field_sum = field_max = ms;
+      for (int i = 0; i < b->n; i++) {
+        solve_ms[i] = ms;  // one time for all: the tuner then picks one PCG count for every bucket
+        newton[i] = ss[i].newton_it;
+      }
+      for (int i = 0; i < b->n; i++)
+        if (status[i] != 1)
+          SF_REQUIRE(false, status[i] == 3 ? SF_ERR_DIVERGED : SF_ERR_NOT_CONVERGED,
+                     "instance " + std::to_string(i) +
+                         (status[i] == 3 ? ": Solver diverged (non-finite residual)"
+                                         : ": Poisson solve did not reach the residual tolerance"));
+    } else {
+    // the learned warm start is per context: the instances' own solves on their streams,
+    // issued by the host thread pool
     const int T = b->pool->size();
     b->pool->run([&](int w) {
       for (int i = w; i < b->n; i += T) {
@@ -459,6 +487,11 @@ int sf_batch_step(sf_batch* b, double dt, const sf_poisson_params* prm, sf_batch
       }
     });
     SF_REQUIRE(errs.empty(), SF_ERR_CUDA, errs);
+    for (int i = 0; i < b->n; i++) {
+      field_sum += solve_ms[i];
+      field_max = std::max(field_max, solve_ms[i]);
+    }
+    }
     float dev_ms = 0.f;
     SF_CUDA(cudaEventElapsedTime(&dev_ms, b->ev0, b->ev1));
     // autotuner bookkeeping
@@ -503,13 +536,11 @@ int sf_batch_step(sf_batch* b, double dt, const sf_poisson_params* prm, sf_batch
     b->steps++;
     if (st) {
       st->particles = 0;
-      st->solve_ms_sum = 0;
-      st->solve_ms_max = 0;
+      st->solve_ms_sum = field_sum;
+      st->solve_ms_max = field_max;
       st->newton_it_mean = 0;
       for (int i = 0; i < b->n; i++) {
         st->particles += nn[i] - dd[i];
-        st->solve_ms_sum += solve_ms[i];
-        st->solve_ms_max = std::max(st->solve_ms_max, solve_ms[i]);
         st->newton_it_mean += newton[i];
       }
       st->newton_it_mean /= b->n;

@@ -253,6 +253,15 @@ namespace sf {
 // batched phases of one step, all on `stream` (sf_push.cu, sf_source.cu)
 void batch_inject(const BatchDev& b, cudaStream_t stream, int num_sms);
 void batch_push(const BatchDev& b, cudaStream_t stream, int num_sms, int blocks_per_sm, int slow_blocks_per_sm);
+// batched field phase (sf_poisson.cu): rho, the nonlinear solve and E of every context on
+// one stream, each stage one launch for all; results equal the contexts' own
+// sf_update_rho + sf_poisson_nl + sf_efield bit for bit
+struct BatchPoisson;
+BatchPoisson* batch_poisson_create(sf_ctx* const* ctxs, int n, int num_sms, cudaStream_t stream);
+void batch_poisson_destroy(BatchPoisson* bp);
+// status[i]: 1 converged, 2 not converged, 3 diverged; returns the phase's time (ms)
+float batch_poisson_step(BatchPoisson* bp, const sf_poisson_params& prm, const int* iters, sf_solve_stats* st,
+                         int* status);
 }  // namespace sf
 
 struct SfPoisson;    // sf_poisson.cu

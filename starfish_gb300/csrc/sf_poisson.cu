@@ -189,7 +189,7 @@ __device__ void cta_smooth(float* y, const float* r, const float* P, const uint8
     }
 }
 
-__global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseDesc D, LevelView top, int nu1, int nu2) {
+__device__ __forceinline__ void coarse_vcycle_body(const CoarseDesc& D, const LevelView& top, int nu1, int nu2) {
   extern __shared__ __align__(16) unsigned char sm[];
   float* Y = reinterpret_cast<float*>(sm);
   float* R = Y + D.total;
@@ -256,6 +256,10 @@ __global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseDesc D, LevelView 
   for (int u = threadIdx.x; u < n0; u += blockDim.x) top.y[u] = Y[u];
 }
 
+__global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseDesc D, LevelView top, int nu1, int nu2) {
+  coarse_vcycle_body(D, top, nu1, nu2);
+}
+
 // ------------------------------------------------------------------------------------
 // FP64 outer loop
 // ------------------------------------------------------------------------------------
@@ -270,7 +274,7 @@ struct NlArgs {
 
 constexpr int RB = 256;
 
-__device__ inline void block_sum2(double a, double b, double* part, bool max2) {
+__device__ inline void block_sum2(double a, double b, double* part, bool max2, int bidx) {
   __shared__ double sh[2][RB / 32];
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_down_sync(0xffffffffu, a, o);
@@ -289,13 +293,13 @@ __device__ inline void block_sum2(double a, double b, double* part, bool max2) {
       x += sh[0][w];
       y = max2 ? fmax(y, sh[1][w]) : y + sh[1][w];
     }
-    part[2 * blockIdx.x] = x;
-    part[2 * blockIdx.x + 1] = y;
+    part[2 * bidx] = x;
+    part[2 * bidx + 1] = y;
   }
 }
 
 // per block: sum of a, max of b, max of c -> part[3 * block + {0, 1, 2}]
-__device__ inline void block_sum_max_max(double a, double b, double c, double* part) {
+__device__ inline void block_sum_max_max(double a, double b, double c, double* part, int bidx) {
   __shared__ double sh[3][RB / 32];
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_down_sync(0xffffffffu, a, o);
@@ -316,9 +320,9 @@ __device__ inline void block_sum_max_max(double a, double b, double c, double* p
       y = fmax(y, sh[1][w]);
       z = fmax(z, sh[2][w]);
     }
-    part[3 * blockIdx.x] = x;
-    part[3 * blockIdx.x + 1] = y;
-    part[3 * blockIdx.x + 2] = z;
+    part[3 * bidx] = x;
+    part[3 * bidx + 1] = y;
+    part[3 * bidx + 2] = z;
   }
 }
 
@@ -331,13 +335,15 @@ __device__ inline void block_sum_max_max(double a, double b, double c, double* p
 // the Boltzmann term is small next to them and its exponential is taken in FP32 unless
 // a.fp64_exp: its relative error is at most |arg| 2^-24 (rounding of the argument) plus
 // 2^-22, and the host switches to FP64 when that bound could reach the tolerance.
-__global__ void __launch_bounds__(RB) k_nl_residual(NlArgs a, const double* __restrict__ x,
-                                                    const double* __restrict__ b0, const uint8_t* __restrict__ type,
-                                                    float* __restrict__ F32, float* __restrict__ P32,
-                                                    double* __restrict__ partial) {
+// Blocks bidx = 0..G-1 of one mesh (the single and the batched launch share it, so that
+// the partial sums, and with them every reduction, are the same bit for bit).
+__device__ __forceinline__ void nl_residual_body(const NlArgs& a, const double* __restrict__ x,
+                                                 const double* __restrict__ b0, const uint8_t* __restrict__ type,
+                                                 float* __restrict__ F32, float* __restrict__ P32,
+                                                 double* __restrict__ partial, int bidx, int G) {
   const int n = a.ni * a.nj;
   double s2 = 0.0, smax = 0.0, emax = 0.0;
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+  for (int u = bidx * RB + threadIdx.x; u < n; u += G * RB) {
     const uint8_t t = type[u];
     const double xc = x[u];
     double F, Fs, P = 0.0;
@@ -368,10 +374,18 @@ __global__ void __launch_bounds__(RB) k_nl_residual(NlArgs a, const double* __re
     s2 += F * F;
     smax = fmax(smax, fabs(F));
   }
-  block_sum_max_max(s2, smax, emax, partial);
+  block_sum_max_max(s2, smax, emax, partial, bidx);
 }
 
-__global__ void k_reduce_partials3(const double* partial, int nb, double* out) {
+__global__ void __launch_bounds__(RB) k_nl_residual(NlArgs a, const double* __restrict__ x,
+                                                    const double* __restrict__ b0, const uint8_t* __restrict__ type,
+                                                    float* __restrict__ F32, float* __restrict__ P32,
+                                                    double* __restrict__ partial) {
+  nl_residual_body(a, x, b0, type, F32, P32, partial, blockIdx.x, gridDim.x);
+}
+
+// one block of 256 threads
+__device__ __forceinline__ void reduce3_body(const double* partial, int nb, double* out) {
   __shared__ double sa[256], sb[256], sc[256];
   double a = 0, b = 0, c = 0;
   for (int k = threadIdx.x; k < nb; k += blockDim.x) {
@@ -398,7 +412,10 @@ __global__ void k_reduce_partials3(const double* partial, int nb, double* out) {
   }
 }
 
-__global__ void k_reduce_partials(const double* partial, int nb, double* out, int max2) {
+__global__ void k_reduce_partials3(const double* partial, int nb, double* out) { reduce3_body(partial, nb, out); }
+
+// one block of 256 threads
+__device__ __forceinline__ void reduce2_body(const double* partial, int nb, double* out, int max2) {
   __shared__ double s2[256], sm[256];
   double a2 = 0, am = 0;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -421,49 +438,68 @@ __global__ void k_reduce_partials(const double* partial, int nb, double* out, in
   }
 }
 
+__global__ void k_reduce_partials(const double* partial, int nb, double* out, int max2) {
+  reduce2_body(partial, nb, out, max2);
+}
+
 // ---- flexible preconditioned CG on J y = F (FP32 vectors, FP64 dot products) -------
 // scalars: sc[0] = r.z, sc[1] = p.Jp, sc[2] = alpha, sc[3] = beta, sc[4..5] = reduction out
 enum { SC_RZ = 0, SC_PQ = 1, SC_ALPHA = 2, SC_BETA = 3, SC_RED = 4 };
 
 // q = J p and the partial sums of p.q
-__global__ void __launch_bounds__(RB) k_cg_matvec(LevelView L, const float* __restrict__ p, float* __restrict__ q,
-                                                  double* __restrict__ partial) {
+__device__ __forceinline__ void cg_matvec_body(const LevelView& L, const float* __restrict__ p, float* __restrict__ q,
+                                               double* __restrict__ partial, int bidx, int G) {
   const int n = L.ni * L.nj;
   float s = 0.f;  // a thread sums a few dozen products; blocks and the grid sum in FP64
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+  for (int u = bidx * RB + threadIdx.x; u < n; u += G * RB) {
     const float qu = apply_J(L.type[u], p, L.P[u], u, L.ni, L.cx, L.cy);
     q[u] = qu;
     s = fmaf(p[u], qu, s);
   }
-  block_sum2((double)s, 0.0, partial, false);
+  block_sum2((double)s, 0.0, partial, false, bidx);
+}
+
+__global__ void __launch_bounds__(RB) k_cg_matvec(LevelView L, const float* __restrict__ p, float* __restrict__ q,
+                                                  double* __restrict__ partial) {
+  cg_matvec_body(L, p, q, partial, blockIdx.x, gridDim.x);
 }
 
 // x += alpha p, r -= alpha q, zo = z
+__device__ __forceinline__ void cg_axpy_node(int u, float al, const float* __restrict__ p, const float* __restrict__ q,
+                                             float* __restrict__ x, float* __restrict__ r, const float* __restrict__ z,
+                                             float* __restrict__ zo) {
+  x[u] += al * p[u];
+  r[u] -= al * q[u];
+  zo[u] = z[u];
+}
+
 __global__ void k_cg_axpy(int n, const double* __restrict__ sc, const float* __restrict__ p, const float* __restrict__ q,
                           float* __restrict__ x, float* __restrict__ r, const float* __restrict__ z, float* __restrict__ zo) {
   const float al = (float)sc[SC_ALPHA];
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
-    x[u] += al * p[u];
-    r[u] -= al * q[u];
-    zo[u] = z[u];
-  }
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
+    cg_axpy_node(u, al, p, q, x, r, z, zo);
 }
 
 // partial sums of r.z and r.(z - zo)
-__global__ void __launch_bounds__(RB) k_cg_dots(int n, const float* __restrict__ r, const float* __restrict__ z,
-                                                const float* __restrict__ zo, double* __restrict__ partial) {
+__device__ __forceinline__ void cg_dots_body(int n, const float* __restrict__ r, const float* __restrict__ z,
+                                             const float* __restrict__ zo, double* __restrict__ partial, int bidx,
+                                             int G) {
   float a = 0.f, b = 0.f;  // per-thread FP32, blocks and the grid in FP64
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+  for (int u = bidx * RB + threadIdx.x; u < n; u += G * RB) {
     const float ru = r[u], zu = z[u];
     a = fmaf(ru, zu, a);
     b = fmaf(ru, zu - zo[u], b);
   }
-  block_sum2((double)a, (double)b, partial, false);
+  block_sum2((double)a, (double)b, partial, false, bidx);
+}
+
+__global__ void __launch_bounds__(RB) k_cg_dots(int n, const float* __restrict__ r, const float* __restrict__ z,
+                                                const float* __restrict__ zo, double* __restrict__ partial) {
+  cg_dots_body(n, r, z, zo, partial, blockIdx.x, gridDim.x);
 }
 
 // scalar updates of the CG recurrence (one thread)
-__global__ void k_cg_scalars(double* sc, int stage) {
-  if (threadIdx.x != 0) return;
+__device__ __forceinline__ void cg_scalars_body(double* sc, int stage) {
   if (stage == 0) {            // after the first preconditioning: rz = r.z
     sc[SC_RZ] = sc[SC_RED];
   } else if (stage == 1) {     // after p.q: alpha = rz / pq
@@ -475,29 +511,45 @@ __global__ void k_cg_scalars(double* sc, int stage) {
   }
 }
 
+__global__ void k_cg_scalars(double* sc, int stage) {
+  if (threadIdx.x == 0) cg_scalars_body(sc, stage);
+}
+
 // p = z + beta p; the first direction is z itself (p holds no value yet: not even its
 // product with 0 may be formed, it could be a NaN pattern)
+__device__ __forceinline__ void cg_pupdate_node(int u, int first, float be, const float* __restrict__ z,
+                                                float* __restrict__ p) {
+  p[u] = first ? z[u] : z[u] + be * p[u];
+}
+
 __global__ void k_cg_pupdate(int n, const double* __restrict__ sc, int first, const float* __restrict__ z,
                              float* __restrict__ p) {
   const float be = first ? 0.f : (float)sc[SC_BETA];
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
-    p[u] = first ? z[u] : z[u] + be * p[u];
+    cg_pupdate_node(u, first, be, z, p);
 }
 
 // x -= y, each node's step limited to max_step (10 kTe): far from the solution an
 // undamped Newton step on the exponential can overshoot into overflow; near it the
 // steps are tiny and the limit never acts, so the converged potential is unchanged
+__device__ __forceinline__ void update_phi_node(int u, double* __restrict__ x, const float* __restrict__ y,
+                                                double max_step) {
+  x[u] -= fmin(fmax((double)y[u], -max_step), max_step);
+}
+
 __global__ void k_update_phi(int n, double* __restrict__ x, const float* __restrict__ y, double max_step) {
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
-    x[u] -= fmin(fmax((double)y[u], -max_step), max_step);
+    update_phi_node(u, x, y, max_step);
+}
+
+__device__ __forceinline__ double b0_value(uint8_t t, double bc, double rho, double inv_eps) {
+  return (t == NC_FIXED) ? bc : (t == NC_INTERIOR ? -rho * inv_eps : 0.0);
 }
 
 __global__ void k_build_b0(int n, const double* __restrict__ rho, const double* __restrict__ bc,
                            const uint8_t* __restrict__ type, double inv_eps, double* __restrict__ b0) {
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
-    const uint8_t t = type[u];
-    b0[u] = (t == NC_FIXED) ? bc[u] : (t == NC_INTERIOR ? -rho[u] * inv_eps : 0.0);
-  }
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
+    b0[u] = b0_value(type[u], bc[u], rho[u], inv_eps);
 }
 
 __global__ void k_fix_phi(int n, double* __restrict__ x, const double* __restrict__ bc, const uint8_t* __restrict__ type) {
@@ -507,10 +559,10 @@ __global__ void k_fix_phi(int n, double* __restrict__ x, const double* __restric
 
 // E = -grad(phi): central differences inside, one-sided on the mesh edges
 // (the rows Solver.getNodeGradient assembles, Solver.java:559-611)
-__global__ void k_efield(int ni, int nj, double inv_dx, double inv_dy, const double* __restrict__ phi,
-                         double* __restrict__ efi, double* __restrict__ efj, float2* __restrict__ E) {
-  const int n = ni * nj;
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+__device__ __forceinline__ void efield_node(int u, int ni, int nj, double inv_dx, double inv_dy,
+                                            const double* __restrict__ phi, double* __restrict__ efi,
+                                            double* __restrict__ efj, float2* __restrict__ E) {
+  {
     const int j = u / ni, i = u - j * ni;
     double gi, gj;
     if (i == 0) gi = (phi[u + 1] - phi[u]) * inv_dx;
@@ -525,6 +577,13 @@ __global__ void k_efield(int ni, int nj, double inv_dx, double inv_dy, const dou
   }
 }
 
+__global__ void k_efield(int ni, int nj, double inv_dx, double inv_dy, const double* __restrict__ phi,
+                         double* __restrict__ efi, double* __restrict__ efj, float2* __restrict__ E) {
+  const int n = ni * nj;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
+    efield_node(u, ni, nj, inv_dx, inv_dy, phi, efi, efj, E);
+}
+
 __global__ void k_boltzmann(int n, const double* __restrict__ phi, double n0, double inv_kTe, double phi0,
                             double* __restrict__ ne) {
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
@@ -533,8 +592,10 @@ __global__ void k_boltzmann(int n, const double* __restrict__ phi, double n0, do
   }
 }
 
+__device__ __forceinline__ double rho_add(double acc, double q, double nd) { return acc + q * nd; }
+
 __global__ void k_rho_add(int n, const double* __restrict__ nd, double q, double* __restrict__ rho) {
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) rho[u] += q * nd[u];
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) rho[u] = rho_add(rho[u], q, nd[u]);
 }
 
 }  // namespace
@@ -598,7 +659,9 @@ static SfPoisson* poisson_get(sf_ctx* ctx) {
   ps->cg_q = (float*)dalloc(ctx, ps, 4 * nn);
   ps->cg_zo = (float*)dalloc(ctx, ps, 4 * nn);
   ps->type0 = (uint8_t*)dalloc(ctx, ps, nn);
-  ps->red_blocks = ctx->num_sms * 4;
+  // the partition of every reduction depends on the mesh alone (a batched solve of the
+  // same mesh reproduces the sums bit for bit)
+  ps->red_blocks = std::min<int>(ctx->num_sms * 4, (int)((nn + RB - 1) / RB));
   ps->partial = (double*)dalloc(ctx, ps, 24 * (size_t)ps->red_blocks);
   ps->red = (double*)dalloc(ctx, ps, 24);
   ps->sc = (double*)dalloc(ctx, ps, 8 * 8);
@@ -1025,3 +1088,633 @@ int sf_boltzmann(sf_ctx* ctx, double* ne) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------
+// Batched field phase: rho, the nonlinear solve and E of many contexts (sf_batch) with
+// one launch per stage for all of them.  Every stage runs the per-node and per-block
+// bodies of the single-context kernels on each instance's own buffers, with the same
+// reduction partition, so every instance gets the potential its own sf_poisson_nl would
+// give, bit for bit.  Convergence is decided per instance on the device; the host reads
+// one count per Newton round for the whole batch.
+// ------------------------------------------------------------------------------------
+namespace {
+
+constexpr int BP_MAX_SPECIES = 8;
+constexpr int ET = 256;  // nodes per block of the elementwise and level kernels
+
+struct BPInst {
+  int ni, nj, nn, red_blocks;
+  double inv_dx, inv_dy;
+  NlArgs nl;  // mesh part of the residual arguments (the step's parameters are added per launch)
+  double *phi, *b0, *rho, *efi, *efj, *partial, *red, *sc;
+  const double* bc;
+  const uint8_t* type0;
+  float2* E;
+  float *cg_x, *cg_p, *cg_q, *cg_zo;
+  int nspecies;
+  const double* nd[BP_MAX_SPECIES];
+  double q[BP_MAX_SPECIES];
+  int cs;
+  LevelView lv[MAX_LEVELS];
+  CoarseDesc cd;
+  // state of the current step
+  int iters;     // PCG iterations per Newton step
+  int fp64_exp;  // sticky, as SfPoisson::fp64_exp
+  int live;      // the residual is evaluated in this round
+  int run;       // a Newton step is taken in this round
+  int redo;      // the residual is evaluated again with the FP64 exponential
+  int it, vcount, status;  // status: 0 running, 1 converged, 2 not converged, 3 diverged
+  double res, res_inf, res0;
+};
+
+struct BPParams {
+  double C_n0, inv_kTe, phi0, inv_eps, tol, max_step;
+  int linear, max_it;
+};
+
+struct BPStat {
+  int status, it, vcount, fp64_exp;
+  double res, res_inf, res0;
+};
+
+enum { BP_LIVE = 0, BP_REDO = 1, BP_RUN = 2 };
+
+__device__ __forceinline__ bool bp_part(const BPInst& I, int mode, int kmin) {
+  if (mode == BP_LIVE) return I.live != 0;
+  if (mode == BP_REDO) return I.redo != 0;
+  return I.run != 0 && I.iters > kmin;
+}
+
+// instance owning block b of a launch: start[i] <= b < start[i + 1]
+__device__ __forceinline__ int bp_find(const int* __restrict__ start, int n, int b) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (start[mid] <= b) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// iters[0..n): PCG iterations per Newton step, iters[n..2n): the sticky FP64 choice
+__global__ void kb_init(BPInst* I, int n, const int* __restrict__ iters) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  BPInst& s = I[i];
+  s.iters = iters[i];
+  s.fp64_exp = iters[n + i];
+  s.live = 1;
+  s.run = 0;
+  s.redo = 0;
+  s.it = 0;
+  s.vcount = 0;
+  s.status = 0;
+  s.res = s.res_inf = 0.0;
+  s.res0 = -1.0;
+}
+
+// rho = sum q nd (sf_update_rho), b0 (k_build_b0), fixed rows of phi (k_fix_phi)
+__global__ void kb_rho_b0(BPInst* I, int n, const int* __restrict__ start, const BPParams* __restrict__ pr) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (u >= s.nn) return;
+  double r = 0.0;
+  for (int k = 0; k < s.nspecies; k++) r = rho_add(r, s.q[k], s.nd[k][u]);
+  s.rho[u] = r;
+  const uint8_t t = s.type0[u];
+  s.b0[u] = b0_value(t, s.bc[u], r, pr->inv_eps);
+  if (t == NC_FIXED) s.phi[u] = s.bc[u];
+}
+
+__global__ void __launch_bounds__(RB) kb_nl_residual(BPInst* I, int n, const int* __restrict__ start,
+                                                     const BPParams* __restrict__ pr, int mode) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, mode, 0)) return;
+  NlArgs a = s.nl;
+  a.C_n0 = pr->C_n0;
+  a.inv_kTe = pr->inv_kTe;
+  a.phi0 = pr->phi0;
+  a.linear = pr->linear;
+  a.fp64_exp = s.fp64_exp;
+  nl_residual_body(a, s.phi, s.b0, s.type0, s.lv[0].r, s.lv[0].P, s.partial, blockIdx.x - start[i], s.red_blocks);
+}
+
+__global__ void kb_reduce3(BPInst* I, int mode) {
+  const BPInst& s = I[blockIdx.x];
+  if (!bp_part(s, mode, 0)) return;
+  reduce3_body(s.partial, s.red_blocks, s.red);
+}
+
+// the FP32 exponential's error bound against the tolerance (the residual lambda of sf_poisson_nl)
+__global__ void kb_check_exp(BPInst* I, int n, const BPParams* __restrict__ pr) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  BPInst& s = I[i];
+  s.redo = 0;
+  if (s.live && !s.fp64_exp && s.red[2] / sqrt((double)s.nn) > 0.01 * pr->tol) {
+    s.fp64_exp = 1;
+    s.redo = 1;
+  }
+}
+
+// one check of the Newton loop of sf_poisson_nl per live instance; run_count counts the
+// instances that take a step in this round
+__global__ void kb_newton_control(BPInst* I, int n, const BPParams* __restrict__ pr, int* run_count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  BPInst& s = I[i];
+  s.run = 0;
+  if (!s.live) return;
+  const double res = sqrt(s.red[0]) / s.nn;
+  s.res = res;
+  s.res_inf = s.red[1];
+  if (s.res0 < 0) s.res0 = res;
+  if (!isfinite(res)) {
+    s.status = 3;
+  } else if (res < pr->tol) {
+    s.status = 1;
+  } else if (s.it == pr->max_it) {
+    s.status = 2;
+  } else {
+    s.run = 1;
+    s.it++;
+    s.vcount += s.iters;
+    atomicAdd(run_count, 1);
+    return;
+  }
+  s.live = 0;
+}
+
+// level kernels over the instances whose grid levels include l (l < cs)
+__global__ void kb_restrict_P(BPInst* I, int n, const int* __restrict__ start, int l, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  const LevelView& F = s.lv[l];
+  const LevelView& Cl = s.lv[l + 1];
+  const int uc = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (uc >= Cl.ni * Cl.nj) return;
+  const int J = uc / Cl.ni, Ii = uc - J * Cl.ni;
+  Cl.P[uc] = F.P[(2 * J) * F.ni + 2 * Ii];
+}
+
+__global__ void kb_zero_y(BPInst* I, int n, const int* __restrict__ start, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (u < s.nn) s.lv[0].y[u] = 0.f;
+}
+
+__global__ void kb_smooth(BPInst* I, int n, const int* __restrict__ start, int l, int color, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  const LevelView& L = s.lv[l];
+  const int hw = (L.ni + 1) / 2;
+  const int v = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  const int j = v / hw;
+  if (j >= L.nj) return;
+  const int ii = 2 * (v - j * hw) + ((j + color) & 1);
+  if (ii >= L.ni) return;
+  const int u = j * L.ni + ii;
+  L.y[u] = gs_value(L.type[u], L.y, L.r[u], L.P[u], u, L.ni, L.cx, L.cy);
+}
+
+__global__ void kb_resid(BPInst* I, int n, const int* __restrict__ start, int l, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  const LevelView& L = s.lv[l];
+  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (u >= L.ni * L.nj) return;
+  L.t[u] = L.r[u] - apply_J(L.type[u], L.y, L.P[u], u, L.ni, L.cx, L.cy);
+}
+
+__global__ void kb_restrict(BPInst* I, int n, const int* __restrict__ start, int l, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  const LevelView& F = s.lv[l];
+  const LevelView& Cl = s.lv[l + 1];
+  const int uc = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (uc >= Cl.ni * Cl.nj) return;
+  const int J = uc / Cl.ni, Ii = uc - J * Cl.ni;
+  Cl.r[uc] = restrict_value(F.t, Cl.type[uc], Ii, J, F.ni, Cl.ni, Cl.nj);
+  Cl.y[uc] = 0.f;
+}
+
+__global__ void kb_prolong(BPInst* I, int n, const int* __restrict__ start, int l, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  const LevelView& F = s.lv[l];
+  const LevelView& Cl = s.lv[l + 1];
+  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (u >= F.ni * F.nj) return;
+  if (F.type[u] == NC_FIXED) return;
+  const int j = u / F.ni, ii = u - j * F.ni;
+  F.y[u] += prolong_value(Cl.y, ii, j, Cl.ni);
+}
+
+__global__ void __launch_bounds__(1024) kb_coarse_vcycle(BPInst* I, int nu1, int nu2, int kmin) {
+  const BPInst& s = I[blockIdx.x];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  coarse_vcycle_body(s.cd, s.lv[s.cs], nu1, nu2);
+}
+
+// fine-level PCG stages
+__global__ void kb_zero_cg(BPInst* I, int n, const int* __restrict__ start, int which, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (u < s.nn) (which == 0 ? s.cg_x : s.cg_zo)[u] = 0.f;
+}
+
+__global__ void __launch_bounds__(RB) kb_cg_dots(BPInst* I, int n, const int* __restrict__ start, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  cg_dots_body(s.nn, s.lv[0].r, s.lv[0].y, s.cg_zo, s.partial, blockIdx.x - start[i], s.red_blocks);
+}
+
+__global__ void __launch_bounds__(RB) kb_cg_matvec(BPInst* I, int n, const int* __restrict__ start, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  cg_matvec_body(s.lv[0], s.cg_p, s.cg_q, s.partial, blockIdx.x - start[i], s.red_blocks);
+}
+
+__global__ void kb_reduce2(BPInst* I, int kmin) {
+  const BPInst& s = I[blockIdx.x];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  reduce2_body(s.partial, s.red_blocks, s.sc + SC_RED, 0);
+}
+
+__global__ void kb_cg_scalars(BPInst* I, int n, int stage, int kmin) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  cg_scalars_body(s.sc, stage);
+}
+
+__global__ void kb_cg_axpy(BPInst* I, int n, const int* __restrict__ start, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (u < s.nn) cg_axpy_node(u, (float)s.sc[SC_ALPHA], s.cg_p, s.cg_q, s.cg_x, s.lv[0].r, s.lv[0].y, s.cg_zo);
+}
+
+__global__ void kb_cg_pupdate(BPInst* I, int n, const int* __restrict__ start, int first, int kmin) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, kmin)) return;
+  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (u < s.nn) cg_pupdate_node(u, first, first ? 0.f : (float)s.sc[SC_BETA], s.lv[0].y, s.cg_p);
+}
+
+__global__ void kb_update_phi(BPInst* I, int n, const int* __restrict__ start, const BPParams* __restrict__ pr) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  if (!bp_part(s, BP_RUN, 0)) return;
+  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (u < s.nn) update_phi_node(u, s.phi, s.cg_x, pr->max_step);
+}
+
+__global__ void kb_efield(BPInst* I, int n, const int* __restrict__ start) {
+  const int i = bp_find(start, n, blockIdx.x);
+  const BPInst& s = I[i];
+  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (u < s.nn) efield_node(u, s.ni, s.nj, s.inv_dx, s.inv_dy, s.phi, s.efi, s.efj, s.E);
+}
+
+__global__ void kb_collect(const BPInst* I, int n, BPStat* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const BPInst& s = I[i];
+  out[i] = BPStat{s.status, s.it, s.vcount, s.fp64_exp, s.res, s.res_inf, s.res0};
+}
+
+}  // namespace
+
+namespace sf {
+
+struct BatchPoisson {
+  int n = 0, num_sms = 0;
+  std::vector<sf_ctx*> ctx;
+  std::vector<int> nspecies;  // charged species per context when the table was built
+  BPInst* d_inst = nullptr;
+  int* d_tab = nullptr;        // block prefixes of every launch kind, n + 1 each
+  int* d_iters = nullptr;
+  int* d_run = nullptr;
+  BPParams* d_prm = nullptr;
+  BPStat* d_stat = nullptr;
+  // table offsets into d_tab and total blocks
+  int fine_off = 0, fine_tot = 0, red_off = 0, red_tot = 0, zero_off = 0, zero_tot = 0;
+  std::vector<int> lvl_off, lvl_tot, lvlc_off, lvlc_tot, half_off, half_tot;  // per grid level
+  int max_cs = 0;
+  size_t coarse_smem = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // Newton round by max PCG iterations
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+template <typename F>
+static void bp_table(std::vector<int>& tab, int n, F blocks, int& off, int& tot) {
+  off = (int)tab.size();
+  int acc = 0;
+  for (int i = 0; i < n; i++) {
+    tab.push_back(acc);
+    acc += blocks(i);
+  }
+  tab.push_back(acc);
+  tot = acc;
+}
+
+static void bp_vcycle(BatchPoisson* bp, cudaStream_t s, int kmin) {
+  const int n = bp->n;
+  BPInst* I = bp->d_inst;
+  if (bp->zero_tot > 0) kb_zero_y<<<bp->zero_tot, ET, 0, s>>>(I, n, bp->d_tab + bp->zero_off, kmin);
+  for (int l = 0; l < bp->max_cs; l++) {
+    const int* half = bp->d_tab + bp->half_off[l];
+    for (int k = 0; k < 2; k++) {
+      kb_smooth<<<bp->half_tot[l], ET, 0, s>>>(I, n, half, l, 0, kmin);
+      kb_smooth<<<bp->half_tot[l], ET, 0, s>>>(I, n, half, l, 1, kmin);
+    }
+    kb_resid<<<bp->lvl_tot[l], ET, 0, s>>>(I, n, bp->d_tab + bp->lvl_off[l], l, kmin);
+    kb_restrict<<<bp->lvlc_tot[l], ET, 0, s>>>(I, n, bp->d_tab + bp->lvlc_off[l], l, kmin);
+  }
+  kb_coarse_vcycle<<<n, 1024, bp->coarse_smem, s>>>(I, 2, 2, kmin);
+  for (int l = bp->max_cs - 1; l >= 0; l--) {
+    kb_prolong<<<bp->lvl_tot[l], ET, 0, s>>>(I, n, bp->d_tab + bp->lvl_off[l], l, kmin);
+    const int* half = bp->d_tab + bp->half_off[l];
+    for (int k = 0; k < 2; k++) {
+      kb_smooth<<<bp->half_tot[l], ET, 0, s>>>(I, n, half, l, 1, kmin);
+      kb_smooth<<<bp->half_tot[l], ET, 0, s>>>(I, n, half, l, 0, kmin);
+    }
+  }
+}
+
+// One Newton round of every live instance: the residual (again in FP64 where the FP32
+// exponential's bound fails), the convergence check, and for the instances that go on
+// the Newton step: restriction of P, PCG with the instance's iterations, phi update.
+static void bp_round(BatchPoisson* bp, cudaStream_t s, int max_iters) {
+  const int n = bp->n;
+  BPInst* I = bp->d_inst;
+  const int* fine = bp->d_tab + bp->fine_off;
+  const int* red = bp->d_tab + bp->red_off;
+  const int tb = 128, tg = (n + tb - 1) / tb;
+  SF_CUDA(cudaMemsetAsync(bp->d_run, 0, sizeof(int), s));
+  kb_nl_residual<<<bp->red_tot, RB, 0, s>>>(I, n, red, bp->d_prm, BP_LIVE);
+  kb_reduce3<<<n, 256, 0, s>>>(I, BP_LIVE);
+  kb_check_exp<<<tg, tb, 0, s>>>(I, n, bp->d_prm);
+  kb_nl_residual<<<bp->red_tot, RB, 0, s>>>(I, n, red, bp->d_prm, BP_REDO);
+  kb_reduce3<<<n, 256, 0, s>>>(I, BP_REDO);
+  kb_newton_control<<<tg, tb, 0, s>>>(I, n, bp->d_prm, bp->d_run);
+  for (int l = 0; l < bp->max_cs; l++)
+    kb_restrict_P<<<bp->lvlc_tot[l], ET, 0, s>>>(I, n, bp->d_tab + bp->lvlc_off[l], l, 0);
+  kb_zero_cg<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, 0, 0);
+  bp_vcycle(bp, s, 0);
+  kb_zero_cg<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, 1, 0);
+  kb_cg_dots<<<bp->red_tot, RB, 0, s>>>(I, n, red, 0);
+  kb_reduce2<<<n, 256, 0, s>>>(I, 0);
+  kb_cg_scalars<<<tg, tb, 0, s>>>(I, n, 0, 0);
+  kb_cg_pupdate<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, 1, 0);
+  for (int k = 0; k < max_iters; k++) {
+    kb_cg_matvec<<<bp->red_tot, RB, 0, s>>>(I, n, red, k);
+    kb_reduce2<<<n, 256, 0, s>>>(I, k);
+    kb_cg_scalars<<<tg, tb, 0, s>>>(I, n, 1, k);
+    kb_cg_axpy<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, k);
+    if (k == max_iters - 1) break;
+    bp_vcycle(bp, s, k + 1);
+    kb_cg_dots<<<bp->red_tot, RB, 0, s>>>(I, n, red, k + 1);
+    kb_reduce2<<<n, 256, 0, s>>>(I, k + 1);
+    kb_cg_scalars<<<tg, tb, 0, s>>>(I, n, 2, k + 1);
+    kb_cg_pupdate<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, 0, k + 1);
+  }
+  kb_update_phi<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, bp->d_prm);
+  SF_CUDA(cudaGetLastError());
+}
+
+static cudaGraphExec_t bp_graph(BatchPoisson* bp, int max_iters) {
+  for (auto& g : bp->graphs)
+    if (g.first == max_iters) return g.second;
+  cudaGraph_t graph = nullptr;
+  SF_CUDA(cudaStreamBeginCapture(bp->stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    bp_round(bp, bp->stream, max_iters);
+  } catch (...) {
+    cudaStreamEndCapture(bp->stream, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    throw;
+  }
+  SF_CUDA(cudaStreamEndCapture(bp->stream, &graph));
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&ex, graph, 0);
+  cudaGraphDestroy(graph);
+  SF_CUDA(e);
+  bp->graphs.push_back({max_iters, ex});
+  return ex;
+}
+
+static int charged_species(const sf_ctx* c) {
+  int k = 0;
+  for (const SfSpecies* sp : c->species)
+    if (sp->charge != 0) k++;
+  return k;
+}
+
+// the instance table from the contexts' current state
+static void bp_fill(BatchPoisson* bp) {
+  std::vector<BPInst> h(bp->n);
+  bp->nspecies.assign(bp->n, 0);
+  for (int i = 0; i < bp->n; i++) {
+    sf_ctx* c = bp->ctx[i];
+    SfPoisson* ps = poisson_get(c);
+    BPInst& s = h[i];
+    std::memset(&s, 0, sizeof(s));
+    s.ni = c->ni;
+    s.nj = c->nj;
+    s.nn = c->ni * c->nj;
+    s.red_blocks = ps->red_blocks;
+    s.inv_dx = 1.0 / c->dh[0];
+    s.inv_dy = 1.0 / c->dh[1];
+    s.nl.ni = c->ni;
+    s.nl.nj = c->nj;
+    s.nl.dx = c->dh[0];
+    s.nl.dy = c->dh[1];
+    s.nl.cx = 1.0 / (s.nl.dx * s.nl.dx);
+    s.nl.cy = 1.0 / (s.nl.dy * s.nl.dy);
+    s.phi = ps->phi;
+    s.b0 = ps->b0;
+    s.rho = ps->rho;
+    s.efi = ps->efi;
+    s.efj = ps->efj;
+    s.partial = ps->partial;
+    s.red = ps->red;
+    s.sc = ps->sc;
+    s.bc = ps->bc;
+    s.type0 = ps->type0;
+    s.E = c->E;
+    s.cg_x = ps->cg_x;
+    s.cg_p = ps->cg_p;
+    s.cg_q = ps->cg_q;
+    s.cg_zo = ps->cg_zo;
+    for (const SfSpecies* sp : c->species) {
+      if (sp->charge == 0) continue;
+      SF_REQUIRE(s.nspecies < BP_MAX_SPECIES, SF_ERR_ARG, "too many charged species for the batched solve");
+      s.nd[s.nspecies] = sp->nd;
+      s.q[s.nspecies] = sp->charge;
+      s.nspecies++;
+    }
+    bp->nspecies[i] = s.nspecies;
+    s.cs = ps->cs;
+    for (size_t l = 0; l < ps->lv.size(); l++) s.lv[l] = ps->lv[l];
+    s.cd = ps->cd;
+    s.fp64_exp = ps->fp64_exp ? 1 : 0;
+  }
+  copy_wait(bp->d_inst, h.data(), sizeof(BPInst) * bp->n, cudaMemcpyHostToDevice, bp->stream);
+}
+
+BatchPoisson* batch_poisson_create(sf_ctx* const* ctxs, int n, int num_sms, cudaStream_t stream) {
+  auto* bp = new BatchPoisson();
+  try {
+    bp->n = n;
+    bp->num_sms = num_sms;
+    bp->stream = stream;
+    bp->ctx.assign(ctxs, ctxs + n);
+    std::vector<SfPoisson*> ps(n);
+    for (int i = 0; i < n; i++) {
+      SF_REQUIRE(ctxs[i]->domain == SF_DOMAIN_XY, SF_ERR_ARG, "the batched solve takes XY meshes");
+      ps[i] = poisson_get(ctxs[i]);
+      bp->max_cs = std::max(bp->max_cs, ps[i]->cs);
+      bp->coarse_smem = std::max(bp->coarse_smem, ps[i]->coarse_smem);
+    }
+    std::vector<int> tab;
+    bp_table(tab, n, [&](int i) { return (ps[i]->ni * ps[i]->nj + ET - 1) / ET; }, bp->fine_off, bp->fine_tot);
+    bp_table(tab, n, [&](int i) { return ps[i]->red_blocks; }, bp->red_off, bp->red_tot);
+    bp_table(tab, n, [&](int i) { return ps[i]->cs > 0 ? (ps[i]->ni * ps[i]->nj + ET - 1) / ET : 0; }, bp->zero_off,
+             bp->zero_tot);
+    bp->lvl_off.resize(bp->max_cs);
+    bp->lvl_tot.resize(bp->max_cs);
+    bp->lvlc_off.resize(bp->max_cs);
+    bp->lvlc_tot.resize(bp->max_cs);
+    bp->half_off.resize(bp->max_cs);
+    bp->half_tot.resize(bp->max_cs);
+    for (int l = 0; l < bp->max_cs; l++) {
+      auto on = [&](int i) { return l < ps[i]->cs; };
+      bp_table(tab, n, [&](int i) { return on(i) ? (ps[i]->lv[l].ni * ps[i]->lv[l].nj + ET - 1) / ET : 0; },
+               bp->lvl_off[l], bp->lvl_tot[l]);
+      bp_table(tab, n,
+               [&](int i) { return on(i) ? (ps[i]->lv[l + 1].ni * ps[i]->lv[l + 1].nj + ET - 1) / ET : 0; },
+               bp->lvlc_off[l], bp->lvlc_tot[l]);
+      bp_table(tab, n,
+               [&](int i) { return on(i) ? (ps[i]->lv[l].nj * ((ps[i]->lv[l].ni + 1) / 2) + ET - 1) / ET : 0; },
+               bp->half_off[l], bp->half_tot[l]);
+    }
+    SF_CUDA(cudaMalloc(&bp->d_tab, sizeof(int) * tab.size()));
+    copy_wait(bp->d_tab, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, stream);
+    SF_CUDA(cudaMalloc(&bp->d_inst, sizeof(BPInst) * n));
+    SF_CUDA(cudaMalloc(&bp->d_iters, sizeof(int) * 2 * n));
+    SF_CUDA(cudaFuncSetAttribute(kb_coarse_vcycle, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)COARSE_SMEM_MAX));
+    SF_CUDA(cudaMalloc(&bp->d_run, sizeof(int)));
+    SF_CUDA(cudaMalloc(&bp->d_prm, sizeof(BPParams)));
+    SF_CUDA(cudaMalloc(&bp->d_stat, sizeof(BPStat) * n));
+    SF_CUDA(cudaEventCreate(&bp->ev0));
+    SF_CUDA(cudaEventCreate(&bp->ev1));
+    bp_fill(bp);
+    return bp;
+  } catch (...) {
+    batch_poisson_destroy(bp);
+    throw;
+  }
+}
+
+void batch_poisson_destroy(BatchPoisson* bp) {
+  if (!bp) return;
+  if (bp->stream) cudaStreamSynchronize(bp->stream);
+  for (auto& g : bp->graphs) cudaGraphExecDestroy(g.second);
+  void* ptrs[] = {bp->d_inst, bp->d_tab, bp->d_iters, bp->d_run, bp->d_prm, bp->d_stat};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (bp->ev0) cudaEventDestroy(bp->ev0);
+  if (bp->ev1) cudaEventDestroy(bp->ev1);
+  delete bp;
+}
+
+// rho of the contexts' species, the nonlinear solve of every instance and E, on the
+// batch stream.  iters: PCG iterations per Newton step per instance.  Returns the time
+// of the whole phase; st[i] gets each instance's Newton count, V-cycles and residuals.
+float batch_poisson_step(BatchPoisson* bp, const sf_poisson_params& prm, const int* iters, sf_solve_stats* st,
+                         int* status) {
+  SF_REQUIRE(prm.eps > 0 && prm.tol > 0 && prm.max_it > 0, SF_ERR_ARG, "bad solver parameters");
+  SF_REQUIRE(prm.linear || (prm.kTe0 > 0 && prm.n0 > 0), SF_ERR_ARG, "Boltzmann electrons need n0 > 0 and kTe0 > 0");
+  cudaStream_t s = bp->stream;
+  bool refill = false;
+  for (int i = 0; i < bp->n; i++) refill |= charged_species(bp->ctx[i]) != bp->nspecies[i];
+  if (refill) bp_fill(bp);
+  BPParams h;
+  h.C_n0 = QE / prm.eps * prm.n0;
+  h.inv_kTe = prm.linear ? 0.0 : 1.0 / prm.kTe0;
+  h.phi0 = prm.phi0;
+  h.inv_eps = 1.0 / prm.eps;
+  h.tol = prm.tol;
+  h.max_step = prm.linear ? 1e300 : 10.0 * prm.kTe0;
+  h.linear = prm.linear ? 1 : 0;
+  h.max_it = prm.max_it;
+  int max_iters = 1;
+  std::vector<int> init(2 * bp->n);
+  for (int i = 0; i < bp->n; i++) {
+    SF_REQUIRE(iters[i] >= 1, SF_ERR_ARG, "PCG iterations per Newton step must be >= 1");
+    max_iters = std::max(max_iters, iters[i]);
+    init[i] = iters[i];
+    init[bp->n + i] = bp->ctx[i]->poisson->fp64_exp ? 1 : 0;  // the contexts hold the sticky choice
+  }
+  SF_CUDA(cudaEventRecord(bp->ev0, s));
+  SF_CUDA(cudaMemcpyAsync(bp->d_prm, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+  SF_CUDA(cudaMemcpyAsync(bp->d_iters, init.data(), sizeof(int) * 2 * bp->n, cudaMemcpyHostToDevice, s));
+  const int tg = (bp->n + 127) / 128;
+  kb_init<<<tg, 128, 0, s>>>(bp->d_inst, bp->n, bp->d_iters);
+  kb_rho_b0<<<bp->fine_tot, ET, 0, s>>>(bp->d_inst, bp->n, bp->d_tab + bp->fine_off, bp->d_prm);
+  SF_CUDA(cudaGetLastError());
+  cudaGraphExec_t g = bp_graph(bp, max_iters);
+  for (int r = 0; r <= prm.max_it; r++) {
+    SF_CUDA(cudaGraphLaunch(g, s));
+    int run = 0;
+    SF_CUDA(cudaMemcpyAsync(&run, bp->d_run, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SF_CUDA(cudaStreamSynchronize(s));
+    if (run == 0) break;
+  }
+  kb_efield<<<bp->fine_tot, ET, 0, s>>>(bp->d_inst, bp->n, bp->d_tab + bp->fine_off);
+  kb_collect<<<tg, 128, 0, s>>>(bp->d_inst, bp->n, bp->d_stat);
+  SF_CUDA(cudaGetLastError());
+  SF_CUDA(cudaEventRecord(bp->ev1, s));
+  std::vector<BPStat> hs(bp->n);
+  SF_CUDA(cudaMemcpyAsync(hs.data(), bp->d_stat, sizeof(BPStat) * bp->n, cudaMemcpyDeviceToHost, s));
+  SF_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  SF_CUDA(cudaEventElapsedTime(&ms, bp->ev0, bp->ev1));
+  for (int i = 0; i < bp->n; i++) {
+    SfPoisson* ps = bp->ctx[i]->poisson;
+    ps->rho_set = true;
+    ps->prm = prm;
+    ps->have_prm = true;
+    ps->fp64_exp = hs[i].fp64_exp != 0;
+    bp->ctx[i]->efield_set = true;
+    status[i] = hs[i].status;
+    st[i].newton_it = hs[i].it;
+    st[i].vcycles = hs[i].vcount;
+    st[i].residual = hs[i].res;
+    st[i].residual_inf = hs[i].res_inf;
+    st[i].initial_residual = hs[i].res0;
+    st[i].ms = ms;
+  }
+  return ms;
+}
+
+}  // namespace sf

@@ -438,6 +438,7 @@ def main():
     ap.add_argument("--dsmc-steps", type=int, default=20)
     ap.add_argument("--batch-steps", type=int, default=16)
     ap.add_argument("--batch-threads", type=int, default=16)
+    ap.add_argument("--batch-instances", type=int, default=256)
     ap.add_argument("--batch-unbatched-steps", type=int, default=3)
     ap.add_argument("--only-batch", action="store_true",
                     help="run only the batched-instances leg and print its result line")
@@ -448,8 +449,8 @@ def main():
     if args.only_batch:
         from starfish_gb300 import build as B
         B.build()
-        print(json.dumps(batch_bench(steps=args.batch_steps, threads=args.batch_threads,
-                                     unbatched_steps=args.batch_unbatched_steps)))
+        print(json.dumps(batch_bench(n_instances=args.batch_instances, steps=args.batch_steps,
+                                     threads=args.batch_threads, unbatched_steps=args.batch_unbatched_steps)))
         return
 
     import torch
@@ -576,7 +577,7 @@ def main():
     if args.dsmc_steps > 0:
         line["dsmc"] = dsmc_jet_bench(steps=args.dsmc_steps)
     if args.batch_steps > 0:
-        line["batch"] = batch_bench(steps=args.batch_steps, threads=args.batch_threads,
+        line["batch"] = batch_bench(n_instances=args.batch_instances, steps=args.batch_steps, threads=args.batch_threads,
                                     unbatched_steps=args.batch_unbatched_steps)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1

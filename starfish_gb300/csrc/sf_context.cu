@@ -33,6 +33,7 @@ sf::MeshView sf_ctx::mesh_view() const {
   m.node_seg_ptr = node_seg_ptr;
   m.node_seg_idx = node_seg_idx;
   m.seg_xy = d_seg_xy;
+  m.seg_lc = d_seg_lc;
   m.seg_btype = d_seg_btype;
   m.face_type = d_face_type;
   m.node_vol = d_node_vol;
@@ -588,9 +589,23 @@ int sf_ctx_create(const sf_mesh_desc* md, int device, sf_ctx** out) {
     if (!idx.empty())
       copy_wait(ctx->node_seg_idx, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, ctx->stream);
     SF_CUDA(cudaMalloc(&ctx->d_seg_xy, sizeof(Seg4) * std::max(ctx->nseg, 1)));
+    SF_CUDA(cudaMalloc(&ctx->d_seg_lc, sizeof(SegLC) * std::max(ctx->nseg, 1)));
     SF_CUDA(cudaMalloc(&ctx->d_seg_btype, sizeof(int) * std::max(ctx->nseg, 1)));
     if (ctx->nseg > 0) {
       copy_wait(ctx->d_seg_xy, ctx->seg_xy.data(), sizeof(Seg4) * ctx->nseg, cudaMemcpyHostToDevice, ctx->stream);
+      std::vector<SegLC> lcs(ctx->nseg);
+      for (int s = 0; s < ctx->nseg; s++) {
+        int ib[4];
+        float fr[4];
+        for (int q = 0; q < 4; q++) {
+          const double l = (ctx->seg_xy[4 * (size_t)s + q] - ctx->x0[q & 1]) / ctx->dh[q & 1];
+          const double b = std::floor(l);
+          ib[q] = (int)b;
+          fr[q] = (float)(l - b);
+        }
+        lcs[s] = SegLC{ib[0], ib[1], ib[2], ib[3], fr[0], fr[1], fr[2], fr[3]};
+      }
+      copy_wait(ctx->d_seg_lc, lcs.data(), sizeof(SegLC) * ctx->nseg, cudaMemcpyHostToDevice, ctx->stream);
       copy_wait(ctx->d_seg_btype, ctx->seg_btype.data(), sizeof(int) * ctx->nseg, cudaMemcpyHostToDevice, ctx->stream);
     }
     SF_CUDA(cudaMalloc(&ctx->d_face_type, 4 * (size_t)ctx->nmax));
@@ -639,7 +654,7 @@ int sf_ctx_destroy(sf_ctx* ctx) {
       if (p) cudaFree(p);
     delete sp;
   }
-  void* ptrs[] = {ctx->E, ctx->seg_dist, ctx->node_seg_ptr, ctx->node_seg_idx, ctx->d_seg_xy,
+  void* ptrs[] = {ctx->E, ctx->seg_dist, ctx->node_seg_ptr, ctx->node_seg_idx, ctx->d_seg_xy, ctx->d_seg_lc,
                   ctx->d_seg_btype, ctx->d_face_type, ctx->d_node_vol, ctx->slow_idx, ctx->counters,
                   ctx->stats_partial, ctx->bins, ctx->bins_tmp, ctx->scan_blocks, ctx->dscratch};
   for (void* p : ptrs)

@@ -51,6 +51,14 @@ struct alignas(16) Seg4 {
   double x, y, z, w;
 };
 
+// The same end points in cells from the mesh origin, split into an integer cell and an
+// FP32 fraction: an end point relative to a cell is an exact integer difference plus one
+// FP32 add (no FP64 work in the FP32 segment tests).
+struct alignas(16) SegLC {
+  int i1, j1, i2, j2;
+  float f1, g1, f2, g2;
+};
+
 // Packed cell word: (j << 16) | i.  Meshes are limited to 65535 nodes per direction.
 __host__ __device__ inline uint32_t pack_cell(int i, int j) { return ((uint32_t)j << 16) | (uint32_t)i; }
 __host__ __device__ inline int cell_i(uint32_t c) { return (int)(c & 0xFFFFu); }
@@ -79,6 +87,7 @@ struct MeshView {
   const int* node_seg_ptr;      // ni*nj+1
   const int* node_seg_idx;
   const Seg4* seg_xy;        // x1, y1, x2, y2
+  const SegLC* seg_lc;       // the same end points in cells from the mesh origin
   const int* seg_btype;
   const int8_t* face_type;      // 4*nmax
   const double* node_vol;       // ni*nj
@@ -304,6 +313,7 @@ struct sf_ctx {
   int* node_seg_ptr = nullptr;
   int* node_seg_idx = nullptr;
   sf::Seg4* d_seg_xy = nullptr;
+  sf::SegLC* d_seg_lc = nullptr;
   int* d_seg_btype = nullptr;
   int8_t* d_face_type = nullptr;
   double* d_node_vol = nullptr;

@@ -89,10 +89,15 @@ struct Kahan {
 // atomics cannot overflow (<= 1024 particles per tile), then flushed with one 64-bit
 // global atomic per touched node.  Tiles whose box does not fit (unsorted input) fall
 // back to 64-bit global atomics per corner.
+__device__ bool may_hit_fp32(const MeshView& m, int i, int j, float fx, float fy, float gx, float gy);
+
 // One tile (TILE particles from t0) of the fused push + deposit: load, push, fast-path
 // test, enqueue of slow candidates, shared-memory deposit of the tile's box and its
-// flush.  Shared by k_push (one mesh) and k_push_batch (many instances).
-template <int DOM, bool STATS, bool MOM>
+// flush.  Shared by k_push (one mesh) and k_push_batch (many instances).  PRE (XY): a
+// particle that fails the distance test is given the exact path's FP32 pre-filter here,
+// and finishes here when no candidate segment can be on its path (moves of many cells,
+// as in small meshes at large dt, would otherwise mostly queue for the exact path).
+template <int DOM, bool STATS, bool MOM, bool PRE = false>
 __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView& P, const PushArgs& a, int64_t t0,
                                           unsigned long long* __restrict__ count, long long* __restrict__ mom,
                                           int* __restrict__ slow_idx, unsigned long long* __restrict__ counters,
@@ -145,9 +150,12 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
         float vz = lvz[k];
         // move in logical coordinates (x += v dt; XtoL)
         float nfx, nfy, nvx = v.x, nvy = v.y, nvz = vz;
+        float gx = 0.f, gy = 0.f;  // XY: the new position in cells from (i, j), before reduction
         if (DOM == SF_DOMAIN_XY) {
           nfx = f.x + v.x * a.dt_dx;
           nfy = f.y + v.y * a.dt_dy;
+          gx = nfx;
+          gy = nfy;
         } else if (DOM == SF_DOMAIN_ZR) {
           // rotateToZR (KineticMaterial.java:444-462) relative to the cell radius rj
           nfx = f.x + v.x * a.dt_dx;
@@ -186,7 +194,9 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
         const int i2 = i + di, j2 = j + dj;
         const int span = max(abs(di), abs(dj)) + 1;
         const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
-        const bool clear = (int)__ldg(&m.seg_dist[j * m.ni + i]) > span;
+        bool clear = (int)__ldg(&m.seg_dist[j * m.ni + i]) > span;
+        if (PRE && DOM == SF_DOMAIN_XY && !clear)
+          clear = !may_hit_fp32(m, i, j, f.x, f.y, gx, gy);
         if (inside && clear) {
           __stcs(&P.cell[p], pack_cell(i2, j2));
           __stcs(&P.frac[p], make_float2(nfx, nfy));
@@ -415,6 +425,42 @@ __device__ double sample_maxw_speed(Philox& r, double v_th) {
 }
 
 
+// Conservative FP32 test of one segment (a, b) against the straight path f -> g, all in
+// cells: false means the two cannot intersect within the reference's tolerances
+// (LinearSegment.intersect accepts parameters within 1e-7 outside [0, 1]; this test's
+// margin is far wider than FP32 rounding of coordinates up to a few thousand cells).
+// Near-parallel or near-touching cases answer true.
+// Also classifies (seg_class_fp32): 0 cannot intersect; 1 intersects with both parameters
+// at least the same margin inside (0, 1), *tseg = the segment parameter; 2 undecided.
+__device__ __forceinline__ int seg_class_fp32(float ax, float ay, float bx, float by, float fx, float fy, float gx,
+                                              float gy, float* tseg) {
+  const float rx = gx - fx, ry = gy - fy;
+  const float rl = fabsf(rx) + fabsf(ry);
+  const float sx = bx - ax, sy = by - ay;
+  const float sl = fabsf(sx) + fabsf(sy);
+  const float den = rx * sy - ry * sx;
+  const float qx = ax - fx, qy = ay - fy;
+  const float tn = qx * sy - qy * sx;  // t_part * den
+  const float un = qx * ry - qy * rx;  // t_seg * den
+  const float lim = fabsf(den);
+  const float tol = 1e-3f * lim + 1e-4f * (rl + 1.f) * (sl + 1.f) * (1.f + fabsf(qx) + fabsf(qy));
+  if (lim <= tol) return 2;  // (near) parallel
+  const float sgn = den > 0.f ? 1.f : -1.f;
+  const float t1 = tn * sgn, t0 = un * sgn;
+  if (!(t1 >= -tol && t1 <= lim + tol && t0 >= -tol && t0 <= lim + tol)) return 0;
+  if (t1 >= tol && t1 <= lim - tol && t0 >= tol && t0 <= lim - tol) {
+    *tseg = t0 / lim;
+    return 1;
+  }
+  return 2;
+}
+
+__device__ __forceinline__ bool seg_may_cross_fp32(float ax, float ay, float bx, float by, float fx, float fy,
+                                                   float gx, float gy) {
+  float t;
+  return seg_class_fp32(ax, ay, bx, by, fx, fy, gx, gy, &t) != 0;
+}
+
 // Visits the DIRICHLET/SINK segments that KineticMaterial.ProcessBoundary collects for
 // the node box [i_min..i_max] x [j_min..j_max] (KineticMaterial.java:480-515); f(s)
 // returning true stops the walk.  With few segments all of them are visited directly:
@@ -466,7 +512,17 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
   if (j_max >= m.nj) j_max = m.nj - 1;
   double tp_min = 2.0, tsurf_min = 0;
   int seg_min = -1;
+  // the path in cells from the old position's cell: segments that the FP32 test clears
+  // cannot intersect it, and their FP64 intersection (which would give no hit) is skipped
+  const double bi = floor(lc_old[0]), bj = floor(lc_old[1]);
+  const int io = (int)bi, jo = (int)bj;
+  const float ofx = (float)(lc_old[0] - bi), ofy = (float)(lc_old[1] - bj);
+  const float ngx = (float)(lc[0] - bi), ngy = (float)(lc[1] - bj);
   for_each_candidate(m, i_min, i_max, j_min, j_max, [&](int s) {
+    const SegLC sl = m.seg_lc[s];
+    if (!seg_may_cross_fp32((float)(sl.i1 - io) + sl.f1, (float)(sl.j1 - jo) + sl.g1, (float)(sl.i2 - io) + sl.f2,
+                            (float)(sl.j2 - jo) + sl.g2, ofx, ofy, ngx, ngy))
+      return false;
     const Seg4 sxy = m.seg_xy[s];
     double t[2];
     seg_intersect(sxy, old, pos, t);
@@ -666,30 +722,47 @@ __device__ bool may_hit_fp32(const MeshView& m, int i, int j, float fx, float fy
   j_min = max(j_min, 0);
   i_max = min(i_max, m.ni - 1);
   j_max = min(j_max, m.nj - 1);
-  const float rx = gx - fx, ry = gy - fy;
-  const float rl = fabsf(rx) + fabsf(ry);
-  const double idx = 1.0 / m.dh[0], idy = 1.0 / m.dh[1];
   bool hit = false;
   for_each_candidate(m, i_min, i_max, j_min, j_max, [&](int sgi) {
-    const Seg4 sg = m.seg_xy[sgi];
-    // end points in cells relative to node (i, j)
-    const float ax = (float)((sg.x - m.x0[0]) * idx - i), ay = (float)((sg.y - m.x0[1]) * idy - j);
-    const float bx = (float)((sg.z - m.x0[0]) * idx - i), by = (float)((sg.w - m.x0[1]) * idy - j);
-    const float sx = bx - ax, sy = by - ay;
-    const float sl = fabsf(sx) + fabsf(sy);
-    const float den = rx * sy - ry * sx;
-    const float qx = ax - fx, qy = ay - fy;
-    const float tn = qx * sy - qy * sx;  // t_part * den
-    const float un = qx * ry - qy * rx;  // t_seg * den
-    const float lim = fabsf(den);
-    const float tol = 1e-3f * lim + 1e-4f * (rl + 1.f) * (sl + 1.f) * (1.f + fabsf(qx) + fabsf(qy));
-    if (lim <= tol) return hit = true;  // (near) parallel
-    const float sgn = den > 0.f ? 1.f : -1.f;
-    const float t1 = tn * sgn, t0 = un * sgn;
-    if (t1 >= -tol && t1 <= lim + tol && t0 >= -tol && t0 <= lim + tol) return hit = true;
-    return false;
+    const SegLC sl = m.seg_lc[sgi];  // end points in cells relative to node (i, j)
+    return hit = seg_may_cross_fp32((float)(sl.i1 - i) + sl.f1, (float)(sl.j1 - j) + sl.g1, (float)(sl.i2 - i) + sl.f2,
+                                    (float)(sl.j2 - j) + sl.g2, fx, fy, gx, gy);
   });
   return hit;
+}
+
+// The straight path (i + fx, j + fy) -> (i + gx, j + gy) meets exactly one candidate
+// segment, clearly inside both of their parameter ranges, and can meet no other: the
+// exact path's nearest hit (ProcessBoundary, KineticMaterial.java:480-515) is that
+// segment.  *seg, *tseg: the segment and the parameter along it.
+__device__ bool single_hit_fp32(const MeshView& m, int i, int j, float fx, float fy, float gx, float gy, int* seg,
+                                float* tseg) {
+  int i_min = i + (int)floorf(fminf(fx, gx)), i_max = i + (int)floorf(fmaxf(fx, gx));
+  int j_min = j + (int)floorf(fminf(fy, gy)), j_max = j + (int)floorf(fmaxf(fy, gy));
+  i_min = max(i_min, 0);
+  j_min = max(j_min, 0);
+  i_max = min(i_max, m.ni - 1);
+  j_max = min(j_max, m.nj - 1);
+  int found = -1, undecided = 0;
+  float tf = 0.f;
+  for_each_candidate(m, i_min, i_max, j_min, j_max, [&](int sgi) {
+    const SegLC sl = m.seg_lc[sgi];
+    float t;
+    const int c = seg_class_fp32((float)(sl.i1 - i) + sl.f1, (float)(sl.j1 - j) + sl.g1, (float)(sl.i2 - i) + sl.f2,
+                                 (float)(sl.j2 - j) + sl.g2, fx, fy, gx, gy, &t);
+    if (c == 0 || sgi == found) return false;
+    if (c == 2 || found >= 0) {
+      undecided = 1;
+      return true;
+    }
+    found = sgi;
+    tf = t;
+    return false;
+  });
+  if (undecided || found < 0) return false;
+  *seg = found;
+  *tseg = tf;
+  return true;
 }
 
 // The exact path over the slow-queue entries t_first, t_first + t_stride, ... below t_end
@@ -765,6 +838,27 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
           atomicAdd(&sa.counters[1], 1ULL);
           atomicAdd(&sa.counters[3], 1ULL);
           continue;
+        }
+      } else {
+        // a clear hit of one absorbing segment (the common case of ions striking an
+        // electrode): the exact path would take the same segment and remove the
+        // particle there; only the flux and deposit shares need the hit point
+        int hs;
+        float ht;
+        if (single_hit_fp32(m, i, j, f.x, f.y, gx, gy, &hs, &ht)) {
+          const int model = sa.sv.model[hs];
+          if (model != SF_SURF_PASS && model != SF_SURF_NONE && model != SF_SURF_SPECULAR &&
+              model != SF_SURF_DIFFUSE) {
+            atomicAdd(&sa.stats_slow[5], a.spwt * a.charge);
+            const double w1 = a.spwt * (1 - (double)ht), w2 = a.spwt * (double)ht;
+            atomicAdd(&sa.sv.flux[2 * hs], w1);
+            atomicAdd(&sa.sv.flux[2 * hs + 1], w2);
+            atomicAdd(&sa.sv.deposit[2 * hs], w1);
+            atomicAdd(&sa.sv.deposit[2 * hs + 1], w2);
+            P.cell[p] = DEAD;
+            atomicAdd(&sa.counters[1], 1ULL);
+            continue;
+          }
         }
       }
     }
@@ -1032,7 +1126,7 @@ __global__ void k_batch_zero(BatchDev b) {
 }
 
 template <int DOM>
-__global__ void __launch_bounds__(PB, 4) k_push_batch(BatchDev b) {
+__global__ void __launch_bounds__(PB, 2) k_push_batch(BatchDev b) {
   __shared__ unsigned acc_lo[SBOX];
   __shared__ unsigned acc_hi[SBOX];
   __shared__ int sred[4][PB / 32];
@@ -1044,7 +1138,7 @@ __global__ void __launch_bounds__(PB, 4) k_push_batch(BatchDev b) {
     const BatchInst& I = b.insts[i];
     ParticlesView P = I.P;
     P.n = b.n_dev[i];
-    push_tile<DOM, false, false>(I.m, P, I.a, (gt - b.tile_start[i]) * TILE, I.count, nullptr, I.slow_idx,
+    push_tile<DOM, false, false, true>(I.m, P, I.a, (gt - b.tile_start[i]) * TILE, I.count, nullptr, I.slow_idx,
                                  I.sa.counters, SampleView{nullptr, nullptr}, acc_lo, acc_hi, sred, st_px, st_py,
                                  st_pz, st_e, st_n);
   }

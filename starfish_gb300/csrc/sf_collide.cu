@@ -52,18 +52,18 @@ __device__ inline float sigma_eval(const SigmaDev& s, float g) {
 // ModelElastic post-collision relative velocity (DSMC.java:389-427), equal masses
 __device__ inline void elastic_vr(Philox& rng, float vss_inv, const float g[3], float g_mag, float vr[3]) {
   if (fabsf(vss_inv - 1.f) < 1e-4f) {
-    const float B = 2.f * (float)rng.uniform() - 1.f;
+    const float B = 2.f * rng.uniformf() - 1.f;
     const float A = sqrtf(fmaxf(1.f - B * B, 0.f));
     vr[0] = B * g_mag;
-    const float C = 2.f * (float)PI * (float)rng.uniform();
+    const float C = 2.f * (float)PI * rng.uniformf();
     float sC, cC;
     __sincosf(C, &sC, &cC);
     vr[1] = A * cC * g_mag;
     vr[2] = A * sC * g_mag;
   } else {
-    const float B = 2.f * __powf((float)rng.uniform(), vss_inv) - 1.f;
+    const float B = 2.f * __powf(rng.uniformf(), vss_inv) - 1.f;
     const float A = sqrtf(fmaxf(1.f - B * B, 0.f));
-    const float C = 2.f * (float)PI * (float)rng.uniform();
+    const float C = 2.f * (float)PI * rng.uniformf();
     float SC, OC;
     __sincosf(C, &SC, &OC);
     const float D = sqrtf(g[1] * g[1] + g[2] * g[2]);
@@ -93,7 +93,7 @@ __device__ inline bool collide_pair(ParticlesView& P, int64_t a, int64_t b, cons
   const float g_mag = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
   const float sigma_cr = g_mag * sigma_eval(sg, g_mag);
   smax_new = fmaxf(smax_new, sigma_cr);
-  if (!((float)rng.uniform() < sigma_cr / smax)) return false;
+  if (!(rng.uniformf() < sigma_cr / smax)) return false;
   const float vc[3] = {0.5f * (va.x + vb.x), 0.5f * (va.y + vb.y), 0.5f * (wa + wb)};
   float vr[3];
   elastic_vr(rng, sg.vss_inv, g, g_mag, vr);
@@ -408,7 +408,7 @@ __global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, i
     const float g = sqrtf(gx * gx + gy * gy + gz * gz);
     const float Pc = 1.f - __expf(-sigma_eval(sg, g) * g * dt * den);
     Philox rng(seed, RNG_MCC, (uint64_t)p, step);
-    if (Pc < (float)rng.uniform()) continue;
+    if (Pc < rng.uniformf()) continue;
     // Material.sampleMaxwellianVelocity (Material.java:880-896): mean + SampleMaxw3D(v_th)
     float T = gather_node(tg.T, m.ni, i, j, f.x, f.y);
     if (T < 0.f) T = 0.f;
@@ -416,7 +416,7 @@ __global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, i
     float vt[3] = {tu, tv, tw};
     for (int d = 0; d < 3; d++) {
       float s = 0.f;
-      for (int k = 0; k < 12; k++) s += (float)rng.uniform();
+      for (int k = 0; k < 12; k++) s += rng.uniformf();
       vt[d] += (vth * 1.2f) * 0.70710678f * (s - 6.f);
     }
     // pre-collision "energy" 0.5 m |v| (Vec.mag3, as in MCC.java:204)
@@ -444,11 +444,7 @@ __global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, i
           const double v_th = sqrt(2 * KB * Tt / ex.prod_mass);
           for (int k = 0; k < mp_gen; k++) {
             double v3[3];
-            for (int d = 0; d < 3; d++) {
-              double s = 0.0;
-              for (int q = 0; q < 12; q++) s += rng.uniform();
-              v3[d] = (v_th * 1.2) * 0.7071067811865476 * (s - 6.0);  // Utils.SampleMaxw3D
-            }
+            for (int d = 0; d < 3; d++) v3[d] = (v_th * 1.2) * rng.maxw1d_unit();  // Utils.SampleMaxw3D
             if (!mcc_append(m, ex.Pi, ex.cap_i, &cnt[2], c, f, v3, ex.qm_halfdt_prod)) atomicAdd(&cnt[3], 1ULL);
           }
           if (ex.dn) {
@@ -466,9 +462,9 @@ __global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, i
       const float gg[3] = {vxy.x - vt[0], vxy.y - vt[1], vz - vt[2]};
       const float g_mag = sqrtf(gg[0] * gg[0] + gg[1] * gg[1] + gg[2] * gg[2]);
       const float vc[3] = {rm1 * vxy.x + rm2 * vt[0], rm1 * vxy.y + rm2 * vt[1], rm1 * vz + rm2 * vt[2]};
-      const float B = 2.f * (float)rng.uniform() - 1.f;
+      const float B = 2.f * rng.uniformf() - 1.f;
       const float A = sqrtf(fmaxf(1.f - B * B, 0.f));
-      const float C = 2.f * (float)PI * (float)rng.uniform();
+      const float C = 2.f * (float)PI * rng.uniformf();
       float sC, cC;
       __sincosf(C, &sC, &cC);
       const float vr[3] = {B * g_mag, A * cC * g_mag, A * sC * g_mag};

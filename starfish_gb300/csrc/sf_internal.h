@@ -172,10 +172,19 @@ struct Philox {
     left--;
     return v;
   }
-  // uniform in [0,1) with 53 random bits
-  __device__ inline double uniform() {
-    uint32_t a = next_u32() >> 5, b = next_u32() >> 6;
-    return ((double)a * 67108864.0 + (double)b) * (1.0 / 9007199254740992.0);
+  // uniform in [0,1) with 53 random bits (the 53-bit integer is formed in integer
+  // arithmetic: one conversion on the FP64 pipe)
+  __device__ inline uint64_t bits53() {
+    const uint32_t a = next_u32() >> 5, b = next_u32() >> 6;
+    return ((uint64_t)a << 26) | b;
+  }
+  __device__ inline double uniform() { return (double)bits53() * (1.0 / 9007199254740992.0); }
+  // Utils.SampleMaxw1D(1) of the reference: sqrt(1/2) (sum of 12 uniforms - 6); the 12
+  // 53-bit uniforms are summed exactly as integers and converted once
+  __device__ inline double maxw1d_unit() {
+    uint64_t s = 0;
+    for (int k = 0; k < 12; k++) s += bits53();
+    return 0.7071067811865476 * ((double)s * (1.0 / 9007199254740992.0) - 6.0);
   }
   // uniform in [0,1) with 24 random bits
   __device__ inline float uniformf() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }

@@ -40,12 +40,7 @@ __device__ inline double frustum_t(double f, double r1, double r2) {
   return f * S / (r1 + sqrt(r1 * r1 + (r2 - r1) * f * S));
 }
 
-__device__ inline double maxw1d_unit(Philox& r) {
-  // Utils.SampleMaxw1D(1): sqrt(1/2) * (sum of 12 uniforms - 6)
-  double s = 0.0;
-  for (int k = 0; k < 12; k++) s += r.uniform();
-  return 0.7071067811865476 * (s - 6.0);
-}
+__device__ inline double maxw1d_unit(Philox& r) { return r.maxw1d_unit(); }
 
 // Particle k of this step's injection on the segment of a; appended at a.base + slot.
 __device__ __forceinline__ void inject_one(const MeshView& m, const ParticlesView& P, const InjectArgs& a, int64_t k,

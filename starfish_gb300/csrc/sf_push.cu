@@ -431,9 +431,10 @@ __device__ double sample_maxw_speed(Philox& r, double v_th) {
 // margin is far wider than FP32 rounding of coordinates up to a few thousand cells).
 // Near-parallel or near-touching cases answer true.
 // Also classifies (seg_class_fp32): 0 cannot intersect; 1 intersects with both parameters
-// at least the same margin inside (0, 1), *tseg = the segment parameter; 2 undecided.
+// at least the same margin inside (0, 1): *tseg, *tpart = the segment and path parameters,
+// each within *marg of the exact values; 2 undecided.
 __device__ __forceinline__ int seg_class_fp32(float ax, float ay, float bx, float by, float fx, float fy, float gx,
-                                              float gy, float* tseg) {
+                                              float gy, float* tseg, float* tpart = nullptr, float* marg = nullptr) {
   const float rx = gx - fx, ry = gy - fy;
   const float rl = fabsf(rx) + fabsf(ry);
   const float sx = bx - ax, sy = by - ay;
@@ -450,6 +451,8 @@ __device__ __forceinline__ int seg_class_fp32(float ax, float ay, float bx, floa
   if (!(t1 >= -tol && t1 <= lim + tol && t0 >= -tol && t0 <= lim + tol)) return 0;
   if (t1 >= tol && t1 <= lim - tol && t0 >= tol && t0 <= lim - tol) {
     *tseg = t0 / lim;
+    if (tpart) *tpart = t1 / lim;
+    if (marg) *marg = tol / lim;
     return 1;
   }
   return 2;
@@ -731,12 +734,13 @@ __device__ bool may_hit_fp32(const MeshView& m, int i, int j, float fx, float fy
   return hit;
 }
 
-// The straight path (i + fx, j + fy) -> (i + gx, j + gy) meets exactly one candidate
-// segment, clearly inside both of their parameter ranges, and can meet no other: the
-// exact path's nearest hit (ProcessBoundary, KineticMaterial.java:480-515) is that
-// segment.  *seg, *tseg: the segment and the parameter along it.
-__device__ bool single_hit_fp32(const MeshView& m, int i, int j, float fx, float fy, float gx, float gy, int* seg,
-                                float* tseg) {
+// Every candidate segment either cannot meet the straight path (i + fx, j + fy) ->
+// (i + gx, j + gy) or meets it clearly inside both parameter ranges, and the nearest of
+// those crossings is clearly nearer than the next: the exact path's hit (ProcessBoundary,
+// KineticMaterial.java:480-515, the smallest path parameter) is that segment.  *seg,
+// *tseg: the segment and the parameter along it.
+__device__ bool first_hit_fp32(const MeshView& m, int i, int j, float fx, float fy, float gx, float gy, int* seg,
+                               float* tseg) {
   int i_min = i + (int)floorf(fminf(fx, gx)), i_max = i + (int)floorf(fmaxf(fx, gx));
   int j_min = j + (int)floorf(fminf(fy, gy)), j_max = j + (int)floorf(fmaxf(fy, gy));
   i_min = max(i_min, 0);
@@ -744,22 +748,32 @@ __device__ bool single_hit_fp32(const MeshView& m, int i, int j, float fx, float
   i_max = min(i_max, m.ni - 1);
   j_max = min(j_max, m.nj - 1);
   int found = -1, undecided = 0;
-  float tf = 0.f;
+  float tf = 0.f, tb = 2.f, mb = 0.f, t2 = 2.f, m2 = 0.f;  // nearest crossing and the next
   for_each_candidate(m, i_min, i_max, j_min, j_max, [&](int sgi) {
     const SegLC sl = m.seg_lc[sgi];
-    float t;
+    float ts, tp, mg;
     const int c = seg_class_fp32((float)(sl.i1 - i) + sl.f1, (float)(sl.j1 - j) + sl.g1, (float)(sl.i2 - i) + sl.f2,
-                                 (float)(sl.j2 - j) + sl.g2, fx, fy, gx, gy, &t);
-    if (c == 0 || sgi == found) return false;
-    if (c == 2 || found >= 0) {
+                                 (float)(sl.j2 - j) + sl.g2, fx, fy, gx, gy, &ts, &tp, &mg);
+    if (c == 0) return false;
+    if (c == 2) {
       undecided = 1;
       return true;
     }
-    found = sgi;
-    tf = t;
+    if (tp < tb) {
+      t2 = tb;
+      m2 = mb;
+      found = sgi;
+      tb = tp;
+      mb = mg;
+      tf = ts;
+    } else if (tp < t2) {
+      t2 = tp;
+      m2 = mg;
+    }
     return false;
   });
   if (undecided || found < 0) return false;
+  if (t2 < 2.f && !(t2 - tb > 2.f * (mb + m2))) return false;  // the two nearest are not clearly ordered
   *seg = found;
   *tseg = tf;
   return true;
@@ -840,12 +854,12 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
           continue;
         }
       } else {
-        // a clear hit of one absorbing segment (the common case of ions striking an
+        // a clear first hit of an absorbing segment (the common case of ions striking an
         // electrode): the exact path would take the same segment and remove the
         // particle there; only the flux and deposit shares need the hit point
         int hs;
         float ht;
-        if (single_hit_fp32(m, i, j, f.x, f.y, gx, gy, &hs, &ht)) {
+        if (first_hit_fp32(m, i, j, f.x, f.y, gx, gy, &hs, &ht)) {
           const int model = sa.sv.model[hs];
           if (model != SF_SURF_PASS && model != SF_SURF_NONE && model != SF_SURF_SPECULAR &&
               model != SF_SURF_DIFFUSE) {

@@ -305,7 +305,7 @@ def batch_bench(n_instances=256, steps=16, warmup=10, threads=16, dt=5e-7, unbat
         t_setup = time.perf_counter() - t_setup
         for _ in range(warmup):
             batch.step(dt, solvers[0])
-        psteps, dev_ms, solve_sum, solve_max, newton = 0, 0.0, 0.0, 0.0, 0.0
+        psteps, dev_ms, solve_sum, solve_max, newton, newton_max = 0, 0.0, 0.0, 0.0, 0.0, 0
         live = sum(km.get_np() for km in kms)
         t0 = time.perf_counter()
         for _ in range(steps):
@@ -316,6 +316,7 @@ def batch_bench(n_instances=256, steps=16, warmup=10, threads=16, dt=5e-7, unbat
             solve_sum += st["solve_ms_sum"]
             solve_max = max(solve_max, st["solve_ms_max"])
             newton += st["newton_it_mean"]
+            newton_max = max(newton_max, st["newton_it_max"])
         wall = time.perf_counter() - t0
         tuning = batch.tuning()
         batch.close()
@@ -347,7 +348,7 @@ def batch_bench(n_instances=256, steps=16, warmup=10, threads=16, dt=5e-7, unbat
                 "steps": steps, "warmup": warmup, "instances": n_instances,
                 "particles_live_end": live, "mesh_nodes": [min(sizes), max(sizes)],
                 "device_phase_ms": dev_ms / steps, "solve_ms_sum_per_step": solve_sum / steps,
-                "solve_ms_max": solve_max, "newton_it_mean": newton / steps,
+                "solve_ms_max": solve_max, "newton_it_mean": newton / steps, "newton_it_max": newton_max,
                 "host_threads": threads, "tuning": tuning, "setup_s": t_setup,
                 "timing": "wall clock of sf_batch_step (host threads and graph launches included)",
                 "unbatched": None if unbatched_steps <= 0 else {
@@ -439,6 +440,7 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=16)
     ap.add_argument("--batch-threads", type=int, default=16)
     ap.add_argument("--batch-instances", type=int, default=256)
+    ap.add_argument("--batch-warmup", type=int, default=10)
     ap.add_argument("--batch-unbatched-steps", type=int, default=3)
     ap.add_argument("--only-batch", action="store_true",
                     help="run only the batched-instances leg and print its result line")
@@ -450,7 +452,8 @@ def main():
         from starfish_gb300 import build as B
         B.build()
         print(json.dumps(batch_bench(n_instances=args.batch_instances, steps=args.batch_steps,
-                                     threads=args.batch_threads, unbatched_steps=args.batch_unbatched_steps)))
+                                     warmup=args.batch_warmup, threads=args.batch_threads,
+                                     unbatched_steps=args.batch_unbatched_steps)))
         return
 
     import torch

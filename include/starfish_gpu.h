@@ -344,6 +344,7 @@ typedef struct {
   double solve_ms_sum;       /* device time of the instances' Poisson solves, summed       */
   double solve_ms_max;       /* ... and the longest one                                    */
   double newton_it_mean;     /* Newton steps per solve                                     */
+  int32_t newton_it_max;     /* most Newton steps of any instance in this step             */
   int32_t capacity_overflow; /* a source hit an instance's capacity (step returns SF_ERR_OOM) */
 } sf_batch_stats;
 int sf_batch_create(sf_ctx** ctxs, const int32_t* sids, int32_t n, int32_t threads, sf_batch** out);

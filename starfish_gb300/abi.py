@@ -206,7 +206,8 @@ EXPORTS.update({
 
 class BatchStats(C.Structure):
     _fields_ = [("particles", C.c_int64), ("device_phase_ms", C.c_double), ("solve_ms_sum", C.c_double),
-                ("solve_ms_max", C.c_double), ("newton_it_mean", C.c_double), ("capacity_overflow", C.c_int32)]
+                ("solve_ms_max", C.c_double), ("newton_it_mean", C.c_double), ("newton_it_max", C.c_int32),
+                ("capacity_overflow", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -539,9 +539,11 @@ int sf_batch_step(sf_batch* b, double dt, const sf_poisson_params* prm, sf_batch
       st->solve_ms_sum = field_sum;
       st->solve_ms_max = field_max;
       st->newton_it_mean = 0;
+      st->newton_it_max = 0;
       for (int i = 0; i < b->n; i++) {
         st->particles += nn[i] - dd[i];
         st->newton_it_mean += newton[i];
+        st->newton_it_max = std::max(st->newton_it_max, newton[i]);
       }
       st->newton_it_mean /= b->n;
       st->device_phase_ms = dev_ms;

@@ -1095,7 +1095,9 @@ int sf_boltzmann(sf_ctx* ctx, double* ne) {
 // bodies of the single-context kernels on each instance's own buffers, with the same
 // reduction partition, so every instance gets the potential its own sf_poisson_nl would
 // give, bit for bit.  Convergence is decided per instance on the device; the host reads
-// one count per Newton round for the whole batch.
+// one count per Newton round for the whole batch.  After every check the instances still
+// iterating are listed with the prefixes of their blocks, and the stage kernels loop over
+// those blocks only, so that the late rounds of a few slow instances cost little.
 // ------------------------------------------------------------------------------------
 namespace {
 
@@ -1120,7 +1122,7 @@ struct BPInst {
   // state of the current step
   int iters;     // PCG iterations per Newton step
   int fp64_exp;  // sticky, as SfPoisson::fp64_exp
-  int live;      // the residual is evaluated in this round
+  int live;      // still iterating (after a check: a Newton step is taken in this round)
   int run;       // a Newton step is taken in this round
   int redo;      // the residual is evaluated again with the FP64 exponential
   int it, vcount, status;  // status: 0 running, 1 converged, 2 not converged, 3 diverged
@@ -1137,6 +1139,15 @@ struct BPStat {
   double res, res_inf, res0;
 };
 
+// The blocks of one launch kind over the live instances: list[0..*cnt) their ids,
+// start[k] the first block of list[k], *total all blocks of the kind.
+struct BPWork {
+  const int* list;
+  const int* cnt;
+  const int* start;
+  const int* total;
+};
+
 enum { BP_LIVE = 0, BP_REDO = 1, BP_RUN = 2 };
 
 __device__ __forceinline__ bool bp_part(const BPInst& I, int mode, int kmin) {
@@ -1145,7 +1156,7 @@ __device__ __forceinline__ bool bp_part(const BPInst& I, int mode, int kmin) {
   return I.run != 0 && I.iters > kmin;
 }
 
-// instance owning block b of a launch: start[i] <= b < start[i + 1]
+// entry owning block b: start[k] <= b < start[k + 1]
 __device__ __forceinline__ int bp_find(const int* __restrict__ start, int n, int b) {
   int lo = 0, hi = n;
   while (hi - lo > 1) {
@@ -1156,8 +1167,67 @@ __device__ __forceinline__ int bp_find(const int* __restrict__ start, int n, int
   return lo;
 }
 
-// iters[0..n): PCG iterations per Newton step, iters[n..2n): the sticky FP64 choice
+// Exclusive prefix of val(0..n-1) into out[0..n] (out[n] = total) by one block whose size
+// is a multiple of 32; val(i) is called once per i
+template <typename F>
+__device__ void bp_prefix(int n, F val, int* __restrict__ out) {
+  __shared__ int wsum[32];
+  __shared__ int carry;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const int v = i < n ? val(i) : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = lane < nwarps ? wsum[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    const int before = carry + (warp > 0 ? wsum[warp - 1] : 0) + x - v;
+    if (i < n) out[i] = before;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = before + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+  __syncthreads();
+}
+
+// The live instances (act_list, *act_cnt) and, for every kind k, the prefix of their
+// blocks (act_start + k (n + 1)) and its total (act_total[k]).  tab + koff[k] is the
+// static block prefix of kind k over all instances.  One block.
+__global__ void __launch_bounds__(1024) kb_compact(const BPInst* I, int n, const int* __restrict__ tab,
+                                                   const int* __restrict__ koff, int nkinds, int* act_pos,
+                                                   int* act_list, int* act_cnt, int* act_start,
+                                                   int* act_total) {
+  bp_prefix(n, [&](int i) { return I[i].live ? 1 : 0; }, act_pos);
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    if (I[i].live) act_list[act_pos[i]] = i;
+  const int cnt = act_pos[n];
+  if (threadIdx.x == 0) *act_cnt = cnt;
+  __syncthreads();
+  for (int k = 0; k < nkinds; k++) {
+    const int* t = tab + koff[k];
+    int* st = act_start + k * (n + 1);
+    bp_prefix(cnt, [&](int q) { const int i = act_list[q]; return t[i + 1] - t[i]; }, st);
+    if (threadIdx.x == 0) act_total[k] = st[cnt];
+  }
+}
+
 __global__ void kb_init(BPInst* I, int n, const int* __restrict__ iters) {
+  // iters[0..n): PCG iterations per Newton step, iters[n..2n): the sticky FP64 choice
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   BPInst& s = I[i];
@@ -1173,7 +1243,7 @@ __global__ void kb_init(BPInst* I, int n, const int* __restrict__ iters) {
   s.res0 = -1.0;
 }
 
-// rho = sum q nd (sf_update_rho), b0 (k_build_b0), fixed rows of phi (k_fix_phi)
+// rho = sum q nd (sf_update_rho), b0 (k_build_b0), fixed rows of phi (k_fix_phi); all instances
 __global__ void kb_rho_b0(BPInst* I, int n, const int* __restrict__ start, const BPParams* __restrict__ pr) {
   const int i = bp_find(start, n, blockIdx.x);
   const BPInst& s = I[i];
@@ -1187,18 +1257,28 @@ __global__ void kb_rho_b0(BPInst* I, int n, const int* __restrict__ start, const
   if (t == NC_FIXED) s.phi[u] = s.bc[u];
 }
 
-__global__ void __launch_bounds__(RB) kb_nl_residual(BPInst* I, int n, const int* __restrict__ start,
-                                                     const BPParams* __restrict__ pr, int mode) {
+__global__ void kb_efield(BPInst* I, int n, const int* __restrict__ start) {
   const int i = bp_find(start, n, blockIdx.x);
   const BPInst& s = I[i];
-  if (!bp_part(s, mode, 0)) return;
-  NlArgs a = s.nl;
-  a.C_n0 = pr->C_n0;
-  a.inv_kTe = pr->inv_kTe;
-  a.phi0 = pr->phi0;
-  a.linear = pr->linear;
-  a.fp64_exp = s.fp64_exp;
-  nl_residual_body(a, s.phi, s.b0, s.type0, s.lv[0].r, s.lv[0].P, s.partial, blockIdx.x - start[i], s.red_blocks);
+  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
+  if (u < s.nn) efield_node(u, s.ni, s.nj, s.inv_dx, s.inv_dy, s.phi, s.efi, s.efj, s.E);
+}
+
+__global__ void __launch_bounds__(RB) kb_nl_residual(BPInst* I, BPWork w, const BPParams* __restrict__ pr, int mode) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, mode, 0)) continue;
+    NlArgs a = s.nl;
+    a.C_n0 = pr->C_n0;
+    a.inv_kTe = pr->inv_kTe;
+    a.phi0 = pr->phi0;
+    a.linear = pr->linear;
+    a.fp64_exp = s.fp64_exp;
+    nl_residual_body(a, s.phi, s.b0, s.type0, s.lv[0].r, s.lv[0].P, s.partial, b - w.start[k], s.red_blocks);
+    __syncthreads();  // the block sums' shared memory is used again
+  }
 }
 
 __global__ void kb_reduce3(BPInst* I, int mode) {
@@ -1220,7 +1300,7 @@ __global__ void kb_check_exp(BPInst* I, int n, const BPParams* __restrict__ pr) 
 }
 
 // one check of the Newton loop of sf_poisson_nl per live instance; run_count counts the
-// instances that take a step in this round
+// instances that take a step in this round (they stay live, the others leave)
 __global__ void kb_newton_control(BPInst* I, int n, const BPParams* __restrict__ pr, int* run_count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -1247,105 +1327,140 @@ __global__ void kb_newton_control(BPInst* I, int n, const BPParams* __restrict__
   s.live = 0;
 }
 
-// level kernels over the instances whose grid levels include l (l < cs)
-__global__ void kb_restrict_P(BPInst* I, int n, const int* __restrict__ start, int l, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  const LevelView& F = s.lv[l];
-  const LevelView& Cl = s.lv[l + 1];
-  const int uc = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  if (uc >= Cl.ni * Cl.nj) return;
-  const int J = uc / Cl.ni, Ii = uc - J * Cl.ni;
-  Cl.P[uc] = F.P[(2 * J) * F.ni + 2 * Ii];
+// level kernels: grid level l of the live instances with l < cs
+__global__ void kb_restrict_P(BPInst* I, BPWork w, int l, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    const LevelView& F = s.lv[l];
+    const LevelView& Cl = s.lv[l + 1];
+    const int uc = (b - w.start[k]) * ET + threadIdx.x;
+    if (uc >= Cl.ni * Cl.nj) continue;
+    const int J = uc / Cl.ni, Ii = uc - J * Cl.ni;
+    Cl.P[uc] = F.P[(2 * J) * F.ni + 2 * Ii];
+  }
 }
 
-__global__ void kb_zero_y(BPInst* I, int n, const int* __restrict__ start, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  if (u < s.nn) s.lv[0].y[u] = 0.f;
+__global__ void kb_zero_y(BPInst* I, BPWork w, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    const int u = (b - w.start[k]) * ET + threadIdx.x;
+    if (u < s.nn) s.lv[0].y[u] = 0.f;
+  }
 }
 
-__global__ void kb_smooth(BPInst* I, int n, const int* __restrict__ start, int l, int color, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  const LevelView& L = s.lv[l];
-  const int hw = (L.ni + 1) / 2;
-  const int v = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  const int j = v / hw;
-  if (j >= L.nj) return;
-  const int ii = 2 * (v - j * hw) + ((j + color) & 1);
-  if (ii >= L.ni) return;
-  const int u = j * L.ni + ii;
-  L.y[u] = gs_value(L.type[u], L.y, L.r[u], L.P[u], u, L.ni, L.cx, L.cy);
+__global__ void kb_smooth(BPInst* I, BPWork w, int l, int color, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    const LevelView& L = s.lv[l];
+    const int hw = (L.ni + 1) / 2;
+    const int v = (b - w.start[k]) * ET + threadIdx.x;
+    const int j = v / hw;
+    if (j >= L.nj) continue;
+    const int ii = 2 * (v - j * hw) + ((j + color) & 1);
+    if (ii >= L.ni) continue;
+    const int u = j * L.ni + ii;
+    L.y[u] = gs_value(L.type[u], L.y, L.r[u], L.P[u], u, L.ni, L.cx, L.cy);
+  }
 }
 
-__global__ void kb_resid(BPInst* I, int n, const int* __restrict__ start, int l, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  const LevelView& L = s.lv[l];
-  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  if (u >= L.ni * L.nj) return;
-  L.t[u] = L.r[u] - apply_J(L.type[u], L.y, L.P[u], u, L.ni, L.cx, L.cy);
+__global__ void kb_resid(BPInst* I, BPWork w, int l, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    const LevelView& L = s.lv[l];
+    const int u = (b - w.start[k]) * ET + threadIdx.x;
+    if (u >= L.ni * L.nj) continue;
+    L.t[u] = L.r[u] - apply_J(L.type[u], L.y, L.P[u], u, L.ni, L.cx, L.cy);
+  }
 }
 
-__global__ void kb_restrict(BPInst* I, int n, const int* __restrict__ start, int l, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  const LevelView& F = s.lv[l];
-  const LevelView& Cl = s.lv[l + 1];
-  const int uc = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  if (uc >= Cl.ni * Cl.nj) return;
-  const int J = uc / Cl.ni, Ii = uc - J * Cl.ni;
-  Cl.r[uc] = restrict_value(F.t, Cl.type[uc], Ii, J, F.ni, Cl.ni, Cl.nj);
-  Cl.y[uc] = 0.f;
+__global__ void kb_restrict(BPInst* I, BPWork w, int l, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    const LevelView& F = s.lv[l];
+    const LevelView& Cl = s.lv[l + 1];
+    const int uc = (b - w.start[k]) * ET + threadIdx.x;
+    if (uc >= Cl.ni * Cl.nj) continue;
+    const int J = uc / Cl.ni, Ii = uc - J * Cl.ni;
+    Cl.r[uc] = restrict_value(F.t, Cl.type[uc], Ii, J, F.ni, Cl.ni, Cl.nj);
+    Cl.y[uc] = 0.f;
+  }
 }
 
-__global__ void kb_prolong(BPInst* I, int n, const int* __restrict__ start, int l, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  const LevelView& F = s.lv[l];
-  const LevelView& Cl = s.lv[l + 1];
-  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  if (u >= F.ni * F.nj) return;
-  if (F.type[u] == NC_FIXED) return;
-  const int j = u / F.ni, ii = u - j * F.ni;
-  F.y[u] += prolong_value(Cl.y, ii, j, Cl.ni);
+__global__ void kb_prolong(BPInst* I, BPWork w, int l, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    const LevelView& F = s.lv[l];
+    const LevelView& Cl = s.lv[l + 1];
+    const int u = (b - w.start[k]) * ET + threadIdx.x;
+    if (u >= F.ni * F.nj) continue;
+    if (F.type[u] == NC_FIXED) continue;
+    const int j = u / F.ni, ii = u - j * F.ni;
+    F.y[u] += prolong_value(Cl.y, ii, j, Cl.ni);
+  }
 }
 
-__global__ void __launch_bounds__(1024) kb_coarse_vcycle(BPInst* I, int nu1, int nu2, int kmin) {
-  const BPInst& s = I[blockIdx.x];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  coarse_vcycle_body(s.cd, s.lv[s.cs], nu1, nu2);
+// one CTA per live instance at a time (the single-CTA end of the V-cycle)
+__global__ void __launch_bounds__(1024) kb_coarse_vcycle(BPInst* I, const int* __restrict__ list,
+                                                         const int* __restrict__ cnt, int nu1, int nu2, int kmin) {
+  const int c = *cnt;
+  for (int k = blockIdx.x; k < c; k += gridDim.x) {
+    const BPInst& s = I[list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    coarse_vcycle_body(s.cd, s.lv[s.cs], nu1, nu2);
+    __syncthreads();  // the shared arrays are used again
+  }
 }
 
 // fine-level PCG stages
-__global__ void kb_zero_cg(BPInst* I, int n, const int* __restrict__ start, int which, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  if (u < s.nn) (which == 0 ? s.cg_x : s.cg_zo)[u] = 0.f;
+__global__ void kb_zero_cg(BPInst* I, BPWork w, int which, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    const int u = (b - w.start[k]) * ET + threadIdx.x;
+    if (u < s.nn) (which == 0 ? s.cg_x : s.cg_zo)[u] = 0.f;
+  }
 }
 
-__global__ void __launch_bounds__(RB) kb_cg_dots(BPInst* I, int n, const int* __restrict__ start, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  cg_dots_body(s.nn, s.lv[0].r, s.lv[0].y, s.cg_zo, s.partial, blockIdx.x - start[i], s.red_blocks);
+__global__ void __launch_bounds__(RB) kb_cg_dots(BPInst* I, BPWork w, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    cg_dots_body(s.nn, s.lv[0].r, s.lv[0].y, s.cg_zo, s.partial, b - w.start[k], s.red_blocks);
+    __syncthreads();
+  }
 }
 
-__global__ void __launch_bounds__(RB) kb_cg_matvec(BPInst* I, int n, const int* __restrict__ start, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  cg_matvec_body(s.lv[0], s.cg_p, s.cg_q, s.partial, blockIdx.x - start[i], s.red_blocks);
+__global__ void __launch_bounds__(RB) kb_cg_matvec(BPInst* I, BPWork w, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    cg_matvec_body(s.lv[0], s.cg_p, s.cg_q, s.partial, b - w.start[k], s.red_blocks);
+    __syncthreads();
+  }
 }
 
 __global__ void kb_reduce2(BPInst* I, int kmin) {
@@ -1362,35 +1477,37 @@ __global__ void kb_cg_scalars(BPInst* I, int n, int stage, int kmin) {
   cg_scalars_body(s.sc, stage);
 }
 
-__global__ void kb_cg_axpy(BPInst* I, int n, const int* __restrict__ start, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  if (u < s.nn) cg_axpy_node(u, (float)s.sc[SC_ALPHA], s.cg_p, s.cg_q, s.cg_x, s.lv[0].r, s.lv[0].y, s.cg_zo);
+__global__ void kb_cg_axpy(BPInst* I, BPWork w, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    const int u = (b - w.start[k]) * ET + threadIdx.x;
+    if (u < s.nn) cg_axpy_node(u, (float)s.sc[SC_ALPHA], s.cg_p, s.cg_q, s.cg_x, s.lv[0].r, s.lv[0].y, s.cg_zo);
+  }
 }
 
-__global__ void kb_cg_pupdate(BPInst* I, int n, const int* __restrict__ start, int first, int kmin) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, kmin)) return;
-  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  if (u < s.nn) cg_pupdate_node(u, first, first ? 0.f : (float)s.sc[SC_BETA], s.lv[0].y, s.cg_p);
+__global__ void kb_cg_pupdate(BPInst* I, BPWork w, int first, int kmin) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, kmin)) continue;
+    const int u = (b - w.start[k]) * ET + threadIdx.x;
+    if (u < s.nn) cg_pupdate_node(u, first, first ? 0.f : (float)s.sc[SC_BETA], s.lv[0].y, s.cg_p);
+  }
 }
 
-__global__ void kb_update_phi(BPInst* I, int n, const int* __restrict__ start, const BPParams* __restrict__ pr) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  if (!bp_part(s, BP_RUN, 0)) return;
-  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  if (u < s.nn) update_phi_node(u, s.phi, s.cg_x, pr->max_step);
-}
-
-__global__ void kb_efield(BPInst* I, int n, const int* __restrict__ start) {
-  const int i = bp_find(start, n, blockIdx.x);
-  const BPInst& s = I[i];
-  const int u = (blockIdx.x - start[i]) * ET + threadIdx.x;
-  if (u < s.nn) efield_node(u, s.ni, s.nj, s.inv_dx, s.inv_dy, s.phi, s.efi, s.efj, s.E);
+__global__ void kb_update_phi(BPInst* I, BPWork w, const BPParams* __restrict__ pr) {
+  const int tot = *w.total, cnt = *w.cnt;
+  for (int b = blockIdx.x; b < tot; b += gridDim.x) {
+    const int k = bp_find(w.start, cnt, b);
+    const BPInst& s = I[w.list[k]];
+    if (!bp_part(s, BP_RUN, 0)) continue;
+    const int u = (b - w.start[k]) * ET + threadIdx.x;
+    if (u < s.nn) update_phi_node(u, s.phi, s.cg_x, pr->max_step);
+  }
 }
 
 __global__ void kb_collect(const BPInst* I, int n, BPStat* out) {
@@ -1409,20 +1526,112 @@ struct BatchPoisson {
   std::vector<sf_ctx*> ctx;
   std::vector<int> nspecies;  // charged species per context when the table was built
   BPInst* d_inst = nullptr;
-  int* d_tab = nullptr;        // block prefixes of every launch kind, n + 1 each
+  int* d_tab = nullptr;   // static block prefixes of every kind, n + 1 each
+  int* d_koff = nullptr;  // offset of each kind's prefix in d_tab
   int* d_iters = nullptr;
   int* d_run = nullptr;
   BPParams* d_prm = nullptr;
   BPStat* d_stat = nullptr;
-  // table offsets into d_tab and total blocks
-  int fine_off = 0, fine_tot = 0, red_off = 0, red_tot = 0, zero_off = 0, zero_tot = 0;
-  std::vector<int> lvl_off, lvl_tot, lvlc_off, lvlc_tot, half_off, half_tot;  // per grid level
+  // the live list and its per-kind prefixes
+  int *d_act_pos = nullptr, *d_act_list = nullptr, *d_act_cnt = nullptr, *d_act_start = nullptr,
+      *d_act_total = nullptr;
+  // kinds: 0 fine level, 1 reduction blocks, 2 level-0 zero fill (cs > 0), then per grid
+  // level l: 3 + 3 l the level, 4 + 3 l the next coarser level, 5 + 3 l one colour
+  int nkinds = 0;
+  std::vector<int> koff, ktot;  // static offset in d_tab and total blocks per kind
   int max_cs = 0;
   size_t coarse_smem = 0;
   cudaStream_t stream = nullptr;
   std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // Newton round by max PCG iterations
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
+
+enum { BK_FINE = 0, BK_RED = 1, BK_ZERO = 2 };
+static inline int bk_lvl(int l) { return 3 + 3 * l; }
+static inline int bk_lvlc(int l) { return 4 + 3 * l; }
+static inline int bk_half(int l) { return 5 + 3 * l; }
+
+static BPWork bp_work(const BatchPoisson* bp, int kind) {
+  return BPWork{bp->d_act_list, bp->d_act_cnt, bp->d_act_start + kind * (bp->n + 1), bp->d_act_total + kind};
+}
+
+// grid of a stage kernel: the kind's blocks over all instances, at most 8 per SM (the
+// kernels loop over the live blocks)
+static int bp_grid(const BatchPoisson* bp, int kind) {
+  return std::max(1, std::min(bp->ktot[kind], bp->num_sms * 8));
+}
+
+static void bp_compact(BatchPoisson* bp, cudaStream_t s) {
+  kb_compact<<<1, 1024, 0, s>>>(bp->d_inst, bp->n, bp->d_tab, bp->d_koff, bp->nkinds, bp->d_act_pos,
+                                bp->d_act_list, bp->d_act_cnt, bp->d_act_start, bp->d_act_total);
+}
+
+static void bp_vcycle(BatchPoisson* bp, cudaStream_t s, int kmin) {
+  BPInst* I = bp->d_inst;
+  if (bp->ktot[BK_ZERO] > 0) kb_zero_y<<<bp_grid(bp, BK_ZERO), ET, 0, s>>>(I, bp_work(bp, BK_ZERO), kmin);
+  for (int l = 0; l < bp->max_cs; l++) {
+    const BPWork half = bp_work(bp, bk_half(l));
+    const int gh = bp_grid(bp, bk_half(l));
+    for (int k = 0; k < 2; k++) {
+      kb_smooth<<<gh, ET, 0, s>>>(I, half, l, 0, kmin);
+      kb_smooth<<<gh, ET, 0, s>>>(I, half, l, 1, kmin);
+    }
+    kb_resid<<<bp_grid(bp, bk_lvl(l)), ET, 0, s>>>(I, bp_work(bp, bk_lvl(l)), l, kmin);
+    kb_restrict<<<bp_grid(bp, bk_lvlc(l)), ET, 0, s>>>(I, bp_work(bp, bk_lvlc(l)), l, kmin);
+  }
+  kb_coarse_vcycle<<<bp->n, 1024, bp->coarse_smem, s>>>(I, bp->d_act_list, bp->d_act_cnt, 2, 2, kmin);
+  for (int l = bp->max_cs - 1; l >= 0; l--) {
+    kb_prolong<<<bp_grid(bp, bk_lvl(l)), ET, 0, s>>>(I, bp_work(bp, bk_lvl(l)), l, kmin);
+    const BPWork half = bp_work(bp, bk_half(l));
+    const int gh = bp_grid(bp, bk_half(l));
+    for (int k = 0; k < 2; k++) {
+      kb_smooth<<<gh, ET, 0, s>>>(I, half, l, 1, kmin);
+      kb_smooth<<<gh, ET, 0, s>>>(I, half, l, 0, kmin);
+    }
+  }
+}
+
+// One Newton round of every live instance: the residual (again in FP64 where the FP32
+// exponential's bound fails), the convergence check, the list of the instances going on,
+// and their Newton step: restriction of P, PCG with the instance's iterations, phi update.
+static void bp_round(BatchPoisson* bp, cudaStream_t s, int max_iters) {
+  const int n = bp->n;
+  BPInst* I = bp->d_inst;
+  const BPWork fine = bp_work(bp, BK_FINE), red = bp_work(bp, BK_RED);
+  const int gf = bp_grid(bp, BK_FINE), gr = bp_grid(bp, BK_RED);
+  const int tb = 128, tg = (n + tb - 1) / tb;
+  SF_CUDA(cudaMemsetAsync(bp->d_run, 0, sizeof(int), s));
+  kb_nl_residual<<<gr, RB, 0, s>>>(I, red, bp->d_prm, BP_LIVE);
+  kb_reduce3<<<n, 256, 0, s>>>(I, BP_LIVE);
+  kb_check_exp<<<tg, tb, 0, s>>>(I, n, bp->d_prm);
+  kb_nl_residual<<<gr, RB, 0, s>>>(I, red, bp->d_prm, BP_REDO);
+  kb_reduce3<<<n, 256, 0, s>>>(I, BP_REDO);
+  kb_newton_control<<<tg, tb, 0, s>>>(I, n, bp->d_prm, bp->d_run);
+  bp_compact(bp, s);
+  for (int l = 0; l < bp->max_cs; l++)
+    kb_restrict_P<<<bp_grid(bp, bk_lvlc(l)), ET, 0, s>>>(I, bp_work(bp, bk_lvlc(l)), l, 0);
+  kb_zero_cg<<<gf, ET, 0, s>>>(I, fine, 0, 0);
+  bp_vcycle(bp, s, 0);
+  kb_zero_cg<<<gf, ET, 0, s>>>(I, fine, 1, 0);
+  kb_cg_dots<<<gr, RB, 0, s>>>(I, red, 0);
+  kb_reduce2<<<n, 256, 0, s>>>(I, 0);
+  kb_cg_scalars<<<tg, tb, 0, s>>>(I, n, 0, 0);
+  kb_cg_pupdate<<<gf, ET, 0, s>>>(I, fine, 1, 0);
+  for (int k = 0; k < max_iters; k++) {
+    kb_cg_matvec<<<gr, RB, 0, s>>>(I, red, k);
+    kb_reduce2<<<n, 256, 0, s>>>(I, k);
+    kb_cg_scalars<<<tg, tb, 0, s>>>(I, n, 1, k);
+    kb_cg_axpy<<<gf, ET, 0, s>>>(I, fine, k);
+    if (k == max_iters - 1) break;
+    bp_vcycle(bp, s, k + 1);
+    kb_cg_dots<<<gr, RB, 0, s>>>(I, red, k + 1);
+    kb_reduce2<<<n, 256, 0, s>>>(I, k + 1);
+    kb_cg_scalars<<<tg, tb, 0, s>>>(I, n, 2, k + 1);
+    kb_cg_pupdate<<<gf, ET, 0, s>>>(I, fine, 0, k + 1);
+  }
+  kb_update_phi<<<gf, ET, 0, s>>>(I, fine, bp->d_prm);
+  SF_CUDA(cudaGetLastError());
+}
 
 template <typename F>
 static void bp_table(std::vector<int>& tab, int n, F blocks, int& off, int& tot) {
@@ -1434,71 +1643,6 @@ static void bp_table(std::vector<int>& tab, int n, F blocks, int& off, int& tot)
   }
   tab.push_back(acc);
   tot = acc;
-}
-
-static void bp_vcycle(BatchPoisson* bp, cudaStream_t s, int kmin) {
-  const int n = bp->n;
-  BPInst* I = bp->d_inst;
-  if (bp->zero_tot > 0) kb_zero_y<<<bp->zero_tot, ET, 0, s>>>(I, n, bp->d_tab + bp->zero_off, kmin);
-  for (int l = 0; l < bp->max_cs; l++) {
-    const int* half = bp->d_tab + bp->half_off[l];
-    for (int k = 0; k < 2; k++) {
-      kb_smooth<<<bp->half_tot[l], ET, 0, s>>>(I, n, half, l, 0, kmin);
-      kb_smooth<<<bp->half_tot[l], ET, 0, s>>>(I, n, half, l, 1, kmin);
-    }
-    kb_resid<<<bp->lvl_tot[l], ET, 0, s>>>(I, n, bp->d_tab + bp->lvl_off[l], l, kmin);
-    kb_restrict<<<bp->lvlc_tot[l], ET, 0, s>>>(I, n, bp->d_tab + bp->lvlc_off[l], l, kmin);
-  }
-  kb_coarse_vcycle<<<n, 1024, bp->coarse_smem, s>>>(I, 2, 2, kmin);
-  for (int l = bp->max_cs - 1; l >= 0; l--) {
-    kb_prolong<<<bp->lvl_tot[l], ET, 0, s>>>(I, n, bp->d_tab + bp->lvl_off[l], l, kmin);
-    const int* half = bp->d_tab + bp->half_off[l];
-    for (int k = 0; k < 2; k++) {
-      kb_smooth<<<bp->half_tot[l], ET, 0, s>>>(I, n, half, l, 1, kmin);
-      kb_smooth<<<bp->half_tot[l], ET, 0, s>>>(I, n, half, l, 0, kmin);
-    }
-  }
-}
-
-// One Newton round of every live instance: the residual (again in FP64 where the FP32
-// exponential's bound fails), the convergence check, and for the instances that go on
-// the Newton step: restriction of P, PCG with the instance's iterations, phi update.
-static void bp_round(BatchPoisson* bp, cudaStream_t s, int max_iters) {
-  const int n = bp->n;
-  BPInst* I = bp->d_inst;
-  const int* fine = bp->d_tab + bp->fine_off;
-  const int* red = bp->d_tab + bp->red_off;
-  const int tb = 128, tg = (n + tb - 1) / tb;
-  SF_CUDA(cudaMemsetAsync(bp->d_run, 0, sizeof(int), s));
-  kb_nl_residual<<<bp->red_tot, RB, 0, s>>>(I, n, red, bp->d_prm, BP_LIVE);
-  kb_reduce3<<<n, 256, 0, s>>>(I, BP_LIVE);
-  kb_check_exp<<<tg, tb, 0, s>>>(I, n, bp->d_prm);
-  kb_nl_residual<<<bp->red_tot, RB, 0, s>>>(I, n, red, bp->d_prm, BP_REDO);
-  kb_reduce3<<<n, 256, 0, s>>>(I, BP_REDO);
-  kb_newton_control<<<tg, tb, 0, s>>>(I, n, bp->d_prm, bp->d_run);
-  for (int l = 0; l < bp->max_cs; l++)
-    kb_restrict_P<<<bp->lvlc_tot[l], ET, 0, s>>>(I, n, bp->d_tab + bp->lvlc_off[l], l, 0);
-  kb_zero_cg<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, 0, 0);
-  bp_vcycle(bp, s, 0);
-  kb_zero_cg<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, 1, 0);
-  kb_cg_dots<<<bp->red_tot, RB, 0, s>>>(I, n, red, 0);
-  kb_reduce2<<<n, 256, 0, s>>>(I, 0);
-  kb_cg_scalars<<<tg, tb, 0, s>>>(I, n, 0, 0);
-  kb_cg_pupdate<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, 1, 0);
-  for (int k = 0; k < max_iters; k++) {
-    kb_cg_matvec<<<bp->red_tot, RB, 0, s>>>(I, n, red, k);
-    kb_reduce2<<<n, 256, 0, s>>>(I, k);
-    kb_cg_scalars<<<tg, tb, 0, s>>>(I, n, 1, k);
-    kb_cg_axpy<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, k);
-    if (k == max_iters - 1) break;
-    bp_vcycle(bp, s, k + 1);
-    kb_cg_dots<<<bp->red_tot, RB, 0, s>>>(I, n, red, k + 1);
-    kb_reduce2<<<n, 256, 0, s>>>(I, k + 1);
-    kb_cg_scalars<<<tg, tb, 0, s>>>(I, n, 2, k + 1);
-    kb_cg_pupdate<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, 0, k + 1);
-  }
-  kb_update_phi<<<bp->fine_tot, ET, 0, s>>>(I, n, fine, bp->d_prm);
-  SF_CUDA(cudaGetLastError());
 }
 
 static cudaGraphExec_t bp_graph(BatchPoisson* bp, int max_iters) {
@@ -1596,29 +1740,28 @@ BatchPoisson* batch_poisson_create(sf_ctx* const* ctxs, int n, int num_sms, cuda
       bp->coarse_smem = std::max(bp->coarse_smem, ps[i]->coarse_smem);
     }
     std::vector<int> tab;
-    bp_table(tab, n, [&](int i) { return (ps[i]->ni * ps[i]->nj + ET - 1) / ET; }, bp->fine_off, bp->fine_tot);
-    bp_table(tab, n, [&](int i) { return ps[i]->red_blocks; }, bp->red_off, bp->red_tot);
-    bp_table(tab, n, [&](int i) { return ps[i]->cs > 0 ? (ps[i]->ni * ps[i]->nj + ET - 1) / ET : 0; }, bp->zero_off,
-             bp->zero_tot);
-    bp->lvl_off.resize(bp->max_cs);
-    bp->lvl_tot.resize(bp->max_cs);
-    bp->lvlc_off.resize(bp->max_cs);
-    bp->lvlc_tot.resize(bp->max_cs);
-    bp->half_off.resize(bp->max_cs);
-    bp->half_tot.resize(bp->max_cs);
+    bp->nkinds = 3 + 3 * bp->max_cs;
+    bp->koff.assign(bp->nkinds, 0);
+    bp->ktot.assign(bp->nkinds, 0);
+    auto add = [&](int kind, auto blocks) { bp_table(tab, n, blocks, bp->koff[kind], bp->ktot[kind]); };
+    add(BK_FINE, [&](int i) { return (ps[i]->ni * ps[i]->nj + ET - 1) / ET; });
+    add(BK_RED, [&](int i) { return ps[i]->red_blocks; });
+    add(BK_ZERO, [&](int i) { return ps[i]->cs > 0 ? (ps[i]->ni * ps[i]->nj + ET - 1) / ET : 0; });
     for (int l = 0; l < bp->max_cs; l++) {
       auto on = [&](int i) { return l < ps[i]->cs; };
-      bp_table(tab, n, [&](int i) { return on(i) ? (ps[i]->lv[l].ni * ps[i]->lv[l].nj + ET - 1) / ET : 0; },
-               bp->lvl_off[l], bp->lvl_tot[l]);
-      bp_table(tab, n,
-               [&](int i) { return on(i) ? (ps[i]->lv[l + 1].ni * ps[i]->lv[l + 1].nj + ET - 1) / ET : 0; },
-               bp->lvlc_off[l], bp->lvlc_tot[l]);
-      bp_table(tab, n,
-               [&](int i) { return on(i) ? (ps[i]->lv[l].nj * ((ps[i]->lv[l].ni + 1) / 2) + ET - 1) / ET : 0; },
-               bp->half_off[l], bp->half_tot[l]);
+      add(bk_lvl(l), [&](int i) { return on(i) ? (ps[i]->lv[l].ni * ps[i]->lv[l].nj + ET - 1) / ET : 0; });
+      add(bk_lvlc(l), [&](int i) { return on(i) ? (ps[i]->lv[l + 1].ni * ps[i]->lv[l + 1].nj + ET - 1) / ET : 0; });
+      add(bk_half(l), [&](int i) { return on(i) ? (ps[i]->lv[l].nj * ((ps[i]->lv[l].ni + 1) / 2) + ET - 1) / ET : 0; });
     }
     SF_CUDA(cudaMalloc(&bp->d_tab, sizeof(int) * tab.size()));
     copy_wait(bp->d_tab, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, stream);
+    SF_CUDA(cudaMalloc(&bp->d_koff, sizeof(int) * bp->nkinds));
+    copy_wait(bp->d_koff, bp->koff.data(), sizeof(int) * bp->nkinds, cudaMemcpyHostToDevice, stream);
+    SF_CUDA(cudaMalloc(&bp->d_act_pos, sizeof(int) * (n + 1)));
+    SF_CUDA(cudaMalloc(&bp->d_act_list, sizeof(int) * n));
+    SF_CUDA(cudaMalloc(&bp->d_act_cnt, sizeof(int)));
+    SF_CUDA(cudaMalloc(&bp->d_act_start, sizeof(int) * (size_t)bp->nkinds * (n + 1)));
+    SF_CUDA(cudaMalloc(&bp->d_act_total, sizeof(int) * bp->nkinds));
     SF_CUDA(cudaMalloc(&bp->d_inst, sizeof(BPInst) * n));
     SF_CUDA(cudaMalloc(&bp->d_iters, sizeof(int) * 2 * n));
     SF_CUDA(cudaFuncSetAttribute(kb_coarse_vcycle, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)COARSE_SMEM_MAX));
@@ -1639,7 +1782,8 @@ void batch_poisson_destroy(BatchPoisson* bp) {
   if (!bp) return;
   if (bp->stream) cudaStreamSynchronize(bp->stream);
   for (auto& g : bp->graphs) cudaGraphExecDestroy(g.second);
-  void* ptrs[] = {bp->d_inst, bp->d_tab, bp->d_iters, bp->d_run, bp->d_prm, bp->d_stat};
+  void* ptrs[] = {bp->d_inst, bp->d_tab,      bp->d_koff,     bp->d_iters,     bp->d_run,       bp->d_prm,
+                  bp->d_stat, bp->d_act_pos, bp->d_act_list, bp->d_act_cnt, bp->d_act_start, bp->d_act_total};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (bp->ev0) cudaEventDestroy(bp->ev0);
@@ -1680,7 +1824,8 @@ float batch_poisson_step(BatchPoisson* bp, const sf_poisson_params& prm, const i
   SF_CUDA(cudaMemcpyAsync(bp->d_iters, init.data(), sizeof(int) * 2 * bp->n, cudaMemcpyHostToDevice, s));
   const int tg = (bp->n + 127) / 128;
   kb_init<<<tg, 128, 0, s>>>(bp->d_inst, bp->n, bp->d_iters);
-  kb_rho_b0<<<bp->fine_tot, ET, 0, s>>>(bp->d_inst, bp->n, bp->d_tab + bp->fine_off, bp->d_prm);
+  kb_rho_b0<<<bp->ktot[BK_FINE], ET, 0, s>>>(bp->d_inst, bp->n, bp->d_tab + bp->koff[BK_FINE], bp->d_prm);
+  bp_compact(bp, s);  // every instance is live
   SF_CUDA(cudaGetLastError());
   cudaGraphExec_t g = bp_graph(bp, max_iters);
   for (int r = 0; r <= prm.max_it; r++) {
@@ -1690,7 +1835,7 @@ float batch_poisson_step(BatchPoisson* bp, const sf_poisson_params& prm, const i
     SF_CUDA(cudaStreamSynchronize(s));
     if (run == 0) break;
   }
-  kb_efield<<<bp->fine_tot, ET, 0, s>>>(bp->d_inst, bp->n, bp->d_tab + bp->fine_off);
+  kb_efield<<<bp->ktot[BK_FINE], ET, 0, s>>>(bp->d_inst, bp->n, bp->d_tab + bp->koff[BK_FINE]);
   kb_collect<<<tg, 128, 0, s>>>(bp->d_inst, bp->n, bp->d_stat);
   SF_CUDA(cudaGetLastError());
   SF_CUDA(cudaEventRecord(bp->ev1, s));

@@ -410,18 +410,16 @@ __device__ inline void seg_normal_tangent(const Seg4 s, double n[3], double tg[3
   n[0] = -dy; n[1] = dx; n[2] = 0;
 }
 
-__device__ double sample_maxw_speed(Philox& r, double v_th) {
-  // Utils.SampleMaxwSpeed (core/common/Utils.java:69-87), rejection bounded at 10^4 tries
-  double bin_max = 6 * v_th;
-  double a = 4 / (sqrt(PI) * v_th * v_th * v_th);
-  double fm_max = 4 / (sqrt(PI) * v_th) * exp(-1.0);
-  double v = v_th;
+// Utils.SampleMaxwSpeed (core/common/Utils.java:69-87), rejection bounded at 10^4 tries.
+// A sampled speed needs no more than FP32: the draws and the acceptance test are FP32
+// (f/f_max = (v/v_th)^2 e^(1 - (v/v_th)^2), the reference's ratio in closed form).
+__device__ float sample_maxw_speed(Philox& r, float v_th) {
+  float x = 1.f;  // v / v_th
   for (int tries = 0; tries < 10000; tries++) {
-    v = r.uniform() * bin_max;
-    double fm = a * v * v * exp(-v * v / (v_th * v_th));
-    if ((fm / fm_max) > r.uniform()) return v;
+    x = r.uniformf() * 6.f;
+    if (x * x * __expf(1.f - x * x) > r.uniformf()) break;
   }
-  return v;
+  return x * v_th;
 }
 
 
@@ -570,14 +568,16 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
       case SF_SURF_DIFFUSE: {  // SurfaceInteraction.java:153-213 (cosine emission)
         const float4 pr = sa.sv.param[seg_min];
         const double v_refl = sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]) * pr.y;
-        const double v_diff = sample_maxw_speed(rng, pr.x);
+        const double v_diff = (double)sample_maxw_speed(rng, pr.x);
         const double v_mag = v_refl + pr.z * (v_diff - v_refl);
-        // Vec.lambertianVector (core/common/Vec.java:450-471)
-        double cosphi = sqrt(1.0 - rng.uniform());
-        if (cosphi > 0.99999) cosphi = 0.99999;
-        const double theta = 2 * PI * rng.uniform();
-        const double sinphi = sqrt(1.0 - cosphi * cosphi);
-        const double c_t = cos(theta) * sinphi, c_n = cosphi, c_p = sin(theta) * sinphi;
+        // Vec.lambertianVector (core/common/Vec.java:450-471), the random direction in FP32
+        float cosphi = sqrtf(1.f - rng.uniformf());
+        if (cosphi > 0.99999f) cosphi = 0.99999f;
+        const float theta = 2.f * (float)PI * rng.uniformf();
+        const float sinphi = sqrtf(1.f - cosphi * cosphi);
+        float st, ct;
+        __sincosf(theta, &st, &ct);
+        const double c_t = (double)(ct * sinphi), c_n = (double)cosphi, c_p = (double)(st * sinphi);
         const double pz[3] = {0, 0, 1};
         for (int q = 0; q < 3; q++) vel[q] = v_mag * (c_t * tg[q] + c_n * n[q] + c_p * pz[q]);
         alive = true;

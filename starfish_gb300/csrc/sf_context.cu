@@ -26,6 +26,8 @@ sf::MeshView sf_ctx::mesh_view() const {
   m.x0[1] = x0[1];
   m.dh[0] = dh[0];
   m.dh[1] = dh[1];
+  m.inv_dh[0] = 1.0 / dh[0];
+  m.inv_dh[1] = 1.0 / dh[1];
   m.inv_dx = (float)(1.0 / dh[0]);
   m.inv_dy = (float)(1.0 / dh[1]);
   m.E = E;

@@ -80,6 +80,7 @@ __host__ __device__ inline void key_cell(uint32_t key, int ntx, int& i, int& j) 
 struct MeshView {
   int ni, nj, nmax, domain;
   double x0[2], dh[2];
+  double inv_dh[2];             // 1 / dh (the exact path multiplies: an FP64 division is ~10x dearer)
   float inv_dx, inv_dy;
   const float2* E;              // ni*nj (efi, efj) FP32
   const uint8_t* seg_dist;      // ni*nj Chebyshev distance to the nearest node listing a

@@ -529,10 +529,12 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
     seg_intersect(sxy, old, pos, t);
     const double t_part = t[1];
     if (t_part > 0) {
-      double n[3], tg[3];
-      seg_normal_tangent(sxy, n, tg);
-      const double acs = (n[0] * vel[0] + n[1] * vel[1]) / sqrt(vel[0] * vel[0] + vel[1] * vel[1]);
-      if (t_part < FLT_EPS_REF && acs > 0) return false;
+      if (t_part < FLT_EPS_REF) {  // leaving the surface it starts on (acs > 0): no hit
+        double n[3], tg[3];
+        seg_normal_tangent(sxy, n, tg);
+        const double acs = (n[0] * vel[0] + n[1] * vel[1]) / sqrt(vel[0] * vel[0] + vel[1] * vel[1]);
+        if (acs > 0) return false;
+      }
       if (t_part < tp_min) {
         tp_min = t_part;
         tsurf_min = t[0];
@@ -546,8 +548,8 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
     tp_min *= 0.9999;
     pos[0] = old[0] + tp_min * (pos[0] - old[0]);
     pos[1] = old[1] + tp_min * (pos[1] - old[1]);
-    lc[0] = (pos[0] - m.x0[0]) / m.dh[0];
-    lc[1] = (pos[1] - m.x0[1]) / m.dh[1];
+    lc[0] = (pos[0] - m.x0[0]) * m.inv_dh[0];
+    lc[1] = (pos[1] - m.x0[1]) * m.inv_dh[1];
     pdt = dt0 * (1 - tp_min);
     if (lc[0] < 0 && lc[0] > -FLT_EPS_REF) lc[0] = 0;
     if (lc[1] < 0 && lc[1] > -FLT_EPS_REF) lc[1] = 0;
@@ -891,7 +893,8 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
       if (DOM == SF_DOMAIN_RZ) {
         const double A = vel[2] * pdt, B = pos[0];
         const double R = sqrt(A * A + B * B);
-        const double cs = R > 0 ? B / R : 1.0, sn = R > 0 ? A / R : 0.0;
+        const double iR = R > 0 ? 1.0 / R : 0.0;
+        const double cs = R > 0 ? B * iR : 1.0, sn = R > 0 ? A * iR : 0.0;
         const double v1 = vel[0], v2 = vel[2];
         pos[0] = R;
         vel[0] = cs * v1 + sn * v2;
@@ -899,14 +902,15 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
       } else if (DOM == SF_DOMAIN_ZR) {
         const double A = vel[2] * pdt, B = pos[1];
         const double R = sqrt(A * A + B * B);
-        const double cs = R > 0 ? B / R : 1.0, sn = R > 0 ? A / R : 0.0;
+        const double iR = R > 0 ? 1.0 / R : 0.0;
+        const double cs = R > 0 ? B * iR : 1.0, sn = R > 0 ? A * iR : 0.0;
         const double v1 = vel[1], v2 = vel[2];
         pos[1] = R;
         vel[1] = cs * v1 + sn * v2;
         vel[2] = -sn * v1 + cs * v2;
       }
-      lc[0] = (pos[0] - m.x0[0]) / m.dh[0];
-      lc[1] = (pos[1] - m.x0[1]) / m.dh[1];
+      lc[0] = (pos[0] - m.x0[0]) * m.inv_dh[0];
+      lc[1] = (pos[1] - m.x0[1]) * m.inv_dh[1];
       periodic = false;
       alive = process_boundary(m, sa, a, pos, vel, lc, pdt, old, lc_old, rng, periodic);
       if (!alive) break;
@@ -918,8 +922,8 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
     }
     if (pdt > 0) atomicAdd(&sa.counters[2], 1ULL);  // remaining time is dropped
     if (periodic) {
-      lc[0] = fmin(fmax((pos[0] - m.x0[0]) / m.dh[0], 0.0), m.ni - 1.0);
-      lc[1] = fmin(fmax((pos[1] - m.x0[1]) / m.dh[1], 0.0), m.nj - 1.0);
+      lc[0] = fmin(fmax((pos[0] - m.x0[0]) * m.inv_dh[0], 0.0), m.ni - 1.0);
+      lc[1] = fmin(fmax((pos[1] - m.x0[1]) * m.inv_dh[1], 0.0), m.nj - 1.0);
     }
     int i = (int)lc[0], j = (int)lc[1];
     if (i > m.ni - 2) i = m.ni - 2;

@@ -177,6 +177,7 @@ BatchInst make_inst(sf_batch* b, int i) {
   I.sa.sv.deposit = sp->deposit;
   I.sa.counters = c->counters;
   I.sa.stats_slow = c->stats_partial + (size_t)8 * (c->stats_blocks - 1);
+  I.sa.stats = 0;  // the batch reports no push totals
   I.count = sp->count;
   I.slow_idx = c->slow_idx;
   I.nd = sp->nd;

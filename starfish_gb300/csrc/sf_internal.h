@@ -129,6 +129,7 @@ struct SlowArgs {
   SurfaceView sv;
   unsigned long long* counters;
   double* stats_slow;   // 5 sums + boundary charge
+  int stats;            // the totals (stats_slow) are wanted
 };
 
 // ---------------------------------------------------------------------------------

@@ -795,10 +795,15 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
   __shared__ double s_stats[8];
   __shared__ double s_seg[4 * SMALL_NSEG];
   __shared__ unsigned long long s_cnt[4];
+  // absorptions decided in FP32 per segment: count and the sum of the segment parameter
+  // in fixed point (2^-24, split in 12-bit halves: a block sees at most 2^31 / 2432
+  // entries, whose sums stay below 2^32)
+  __shared__ unsigned s_ahit[SMALL_NSEG], s_atlo[SMALL_NSEG], s_athi[SMALL_NSEG];
   const bool seg_local = m.nseg <= SMALL_NSEG;
   __syncthreads();  // a block calling this again: the previous call's flush has read everything
   for (int q = threadIdx.x; q < 8; q += blockDim.x) s_stats[q] = 0.0;
   for (int q = threadIdx.x; q < 4 * SMALL_NSEG; q += blockDim.x) s_seg[q] = 0.0;
+  for (int q = threadIdx.x; q < SMALL_NSEG; q += blockDim.x) s_ahit[q] = s_atlo[q] = s_athi[q] = 0u;
   if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0ULL;
   __syncthreads();
   SlowArgs sa = sg;
@@ -813,6 +818,8 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
   // end instead of six per particle on the same few addresses)
   double lst[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   unsigned long long ldone = 0;
+  unsigned nabs = 0;  // absorptions decided in FP32 (boundary charge)
+  const bool want = sg.stats != 0;
   for (unsigned long long t = t_first; t < t_end; t += t_stride) {
     const int64_t p = slow_idx[t];
     const uint32_t c = P.cell[p];
@@ -839,11 +846,13 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
             P.vz[p] = nv[2];
           }
           ldone++;
-          lst[0] += 1.0;
-          lst[1] += (double)nv[0];
-          lst[2] += (double)nv[1];
-          lst[3] += (double)nv[2];
-          lst[4] += (double)sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+          if (want) {
+            lst[0] += 1.0;
+            lst[1] += (double)nv[0];
+            lst[2] += (double)nv[1];
+            lst[3] += (double)nv[2];
+            lst[4] += (double)sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+          }
           float wx, wy;
           scatter_weights<DOM>(nfx, nfy, i2, j2, a, wx, wy);
           deposit_global(m, count, mom, mom_on, smp, i2, j2, nfx, nfy, wx, wy, nv[0], nv[1], nv[2], nn);
@@ -865,12 +874,19 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
           const int model = sa.sv.model[hs];
           if (model != SF_SURF_PASS && model != SF_SURF_NONE && model != SF_SURF_SPECULAR &&
               model != SF_SURF_DIFFUSE) {
-            atomicAdd(&sa.stats_slow[5], a.spwt * a.charge);
-            const double w1 = a.spwt * (1 - (double)ht), w2 = a.spwt * (double)ht;
-            atomicAdd(&sa.sv.flux[2 * hs], w1);
-            atomicAdd(&sa.sv.flux[2 * hs + 1], w2);
-            atomicAdd(&sa.sv.deposit[2 * hs], w1);
-            atomicAdd(&sa.sv.deposit[2 * hs + 1], w2);
+            nabs++;
+            if (seg_local) {
+              const unsigned qt = __float2uint_rn(ht * 16777216.f);
+              atomicAdd(&s_ahit[hs], 1u);
+              atomicAdd(&s_atlo[hs], qt & 0xFFFu);
+              atomicAdd(&s_athi[hs], qt >> 12);
+            } else {
+              const double w1 = a.spwt * (1 - (double)ht), w2 = a.spwt * (double)ht;
+              atomicAdd(&sa.sv.flux[2 * hs], w1);
+              atomicAdd(&sa.sv.flux[2 * hs + 1], w2);
+              atomicAdd(&sa.sv.deposit[2 * hs], w1);
+              atomicAdd(&sa.sv.deposit[2 * hs + 1], w2);
+            }
             P.cell[p] = DEAD;
             atomicAdd(&sa.counters[1], 1ULL);
             continue;
@@ -935,25 +951,46 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
     P.frac[p] = make_float2(fx, fy);
     P.vxy[p] = make_float2((float)vel[0], (float)vel[1]);
     P.vz[p] = (float)vel[2];
-    lst[0] += 1.0;
-    lst[1] += vel[0];
-    lst[2] += vel[1];
-    lst[3] += vel[2];
-    lst[4] += sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+    if (want) {
+      lst[0] += 1.0;
+      lst[1] += vel[0];
+      lst[2] += vel[1];
+      lst[3] += vel[2];
+      lst[4] += sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+    }
     float wx, wy;
     scatter_weights<DOM>(fx, fy, i, j, a, wx, wy);
     deposit_global(m, count, mom, mom_on, smp, i, j, fx, fy, wx, wy, (float)vel[0], (float)vel[1], (float)vel[2], nn);
   }
   for (int o = 16; o > 0; o >>= 1) {
-    for (int q = 0; q < 5; q++) lst[q] += __shfl_down_sync(0xffffffffu, lst[q], o);
+    if (want)
+      for (int q = 0; q < 5; q++) lst[q] += __shfl_down_sync(0xffffffffu, lst[q], o);
     ldone += __shfl_down_sync(0xffffffffu, ldone, o);
+    nabs += __shfl_down_sync(0xffffffffu, nabs, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    for (int q = 0; q < 5; q++)
-      if (lst[q] != 0.0) atomicAdd(&s_stats[q], lst[q]);
+    if (want) {
+      for (int q = 0; q < 5; q++)
+        if (lst[q] != 0.0) atomicAdd(&s_stats[q], lst[q]);
+      if (nabs) atomicAdd(&s_stats[5], (double)nabs * (a.spwt * a.charge));
+    }
     if (ldone) atomicAdd(&s_cnt[3], ldone);
   }
   __syncthreads();
+  // FP32-decided absorptions into the per-segment sums: N hits with parameters t sum to
+  // spwt (N - sum t) at the first end and spwt sum t at the second (flux and deposit)
+  if (seg_local) {
+    for (int q = threadIdx.x; q < m.nseg; q += blockDim.x)
+      if (s_ahit[q]) {
+        const double T = ((double)s_athi[q] * 4096.0 + (double)s_atlo[q]) * (1.0 / 16777216.0);
+        const double w1 = a.spwt * ((double)s_ahit[q] - T), w2 = a.spwt * T;
+        s_seg[2 * q] += w1;
+        s_seg[2 * q + 1] += w2;
+        s_seg[2 * SMALL_NSEG + 2 * q] += w1;
+        s_seg[2 * SMALL_NSEG + 2 * q + 1] += w2;
+      }
+    __syncthreads();
+  }
   for (int q = threadIdx.x; q < 6; q += blockDim.x)
     if (s_stats[q] != 0.0) atomicAdd(&sg.stats_slow[q], s_stats[q]);
   if (threadIdx.x >= 1 && threadIdx.x < 4 && s_cnt[threadIdx.x])
@@ -1293,6 +1330,7 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
     sa.sv.deposit = sp->deposit;
     sa.counters = sc.counters;
     sa.stats_slow = slow_stats;
+    sa.stats = want_stats ? 1 : 0;
     const int sgrid = ctx->num_sms * 16;
     TimedScope ts(ctx, "push_slow");
     ctx->launches++;

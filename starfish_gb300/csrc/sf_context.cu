@@ -309,10 +309,25 @@ __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, Part
     }
     __syncthreads();
     unsigned slot[SORT_IPT], rank[SORT_IPT];
+    // the whole chunk is requested at once (the staging below then needs no second trip
+    // to memory)
+    uint32_t r_cell[SORT_IPT];
+    float2 r_frac[SORT_IPT], r_vxy[SORT_IPT];
+    float r_vz[SORT_IPT];
 #pragma unroll
     for (int k = 0; k < SORT_IPT; k++) {
       const int64_t q = base + k * SORT_B + threadIdx.x;
-      const uint32_t c = (q < src.n) ? src.cell[q] : DEAD;
+      r_cell[k] = DEAD;
+      if (q < src.n) {
+        r_cell[k] = __ldcs(&src.cell[q]);
+        r_frac[k] = __ldcs(&src.frac[q]);
+        r_vxy[k] = __ldcs(&src.vxy[q]);
+        r_vz[k] = __ldcs(&src.vz[q]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < SORT_IPT; k++) {
+      const uint32_t c = r_cell[k];
       slot[k] = SORT_HSIZE;
       if (c == DEAD) continue;
       slot[k] = hash_insert(hkey, cell_key(cell_i(c), cell_j(c), ntx));
@@ -349,12 +364,11 @@ __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, Part
 #pragma unroll
     for (int k = 0; k < SORT_IPT; k++) {
       if (slot[k] >= SORT_HSIZE) continue;
-      const int64_t q = base + k * SORT_B + threadIdx.x;
       const unsigned l = hoff[slot[k]] + rank[k];
-      s_cell[l] = src.cell[q];
-      s_frac[l] = src.frac[q];
-      s_vxy[l] = src.vxy[q];
-      s_vz[l] = src.vz[q];
+      s_cell[l] = r_cell[k];
+      s_frac[l] = r_frac[k];
+      s_vxy[l] = r_vxy[k];
+      s_vz[l] = r_vz[k];
       s_dst[l] = (int)(hcnt[slot[k]] + rank[k]);
     }
     __syncthreads();

@@ -199,6 +199,19 @@ int sf_particles_clear(sf_ctx* ctx, int32_t sid);
  * *rem carries the fractional particle count between calls.  *n_added: particles added. */
 int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg_xy, double den, double v_drift,
                          double temp, double dt, double* rem, int64_t* n_added);
+/* UniformSource on one straight segment (sources/UniformSource.java:36-80): mass flow rate
+ * mdot (kg/s) with the particle count of Source.regenerate; particles at random points of
+ * the segment (area-weighted in RZ / ZR), velocity normal * v_drift with no thermal spread;
+ * the push off the surface and the rewind as sf_source_maxwellian. */
+int sf_source_uniform(sf_ctx* ctx, int32_t sid, const double* seg_xy, double mdot, double v_drift,
+                      double dt, double* rem, int64_t* n_added);
+/* VolumePreloadSource (sources/VolumePreloadSource.java:44-66) through VolumeSource
+ * (core/source/VolumeSource.java:63-170): in every cell ceil(den cellVol / spwt) - 1
+ * particles (when that number exceeds spwt) uniform in the cell, Maxwellian at
+ * max(temp, 50 K) (Utils.SampleMaxw3D with its factor 1.2); points inside solid
+ * boundaries (BoundaryModule.isInternal) are not added; the 1e-6 dt push off and the
+ * -dt/2 rewind of addParticle.  *n_added: particles added. */
+int sf_source_preload(sf_ctx* ctx, int32_t sid, double den, double temp, double dt, int64_t* n_added);
 
 /* ---- fields ----------------------------------------------------------------- */
 /* Sets the electric field used by the push (DomainModule efi/efj, FP64 host -> FP32 device). */

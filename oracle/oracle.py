@@ -88,6 +88,15 @@ def _declare(L):
     L.orc_maxwellian_source.argtypes = [C.c_int64, C.c_int, d, C.c_double, C.c_double, C.c_double,
                                         C.c_double, C.c_double, C.c_double, d, C.c_int, d]
     L.orc_maxwellian_source.restype = C.c_int
+    L.orc_uniform_source.argtypes = [C.c_int64, C.c_int, d, C.c_double, C.c_double, C.c_double, C.c_double,
+                                     C.c_double, d, C.c_int, d]
+    L.orc_uniform_source.restype = C.c_int
+    i32 = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    L.orc_point_internal.argtypes = [C.c_int, d, i32, C.c_double, C.c_double]
+    L.orc_point_internal.restype = C.c_int
+    L.orc_preload.argtypes = [C.c_int64, C.c_int, C.c_int, d, d, C.c_int, C.c_int, d, i32, C.c_double, C.c_double,
+                              C.c_double, C.c_double, C.c_double, C.c_int, d]
+    L.orc_preload.restype = C.c_int
     L.orc_dsmc.argtypes = [C.c_int, C.c_int, d, C.c_int, d, C.c_double, C.c_double, C.c_double,
                            C.c_double, C.c_double, C.c_double, C.c_double, d, d, C.c_int64]
     L.orc_dsmc.restype = C.c_long
@@ -276,6 +285,32 @@ def maxwellian_source(seed, seg_xy, den, v_drift, temp, mass, spwt, dt, rem=0.0,
     n = lib().orc_maxwellian_source(int(seed), int(domain), _f64(seg_xy), den, v_drift, temp, mass, spwt,
                                     dt, r, cap, parts.reshape(-1))
     return parts[:n].copy(), float(r[0])
+
+
+def uniform_source(seed, seg_xy, mdot, v_drift, mass, spwt, dt, rem=0.0, cap=1 << 20, domain=0):
+    """UniformSource on one segment: (particles n x 12, remainder)."""
+    r = np.array([rem], np.float64)
+    parts = np.zeros((cap, 12))
+    n = lib().orc_uniform_source(int(seed), int(domain), _f64(seg_xy), mdot, v_drift, mass, spwt, dt, r, cap,
+                                 parts.reshape(-1))
+    return parts[:n].copy(), float(r[0])
+
+
+def point_internal(seg_xy, seg_btype, x, y):
+    """BoundaryModule.isInternal for straight segments (n x 4 end points, boundary types)."""
+    seg = _f64(np.asarray(seg_xy).reshape(-1))
+    bt = np.ascontiguousarray(seg_btype, np.int32)
+    return bool(lib().orc_point_internal(len(bt), seg, bt, float(x), float(y)))
+
+
+def preload(seed, spec, den, temp, mass, spwt, dt, cap=1 << 22):
+    """VolumePreloadSource on the mesh of spec (MeshSpec with segments): particles n x 12."""
+    parts = np.zeros((cap, 12))
+    seg = _f64(np.asarray(spec.seg_xy).reshape(-1)) if len(spec.seg_xy) else np.zeros(4)
+    bt = np.ascontiguousarray(spec.seg_btype, np.int32) if len(spec.seg_btype) else np.zeros(1, np.int32)
+    n = lib().orc_preload(int(seed), spec.ni, spec.nj, _f64(spec.x0), _f64(spec.dh), int(spec.domain),
+                          len(spec.seg_btype), seg, bt, den, temp, mass, spwt, dt, cap, parts.reshape(-1))
+    return parts[:n].copy()
 
 
 def dsmc(ni, nj, cell_vol, parts, mass, spwt, d_ref, T_ref, omega, vss_alpha, delta_t,

@@ -1247,6 +1247,125 @@ int orc_maxwellian_source(int64_t seed, int domain, const double* seg_xy, double
   return out;
 }
 
+// UniformSource (sources/UniformSource.java:36-80): the count of Source.regenerate from
+// the mass flow rate, positions by Boundary.randomT (area-weighted in RZ / ZR), velocity
+// normal * v_drift, then Source.sampleKinetic's 1e-6 dt push off.
+int orc_uniform_source(int64_t seed, int domain, const double* seg_xy, double mdot, double v_drift, double mass,
+                       double spwt, double dt, double* rem, int cap, double* parts) {
+  JRandom r;
+  r.set_seed(seed);
+  Seg s;
+  s.x1[0] = seg_xy[0]; s.x1[1] = seg_xy[1]; s.x2[0] = seg_xy[2]; s.x2[1] = seg_xy[3];
+  seg_init(s);
+  const double r1 = domain == DOM_RZ ? seg_xy[0] : seg_xy[1], r2 = domain == DOM_RZ ? seg_xy[2] : seg_xy[3];
+  double mp = (mdot * dt) / (mass * spwt) + *rem;
+  int num = (int)mp;
+  *rem = mp - num;
+  int out = 0;
+  Particle* P = reinterpret_cast<Particle*>(parts);
+  for (int k = 0; k < num && out < cap; k++) {
+    double t = r.nextDouble();
+    if (domain != DOM_XY) t = frustum_t(t, r1, r2);
+    Particle& p = P[out];
+    memset(&p, 0, sizeof(Particle));
+    p.pos[0] = seg_xy[0] + t * (seg_xy[2] - seg_xy[0]);
+    p.pos[1] = seg_xy[1] + t * (seg_xy[3] - seg_xy[1]);
+    for (int i = 0; i < 3; i++) p.vel[i] = s.normal[i] * v_drift;
+    for (int i = 0; i < 3; i++) p.pos[i] += p.vel[i] * 1e-6 * dt;
+    p.mpw = spwt;
+    p.alive = 1;
+    out++;
+  }
+  return out;
+}
+
+// Spline.isOnLine (core/boundaries/Spline.java:833-862), straight segment
+static bool on_line(const double* g, const double xp[2]) {
+  double t;
+  if (g[2] != g[0]) {
+    t = (xp[0] - g[0]) / (g[2] - g[0]);
+    if (t < -FLT_EPS || t > 1.0 + FLT_EPS) return false;
+  } else {
+    t = (xp[1] - g[1]) / (g[3] - g[1]);
+    if (t < -FLT_EPS || t > 1.0 + FLT_EPS) return false;
+  }
+  const double d1 = g[0] + t * (g[2] - g[0]) - xp[0], d2 = g[1] + t * (g[3] - g[1]) - xp[1];
+  const double l2 = (g[2] - g[0]) * (g[2] - g[0]) + (g[3] - g[1]) * (g[3] - g[1]);
+  return !((d1 * d1 + d2 * d2) / l2 > FLT_EPS);
+}
+
+// BoundaryModule.isInternal (core/boundaries/BoundaryModule.java:245-251) through
+// Spline.visibleSegment (Spline.java:881-929) and Spline.isInternal (:806-830)
+int orc_point_internal(int nseg, const double* seg_xy, const int* seg_btype, double x, double y) {
+  const double xp[2] = {x, y};
+  for (int s = 0; s < nseg; s++) {
+    if (seg_btype[s] == BT_VIRTUAL || seg_btype[s] == BT_OPEN) continue;
+    const double* g = seg_xy + 4 * s;
+    if (on_line(g, xp)) return 1;
+    const double xc[2] = {0.5 * (g[0] + g[2]), 0.5 * (g[1] + g[3])};
+    bool blocked = false;
+    for (int s2 = 0; s2 < nseg && !blocked; s2++) {
+      if (s2 == s || seg_btype[s2] == BT_VIRTUAL || seg_btype[s2] == BT_OPEN) continue;
+      Seg q;
+      q.x1[0] = seg_xy[4 * s2]; q.x1[1] = seg_xy[4 * s2 + 1]; q.x2[0] = seg_xy[4 * s2 + 2]; q.x2[1] = seg_xy[4 * s2 + 3];
+      seg_init(q);
+      double t[2];
+      seg_intersect(q, xp, xc, t);
+      blocked = t[0] >= 0;
+    }
+    if (blocked) continue;
+    Seg q;
+    q.x1[0] = g[0]; q.x1[1] = g[1]; q.x2[0] = g[2]; q.x2[1] = g[3];
+    seg_init(q);
+    const double rx = x - xc[0], ry = y - xc[1];
+    const double cs = (rx * q.normal[0] + ry * q.normal[1]) / std::sqrt(rx * rx + ry * ry);
+    return cs <= 0 ? 1 : 0;
+  }
+  return 0;
+}
+
+// VolumePreloadSource + VolumeSource (sources/VolumePreloadSource.java:44-66,
+// core/source/VolumeSource.java:63-170): per cell (j-major) ceil(den cellVol / spwt) - 1
+// particles uniform in the cell, SampleMaxw3D at max(temp, 50 K); internal points are
+// not added; 1e-6 dt push off.  Returns the particles written (at most cap).
+int orc_preload(int64_t seed, int ni, int nj, const double* x0, const double* dh, int domain, int nseg,
+                const double* seg_xy, const int* seg_btype, double den, double temp, double mass, double spwt,
+                double dt, int cap, double* parts) {
+  JRandom r;
+  r.set_seed(seed);
+  const double v_th = std::sqrt(2 * KB * std::max(temp, 50.0) / mass);
+  Particle* P = reinterpret_cast<Particle*>(parts);
+  int out = 0;
+  for (int j = 0; j < nj - 1; j++)
+    for (int i = 0; i < ni - 1; i++) {
+      double v = dh[0] * dh[1];
+      if (domain == DOM_RZ) v *= 2 * PI * (x0[0] + (i + 0.5) * dh[0]);
+      if (domain == DOM_ZR) v *= 2 * PI * (x0[1] + (j + 0.5) * dh[1]);
+      double num_rem = den * v;
+      while (num_rem > spwt) {
+        const double ip = i + r.nextDouble(), jp = j + r.nextDouble();
+        double vm[3];
+        sample_maxw_3d(r, v_th, vm);
+        num_rem -= spwt;
+        const double px = x0[0] + ip * dh[0], py = x0[1] + jp * dh[1];
+        if (orc_point_internal(nseg, seg_xy, seg_btype, px, py)) continue;
+        if (out >= cap) continue;
+        Particle& p = P[out];
+        memset(&p, 0, sizeof(Particle));
+        p.pos[0] = px;
+        p.pos[1] = py;
+        for (int q = 0; q < 3; q++) p.vel[q] = vm[q];
+        for (int q = 0; q < 3; q++) p.pos[q] += p.vel[q] * 1e-6 * dt;
+        p.lc[0] = (p.pos[0] - x0[0]) / dh[0];
+        p.lc[1] = (p.pos[1] - x0[1]) / dh[1];
+        p.mpw = spwt;
+        p.alive = 1;
+        out++;
+      }
+    }
+  return out;
+}
+
 // --- DSMC (collisions/DSMC.java:194-454; SigmaPlus.java:38-76) ---------------------
 // Single species (mat1 == mat2), fixed weight.  parts: n x 12 (lc used for binning, vel
 // updated in place).  cell_state: per cell (ni-1)*(nj-1) x 2 doubles {sig_cr_max, rem}.

@@ -120,6 +120,10 @@ EXPORTS = {
     "sf_source_maxwellian": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_double, C.c_double,
                                        C.c_double, C.c_double, C.POINTER(C.c_double),
                                        C.POINTER(C.c_int64)]),
+    "sf_source_uniform": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                    C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "sf_source_preload": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                    C.POINTER(C.c_int64)]),
 }
 
 _lib = None

@@ -192,6 +192,24 @@ struct Philox {
   __device__ inline float uniformf() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
 };
 
+__device__ inline void seg_intersect(const Seg4 s, const double p3[2], const double p4[2], double t[2]) {
+  // LinearSegment.intersect + InfiniteLineIntersect (core/boundaries/LinearSegment.java:113-179)
+  const double x1 = s.x, y1 = s.y, x2 = s.z, y2 = s.w;
+  const double x3 = p3[0], y3 = p3[1], x4 = p4[0], y4 = p4[1];
+  double den = (x1 - x2) * (y3 - y4) - (y1 - y2) * (x3 - x4);
+  if (den == 0) { t[0] = -1; t[1] = -1; return; }
+  double xp0 = ((x1 * y2 - y1 * x2) * (x3 - x4) - (x1 - x2) * (x3 * y4 - y3 * x4)) / den;
+  double xp1 = ((x1 * y2 - y1 * x2) * (y3 - y4) - (y1 - y2) * (x3 * y4 - y3 * x4)) / den;
+  if (fabs(x2 - x1) > 1e-6) t[0] = (xp0 - x1) / (x2 - x1);
+  else t[0] = (xp1 - y1) / (y2 - y1);
+  if (t[0] < -FLT_EPS_REF || t[0] > (1 + FLT_EPS_REF)) { t[0] = -1; t[1] = -1; return; }
+  if (fabs(x4 - x3) > 1e-6) t[1] = (xp0 - x3) / (x4 - x3);
+  else t[1] = (xp1 - y3) / (y4 - y3);
+  if (t[1] < -FLT_EPS_REF || t[1] > (1 + FLT_EPS_REF)) { t[0] = -1; t[1] = -1; return; }
+  t[0] = fmin(fmax(t[0], 0.0), 1.0);
+  t[1] = fmin(fmax(t[1], 0.0), 1.0);
+}
+
 // RNG stream identifiers
 enum : uint32_t { RNG_SURFACE = 1, RNG_DSMC = 2, RNG_MCC = 3, RNG_INJECT = 4, RNG_DSMC_HEAVY = 5 };
 

@@ -113,6 +113,26 @@ class KineticMaterial:
         self._src_rem[key] = rem.value
         return n.value
 
+    def sample_uniform_source(self, seg_xy, mdot, v_drift, dt):
+        """UniformSource on one straight segment: mass flow rate mdot (kg/s), cold beam
+        along the segment normal; returns the number of particles added."""
+        key = ("uniform",) + tuple(np.asarray(seg_xy, np.float64).reshape(-1))
+        rem = C.c_double(self._src_rem.get(key, 0.0))
+        seg = np.ascontiguousarray(seg_xy, np.float64).reshape(-1)
+        n = C.c_int64()
+        self.d.check(self.d.lib.sf_source_uniform(self.d.ctx, self.sid, abi.ptr(seg), float(mdot), float(v_drift),
+                                                  float(dt), C.byref(rem), C.byref(n)))
+        self._src_rem[key] = rem.value
+        return n.value
+
+    def preload(self, den, temp, dt):
+        """VolumePreloadSource: fills every cell at density den (m^-3), temperature temp (K);
+        returns the number of particles added."""
+        n = C.c_int64()
+        self.d.check(self.d.lib.sf_source_preload(self.d.ctx, self.sid, float(den), float(temp), float(dt),
+                                                  C.byref(n)))
+        return n.value
+
     def set_surface(self, seg, model, vth=0.0, c_rest=1.0, c_accom=1.0):
         self.d.check(self.d.lib.sf_species_set_surface(self.d.ctx, self.sid, seg, model, vth,
                                                        c_rest, c_accom))

@@ -326,3 +326,38 @@ def test_oracle_mcc_ex_matches_plain_for_mex_cex():
         out = O.mcc_ex(m, B, me, 40 * 1.66e-27, den, z, z, z, T, 1e-20, 5e-8, model, 3)
         assert ca == out["cols"] > 0
         assert np.array_equal(A, B)
+
+
+def test_oracle_point_internal_electrode_box():
+    """BoundaryModule.isInternal on the 9x9 mm electrode box of the ES-PIC mesh: inside,
+    on an edge and outside points."""
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    seg, bt = spec.seg_xy, spec.seg_btype
+    assert O.point_internal(seg, bt, 0.040, 0.020)          # centre
+    assert O.point_internal(seg, bt, 0.0440, 0.0199)        # inside, near the right side
+    assert O.point_internal(seg, bt, 0.0445, 0.020)         # on the right side
+    assert not O.point_internal(seg, bt, 0.0450, 0.020)     # just outside
+    assert not O.point_internal(seg, bt, 0.005, 0.035)      # far away
+
+
+def test_oracle_preload_and_uniform_source_known_answers():
+    """VolumePreloadSource: ceil(den V / spwt) - 1 particles per cell, none inside the
+    electrode, Maxwellian with the 1.2 factor.  UniformSource: the Source.regenerate count
+    and v = normal * v_drift."""
+    spec = W.es_pic_mesh(41, 21, 1e-3)
+    mass, spwt, den, T, dt = 16 * 1.66053886e-27, 1e3, 1e12, 1000.0, 5e-7
+    parts = O.preload(3, spec, den, T, mass, spwt, dt)
+    per_cell = int(np.ceil(den * 1e-6 / spwt)) - 1
+    total = per_cell * 40 * 20
+    inside_frac = (9e-3 * 9e-3) / (40e-3 * 20e-3)
+    assert abs(parts.shape[0] - total * (1 - inside_frac)) < 6 * np.sqrt(total * inside_frac)
+    assert not any(O.point_internal(spec.seg_xy, spec.seg_btype, x, y) for x, y in parts[:2000, 0:2])
+    sig = 1.2 * np.sqrt(2 * 1.3806503e-23 * T / mass) / np.sqrt(2)
+    assert abs(parts[:, 3:6].std() / sig - 1) < 0.02
+    seg = np.array([0.0, 0.02, 0.0, 0.0])  # normal (-dy, dx)/L = (1, 0)
+    mdot, v = 1e-12, 5000.0
+    p1, rem = O.uniform_source(4, seg, mdot, v, mass, spwt, dt)
+    expect = mdot * dt / (mass * spwt)
+    assert p1.shape[0] == int(expect) and rem == pytest.approx(expect - int(expect))
+    assert np.all(p1[:, 3] == v) and np.all(p1[:, 4] == 0) and np.all(p1[:, 5] == 0)
+    assert np.all((p1[:, 1] >= 0) & (p1[:, 1] <= 0.02))

@@ -168,6 +168,17 @@ int sf_species_set_sort_interval(sf_ctx* ctx, int32_t sid, int32_t interval);
  * MaterialInteraction coefficients.  Default for every segment: SF_SURF_ABSORB. */
 int sf_species_set_surface(sf_ctx* ctx, int32_t sid, int32_t seg, int32_t model, double vth,
                            double c_rest, double c_accom);
+/* Species change at a segment (SurfaceInteraction.java:128-142, 175-193, the product
+ * material of MaterialInteraction): a particle of sid that hits seg with model SPECULAR or
+ * DIFFUSE is removed, and (int)(spwt_sid / spwt_product + rnd) particles of product_sid
+ * start from the hit point (the reference's ParticleListSource, emitted with the 1e-6 dt
+ * push off and the -dt/2 rewind): specular ones with the reflected velocity, diffuse ones
+ * each with its own cosine-law direction and a speed from vth_product (the product's
+ * thermal speed at the wall) and the segment's c_rest, c_accom.  Products carry their
+ * species' weight.  product_sid = -1 clears it.  Products past the product's capacity
+ * make sf_push_deposit return SF_ERR_OOM. */
+int sf_species_set_surface_product(sf_ctx* ctx, int32_t sid, int32_t seg, int32_t product_sid,
+                                   double vth_product);
 /* Appends particles from physical positions (KineticMaterial.addParticle, KineticMaterial.java:759-802):
  * lc = XtoL(pos), clamped to the mesh; if rewind != 0 the velocity is rewound by -dt/2
  * with the current electric field (needs sf_set_efield / a Poisson solve first).

@@ -178,6 +178,8 @@ BatchInst make_inst(sf_batch* b, int i) {
   I.sa.counters = c->counters;
   I.sa.stats_slow = c->stats_partial + (size_t)8 * (c->stats_blocks - 1);
   I.sa.stats = 0;  // the batch reports no push totals
+  I.sa.sv.product = nullptr;  // surface products are per context (sf_push_deposit)
+  I.sa.sv.prod = nullptr;
   I.count = sp->count;
   I.slow_idx = c->slow_idx;
   I.nd = sp->nd;

@@ -665,7 +665,7 @@ int sf_ctx_destroy(sf_ctx* ctx) {
     void* ptrs[] = {sp->cur.cell, sp->cur.frac, sp->cur.vxy,  sp->cur.vz,     sp->alt.cell,  sp->alt.frac,
                     sp->alt.vxy,  sp->alt.vz,   sp->count,    sp->mom,        sp->nd,        sp->uvw,
                     sp->seg_model, sp->seg_param, sp->flux,   sp->deposit,    sp->smp.mom2,  sp->smp.mpc,
-                    sp->samp,     sp->gas};
+                    sp->samp,     sp->gas,      sp->seg_product};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     delete sp;
@@ -675,6 +675,8 @@ int sf_ctx_destroy(sf_ctx* ctx) {
                   ctx->stats_partial, ctx->bins, ctx->bins_tmp, ctx->scan_blocks, ctx->dscratch};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (ctx->d_prod) cudaFree(ctx->d_prod);
+  if (ctx->d_prod_added) cudaFree(ctx->d_prod_added);
   if (ctx->host_pinned) cudaFreeHost(ctx->host_pinned);
   for (auto& p : ctx->timer.pending) {
     cudaEventDestroy(p.second.first);
@@ -742,6 +744,35 @@ int sf_species_set_surface(sf_ctx* ctx, int32_t sid, int32_t seg, int32_t model,
   float4 p = make_float4((float)vth, (float)c_rest, (float)c_accom, 0.f);
   copy_wait(sp->seg_model + seg, &model, sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
   copy_wait(sp->seg_param + seg, &p, sizeof(float4), cudaMemcpyHostToDevice, ctx->stream);
+  SF_API_END(ctx)
+}
+
+int sf_species_set_surface_product(sf_ctx* ctx, int32_t sid, int32_t seg, int32_t product_sid, double vth_product) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(seg >= 0 && seg < ctx->nseg, SF_ERR_ARG, "bad segment index");
+  SF_REQUIRE(product_sid == -1 || (product_sid >= 0 && product_sid < (int)ctx->species.size()), SF_ERR_ARG,
+             "bad product species");
+  SF_REQUIRE(product_sid != sid, SF_ERR_ARG, "the product must differ from the impacting species");
+  SF_REQUIRE(product_sid < 0 || vth_product >= 0, SF_ERR_ARG, "vth_product must be >= 0");
+  SF_REQUIRE(ctx->species.size() <= 64, SF_ERR_ARG, "at most 64 species with surface products");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const int ns = std::max(ctx->nseg, 1);
+  if (!sp->seg_product) {
+    SF_CUDA(cudaMalloc(&sp->seg_product, sizeof(int2) * ns));
+    std::vector<int2> none(ns, make_int2(-1, 0));
+    copy_wait(sp->seg_product, none.data(), sizeof(int2) * ns, cudaMemcpyHostToDevice, ctx->stream);
+  }
+  if (!ctx->d_prod) {
+    SF_CUDA(cudaMalloc(&ctx->d_prod, sizeof(ProductView) * 64));
+    SF_CUDA(cudaMalloc(&ctx->d_prod_added, sizeof(unsigned long long) * 64));
+  }
+  const float v = (float)vth_product;
+  int vb;
+  std::memcpy(&vb, &v, sizeof(vb));
+  const int2 e = make_int2(product_sid, vb);
+  copy_wait(sp->seg_product + seg, &e, sizeof(int2), cudaMemcpyHostToDevice, ctx->stream);
+  if (product_sid >= 0) sp->has_products = true;
   SF_API_END(ctx)
 }
 

@@ -96,11 +96,15 @@ struct MeshView {
   int all_delete;               // every domain face removes exiting particles
 };
 
+struct ProductView;
+
 struct SurfaceView {
   const int* model;     // per segment SF_SURF_*
   const float4* param;  // vth, c_rest, c_accom, unused
   double* flux;         // 2 per segment
   double* deposit;      // 2 per segment
+  const int2* product;  // per segment {product species or -1, vth of the product (float bits)}; null: none
+  const ProductView* prod;  // by species index
 };
 
 struct ParticlesView {
@@ -109,6 +113,17 @@ struct ParticlesView {
   float2* vxy;
   float* vz;
   int64_t n;  // slots in use
+};
+
+// A species that surface impacts turn particles into (the ParticleListSource of the
+// product material): its particles from slot P.n, counted in *added.
+struct ProductView {
+  ParticlesView P;
+  int64_t cap;
+  unsigned long long* added;
+  double spwt;       // the product's (uniform) weight
+  float qm_halfdt;   // (q/m) dt/2 of the addParticle rewind
+  float vth;         // unused (the product's wall vth is per segment)
 };
 
 // Per-launch arguments of the push (sf_push.cu) and of its exact surface path.
@@ -239,6 +254,8 @@ struct SfSpecies {
   bool moments_valid = false;
   int* seg_model = nullptr;
   float4* seg_param = nullptr;
+  int2* seg_product = nullptr;  // per segment {product species or -1, product vth bits}; null until set
+  bool has_products = false;
   double* flux = nullptr;     // 2*nseg
   double* deposit = nullptr;  // 2*nseg
   uint32_t step = 0;          // pushes done (RNG counter)
@@ -358,6 +375,10 @@ struct sf_ctx {
   double* host_pinned = nullptr;           // small pinned staging area
   double* dscratch = nullptr;              // ni*nj FP64 scratch (field transfers)
   std::vector<SfSpecies*> species;
+  // surface impacts that change species: the species views (refreshed per push) and
+  // their append counters, allocated by the first sf_species_set_surface_product
+  sf::ProductView* d_prod = nullptr;
+  unsigned long long* d_prod_added = nullptr;
   SfPoisson* poisson = nullptr;
   SfUnet* unet = nullptr;          // learned warm start of the Poisson solve
   std::vector<SfDsmcState*> dsmc;  // per species DSMC cell state

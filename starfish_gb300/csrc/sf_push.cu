@@ -539,6 +539,7 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
     const Seg4 sxy = m.seg_xy[seg_min];
     double n[3], tg[3];
     seg_normal_tangent(sxy, n, tg);
+    const double v_in = sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
     switch (model) {
       case SF_SURF_PASS:
       case SF_SURF_NONE: alive = true; break;
@@ -568,6 +569,50 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
         break;
       }
       default: alive = false; break;  // ABSORB
+    }
+    if (sa.sv.product && (model == SF_SURF_SPECULAR || model == SF_SURF_DIFFUSE)) {
+      const int2 pe = sa.sv.product[seg_min];
+      if (pe.x >= 0) {
+        // species change (SurfaceInteraction.java:128-142, 175-193): the particle leaves
+        // and (int)(spwt / spwt_product + rnd) product particles start from the hit point
+        // (the ParticleListSource of the product, emitted with Source.sampleKinetic's
+        // 1e-6 dt push off and addParticle's rewind): specular ones with the reflected
+        // velocity, diffuse ones each with its own cosine-law direction and speed
+        const ProductView& Q = sa.sv.prod[pe.x];
+        const float vthp = __int_as_float(pe.y);
+        const float4 pr = sa.sv.param[seg_min];
+        const int count = (int)(a.spwt / Q.spwt + rng.uniform());
+        const double hx = sxy.x + tsurf_min * (sxy.z - sxy.x), hy = sxy.y + tsurf_min * (sxy.w - sxy.y);
+        for (int k = 0; k < count; k++) {
+          double v[3] = {vel[0], vel[1], vel[2]};
+          if (model == SF_SURF_DIFFUSE) {
+            const double v_refl = v_in * pr.y;
+            const double v_mag = v_refl + pr.z * ((double)sample_maxw_speed(rng, vthp) - v_refl);
+            float cosphi = sqrtf(1.f - rng.uniformf());
+            if (cosphi > 0.99999f) cosphi = 0.99999f;
+            const float theta = 2.f * (float)PI * rng.uniformf();
+            const float sinphi = sqrtf(1.f - cosphi * cosphi);
+            float st, ct;
+            __sincosf(theta, &st, &ct);
+            const double c_t = (double)(ct * sinphi), c_n = (double)cosphi, c_p = (double)(st * sinphi);
+            const double pz[3] = {0, 0, 1};
+            for (int q = 0; q < 3; q++) v[q] = v_mag * (c_t * tg[q] + c_n * n[q] + c_p * pz[q]);
+          }
+          const double px = hx + v[0] * 1e-6 * a.dt64, py = hy + v[1] * 1e-6 * a.dt64;
+          const int64_t d = Q.P.n + (int64_t)atomicAdd(Q.added, 1ULL);
+          if (d >= Q.cap) continue;  // counted: the host reports the overflow
+          const double lx = fmin(fmax((px - m.x0[0]) * m.inv_dh[0], 0.0), m.ni - 1.0);
+          const double ly = fmin(fmax((py - m.x0[1]) * m.inv_dh[1], 0.0), m.nj - 1.0);
+          const int ci = min((int)lx, m.ni - 2), cj = min((int)ly, m.nj - 2);
+          const float fx = (float)(lx - ci), fy = (float)(ly - cj);
+          const float2 e = gather_E(m, ci, cj, fx, fy);
+          Q.P.cell[d] = pack_cell(ci, cj);
+          Q.P.frac[d] = make_float2(fx, fy);
+          Q.P.vxy[d] = make_float2((float)v[0] - Q.qm_halfdt * e.x, (float)v[1] - Q.qm_halfdt * e.y);
+          Q.P.vz[d] = (float)v[2];
+        }
+        alive = false;
+      }
     }
     if (!alive) atomicAdd(&sa.stats_slow[5], a.spwt * a.charge);
     if (m.seg_btype[seg_min] == SF_BT_SINK) alive = false;
@@ -1313,6 +1358,26 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
     sa.counters = sc.counters;
     sa.stats_slow = slow_stats;
     sa.stats = want_stats ? 1 : 0;
+    sa.sv.product = nullptr;
+    sa.sv.prod = nullptr;
+    if (sp->has_products) {
+      // the species' current views (the sort swaps buffers) and zeroed append counters
+      std::vector<ProductView> pv(ctx->species.size());
+      for (size_t q = 0; q < pv.size(); q++) {
+        const SfSpecies* o = ctx->species[q];
+        pv[q].P = o->cur;
+        pv[q].P.n = o->n;
+        pv[q].cap = o->cap;
+        pv[q].added = ctx->d_prod_added + q;
+        pv[q].spwt = o->spwt;
+        pv[q].qm_halfdt = (float)(o->charge / o->mass * 0.5 * dt);
+        pv[q].vth = 0.f;
+      }
+      SF_CUDA(cudaMemcpyAsync(ctx->d_prod, pv.data(), sizeof(ProductView) * pv.size(), cudaMemcpyHostToDevice, s));
+      SF_CUDA(cudaMemsetAsync(ctx->d_prod_added, 0, sizeof(unsigned long long) * pv.size(), s));
+      sa.sv.product = sp->seg_product;
+      sa.sv.prod = ctx->d_prod;
+    }
     const int sgrid = ctx->num_sms * 16;
     TimedScope ts(ctx, "push_slow");
     ctx->launches++;
@@ -1357,6 +1422,24 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   SF_CUDA(cudaStreamSynchronize(s));
   timer_collect(ctx);
   sp->n_dead += (int64_t)hc[1];
+  if (sp->has_products) {
+    // product particles appended by surface impacts
+    std::vector<unsigned long long> added(ctx->species.size());
+    copy_wait(added.data(), ctx->d_prod_added, sizeof(unsigned long long) * added.size(), cudaMemcpyDeviceToHost, s);
+    bool over = false;
+    for (size_t q = 0; q < added.size(); q++) {
+      SfSpecies* o = ctx->species[q];
+      const int64_t room = o->cap - o->n;
+      const int64_t k = std::min<int64_t>((int64_t)added[q], room);
+      over |= (int64_t)added[q] > room;
+      if (k > 0) {
+        o->n += k;
+        o->cur.n = o->n;
+        o->sorted = false;
+      }
+    }
+    SF_REQUIRE(!over, SF_ERR_OOM, "surface products exceeded a species' capacity (the excess was dropped)");
+  }
   sp->step++;
   sp->pushes_since_sort++;
   sp->moments_valid = mom;

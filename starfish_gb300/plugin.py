@@ -137,6 +137,13 @@ class KineticMaterial:
         self.d.check(self.d.lib.sf_species_set_surface(self.d.ctx, self.sid, seg, model, vth,
                                                        c_rest, c_accom))
 
+    def set_surface_product(self, seg, product: "KineticMaterial", vth_product=0.0):
+        """Species change at segment seg (SPECULAR or DIFFUSE impacts emit the product
+        species); product None clears it."""
+        self.d.check(self.d.lib.sf_species_set_surface_product(self.d.ctx, self.sid, seg,
+                                                               -1 if product is None else product.sid,
+                                                               float(vth_product)))
+
     def set_sort_interval(self, k):
         self.d.check(self.d.lib.sf_species_set_sort_interval(self.d.ctx, self.sid, int(k)))
 

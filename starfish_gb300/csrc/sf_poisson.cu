@@ -1207,14 +1207,16 @@ __device__ void bp_prefix(int n, F val, int* __restrict__ out) {
 
 // The live instances (act_list, *act_cnt) and, for every kind k, the prefix of their
 // blocks (act_start + k (n + 1)) and its total (act_total[k]).  tab + koff[k] is the
-// static block prefix of kind k over all instances.  One block.
-__global__ void __launch_bounds__(1024) kb_compact(const BPInst* I, int n, const int* __restrict__ tab,
-                                                   const int* __restrict__ koff, int nkinds, int* act_pos,
-                                                   int* act_list, int* act_cnt, int* act_start,
-                                                   int* act_total) {
-  bp_prefix(n, [&](int i) { return I[i].live ? 1 : 0; }, act_pos);
-  for (int i = threadIdx.x; i < n; i += blockDim.x)
-    if (I[i].live) act_list[act_pos[i]] = i;
+// static block prefix of kind k over all instances.  The list follows order[] (the
+// instances by decreasing coarse-cycle size: the longest single-CTA cycles start first).
+// One block.
+__global__ void __launch_bounds__(1024) kb_compact(const BPInst* I, int n, const int* __restrict__ order,
+                                                   const int* __restrict__ tab, const int* __restrict__ koff,
+                                                   int nkinds, int* act_pos, int* act_list, int* act_cnt,
+                                                   int* act_start, int* act_total) {
+  bp_prefix(n, [&](int q) { return I[order[q]].live ? 1 : 0; }, act_pos);
+  for (int q = threadIdx.x; q < n; q += blockDim.x)
+    if (I[order[q]].live) act_list[act_pos[q]] = order[q];
   const int cnt = act_pos[n];
   if (threadIdx.x == 0) *act_cnt = cnt;
   __syncthreads();
@@ -1528,6 +1530,7 @@ struct BatchPoisson {
   BPInst* d_inst = nullptr;
   int* d_tab = nullptr;   // static block prefixes of every kind, n + 1 each
   int* d_koff = nullptr;  // offset of each kind's prefix in d_tab
+  int* d_order = nullptr;  // instances by decreasing coarse-cycle size
   int* d_iters = nullptr;
   int* d_run = nullptr;
   BPParams* d_prm = nullptr;
@@ -1562,8 +1565,8 @@ static int bp_grid(const BatchPoisson* bp, int kind) {
 }
 
 static void bp_compact(BatchPoisson* bp, cudaStream_t s) {
-  kb_compact<<<1, 1024, 0, s>>>(bp->d_inst, bp->n, bp->d_tab, bp->d_koff, bp->nkinds, bp->d_act_pos,
-                                bp->d_act_list, bp->d_act_cnt, bp->d_act_start, bp->d_act_total);
+  kb_compact<<<1, 1024, 0, s>>>(bp->d_inst, bp->n, bp->d_order, bp->d_tab, bp->d_koff, bp->nkinds,
+                                bp->d_act_pos, bp->d_act_list, bp->d_act_cnt, bp->d_act_start, bp->d_act_total);
 }
 
 static void bp_vcycle(BatchPoisson* bp, cudaStream_t s, int kmin) {
@@ -1757,6 +1760,11 @@ BatchPoisson* batch_poisson_create(sf_ctx* const* ctxs, int n, int num_sms, cuda
     copy_wait(bp->d_tab, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, stream);
     SF_CUDA(cudaMalloc(&bp->d_koff, sizeof(int) * bp->nkinds));
     copy_wait(bp->d_koff, bp->koff.data(), sizeof(int) * bp->nkinds, cudaMemcpyHostToDevice, stream);
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return ps[x]->cd.total > ps[y]->cd.total; });
+    SF_CUDA(cudaMalloc(&bp->d_order, sizeof(int) * n));
+    copy_wait(bp->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, stream);
     SF_CUDA(cudaMalloc(&bp->d_act_pos, sizeof(int) * (n + 1)));
     SF_CUDA(cudaMalloc(&bp->d_act_list, sizeof(int) * n));
     SF_CUDA(cudaMalloc(&bp->d_act_cnt, sizeof(int)));
@@ -1782,8 +1790,9 @@ void batch_poisson_destroy(BatchPoisson* bp) {
   if (!bp) return;
   if (bp->stream) cudaStreamSynchronize(bp->stream);
   for (auto& g : bp->graphs) cudaGraphExecDestroy(g.second);
-  void* ptrs[] = {bp->d_inst, bp->d_tab,      bp->d_koff,     bp->d_iters,     bp->d_run,       bp->d_prm,
-                  bp->d_stat, bp->d_act_pos, bp->d_act_list, bp->d_act_cnt, bp->d_act_start, bp->d_act_total};
+  void* ptrs[] = {bp->d_inst,      bp->d_tab,       bp->d_koff,      bp->d_order,     bp->d_iters,
+                  bp->d_run,       bp->d_prm,       bp->d_stat,      bp->d_act_pos,   bp->d_act_list,
+                  bp->d_act_cnt,   bp->d_act_start, bp->d_act_total};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (bp->ev0) cudaEventDestroy(bp->ev0);

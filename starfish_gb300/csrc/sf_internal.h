@@ -203,6 +203,13 @@ struct Philox {
     for (int k = 0; k < 12; k++) s += bits53();
     return 0.7071067811865476 * ((double)s * (1.0 / 9007199254740992.0) - 6.0);
   }
+  // the same sampler from 24-bit uniforms in FP32 (for velocities stored as FP32 anyway):
+  // the integer sum is exact and rounded once
+  __device__ inline float maxw1d_unit_f() {
+    uint32_t s = 0;
+    for (int k = 0; k < 12; k++) s += next_u32() >> 8;
+    return 0.70710678f * ((float)s * (1.0f / 16777216.0f) - 6.0f);
+  }
   // uniform in [0,1) with 24 random bits
   __device__ inline float uniformf() { return (float)(next_u32() >> 8) * (1.0f / 16777216.0f); }
 };

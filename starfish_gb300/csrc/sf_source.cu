@@ -41,7 +41,6 @@ __device__ inline double frustum_t(double f, double r1, double r2) {
   return f * S / (r1 + sqrt(r1 * r1 + (r2 - r1) * f * S));
 }
 
-__device__ inline double maxw1d_unit(Philox& r) { return r.maxw1d_unit(); }
 
 // Particle k of this step's injection on the segment of a; appended at a.base + slot.
 __device__ __forceinline__ void inject_one(const MeshView& m, const ParticlesView& P, const InjectArgs& a, int64_t k,
@@ -55,17 +54,24 @@ __device__ __forceinline__ void inject_one(const MeshView& m, const ParticlesVie
     vx = a.nx * a.v_drift;
     vy = a.ny * a.v_drift;
   } else {
+    // the velocity is stored in FP32: drawn in FP32 (the reference's part.dt draw, which
+    // addParticle overwrites, is skipped)
+    const float vt = (float)(a.v_th * 1.2), dx = (float)(a.nx * a.v_drift), dy = (float)(a.ny * a.v_drift);
+    const float nx = (float)a.nx, ny = (float)a.ny;
+    float fvx = 0.f, fvy = 0.f, fvz = 0.f;
     for (int tries = 0; tries < 64; tries++) {
-      vx = (a.v_th * 1.2) * maxw1d_unit(rng) + a.nx * a.v_drift;
-      vy = (a.v_th * 1.2) * maxw1d_unit(rng) + a.ny * a.v_drift;
-      vz = (a.v_th * 1.2) * maxw1d_unit(rng);
-      (void)rng.uniform();  // part.dt = rnd * dt, overwritten by addParticle
-      if (a.nx * vx + a.ny * vy > 0) break;
+      fvx = vt * rng.maxw1d_unit_f() + dx;
+      fvy = vt * rng.maxw1d_unit_f() + dy;
+      fvz = vt * rng.maxw1d_unit_f();
+      if (nx * fvx + ny * fvy > 0.f) break;
     }
+    vx = fvx;
+    vy = fvy;
+    vz = fvz;
   }
   px += vx * 1e-6 * a.dt;
   py += vy * 1e-6 * a.dt;
-  double lx = (px - m.x0[0]) / m.dh[0], ly = (py - m.x0[1]) / m.dh[1];
+  double lx = (px - m.x0[0]) * m.inv_dh[0], ly = (py - m.x0[1]) * m.inv_dh[1];
   if (!(lx >= 0 && ly >= 0 && lx <= m.ni - 1 && ly <= m.nj - 1)) return;  // outside every mesh
   int i = (int)lx, j = (int)ly;
   if (i > m.ni - 2) i = m.ni - 2;

@@ -155,3 +155,55 @@ def test_solves_independent_of_other_contexts(gpulib):
     finally:
         a.close()
         b.close()
+
+
+def test_failures_reported_and_context_usable(gpulib):
+    """Failure detection without a GPU fault: a NaN in rho gives SF_ERR_DIVERGED, too few
+    Newton steps SF_ERR_NOT_CONVERGED (the Java caller then falls back to its own solver);
+    either way the context solves normally afterwards."""
+    from starfish_gb300.plugin import GpuDomain, PoissonSolver
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    rho = ion_rho(spec, 4)
+    dom = GpuDomain(spec)
+    try:
+        bad = rho.copy()
+        bad[spec.nn // 2 + 10] = np.nan
+        _, st = PoissonSolver(dom, tol=1e-6, max_it=60).solve(rho=bad, phi=np.zeros(spec.nn), check=False)
+        assert st["status"] == abi.SF_ERR_DIVERGED
+        _, st = PoissonSolver(dom, tol=1e-6, max_it=1).solve(rho=rho, phi=np.zeros(spec.nn), check=False)
+        assert st["status"] == abi.SF_ERR_NOT_CONVERGED and st["newton_it"] == 1
+        phi, st = PoissonSolver(dom, tol=1e-6, max_it=60).solve(rho=rho, phi=np.zeros(spec.nn))
+        assert st["status"] == 0 and st["residual"] < 1e-6 and np.all(np.isfinite(phi))
+    finally:
+        dom.close()
+
+
+def test_batch_failure_names_instance_and_batch_recovers(gpulib):
+    """A batched solve that cannot converge in its Newton budget fails the step with the
+    instance named; the batch then steps normally with a sufficient budget."""
+    from starfish_gb300.plugin import GpuBatch, GpuDomain, KineticMaterial, PoissonSolver
+    cases = W.config4(3, seed=5, max_particles=20_000, min_particles=10_000)
+    doms, kms, sol = [], [], []
+    for c in cases:
+        d = GpuDomain(c.mesh)
+        ps = PoissonSolver(d, n0=1e12, Te0=2.0, tol=1e-6, max_it=60)
+        ps.solve(rho=np.zeros(c.mesh.nn), phi=np.zeros(c.mesh.nn))
+        ps.update_gradient_field()
+        km = KineticMaterial(d, c.ion.mass, c.ion.charge, c.ion.spwt, capacity=3 * c.n_particles)
+        pos, vel = W.uniform_maxwellian(c.mesh, c.ion, c.n_particles, c.seed)
+        km.add_particles(pos, vel, rewind=True, dt=5e-7)
+        doms.append(d)
+        kms.append(km)
+        sol.append(ps)
+    batch = GpuBatch(doms, kms, threads=2)
+    try:
+        strict = PoissonSolver(doms[0], n0=1e12, Te0=2.0, tol=1e-14, max_it=2)
+        with pytest.raises(abi.SfError) as e:
+            batch.step(5e-7, strict)
+        assert e.value.code == abi.SF_ERR_NOT_CONVERGED and "instance" in str(e.value)
+        st = batch.step(5e-7, sol[0])
+        assert st["particles"] > 0
+    finally:
+        batch.close()
+        for d in doms:
+            d.close()

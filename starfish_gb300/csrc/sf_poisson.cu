@@ -96,13 +96,25 @@ __device__ __forceinline__ float gs_value(uint8_t t, const float* y, float r, fl
 
 // full weighting inside, injection on the boundary rows (halved: the scaled open-face
 // row of a grid twice as coarse carries half the weight), zero on fixed coarse nodes
-__device__ __forceinline__ float restrict_value(const float* tf, uint8_t tc, int I, int J, int nif, int nic, int njc) {
+// (tf indexed at the coarse node's fine position u with row stride nif)
+__device__ __forceinline__ float restrict_at(const float* tf, int u, int nif, uint8_t tc, bool edge) {
   if (tc == NC_FIXED) return 0.f;
-  const int i = 2 * I, j = 2 * J;
-  const int u = j * nif + i;
-  if (I == 0 || J == 0 || I == nic - 1 || J == njc - 1) return 0.5f * tf[u];
+  if (edge) return 0.5f * tf[u];
   return 0.0625f * (4.f * tf[u] + 2.f * (tf[u - 1] + tf[u + 1] + tf[u - nif] + tf[u + nif]) +
                     (tf[u - nif - 1] + tf[u - nif + 1] + tf[u + nif - 1] + tf[u + nif + 1]));
+}
+
+__device__ __forceinline__ float restrict_value(const float* tf, uint8_t tc, int I, int J, int nif, int nic, int njc) {
+  return restrict_at(tf, (2 * J) * nif + 2 * I, nif, tc, I == 0 || J == 0 || I == nic - 1 || J == njc - 1);
+}
+
+// the same from the four coarse values around fine node (i, j): a = (I, J), b = (I + 1, J),
+// c = (I, J + 1), d = (I + 1, J + 1), the ones outside the stencil unused
+__device__ __forceinline__ float prolong_of(float a, float b, float c, float d, bool oi, bool oj) {
+  if (!oi && !oj) return a;
+  if (oi && !oj) return 0.5f * (a + b);
+  if (!oi && oj) return 0.5f * (a + c);
+  return 0.25f * (a + b + c + d);
 }
 
 __device__ __forceinline__ float prolong_value(const float* yc, int i, int j, int nic) {
@@ -144,6 +156,145 @@ __global__ void k_restrict(LevelView F, LevelView Cl) {
   const int uc = J * Cl.ni + I;
   Cl.r[uc] = restrict_value(F.t, Cl.type[uc], I, J, F.ni, Cl.ni, Cl.nj);
   Cl.y[uc] = 0.f;
+}
+
+// ------------------------------------------------------------------------------------
+// tiled V(2,2) level kernels: one launch per level on the way down (pre-smoothing from
+// zero, residual, restriction) and one on the way up (prolongation, post-smoothing)
+// ------------------------------------------------------------------------------------
+// A block holds its TX x TY tile plus a halo of H nodes (r, P, type, y) in shared memory
+// and runs the level's two red-black Gauss-Seidel sweeps there.  A half-sweep updates a
+// node from its four neighbours only, so after half-sweep s the values are those of the
+// global sweeps on [s, W - s) of the window: with H = 4 the tile's own nodes come out as
+// in four global half-sweeps (same inputs, same arithmetic); H = 6 leaves one more ring
+// for the residual and one for the full-weighting stencil.  Tiles start on even
+// coordinates, so a node's colour is the parity of its window coordinates.
+constexpr int TILE_NT = 256;
+constexpr uint8_t TILE_OUT = 0xFF;  // window node outside the mesh
+
+// four half-sweeps, colours first, 1 - first, first, 1 - first
+template <int WX, int WY>
+__device__ __forceinline__ void tile_sweeps(float* sy, const float* sr, const float* sp, const uint8_t* st, int first,
+                                            float cx, float cy) {
+  constexpr int NI = WX / 2 * WY;
+  for (int s = 0; s < 4; s++) {
+    const int color = (first + s) & 1, lo = s + 1;
+#pragma unroll
+    for (int k0 = 0; k0 < NI; k0 += TILE_NT) {
+      const int k = k0 + threadIdx.x;
+      if (k < NI) {
+        const int ly = k / (WX / 2), lx = 2 * (k % (WX / 2)) + ((ly + color) & 1);
+        if (lx >= lo && lx < WX - lo && ly >= lo && ly < WY - lo) {
+          const int q = ly * WX + lx;
+          const uint8_t t = st[q];
+          if (t != TILE_OUT) sy[q] = gs_value(t, sy, sr[q], sp[q], q, WX, cx, cy);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// pre-smoothing of level F from y = 0, its residual, and the restriction of that to C.r
+// (every V-cycle starts each level's correction from zero, so y is not read)
+template <int TX, int TY>
+__global__ void __launch_bounds__(TILE_NT) k_level_down(LevelView F, LevelView C) {
+  constexpr int H = 6, WX = TX + 2 * H, WY = TY + 2 * H, NW = WX * WY, NL = (NW + TILE_NT - 1) / TILE_NT;
+  __shared__ float sy[NW], sr[NW], sp[NW];
+  __shared__ uint8_t st[NW];
+  const int gi0 = blockIdx.x * TX - H, gj0 = blockIdx.y * TY - H;
+  float vr[NL], vp[NL];
+  uint8_t vt[NL];
+#pragma unroll
+  for (int k = 0; k < NL; k++) {
+    const int q = threadIdx.x + k * TILE_NT;
+    const int gi = gi0 + q % WX, gj = gj0 + q / WX;
+    const bool in = q < NW && gi >= 0 && gi < F.ni && gj >= 0 && gj < F.nj;
+    const int u = in ? gj * F.ni + gi : 0;
+    vr[k] = F.r[u];
+    vp[k] = F.P[u];
+    vt[k] = in ? F.type[u] : TILE_OUT;
+  }
+#pragma unroll
+  for (int k = 0; k < NL; k++) {
+    const int q = threadIdx.x + k * TILE_NT;
+    if (q < NW) {
+      sy[q] = 0.f;
+      sr[q] = vr[k];
+      sp[q] = vp[k];
+      st[q] = vt[k];
+    }
+  }
+  __syncthreads();
+  tile_sweeps<WX, WY>(sy, sr, sp, st, 0, F.cx, F.cy);
+  // the tile's y (read back by the prolongation), and the residual on it plus one ring,
+  // in place of r (a node reads only its own r)
+  for (int k = threadIdx.x; k < TX * TY; k += TILE_NT) {
+    const int gi = blockIdx.x * TX + k % TX, gj = blockIdx.y * TY + k / TX;
+    if (gi < F.ni && gj < F.nj) F.y[gj * F.ni + gi] = sy[(k / TX + H) * WX + k % TX + H];
+  }
+  constexpr int RX = TX + 2, RY = TY + 2;
+  for (int k = threadIdx.x; k < RX * RY; k += TILE_NT) {
+    const int q = (k / RX + H - 1) * WX + k % RX + H - 1;
+    const uint8_t t = st[q];
+    if (t != TILE_OUT) sr[q] = sr[q] - apply_J(t, sy, sp[q], q, WX, F.cx, F.cy);
+  }
+  __syncthreads();
+  constexpr int CX = TX / 2, CY = TY / 2;
+  for (int k = threadIdx.x; k < CX * CY; k += TILE_NT) {
+    const int I = blockIdx.x * CX + k % CX, J = blockIdx.y * CY + k / CX;
+    if (I >= C.ni || J >= C.nj) continue;
+    const int uc = J * C.ni + I;
+    const int q = (2 * (k / CX) + H) * WX + 2 * (k % CX) + H;
+    C.r[uc] = restrict_at(sr, q, WX, C.type[uc], I == 0 || J == 0 || I == C.ni - 1 || J == C.nj - 1);
+  }
+}
+
+// F.y += prolongation of C.y (not on fixed nodes), then the post-smoothing
+template <int TX, int TY>
+__global__ void __launch_bounds__(TILE_NT) k_level_up(LevelView F, LevelView C) {
+  constexpr int H = 4, WX = TX + 2 * H, WY = TY + 2 * H, NW = WX * WY, NL = (NW + TILE_NT - 1) / TILE_NT;
+  __shared__ float sy[NW], sr[NW], sp[NW];
+  __shared__ uint8_t st[NW];
+  const int gi0 = blockIdx.x * TX - H, gj0 = blockIdx.y * TY - H;
+  float vy[NL], vr[NL], vp[NL], ca[NL], cb[NL], cc[NL], cd[NL];
+  uint8_t vt[NL];
+#pragma unroll
+  for (int k = 0; k < NL; k++) {
+    const int q = threadIdx.x + k * TILE_NT;
+    const int gi = gi0 + q % WX, gj = gj0 + q / WX;
+    const bool in = q < NW && gi >= 0 && gi < F.ni && gj >= 0 && gj < F.nj;
+    const int u = in ? gj * F.ni + gi : 0;
+    vy[k] = F.y[u];
+    vr[k] = F.r[u];
+    vp[k] = F.P[u];
+    vt[k] = in ? F.type[u] : TILE_OUT;
+    const int I = in ? gi >> 1 : 0, J = in ? gj >> 1 : 0;
+    const int I1 = min(I + 1, C.ni - 1), J1 = min(J + 1, C.nj - 1);
+    ca[k] = C.y[J * C.ni + I];
+    cb[k] = C.y[J * C.ni + I1];
+    cc[k] = C.y[J1 * C.ni + I];
+    cd[k] = C.y[J1 * C.ni + I1];
+  }
+#pragma unroll
+  for (int k = 0; k < NL; k++) {
+    const int q = threadIdx.x + k * TILE_NT;
+    if (q < NW) {
+      const int gi = gi0 + q % WX, gj = gj0 + q / WX;
+      float y = vy[k];
+      if (vt[k] != TILE_OUT && vt[k] != NC_FIXED) y += prolong_of(ca[k], cb[k], cc[k], cd[k], gi & 1, gj & 1);
+      sy[q] = y;
+      sr[q] = vr[k];
+      sp[q] = vp[k];
+      st[q] = vt[k];
+    }
+  }
+  __syncthreads();
+  tile_sweeps<WX, WY>(sy, sr, sp, st, 1, F.cx, F.cy);
+  for (int k = threadIdx.x; k < TX * TY; k += TILE_NT) {
+    const int gi = blockIdx.x * TX + k % TX, gj = blockIdx.y * TY + k / TX;
+    if (gi < F.ni && gj < F.nj) F.y[gj * F.ni + gi] = sy[(k / TX + H) * WX + k % TX + H];
+  }
 }
 
 __global__ void k_prolong(LevelView Cl, LevelView F) {
@@ -332,9 +483,11 @@ __device__ inline void block_sum_max_max(double a, double b, double c, double* p
 // and P go to the FP32 level 0; per block sum F^2, max |F| of the unscaled F and the
 // largest error bound of an FP32 exponential.
 // The Laplacian is FP64 (its terms cancel to ~1e-14 of their size at the tolerance);
-// the Boltzmann term is small next to them and its exponential is taken in FP32 unless
-// a.fp64_exp: its relative error is at most |arg| 2^-24 (rounding of the argument) plus
-// 2^-22, and the host switches to FP64 when that bound could reach the tolerance.
+// the Boltzmann term is small next to them and is taken in FP32 (exponential, its
+// coefficient and P; the FP64 pipe is the kernel's bound) unless a.fp64_exp or its
+// value leaves the FP32 range: its relative error is at most |arg| 2^-24 (rounding of
+// the argument) plus 2^-22 (expf) plus 2^-23 (the FP32 coefficient and product), and the
+// host switches to FP64 when that bound could reach the tolerance.
 // Blocks bidx = 0..G-1 of one mesh (the single and the batched launch share it, so that
 // the partial sums, and with them every reduction, are the same bit for bit).
 __device__ __forceinline__ void nl_residual_body(const NlArgs& a, const double* __restrict__ x,
@@ -342,11 +495,14 @@ __device__ __forceinline__ void nl_residual_body(const NlArgs& a, const double* 
                                                  float* __restrict__ F32, float* __restrict__ P32,
                                                  double* __restrict__ partial, int bidx, int G) {
   const int n = a.ni * a.nj;
-  double s2 = 0.0, smax = 0.0, emax = 0.0;
+  const float Cf = (float)a.C_n0, kf = (float)a.inv_kTe;
+  double s2 = 0.0, smax = 0.0;
+  float emax = 0.f;
   for (int u = bidx * RB + threadIdx.x; u < n; u += G * RB) {
     const uint8_t t = type[u];
     const double xc = x[u];
-    double F, Fs, P = 0.0;
+    double F, Fs;
+    float P = 0.f;
     switch (t) {
       case NC_FIXED: F = Fs = xc - b0[u]; break;
       case NC_NLEFT: F = (x[u + 1] - xc) / a.dx; Fs = F / a.dx; break;
@@ -358,23 +514,26 @@ __device__ __forceinline__ void nl_residual_body(const NlArgs& a, const double* 
         double ex = 0.0;
         if (!a.linear) {
           const double arg = (xc - a.phi0) * a.inv_kTe;
-          if (a.fp64_exp || arg > 80.0) {
-            ex = a.C_n0 * exp(arg);
+          const float argf = (float)arg;
+          const float exf = (a.fp64_exp || arg > 80.0) ? INFINITY : Cf * expf(argf);
+          if (exf <= 3.0e38f) {
+            ex = (double)exf;
+            P = exf * kf;
+            emax = fmaxf(emax, exf * (fabsf(argf) * 5.9604645e-8f + 3.5762787e-7f));
           } else {
-            ex = a.C_n0 * (double)expf((float)arg);
-            emax = fmax(emax, ex * (fabs(arg) * 5.9604645e-8 + 2.3841858e-7));
+            ex = a.C_n0 * exp(arg);
+            P = (float)(ex * a.inv_kTe);
           }
-          P = ex * a.inv_kTe;
         }
         F = Fs = Ax - (b0[u] + ex);
       }
     }
     F32[u] = (float)Fs;
-    P32[u] = (float)P;
+    P32[u] = P;
     s2 += F * F;
     smax = fmax(smax, fabs(F));
   }
-  block_sum_max_max(s2, smax, emax, partial, bidx);
+  block_sum_max_max(s2, smax, (double)emax, partial, bidx);
 }
 
 __global__ void __launch_bounds__(RB) k_nl_residual(NlArgs a, const double* __restrict__ x,
@@ -774,9 +933,31 @@ static void smooth(sf_ctx* ctx, const LevelView& L, int nu, int first) {
   }
 }
 
+// one tiled level kernel: 64 x 16 tiles on levels of a million nodes or more, 32 x 8 below
+// (shorter per-block chains where the grid is too small to fill the GPU)
+static void level_down(cudaStream_t s, const LevelView& F, const LevelView& C) {
+  if ((size_t)F.ni * F.nj >= (1u << 20))
+    k_level_down<64, 16><<<dim3((F.ni + 63) / 64, (F.nj + 15) / 16), TILE_NT, 0, s>>>(F, C);
+  else
+    k_level_down<32, 8><<<dim3((F.ni + 31) / 32, (F.nj + 7) / 8), TILE_NT, 0, s>>>(F, C);
+}
+static void level_up(cudaStream_t s, const LevelView& F, const LevelView& C) {
+  if ((size_t)F.ni * F.nj >= (1u << 20))
+    k_level_up<64, 16><<<dim3((F.ni + 63) / 64, (F.nj + 15) / 16), TILE_NT, 0, s>>>(F, C);
+  else
+    k_level_up<32, 8><<<dim3((F.ni + 31) / 32, (F.nj + 7) / 8), TILE_NT, 0, s>>>(F, C);
+}
+
 static void vcycle(sf_ctx* ctx, SfPoisson* ps, int nu1, int nu2) {
   cudaStream_t s = ctx->stream;
   const dim3 blk(32, 8);
+  if (nu1 == 2 && nu2 == 2) {
+    for (int l = 0; l < ps->cs; l++) level_down(s, ps->lv[l], ps->lv[l + 1]);
+    k_coarse_vcycle<<<1, 1024, ps->coarse_smem, s>>>(ps->cd, ps->lv[ps->cs], nu1, nu2);
+    for (int l = ps->cs - 1; l >= 0; l--) level_up(s, ps->lv[l], ps->lv[l + 1]);
+    ctx->launches += 2 * ps->cs + 1;
+    return;
+  }
   if (ps->cs > 0) SF_CUDA(cudaMemsetAsync(ps->lv[0].y, 0, 4 * (size_t)ps->lv[0].ni * ps->lv[0].nj, s));
   for (int l = 0; l < ps->cs; l++) {
     const LevelView& L = ps->lv[l];

@@ -42,7 +42,7 @@ struct LevelView {
   float* y;
   float* r;
   float* P;
-  float* t;      // residual scratch
+  float* t;  // residual scratch of the batched global-sweep levels
   const uint8_t* type;
 };
 
@@ -128,37 +128,6 @@ __device__ __forceinline__ float prolong_value(const float* yc, int i, int j, in
 }
 
 // ------------------------------------------------------------------------------------
-// global-memory level kernels
-// ------------------------------------------------------------------------------------
-// one colour of a red-black Gauss-Seidel sweep: nodes with (i + j) & 1 == color
-__global__ void k_smooth(LevelView L, int color) {
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= L.nj) return;
-  const int i = 2 * k + ((j + color) & 1);
-  if (i >= L.ni) return;
-  const int u = j * L.ni + i;
-  L.y[u] = gs_value(L.type[u], L.y, L.r[u], L.P[u], u, L.ni, L.cx, L.cy);
-}
-
-__global__ void k_resid(LevelView L) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= L.ni || j >= L.nj) return;
-  const int u = j * L.ni + i;
-  L.t[u] = L.r[u] - apply_J(L.type[u], L.y, L.P[u], u, L.ni, L.cx, L.cy);
-}
-
-__global__ void k_restrict(LevelView F, LevelView Cl) {
-  const int I = blockIdx.x * blockDim.x + threadIdx.x;
-  const int J = blockIdx.y * blockDim.y + threadIdx.y;
-  if (I >= Cl.ni || J >= Cl.nj) return;
-  const int uc = J * Cl.ni + I;
-  Cl.r[uc] = restrict_value(F.t, Cl.type[uc], I, J, F.ni, Cl.ni, Cl.nj);
-  Cl.y[uc] = 0.f;
-}
-
-// ------------------------------------------------------------------------------------
 // tiled V(2,2) level kernels: one launch per level on the way down (pre-smoothing from
 // zero, residual, restriction) and one on the way up (prolongation, post-smoothing)
 // ------------------------------------------------------------------------------------
@@ -198,11 +167,11 @@ __device__ __forceinline__ void tile_sweeps(float* sy, const float* sr, const fl
 // pre-smoothing of level F from y = 0, its residual, and the restriction of that to C.r
 // (every V-cycle starts each level's correction from zero, so y is not read)
 template <int TX, int TY>
-__global__ void __launch_bounds__(TILE_NT) k_level_down(LevelView F, LevelView C) {
+__device__ __forceinline__ void level_down_body(const LevelView F, const LevelView C, int bx, int by) {
   constexpr int H = 6, WX = TX + 2 * H, WY = TY + 2 * H, NW = WX * WY, NL = (NW + TILE_NT - 1) / TILE_NT;
   __shared__ float sy[NW], sr[NW], sp[NW];
   __shared__ uint8_t st[NW];
-  const int gi0 = blockIdx.x * TX - H, gj0 = blockIdx.y * TY - H;
+  const int gi0 = bx * TX - H, gj0 = by * TY - H;
   float vr[NL], vp[NL];
   uint8_t vt[NL];
 #pragma unroll
@@ -230,7 +199,7 @@ __global__ void __launch_bounds__(TILE_NT) k_level_down(LevelView F, LevelView C
   // the tile's y (read back by the prolongation), and the residual on it plus one ring,
   // in place of r (a node reads only its own r)
   for (int k = threadIdx.x; k < TX * TY; k += TILE_NT) {
-    const int gi = blockIdx.x * TX + k % TX, gj = blockIdx.y * TY + k / TX;
+    const int gi = bx * TX + k % TX, gj = by * TY + k / TX;
     if (gi < F.ni && gj < F.nj) F.y[gj * F.ni + gi] = sy[(k / TX + H) * WX + k % TX + H];
   }
   constexpr int RX = TX + 2, RY = TY + 2;
@@ -242,7 +211,7 @@ __global__ void __launch_bounds__(TILE_NT) k_level_down(LevelView F, LevelView C
   __syncthreads();
   constexpr int CX = TX / 2, CY = TY / 2;
   for (int k = threadIdx.x; k < CX * CY; k += TILE_NT) {
-    const int I = blockIdx.x * CX + k % CX, J = blockIdx.y * CY + k / CX;
+    const int I = bx * CX + k % CX, J = by * CY + k / CX;
     if (I >= C.ni || J >= C.nj) continue;
     const int uc = J * C.ni + I;
     const int q = (2 * (k / CX) + H) * WX + 2 * (k % CX) + H;
@@ -252,11 +221,11 @@ __global__ void __launch_bounds__(TILE_NT) k_level_down(LevelView F, LevelView C
 
 // F.y += prolongation of C.y (not on fixed nodes), then the post-smoothing
 template <int TX, int TY>
-__global__ void __launch_bounds__(TILE_NT) k_level_up(LevelView F, LevelView C) {
+__device__ __forceinline__ void level_up_body(const LevelView F, const LevelView C, int bx, int by) {
   constexpr int H = 4, WX = TX + 2 * H, WY = TY + 2 * H, NW = WX * WY, NL = (NW + TILE_NT - 1) / TILE_NT;
   __shared__ float sy[NW], sr[NW], sp[NW];
   __shared__ uint8_t st[NW];
-  const int gi0 = blockIdx.x * TX - H, gj0 = blockIdx.y * TY - H;
+  const int gi0 = bx * TX - H, gj0 = by * TY - H;
   float vy[NL], vr[NL], vp[NL], ca[NL], cb[NL], cc[NL], cd[NL];
   uint8_t vt[NL];
 #pragma unroll
@@ -292,20 +261,22 @@ __global__ void __launch_bounds__(TILE_NT) k_level_up(LevelView F, LevelView C) 
   __syncthreads();
   tile_sweeps<WX, WY>(sy, sr, sp, st, 1, F.cx, F.cy);
   for (int k = threadIdx.x; k < TX * TY; k += TILE_NT) {
-    const int gi = blockIdx.x * TX + k % TX, gj = blockIdx.y * TY + k / TX;
+    const int gi = bx * TX + k % TX, gj = by * TY + k / TX;
     if (gi < F.ni && gj < F.nj) F.y[gj * F.ni + gi] = sy[(k / TX + H) * WX + k % TX + H];
   }
 }
 
-__global__ void k_prolong(LevelView Cl, LevelView F) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= F.ni || j >= F.nj) return;
-  const int u = j * F.ni + i;
-  if (F.type[u] == NC_FIXED) return;
-  F.y[u] += prolong_value(Cl.y, i, j, Cl.ni);
+template <int TX, int TY>
+__global__ void __launch_bounds__(TILE_NT) k_level_down(LevelView F, LevelView C) {
+  level_down_body<TX, TY>(F, C, blockIdx.x, blockIdx.y);
 }
 
+template <int TX, int TY>
+__global__ void __launch_bounds__(TILE_NT) k_level_up(LevelView F, LevelView C) {
+  level_up_body<TX, TY>(F, C, blockIdx.x, blockIdx.y);
+}
+
+// ------------------------------------------------------------------------------------
 // coarse-grid P: injection of the fine linearisation coefficient
 __global__ void k_restrict_P(LevelView F, LevelView Cl) {
   const int I = blockIdx.x * blockDim.x + threadIdx.x;
@@ -348,11 +319,27 @@ __device__ __forceinline__ void coarse_vcycle_body(const CoarseDesc& D, const Le
   float* T = PP + D.total;
   uint8_t* TY = reinterpret_cast<uint8_t*>(T + D.total);
   const int n0 = D.ni[0] * D.nj[0];
-  for (int u = threadIdx.x; u < n0; u += blockDim.x) {
-    Y[u] = 0.f;
-    R[u] = top.r[u];
-    PP[u] = top.P[u];
-    TY[u] = top.type[u];
+  // top level in: eight loads per thread in flight at a time
+  for (int u0 = 0; u0 < n0; u0 += 8 * blockDim.x) {
+    float rr[8], pp[8];
+    uint8_t tt[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const int u = u0 + threadIdx.x + k * blockDim.x, uu = u < n0 ? u : 0;
+      rr[k] = top.r[uu];
+      pp[k] = top.P[uu];
+      tt[k] = top.type[uu];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const int u = u0 + threadIdx.x + k * blockDim.x;
+      if (u < n0) {
+        Y[u] = 0.f;
+        R[u] = rr[k];
+        PP[u] = pp[k];
+        TY[u] = tt[k];
+      }
+    }
   }
   __syncthreads();
   // coarser levels: type and P by injection
@@ -407,7 +394,7 @@ __device__ __forceinline__ void coarse_vcycle_body(const CoarseDesc& D, const Le
   for (int u = threadIdx.x; u < n0; u += blockDim.x) top.y[u] = Y[u];
 }
 
-__global__ void __launch_bounds__(1024) k_coarse_vcycle(CoarseDesc D, LevelView top, int nu1, int nu2) {
+__global__ void __launch_bounds__(1024, 1) k_coarse_vcycle(CoarseDesc D, LevelView top, int nu1, int nu2) {
   coarse_vcycle_body(D, top, nu1, nu2);
 }
 
@@ -923,16 +910,6 @@ static void restrict_P(sf_ctx* ctx, SfPoisson* ps) {
 
 // z = M^-1 r: one V(nu1,nu2)-cycle on level 0 from zero, r = lv[0].r, z -> lv[0].y
 // nu red-black sweeps on a level; first = the colour updated first in each sweep
-static void smooth(sf_ctx* ctx, const LevelView& L, int nu, int first) {
-  const dim3 blk(32, 8);
-  const dim3 g((L.ni / 2 + 1 + blk.x - 1) / blk.x, (L.nj + blk.y - 1) / blk.y);
-  for (int k = 0; k < nu; k++) {
-    k_smooth<<<g, blk, 0, ctx->stream>>>(L, first);
-    k_smooth<<<g, blk, 0, ctx->stream>>>(L, 1 - first);
-    ctx->launches += 2;
-  }
-}
-
 // one tiled level kernel: 64 x 16 tiles on levels of a million nodes or more, 32 x 8 below
 // (shorter per-block chains where the grid is too small to fill the GPU)
 static void level_down(cudaStream_t s, const LevelView& F, const LevelView& C) {
@@ -948,32 +925,12 @@ static void level_up(cudaStream_t s, const LevelView& F, const LevelView& C) {
     k_level_up<32, 8><<<dim3((F.ni + 31) / 32, (F.nj + 7) / 8), TILE_NT, 0, s>>>(F, C);
 }
 
-static void vcycle(sf_ctx* ctx, SfPoisson* ps, int nu1, int nu2) {
+static void vcycle(sf_ctx* ctx, SfPoisson* ps) {
   cudaStream_t s = ctx->stream;
-  const dim3 blk(32, 8);
-  if (nu1 == 2 && nu2 == 2) {
-    for (int l = 0; l < ps->cs; l++) level_down(s, ps->lv[l], ps->lv[l + 1]);
-    k_coarse_vcycle<<<1, 1024, ps->coarse_smem, s>>>(ps->cd, ps->lv[ps->cs], nu1, nu2);
-    for (int l = ps->cs - 1; l >= 0; l--) level_up(s, ps->lv[l], ps->lv[l + 1]);
-    ctx->launches += 2 * ps->cs + 1;
-    return;
-  }
-  if (ps->cs > 0) SF_CUDA(cudaMemsetAsync(ps->lv[0].y, 0, 4 * (size_t)ps->lv[0].ni * ps->lv[0].nj, s));
-  for (int l = 0; l < ps->cs; l++) {
-    const LevelView& L = ps->lv[l];
-    smooth(ctx, L, nu1, 0);
-    k_resid<<<grid2(L.ni, L.nj, blk), blk, 0, s>>>(L);
-    k_restrict<<<grid2(ps->lv[l + 1].ni, ps->lv[l + 1].nj, blk), blk, 0, s>>>(L, ps->lv[l + 1]);
-    ctx->launches += 2;
-  }
-  k_coarse_vcycle<<<1, 1024, ps->coarse_smem, s>>>(ps->cd, ps->lv[ps->cs], nu1, nu2);
-  ctx->launches++;
-  for (int l = ps->cs - 1; l >= 0; l--) {
-    const LevelView& L = ps->lv[l];
-    k_prolong<<<grid2(L.ni, L.nj, blk), blk, 0, s>>>(ps->lv[l + 1], L);
-    ctx->launches++;
-    smooth(ctx, L, nu2, 1);
-  }
+  for (int l = 0; l < ps->cs; l++) level_down(s, ps->lv[l], ps->lv[l + 1]);
+  k_coarse_vcycle<<<1, 1024, ps->coarse_smem, s>>>(ps->cd, ps->lv[ps->cs], 2, 2);
+  for (int l = ps->cs - 1; l >= 0; l--) level_up(s, ps->lv[l], ps->lv[l + 1]);
+  ctx->launches += 2 * ps->cs + 1;
 }
 
 static void reduce(sf_ctx* ctx, SfPoisson* ps, double* out, int max2) {
@@ -989,7 +946,7 @@ static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters) {
   const int n = L0.ni * L0.nj;
   const int g = grid_for(n, 256, ctx->num_sms * 8);
   SF_CUDA(cudaMemsetAsync(ps->cg_x, 0, 4 * (size_t)n, s));
-  vcycle(ctx, ps, 2, 2);  // z0
+  vcycle(ctx, ps);  // z0
   SF_CUDA(cudaMemsetAsync(ps->cg_zo, 0, 4 * (size_t)n, s));
   k_cg_dots<<<ps->red_blocks, RB, 0, s>>>(n, L0.r, L0.y, ps->cg_zo, ps->partial);
   reduce(ctx, ps, ps->sc + SC_RED, 0);
@@ -1003,7 +960,7 @@ static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters) {
     k_cg_axpy<<<g, 256, 0, s>>>(n, ps->sc, ps->cg_p, ps->cg_q, ps->cg_x, L0.r, L0.y, ps->cg_zo);
     ctx->launches += 3;
     if (k == iters - 1) break;
-    vcycle(ctx, ps, 2, 2);
+    vcycle(ctx, ps);
     k_cg_dots<<<ps->red_blocks, RB, 0, s>>>(n, L0.r, L0.y, ps->cg_zo, ps->partial);
     reduce(ctx, ps, ps->sc + SC_RED, 0);
     k_cg_scalars<<<1, 32, 0, s>>>(ps->sc, 2);
@@ -1601,7 +1558,7 @@ __global__ void kb_prolong(BPInst* I, BPWork w, int l, int kmin) {
 }
 
 // one CTA per live instance at a time (the single-CTA end of the V-cycle)
-__global__ void __launch_bounds__(1024) kb_coarse_vcycle(BPInst* I, const int* __restrict__ list,
+__global__ void __launch_bounds__(1024, 1) kb_coarse_vcycle(BPInst* I, const int* __restrict__ list,
                                                          const int* __restrict__ cnt, int nu1, int nu2, int kmin) {
   const int c = *cnt;
   for (int k = blockIdx.x; k < c; k += gridDim.x) {

@@ -81,7 +81,11 @@ __device__ __forceinline__ float apply_J(uint8_t t, const float* y, float P, int
   }
 }
 
-// Gauss-Seidel value of node u (solves its row of J y = r for y[u])
+// Gauss-Seidel value of node u (solves its row of J y = r for y[u]).  The interior row
+// divides with __fdividef (reciprocal and multiply, 2 ulp): the smoother needs no
+// correctly rounded quotient, and the IEEE division's instruction sequence dominated
+// the sweeps.  The diagonal 2 cx + 2 cy + P stays far below 2^126, where __fdividef
+// would return 0.
 __device__ __forceinline__ float gs_value(uint8_t t, const float* y, float r, float P, int u, int ni, float cx,
                                           float cy) {
   switch (t) {
@@ -90,7 +94,8 @@ __device__ __forceinline__ float gs_value(uint8_t t, const float* y, float r, fl
     case NC_NRIGHT: return y[u - 1] - r / cx;
     case NC_NBOTTOM: return y[u + ni] - r / cy;
     case NC_NTOP: return y[u - ni] - r / cy;
-    default: return (cx * (y[u - 1] + y[u + 1]) + cy * (y[u - ni] + y[u + ni]) - r) / (2.f * cx + 2.f * cy + P);
+    default:
+      return __fdividef(cx * (y[u - 1] + y[u + 1]) + cy * (y[u - ni] + y[u + ni]) - r, 2.f * cx + 2.f * cy + P);
   }
 }
 

@@ -16,8 +16,11 @@
 //     see the embedded electrode only approximately; CG removes those few slow modes.
 //     The operator is made symmetric by scaling the open-face (one-sided gradient) rows
 //     by 1/h, which leaves its solution unchanged.
-// The coarse end of the hierarchy (<= COARSE_NODES nodes) runs inside one CTA out of
-// shared memory, so a V-cycle is a handful of launches.  All inner scalars stay on the
+// The coarse end of the hierarchy runs inside one CTA out of shared memory, so a V-cycle
+// is a handful of launches: from COARSE_NODES nodes down for one mesh, and from
+// COARSE_NODES_BATCH down in the batched solve, where many instances' single-CTA cycles
+// run side by side.  Every level does the same arithmetic in the CTA as in the global
+// level kernels, so the split does not change the result.  All inner scalars stay on the
 // device; the host reads one FP64 residual norm per Newton step.
 #include <algorithm>
 #include <cmath>
@@ -32,7 +35,8 @@ namespace {
 // node classes of the closed-form operator
 enum : uint8_t { NC_INTERIOR = 0, NC_FIXED = 1, NC_NLEFT = 2, NC_NRIGHT = 3, NC_NBOTTOM = 4, NC_NTOP = 5 };
 
-constexpr int COARSE_NODES = 8600;  // a level this small and everything below run in one CTA
+constexpr int COARSE_NODES = 2200;        // one mesh: a level this small and all below in one CTA
+constexpr int COARSE_NODES_BATCH = 8600;  // the same for the batched solve
 constexpr size_t COARSE_SMEM_MAX = 220 * 1024;  // dynamic shared memory bound of the coarse V-cycle
 constexpr int MAX_LEVELS = 16;
 
@@ -298,18 +302,22 @@ __global__ void k_restrict_P(LevelView F, LevelView Cl) {
 __device__ void cta_smooth(float* y, const float* r, const float* P, const uint8_t* ty, int ni, int nj, float cx,
                            float cy, int sweeps, bool rb, float omega = 1.f) {
   const int n = ni * nj;
+  const bool sor = omega != 1.f;  // Gauss-Seidel stores the value itself, as the level kernels do
   for (int s = 0; s < sweeps; s++)
     for (int c = 0; c < 2; c++) {
       const int color = rb ? c : 1 - c;
       if (ni & 1) {
         // odd row length: the colour (i + j) & 1 of node u = j ni + i is u & 1
-        for (int u = 2 * threadIdx.x + color; u < n; u += 2 * blockDim.x)
-          y[u] += omega * (gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy) - y[u]);
+        for (int u = 2 * threadIdx.x + color; u < n; u += 2 * blockDim.x) {
+          const float g = gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy);
+          y[u] = sor ? y[u] + omega * (g - y[u]) : g;
+        }
       } else {
         for (int u = threadIdx.x; u < n; u += blockDim.x) {
           const int j = u / ni, i = u - j * ni;
           if (((i + j) & 1) != color) continue;
-          y[u] += omega * (gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy) - y[u]);
+          const float g = gs_value(ty[u], y, r[u], P[u], u, ni, cx, cy);
+          y[u] = sor ? y[u] + omega * (g - y[u]) : g;
         }
       }
       __syncthreads();
@@ -765,6 +773,9 @@ struct SfPoisson {
   int cs = 0;  // first level of the single-CTA solve
   CoarseDesc cd{};
   size_t coarse_smem = 0;
+  int cs_b = 0;  // the same for the batched solve
+  CoarseDesc cd_b{};
+  size_t coarse_smem_b = 0;
   int red_blocks = 0;
   bool rho_set = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -866,32 +877,36 @@ static SfPoisson* poisson_get(sf_ctx* ctx) {
     ldx *= 2;
     ldy *= 2;
   }
-  // first level small enough for the single-CTA coarse solve
+  // first level small enough for the single-CTA coarse solve (one mesh, batched solve)
   const int nl = (int)ps->lv.size();
-  ps->cs = nl - 1;
-  for (int l = 0; l < nl; l++)
-    if ((size_t)ps->lv[l].ni * ps->lv[l].nj <= (size_t)COARSE_NODES) {
-      ps->cs = l;
-      break;
+  auto split = [&](int nodes) {
+    for (int l = 0; l < nl; l++)
+      if ((size_t)ps->lv[l].ni * ps->lv[l].nj <= (size_t)nodes) return l;
+    return nl - 1;
+  };
+  auto desc = [&](int cs, CoarseDesc& D) {
+    D.n = nl - cs;
+    int off = 0;
+    for (int k = 0; k < D.n; k++) {
+      const LevelView& L = ps->lv[cs + k];
+      D.ni[k] = L.ni;
+      D.nj[k] = L.nj;
+      D.cx[k] = L.cx;
+      D.cy[k] = L.cy;
+      D.off[k] = off;
+      off += L.ni * L.nj;
     }
-  CoarseDesc& D = ps->cd;
-  D.n = nl - ps->cs;
-  int off = 0;
-  for (int k = 0; k < D.n; k++) {
-    const LevelView& L = ps->lv[ps->cs + k];
-    D.ni[k] = L.ni;
-    D.nj[k] = L.nj;
-    D.cx[k] = L.cx;
-    D.cy[k] = L.cy;
-    D.off[k] = off;
-    off += L.ni * L.nj;
-  }
-  D.total = off;
-  const LevelView& Lc = ps->lv[nl - 1];
-  D.coarsest_sweeps = std::min(200, std::max(10, std::max(Lc.ni, Lc.nj)));
-  D.omega = (float)(2.0 / (1.0 + std::sin(PI / std::max(Lc.ni, Lc.nj))));
-  ps->coarse_smem = (size_t)D.total * (4 * sizeof(float) + 1) + 16;
-  SF_REQUIRE(ps->coarse_smem <= COARSE_SMEM_MAX, SF_ERR_ARG,
+    D.total = off;
+    const LevelView& Lc = ps->lv[nl - 1];
+    D.coarsest_sweeps = std::min(200, std::max(10, std::max(Lc.ni, Lc.nj)));
+    D.omega = (float)(2.0 / (1.0 + std::sin(PI / std::max(Lc.ni, Lc.nj))));
+    return (size_t)D.total * (4 * sizeof(float) + 1) + 16;
+  };
+  ps->cs = split(COARSE_NODES);
+  ps->coarse_smem = desc(ps->cs, ps->cd);
+  ps->cs_b = split(COARSE_NODES_BATCH);
+  ps->coarse_smem_b = desc(ps->cs_b, ps->cd_b);
+  SF_REQUIRE(ps->coarse_smem <= COARSE_SMEM_MAX && ps->coarse_smem_b <= COARSE_SMEM_MAX, SF_ERR_ARG,
              "mesh not coarsenable to a level that fits in shared memory (use (2^k)m+1 nodes per direction)");
   // the limit is a property of the kernel on the device, shared by every context: always
   // the same bound, so that a context with a smaller coarse end cannot lower it under the
@@ -1863,9 +1878,9 @@ static void bp_fill(BatchPoisson* bp) {
       s.nspecies++;
     }
     bp->nspecies[i] = s.nspecies;
-    s.cs = ps->cs;
+    s.cs = ps->cs_b;
     for (size_t l = 0; l < ps->lv.size(); l++) s.lv[l] = ps->lv[l];
-    s.cd = ps->cd;
+    s.cd = ps->cd_b;
     s.fp64_exp = ps->fp64_exp ? 1 : 0;
   }
   copy_wait(bp->d_inst, h.data(), sizeof(BPInst) * bp->n, cudaMemcpyHostToDevice, bp->stream);
@@ -1882,8 +1897,8 @@ BatchPoisson* batch_poisson_create(sf_ctx* const* ctxs, int n, int num_sms, cuda
     for (int i = 0; i < n; i++) {
       SF_REQUIRE(ctxs[i]->domain == SF_DOMAIN_XY, SF_ERR_ARG, "the batched solve takes XY meshes");
       ps[i] = poisson_get(ctxs[i]);
-      bp->max_cs = std::max(bp->max_cs, ps[i]->cs);
-      bp->coarse_smem = std::max(bp->coarse_smem, ps[i]->coarse_smem);
+      bp->max_cs = std::max(bp->max_cs, ps[i]->cs_b);
+      bp->coarse_smem = std::max(bp->coarse_smem, ps[i]->coarse_smem_b);
     }
     std::vector<int> tab;
     bp->nkinds = 3 + 3 * bp->max_cs;
@@ -1892,9 +1907,9 @@ BatchPoisson* batch_poisson_create(sf_ctx* const* ctxs, int n, int num_sms, cuda
     auto add = [&](int kind, auto blocks) { bp_table(tab, n, blocks, bp->koff[kind], bp->ktot[kind]); };
     add(BK_FINE, [&](int i) { return (ps[i]->ni * ps[i]->nj + ET - 1) / ET; });
     add(BK_RED, [&](int i) { return ps[i]->red_blocks; });
-    add(BK_ZERO, [&](int i) { return ps[i]->cs > 0 ? (ps[i]->ni * ps[i]->nj + ET - 1) / ET : 0; });
+    add(BK_ZERO, [&](int i) { return ps[i]->cs_b > 0 ? (ps[i]->ni * ps[i]->nj + ET - 1) / ET : 0; });
     for (int l = 0; l < bp->max_cs; l++) {
-      auto on = [&](int i) { return l < ps[i]->cs; };
+      auto on = [&](int i) { return l < ps[i]->cs_b; };
       add(bk_lvl(l), [&](int i) { return on(i) ? (ps[i]->lv[l].ni * ps[i]->lv[l].nj + ET - 1) / ET : 0; });
       add(bk_lvlc(l), [&](int i) { return on(i) ? (ps[i]->lv[l + 1].ni * ps[i]->lv[l + 1].nj + ET - 1) / ET : 0; });
       add(bk_half(l), [&](int i) { return on(i) ? (ps[i]->lv[l].nj * ((ps[i]->lv[l].ni + 1) / 2) + ET - 1) / ET : 0; });
@@ -1905,7 +1920,7 @@ BatchPoisson* batch_poisson_create(sf_ctx* const* ctxs, int n, int num_sms, cuda
     copy_wait(bp->d_koff, bp->koff.data(), sizeof(int) * bp->nkinds, cudaMemcpyHostToDevice, stream);
     std::vector<int> order(n);
     for (int i = 0; i < n; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return ps[x]->cd.total > ps[y]->cd.total; });
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return ps[x]->cd_b.total > ps[y]->cd_b.total; });
     SF_CUDA(cudaMalloc(&bp->d_order, sizeof(int) * n));
     copy_wait(bp->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, stream);
     SF_CUDA(cudaMalloc(&bp->d_act_pos, sizeof(int) * (n + 1)));

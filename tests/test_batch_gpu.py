@@ -36,13 +36,11 @@ def _sorted(lc, vel):
     return a[np.lexsort(a.T[::-1])]
 
 
-def test_batch_step_matches_instances(gpulib):
+def _batch_vs_twins(cases, dt, threads):
     from starfish_gb300.plugin import GpuBatch
-    dt = 5e-7
-    cases = W.config4(6, seed=3, max_particles=200_000, min_particles=20_000)
     A = [_instance(c, dt) for c in cases]
     B = [_instance(c, dt) for c in cases]
-    batch = GpuBatch([a[0] for a in A], [a[1] for a in A], threads=3)
+    batch = GpuBatch([a[0] for a in A], [a[1] for a in A], threads=threads)
     try:
         st = batch.step(dt, A[0][2])  # first step: PCG iterations 2 in every bucket (tuning)
         assert st["particles"] > 0 and st["capacity_overflow"] == 0
@@ -63,6 +61,21 @@ def test_batch_step_matches_instances(gpulib):
         batch.close()
         for d in A + B:
             d[0].close()
+
+
+def test_batch_step_matches_instances(gpulib):
+    _batch_vs_twins(W.config4(6, seed=3, max_particles=200_000, min_particles=20_000), 5e-7, 3)
+
+
+def test_batch_solve_matches_tiled_levels_on_a_large_mesh(gpulib):
+    """A 2049x513 instance (over 2^20 nodes: the per-instance solve runs its finest level
+    on 64x16 tiles and the next ones on 32x8 tiles) against the batched solve's global
+    red-black sweeps: the same values bit for bit."""
+    m = W.es_pic_mesh(2049, 513, 1e-4, electrode_halfwidth=4.5e-3, phi_electrode=-150.0)
+    n = 50_000
+    Lx, Ly = m.lengths()
+    ion = W.IonSpecies(spwt=1e12 * (Lx * Ly - (2 * 4.5e-3) ** 2) / n)
+    _batch_vs_twins([W.BatchCase(m, ion, n, -150.0, 0)], 2e-7, 1)
 
 
 def test_batch_source_and_tuning(gpulib):

@@ -361,3 +361,36 @@ def test_oracle_preload_and_uniform_source_known_answers():
     assert p1.shape[0] == int(expect) and rem == pytest.approx(expect - int(expect))
     assert np.all(p1[:, 3] == v) and np.all(p1[:, 4] == 0) and np.all(p1[:, 5] == 0)
     assert np.all((p1[:, 1] >= 0) & (p1[:, 1] <= 0.02))
+
+
+def test_oracle_dsmc_collision_rate_matches_vhs_theory():
+    """NTC with the Bird 4.63 VHS cross-section in one cell of an equilibrium gas: the
+    expected collisions per step are N^2 w dt <sigma g> / (2 V), where for a Maxwellian
+    relative speed at temperature T
+        <sigma g> = sigma0 (2 k T_ref / m_r)^(omega - 1/2) (2 k T / m_r)^(1 - omega) / Gamma(3/2)
+    (at T = T_ref this is sigma0 times the mean relative speed).  Elastic collisions keep
+    momentum and energy."""
+    import math
+    KB, mass, d, T_ref, om = 1.3806503e-23, 6.63e-26, 4.17e-10, 273.0, 0.81
+    mr = 0.5 * mass
+    sigma0 = math.pi * d * d
+    V, dt, n = 1e-9, 1e-6, 2000
+    for T, seed in ((273.0, 3), (819.0, 4)):
+        rng = np.random.default_rng(seed)
+        P = np.zeros((n, 12))
+        P[:, 3:6] = rng.normal(0.0, math.sqrt(KB * T / mass), (n, 3))
+        P[:, 6:8] = 0.5
+        P[:, 10] = 1
+        sg = sigma0 * (2 * KB * T_ref / mr) ** (om - 0.5) * (2 * KB * T / mr) ** (1 - om) / math.gamma(1.5)
+        spwt = 2e4 * 2 * V / (n * n * dt * sg)  # about 2e4 collisions expected
+        P[:, 9] = spwt
+        state = np.array([[6.0 * sg, 0.0]])  # (sigma g)_max well above every pair's sigma g
+        counts = np.zeros((1, 2))
+        p0, e0 = P[:, 3:6].sum(axis=0), (P[:, 3:6] ** 2).sum()
+        # the pair average over this finite sample differs from the Maxwellian one by
+        # about 1 %, the count by its Poisson spread (0.7 %)
+        got = O.dsmc(2, 2, np.array([V]), P, mass, spwt, d, T_ref, om, 1.0, dt, state, counts, seed)
+        assert got == pytest.approx(2e4, rel=0.04)
+        assert counts[0, 0] == got
+        assert np.allclose(P[:, 3:6].sum(axis=0), p0, atol=1e-9 * np.abs(P[:, 3:6]).sum())
+        assert (P[:, 3:6] ** 2).sum() == pytest.approx(e0, rel=1e-12)

@@ -394,3 +394,31 @@ def test_oracle_dsmc_collision_rate_matches_vhs_theory():
         assert counts[0, 0] == got
         assert np.allclose(P[:, 3:6].sum(axis=0), p0, atol=1e-9 * np.abs(P[:, 3:6]).sum())
         assert (P[:, 3:6] ** 2).sum() == pytest.approx(e0, rel=1e-12)
+
+
+def test_oracle_poisson_boltzmann_debye_shielding():
+    """Boltzmann electrons over a uniform ion background e n0, walls at phi_w << kTe on the
+    left and right, Neumann top and bottom: the linearised equation phi'' = phi / lambda_D^2
+    (lambda_D^2 = eps kTe / (e n0)) has on the grid the exact solution
+        phi_i = phi_w cosh(kappa (i - N/2)) / cosh(kappa N / 2),  cosh kappa = 1 + h^2 / (2 lambda_D^2).
+    The nonlinear solve must agree to the size of the neglected term, (phi / kTe) / 2."""
+    import math
+    QE, EPS = 1.602176565e-19, 8.85418782e-12
+    n0, kTe, phi_w = 1e12, 2.0, 0.01
+    lam = math.sqrt(EPS * kTe / (QE * n0))
+    ni, nj, h = 65, 5, lam / 8
+    node_type = np.full((nj, ni), O.NODE_OPEN, np.int8)
+    node_type[:, 0] = node_type[:, -1] = O.NODE_DIRICHLET
+    face = np.zeros((4, ni), np.int8)
+    face[O.F_TOP, :] = O.DB_SYMMETRY
+    face[O.F_BOTTOM, :] = O.DB_SYMMETRY
+    bc = np.zeros((nj, ni))
+    bc[:, 0] = bc[:, -1] = phi_w
+    m = O.OMesh(ni, nj, [0, 0], [h, h], O.DOM_XY, node_type.reshape(-1), face)
+    phi, it, out = O.poisson_nl(m, bc.reshape(-1), np.full(ni * nj, QE * n0), n0, kTe, 0.0, EPS,
+                                np.zeros(ni * nj), max_it=200000, tol=1e-13, nl_max_it=100, nl_tol=1e-12)
+    kap = math.acosh(1 + h * h / (2 * lam * lam))
+    i = np.arange(ni)
+    exact = phi_w * np.cosh(kap * (i - (ni - 1) / 2)) / np.cosh(kap * (ni - 1) / 2)
+    assert np.max(np.abs(phi.reshape(nj, ni) - exact[None, :])) < 0.5 * phi_w / kTe * phi_w
+    assert phi.reshape(nj, ni)[2, ni // 2] < 0.05 * phi_w  # shielded over 4 Debye lengths

@@ -1,7 +1,8 @@
 """ctypes front-end of the CPU oracle (``sf_oracle.cpp``).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
-and the CPU-baseline legs of ``bench.py`` as the checker.  The product never
+and the CPU-baseline legs of ``bench.py``, to check results against and to time the
+CPU baseline.  The product never
 imports it.  See the header of ``sf_oracle.cpp`` for what is restated and for
 the parity status ("parity unpinned" against the Java reference, which has no
 tests and cannot run here; pinned by analytic known-answer tests instead).

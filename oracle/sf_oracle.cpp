@@ -4,7 +4,8 @@
 // array-of-structs particles like the reference's `Particle` objects), the
 // algorithms of the Java reference for the hot path.  Only the test-suite,
 // `__graft_entry__.smoke()` and the CPU-baseline legs of `bench.py` load it,
-// and only as a checker / baseline.  The product (libstarfish_gpu.so) never
+// and only to check results against and as the CPU baseline.  The product
+// (libstarfish_gpu.so) never
 // links, loads or calls it.
 //
 // Parity status: the Java reference cannot be compiled or run here (no JDK)

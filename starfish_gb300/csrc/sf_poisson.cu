@@ -117,15 +117,7 @@ __device__ __forceinline__ float restrict_value(const float* tf, uint8_t tc, int
   return restrict_at(tf, (2 * J) * nif + 2 * I, nif, tc, I == 0 || J == 0 || I == nic - 1 || J == njc - 1);
 }
 
-// the same from the four coarse values around fine node (i, j): a = (I, J), b = (I + 1, J),
-// c = (I, J + 1), d = (I + 1, J + 1), the ones outside the stencil unused
-__device__ __forceinline__ float prolong_of(float a, float b, float c, float d, bool oi, bool oj) {
-  if (!oi && !oj) return a;
-  if (oi && !oj) return 0.5f * (a + b);
-  if (!oi && oj) return 0.5f * (a + c);
-  return 0.25f * (a + b + c + d);
-}
-
+// bilinear prolongation of the coarse correction yc to fine node (i, j)
 __device__ __forceinline__ float prolong_value(const float* yc, int i, int j, int nic) {
   const int I = i >> 1, J = j >> 1;
   const int uc = J * nic + I;
@@ -134,6 +126,16 @@ __device__ __forceinline__ float prolong_value(const float* yc, int i, int j, in
   if (oi && !oj) return 0.5f * (yc[uc] + yc[uc + 1]);
   if (!oi && oj) return 0.5f * (yc[uc] + yc[uc + nic]);
   return 0.25f * (yc[uc] + yc[uc + 1] + yc[uc + nic] + yc[uc + nic + 1]);
+}
+
+// prolong_value from the four coarse values around fine node (i, j), already loaded:
+// a = (I, J), b = (I + 1, J), c = (I, J + 1), d = (I + 1, J + 1); those outside the
+// stencil are not used
+__device__ __forceinline__ float prolong_of(float a, float b, float c, float d, bool oi, bool oj) {
+  if (!oi && !oj) return a;
+  if (oi && !oj) return 0.5f * (a + b);
+  if (!oi && oj) return 0.5f * (a + c);
+  return 0.25f * (a + b + c + d);
 }
 
 // ------------------------------------------------------------------------------------

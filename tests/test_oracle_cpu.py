@@ -422,3 +422,39 @@ def test_oracle_poisson_boltzmann_debye_shielding():
     exact = phi_w * np.cosh(kap * (i - (ni - 1) / 2)) / np.cosh(kap * (ni - 1) / 2)
     assert np.max(np.abs(phi.reshape(nj, ni) - exact[None, :])) < 0.5 * phi_w / kTe * phi_w
     assert phi.reshape(nj, ni)[2, ni // 2] < 0.05 * phi_w  # shielded over 4 Debye lengths
+
+
+@pytest.mark.parametrize("domain", [O.DOM_ZR, O.DOM_RZ])
+def test_oracle_axisymmetric_rotation_known_answer(domain):
+    """A particle with only a theta velocity w at radius r0 (no field): after dt its radius is
+    sqrt(r0^2 + (w dt)^2), its velocity turns by alpha = atan(w dt / r0) into the radial
+    direction (v_r = w sin alpha, v_theta = w cos alpha) and theta advances by alpha
+    (rotateToZR / rotateToRZ, KineticMaterial.java:424-462)."""
+    ni, nj, dh = 41, 41, 1e-3
+    rad = 1 if domain == O.DOM_ZR else 0  # the radial coordinate: y in ZR, x in RZ
+    x0 = [0.0, 0.0]
+    x0[rad] = 0.01
+    node_type = np.full(ni * nj, O.NODE_OPEN, np.int8)
+    face = np.full((4, ni), O.DB_OPEN, np.int8)
+    m = O.OMesh(ni, nj, x0, [dh, dh], domain, node_type, face)
+    w, dt = 3000.0, 1e-6
+    r0 = np.array([0.012, 0.02, 0.03])
+    parts = np.zeros((3, 12))
+    parts[:, 1 - rad] = 0.02
+    parts[:, rad] = r0
+    parts[:, 6 + (1 - rad)] = 0.02 / dh
+    parts[:, 6 + rad] = (r0 - 0.01) / dh
+    parts[:, 5] = w
+    parts[:, 9] = 1.0
+    parts[:, 10] = 1
+    zero = np.zeros(ni * nj)
+    alive, _, _, _ = O.push(m, zero, zero, 1.6e-19, 6.6e-26, dt, np.zeros((0, 9)), np.zeros(ni * nj + 1),
+                            np.zeros(0), parts)
+    assert alive == 3
+    R = np.hypot(r0, w * dt)
+    assert np.allclose(parts[:, rad], R, rtol=1e-14)
+    assert np.allclose(parts[:, 3 + rad], w * (w * dt) / R, rtol=1e-12)
+    assert np.allclose(parts[:, 5], w * r0 / R, rtol=1e-12)
+    assert np.allclose(parts[:, 1 - rad], 0.02, rtol=1e-15)
+    assert np.allclose(np.abs(parts[:, 2]), np.arctan2(w * dt, r0), rtol=1e-12)
+    assert np.allclose(parts[:, 6 + rad], (R - 0.01) / dh, rtol=1e-12)

@@ -458,3 +458,36 @@ def test_oracle_axisymmetric_rotation_known_answer(domain):
     assert np.allclose(parts[:, 1 - rad], 0.02, rtol=1e-15)
     assert np.allclose(np.abs(parts[:, 2]), np.arctan2(w * dt, r0), rtol=1e-12)
     assert np.allclose(parts[:, 6 + rad], (R - 0.01) / dh, rtol=1e-12)
+
+
+@pytest.mark.parametrize("domain", [O.DOM_ZR, O.DOM_RZ])
+def test_oracle_ruyten_scatter_uniform_density(domain):
+    """Particles uniform in volume over a cylinder from the axis (radius drawn as
+    R sqrt(U)): with Ruyten's radial weights (Field2D.java:254-285) and the annular node
+    volumes the density comes out uniform on every radial row, the axis row and the outer
+    row included, and the deposited weight is conserved exactly."""
+    ni = nj = 21
+    dh = 1e-3
+    rad = 1 if domain == O.DOM_ZR else 0
+    node_type = np.full(ni * nj, O.NODE_OPEN, np.int8)
+    face = np.full((4, ni), O.DB_OPEN, np.int8)
+    m = O.OMesh(ni, nj, [0.0, 0.0], [dh, dh], domain, node_type, face)
+    vol = O.node_volumes(m)
+    rng = np.random.default_rng(2)
+    n = 2_000_000
+    L = (ni - 1) * dh
+    parts = np.zeros((n, 12))
+    parts[:, 6 + rad] = np.sqrt(rng.uniform(0, 1, n)) * L / dh
+    parts[:, 6 + (1 - rad)] = rng.uniform(0, L, n) / dh
+    parts[:, 9] = 1.0
+    parts[:, 10] = 1
+    den = O.update_fields(m, vol, parts)
+    assert (den * vol).sum() == pytest.approx(n, rel=1e-12)
+    d = (den * np.pi * L * L * L / n).reshape(nj, ni)
+    v = vol.reshape(nj, ni)
+    if rad == 0:  # radius along i: radial rows are columns
+        d, v = d.T, v.T
+    # mean over the interior axial positions of each radial row, against its Poisson spread
+    mean = d[:, 1:-1].mean(axis=1)
+    spread = 1 / np.sqrt(n * v[:, ni // 2] / (np.pi * L ** 3) * (ni - 2))
+    assert np.all(np.abs(mean - 1) < 4 * spread), (mean, spread)

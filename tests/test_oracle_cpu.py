@@ -491,3 +491,18 @@ def test_oracle_ruyten_scatter_uniform_density(domain):
     mean = d[:, 1:-1].mean(axis=1)
     spread = 1 / np.sqrt(n * v[:, ni // 2] / (np.pi * L ** 3) * (ni - 2))
     assert np.all(np.abs(mean - 1) < 4 * spread), (mean, spread)
+
+
+@pytest.mark.parametrize("domain", [O.DOM_XY, O.DOM_ZR, O.DOM_RZ])
+def test_oracle_efield_of_linear_potential(domain):
+    """E = -grad(phi) (Solver.evaluateGradient, Solver.java:789-814) is exact for a linear
+    potential on every node, the one-sided edge differences included."""
+    ni, nj, dx, dy = 17, 9, 2e-3, 1e-3
+    node_type = np.full(ni * nj, O.NODE_OPEN, np.int8)
+    face = np.full((4, ni), O.DB_DIRICHLET, np.int8)
+    m = O.OMesh(ni, nj, [0.0, 0.005], [dx, dy], domain, node_type, face)
+    i, j = np.meshgrid(np.arange(ni), np.arange(nj))
+    phi = (3.0 + 120.0 * i * dx - 45.0 * (0.005 + j * dy)).reshape(-1)
+    efi, efj = O.efield(m, phi)
+    assert np.allclose(efi, -120.0, rtol=0, atol=1e-9)
+    assert np.allclose(efj, 45.0, rtol=0, atol=1e-9)

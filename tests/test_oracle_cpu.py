@@ -506,3 +506,28 @@ def test_oracle_efield_of_linear_potential(domain):
     efi, efj = O.efield(m, phi)
     assert np.allclose(efi, -120.0, rtol=0, atol=1e-9)
     assert np.allclose(efj, 45.0, rtol=0, atol=1e-9)
+
+
+def test_oracle_mcc_cex_rate_known_answer():
+    """MCC.perform with CEX (MCC.java:167-221, 287-297) against a cold uniform target: each
+    ion of speed g collides with probability 1 - exp(-n sigma g dt) and then moves with the
+    target's (near-zero) velocity."""
+    spec = W.es_pic_mesh(21, 21, 1e-3, walls=abi.DB_SYMMETRY, electrode_halfwidth=1e-12)
+    spec.node_type[:] = abi.NODE_OPEN
+    m = _omesh(spec)
+    nn, n = spec.nn, 200_000
+    mi = 40 * 1.66053886e-27
+    rng = np.random.default_rng(4)
+    lc = rng.uniform(0.5, 19.5, (n, 2))
+    P = np.zeros((n, 12))
+    P[:, 0:2] = spec.x0 + lc * spec.dh
+    P[:, 6:8] = lc
+    P[:, 3] = 1e4
+    P[:, 9] = 1.0
+    P[:, 10] = 1
+    z = np.zeros(nn)
+    sigma, dt, tden = 1e-19, 1e-6, 1e20
+    cols = O.mcc(m, P, mi, mi, np.full(nn, tden), z, z, z, np.full(nn, 1e-3), sigma, dt, 1, 11)
+    p = 1 - np.exp(-tden * sigma * 1e4 * dt)
+    assert abs(cols - n * p) < 4 * np.sqrt(n * p * (1 - p))
+    assert (np.linalg.norm(P[:, 3:6], axis=1) < 1.0).sum() == cols

@@ -234,10 +234,10 @@ __global__ void k_pack_efield(int nn, const double* __restrict__ efi, const doub
 // probe always ends).  Global memory is then touched once per distinct key per chunk
 // instead of once per particle.
 constexpr int SORT_B = 256;
-constexpr int SORT_IPT = 8;
+constexpr int SORT_IPT = 4;
 constexpr int SORT_CHUNK = SORT_B * SORT_IPT;
-constexpr int SORT_HBITS = 12;
-constexpr int SORT_HSIZE = 1 << SORT_HBITS;  // 4096 >= 2 * SORT_CHUNK
+constexpr int SORT_HBITS = 11;
+constexpr int SORT_HSIZE = 1 << SORT_HBITS;  // 2048 >= 2 * SORT_CHUNK
 constexpr unsigned EMPTY_KEY = 0xFFFFFFFFu;
 
 __device__ inline unsigned hash_slot(unsigned key) { return (key * 2654435761u) >> (32 - SORT_HBITS); }
@@ -498,7 +498,8 @@ void launch_sort(sf_ctx* ctx, SfSpecies* sp) {
     // per device and the same for every context (set-up threads may sort concurrently)
     SF_CUDA(cudaFuncSetAttribute(k_sort_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)SORT_SCATTER_SMEM));
-    const int gs = grid_for((sp->n + SORT_CHUNK - 1) / SORT_CHUNK, 1, ctx->num_sms * 2);
+    // 52 KB of shared memory and 64 registers per block: 4 blocks per SM
+    const int gs = grid_for((sp->n + SORT_CHUNK - 1) / SORT_CHUNK, 1, ctx->num_sms * 4);
     k_sort_scatter<<<gs, SORT_B, SORT_SCATTER_SMEM, ctx->stream>>>(sp->cur, dst, ctx->ntx, ctx->bins_tmp);
     SF_CUDA(cudaGetLastError());
     int total = 0;

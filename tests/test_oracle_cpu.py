@@ -531,3 +531,28 @@ def test_oracle_mcc_cex_rate_known_answer():
     p = 1 - np.exp(-tden * sigma * 1e4 * dt)
     assert abs(cols - n * p) < 4 * np.sqrt(n * p * (1 - p))
     assert (np.linalg.norm(P[:, 3:6], axis=1) < 10.0).sum() == cols  # target thermal speed ~1 m/s
+
+
+def test_oracle_specular_reflection_known_answer():
+    """Ions moving +x into the electrode box's left face (outward normal -x) with the specular
+    handler (SurfaceInteraction.java:104-125): the velocity becomes v + n sqrt(2) |v_xy|,
+    at normal incidence (1 - sqrt(2)) v; they stay on the gas side and keep their y."""
+    spec = W.es_pic_mesh(81, 41, 1e-3)  # box x in [35.5, 44.5] mm, y in [15.5, 24.5] mm
+    m = _omesh(spec)
+    ptr, idx = O.node_segments(m, spec.seg_xy)
+    rng = np.random.default_rng(8)
+    n = 2000
+    lc = np.column_stack([rng.uniform(33.0, 35.0, n), rng.uniform(17.0, 23.0, n)])
+    P = np.zeros((n, 12))
+    P[:, 0:2] = lc * 1e-3
+    P[:, 3] = 8000.0
+    P[:, 6:8] = lc
+    P[:, 9] = 1e6
+    P[:, 10] = 1
+    segs = O.seg_table(spec.seg_xy, spec.seg_btype, O.SURF_SPECULAR)
+    zero = np.zeros(spec.nn)
+    alive, _, _, _ = O.push(m, zero, zero, 1.602e-19, 16 * 1.66053886e-27, 5e-7, segs, ptr, idx, P)
+    assert alive == n
+    assert np.allclose(P[:, 3], 8000.0 * (1 - np.sqrt(2.0)), rtol=1e-12)
+    assert np.all(P[:, 4] == 0.0) and np.all(P[:, 5] == 0.0)
+    assert np.all(P[:, 0] < 0.0355) and np.allclose(P[:, 1], lc[:, 1] * 1e-3, rtol=0, atol=1e-15)

@@ -556,3 +556,33 @@ def test_oracle_specular_reflection_known_answer():
     assert np.allclose(P[:, 3], 8000.0 * (1 - np.sqrt(2.0)), rtol=1e-12)
     assert np.all(P[:, 4] == 0.0) and np.all(P[:, 5] == 0.0)
     assert np.all(P[:, 0] < 0.0355) and np.allclose(P[:, 1], lc[:, 1] * 1e-3, rtol=0, atol=1e-15)
+
+
+def test_oracle_diffuse_reflection_cosine_law():
+    """The diffuse handler with full accommodation (SurfaceInteraction.java:127-213): speeds
+    from the wall's Maxwellian speed distribution (mean 2/sqrt(pi) vth), directions by the
+    cosine law about the outward normal (mean cosine 2/3), all away from the face."""
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    m = _omesh(spec)
+    ptr, idx = O.node_segments(m, spec.seg_xy)
+    rng = np.random.default_rng(9)
+    n = 40000
+    lc = np.column_stack([rng.uniform(33.0, 35.0, n), rng.uniform(17.0, 23.0, n)])
+    P = np.zeros((n, 12))
+    P[:, 0:2] = lc * 1e-3
+    P[:, 3] = 8000.0
+    P[:, 6:8] = lc
+    P[:, 9] = 1e6
+    P[:, 10] = 1
+    mass = 16 * 1.66053886e-27
+    vth = np.sqrt(2 * 1.3806503e-23 * 300.0 / mass)
+    segs = O.seg_table(spec.seg_xy, spec.seg_btype, O.SURF_DIFFUSE, vth=vth, c_rest=1.0, c_accom=1.0)
+    zero = np.zeros(spec.nn)
+    # a short step: the reflected particles cannot reach another face of the box
+    alive, _, _, _ = O.push(m, zero, zero, 1.602e-19, mass, 5e-7, segs, ptr, idx, P)
+    assert alive == n
+    v = P[:, 3:6]
+    speed = np.linalg.norm(v, axis=1)
+    assert np.all(v[:, 0] <= 0)
+    assert abs(speed.mean() / (2 / np.sqrt(np.pi) * vth) - 1) < 0.02
+    assert abs((-v[:, 0] / speed).mean() - 2 / 3) < 0.01

@@ -586,3 +586,33 @@ def test_oracle_diffuse_reflection_cosine_law():
     assert np.all(v[:, 0] <= 0)
     assert abs(speed.mean() / (2 / np.sqrt(np.pi) * vth) - 1) < 0.02
     assert abs((-v[:, 0] / speed).mean() - 2 / 3) < 0.01
+
+
+def test_oracle_absorbed_flux_and_deposit_split():
+    """A beam absorbed by the electrode box's left face (Material.java:759-796 through
+    ProcessBoundary): every ion is removed; the face's two end values of the flux and the
+    deposit hold its weight split linearly by the hit point's position along the face, so
+    the two ends sum to N w and the far end holds w * sum(t)."""
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    m = _omesh(spec)
+    ptr, idx = O.node_segments(m, spec.seg_xy)
+    x1, y1, x2, y2 = spec.seg_xy[0]
+    assert x1 == x2 and abs(x1 - 0.0355) < 1e-12  # the left face
+    rng = np.random.default_rng(10)
+    n, w = 3000, 2.5e5
+    lc = np.column_stack([rng.uniform(33.0, 35.0, n), rng.uniform(16.0, 24.0, n)])
+    P = np.zeros((n, 12))
+    P[:, 0:2] = lc * 1e-3
+    P[:, 3] = 8000.0
+    P[:, 6:8] = lc
+    P[:, 9] = w
+    P[:, 10] = 1
+    segs = O.seg_table(spec.seg_xy, spec.seg_btype, O.SURF_ABSORB)
+    zero = np.zeros(spec.nn)
+    alive, _, flux, dep = O.push(m, zero, zero, 1.602e-19, 16 * 1.66053886e-27, 5e-7, segs, ptr, idx, P)
+    assert alive == 0
+    t = (lc[:, 1] * 1e-3 - y1) / (y2 - y1)
+    for f in (flux, dep):
+        assert f[0] + f[1] == pytest.approx(n * w, rel=1e-12)
+        assert f[1] == pytest.approx(w * t.sum(), rel=1e-9)
+        assert np.all(f[2:] == 0)

@@ -616,3 +616,25 @@ def test_oracle_absorbed_flux_and_deposit_split():
         assert f[0] + f[1] == pytest.approx(n * w, rel=1e-12)
         assert f[1] == pytest.approx(w * t.sum(), rel=1e-9)
         assert np.all(f[2:] == 0)
+
+
+@pytest.mark.parametrize("domain", [O.DOM_ZR, O.DOM_RZ])
+def test_oracle_axisymmetric_operator_on_quadratics(domain):
+    """The FVM assembly on an axisymmetric mesh (Solver.java:451-553) is exact for quadratics
+    at interior nodes, with the reference's scaling: face terms carry the face radius R and
+    rows are divided by nodeVol = 2 pi area r (Mesh.java:998-1020), so A phi equals the
+    cylindrical Laplacian over 2 pi: r^2 -> 4 / 2pi, z^2 -> 2 / 2pi."""
+    ni = nj = 17
+    dh = 1e-3
+    rad = 1 if domain == O.DOM_ZR else 0
+    node_type = np.full(ni * nj, O.NODE_OPEN, np.int8)
+    face = np.full((4, ni), O.DB_DIRICHLET, np.int8)
+    m = O.OMesh(ni, nj, [0.0, 0.0], [dh, dh], domain, node_type, face)
+    p, c, v = O.assemble(m)["A"]
+    i, j = np.meshgrid(np.arange(ni), np.arange(nj))
+    r = (j if rad else i) * dh
+    z = (i if rad else j) * dh
+    for phi, lap in ((r ** 2, 4.0), (z ** 2, 2.0), (r ** 2 + 3 * z ** 2 + 5 * z, 10.0)):
+        f = phi.reshape(-1)
+        Af = np.array([np.dot(v[p[u]:p[u + 1]], f[c[p[u]:p[u + 1]]]) for u in range(ni * nj)]).reshape(nj, ni)
+        assert np.allclose(Af[1:-1, 1:-1], lap / (2 * np.pi), rtol=1e-9)

@@ -392,6 +392,26 @@ def cpu_baseline_sample(cfg, efi, efj, n_sample, threads, steps=1, seed=1):
     return done / t, t
 
 
+def reference_poisson_c0(seed=3):
+    """The oracle's Newton + SOR (omega 1.4; PoissonSolver / LinearSolverGS defaults: Newton
+    tolerance 1e-4, linear tolerance 1e-6 on ||R||_2/N) on the 81x41 ES-PIC mesh, the
+    reference's own CPU-sized case, from phi = 0 with a noisy ion density around 1e12 m^-3.
+    The 2049x1025 solve is out of reach of SOR on the host."""
+    from oracle import oracle as O
+    from starfish_gb300 import workloads as W
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    m = O.OMesh(spec.ni, spec.nj, spec.x0, spec.dh, spec.domain, spec.node_type, spec.face_type)
+    rng = np.random.default_rng(seed)
+    rho = 1.602176565e-19 * 1e12 * (1 + 0.2 * rng.standard_normal(spec.nn))
+    t0 = time.perf_counter()
+    phi, it, out = O.poisson_nl(m, spec.bc_value, rho, 1e12, 2.0, 0.0, 8.85418782e-12, np.zeros(spec.nn),
+                                max_it=200000, tol=1e-6, nl_max_it=100, nl_tol=1e-4)
+    ms = 1e3 * (time.perf_counter() - t0)
+    res = O.poisson_residual(m, spec.bc_value, rho, 1e12, 2.0, 0.0, 8.85418782e-12, phi) / spec.nn
+    return {"workload": "es_pic_81x41 cold solve", "ms_per_solve": ms, "newton_it": int(it),
+            "linear_sweeps": int(out[1]), "residual": float(res), "cores": 1, "kind": "port"}
+
+
 def run_reference(args):
     """Reference arm: the CPU restatement with all host threads, same workload and metric."""
     rank = int(os.environ.get("RANK", "0"))
@@ -423,6 +443,7 @@ def run_reference(args):
                          "sample": f"{n_sample} particles of the 64M workload per step, "
                                    f"{args.steps} steps, push on {threads} threads + serial scatter"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "poisson": reference_poisson_c0(),
     }
     print(json.dumps(line))
 

@@ -29,3 +29,5 @@ def test_reference_arm_json_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    ps = d["poisson"]
+    assert ps["ms_per_solve"] > 0 and ps["newton_it"] >= 1 and ps["residual"] < 1e-5

@@ -638,3 +638,22 @@ def test_oracle_axisymmetric_operator_on_quadratics(domain):
         f = phi.reshape(-1)
         Af = np.array([np.dot(v[p[u]:p[u + 1]], f[c[p[u]:p[u + 1]]]) for u in range(ni * nj)]).reshape(nj, ni)
         assert np.allclose(Af[1:-1, 1:-1], lap / (2 * np.pi), rtol=1e-9)
+
+
+def test_oracle_xy_maxwellian_source_known_answer():
+    """MaxwellianSource on an XY inlet (MaxwellianSource.java:93-125, Source.java:167-198):
+    the count per step is den L (v_drift + v_mean / 4) dt / w with the fraction carried;
+    the velocity is the drift along the inward normal plus SampleMaxw3D (the sampler's 1.2
+    spread factor, Utils.java:27-57); positions are uniform along the segment."""
+    seg = np.array([0.0, 0.04, 0.0, 0.0])
+    mass = 16 * 1.66053886e-27
+    den, vd, T, spwt, dt = 1e12, 7000.0, 1000.0, 5e2, 5e-7
+    parts, rem = O.maxwellian_source(7, seg, den, vd, T, mass, spwt, dt, cap=1 << 22, domain=0)
+    v_mean = np.sqrt(8 * 1.3806503e-23 * T / (np.pi * mass))
+    expect = den * 0.04 * (vd + v_mean / 4) * dt / spwt
+    assert parts.shape[0] == int(expect) and rem == pytest.approx(expect - int(expect), abs=1e-6)
+    sig = np.sqrt(1.3806503e-23 * T / mass)
+    assert parts[:, 3].mean() == pytest.approx(vd, abs=6 * 1.2 * sig / np.sqrt(parts.shape[0]))
+    assert parts[:, 4].std() == pytest.approx(1.2 * sig, rel=0.01)
+    assert parts[:, 1].mean() == pytest.approx(0.02, abs=6 * 0.04 / np.sqrt(12 * parts.shape[0]))
+    assert parts[:, 1].min() >= 0.0 and parts[:, 1].max() <= 0.04

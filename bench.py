@@ -392,6 +392,18 @@ def cpu_baseline_sample(cfg, efi, efj, n_sample, threads, steps=1, seed=1):
     return done / t, t
 
 
+def aggregate_over_ranks(ms, psteps, device):
+    """One replica per rank: the slowest rank's timed milliseconds and the particle-steps of
+    all ranks, over the default process group."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    tot = torch.tensor([float(psteps)], dtype=torch.float64, device=device)
+    dist.all_reduce(tot)
+    return t.item(), tot.item()
+
+
 def reference_poisson_c0(seed=3):
     """The oracle's Newton + SOR (omega 1.4; PoissonSolver / LinearSolverGS defaults: Newton
     tolerance 1e-4, linear tolerance 1e-6 on ||R||_2/N) on the 81x41 ES-PIC mesh, the
@@ -524,15 +536,10 @@ def main():
     sort_ms, sort_n = dom.kernel_time("sort")
     slow_ms, slow_n = dom.kernel_time("push_slow")
     dom.timing(False)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
     if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tot = torch.tensor([float(psteps)], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(tot)
-        psteps_all = tot.item()
+        ms, psteps_all = aggregate_over_ranks(ms, psteps, "cuda")
     else:
         psteps_all = float(psteps)
-    ms = t.item()
     value = psteps_all / (ms / 1e3)
 
     # ---- end-to-end through the C ABI with host buffers ----

@@ -260,8 +260,10 @@ int sf_samples_compute(sf_ctx* ctx, int32_t sid, double T_init, int64_t* num_sam
  *  - the species may hold at most 2^21 (2,097,152) particle slots (live + removed
  *    since the last sort); a larger species is rejected with SF_ERR_ARG;
  *  - the first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress) and caches it; make that first call before any stream
- *    capture;
+ *    (cudaGetSymbolAddress) and caches it for the life of the process; make that first
+ *    call before any stream capture.  A device reset (cudaDeviceReset) discards the
+ *    array and leaves the cached address stale, so a host that resets a device must
+ *    not call this entry point again in that process;
  *  - every call, from every context on the device, shares the one array: calls whose
  *    GPU work overlaps (other threads, other contexts' streams) race on it.  Calls
  *    from one thread are safe, since each call waits for its own work to finish. */
@@ -401,13 +403,30 @@ typedef struct {
  * (a counting sort of the species), then per cell the NTC selection count
  * nsel = (n1 w / Vc) n2 dt (sigma g)max / 2 + rem, random pairs accepted with
  * sigma(g) g / (sigma g)max, and the elastic VHS/VSS scattering of ModelElastic.
- * dt: frequency * dt of the reference.  sig_cr_max0: initial (sigma g)max of every cell
- * (DSMC element sig_cr_max, default 1e-16).  *n_coll: collisions performed. */
+ * Every ordered pair of two distinct particles of a cell is an equally likely
+ * candidate, as in the reference; the candidates of one parallel round share no
+ * particle.  dt: frequency * dt of the reference.  sig_cr_max0: initial (sigma g)max of
+ * every cell (DSMC element sig_cr_max, default 1e-16).  *n_coll: collisions performed. */
 int sf_dsmc(sf_ctx* ctx, int32_t sid, const sf_sigma* sigma, double dt, double sig_cr_max0,
             int64_t* n_coll);
+/* DSMC.perform for the pair="mat1,mat2" of two kinetic species (DSMC.java:259-453):
+ * both species are binned; nsel = (n1 w1 / Vc) n2 dt (sigma g)max / (Pab + (w2/w1) Pba),
+ * doubled for two species, + rem, with Boyd's Pab = min(1, w2/w1), Pba = min(1, w1/w2);
+ * each candidate is one uniform particle of each species; ModelElastic with the reduced
+ * masses, and when the weights differ each particle's velocity changes with probability
+ * w_other / w_self (Boyd 1996).  sigma1 holds the cross-section model and coefficients
+ * and mat1's diameter, reference temperature, viscosity index and VSS alpha; sigma2
+ * holds mat2's (its model and coefficients are not used); Bird 4.63 takes
+ * d = d1 + d2 over 4 (SigmaBird463.init), the mean T_ref and omega, and vss_inv =
+ * (1/alpha1 + 1/alpha2) / 2.  sid1 == sid2 is sf_dsmc (sigma2 may be NULL). */
+int sf_dsmc_pair(sf_ctx* ctx, int32_t sid1, int32_t sid2, const sf_sigma* sigma1, const sf_sigma* sigma2,
+                 double dt, double sig_cr_max0, int64_t* n_coll);
 /* Per-cell collision sums accumulated by sf_dsmc ((ni-1)*(nj-1) each, j-major):
- * count (col-count-sum) and weight (col-real-sum), DSMC.java:241-247. */
+ * count (col-count-sum) and weight (col-real-sum, 0.5 (w1 + w2) per collision),
+ * DSMC.java:241-247,344. */
 int sf_dsmc_get_counts(sf_ctx* ctx, int32_t sid, double* count_sum, double* real_sum);
+/* The same sums for the pair (sid1, sid2) of sf_dsmc_pair. */
+int sf_dsmc_pair_get_counts(sf_ctx* ctx, int32_t sid1, int32_t sid2, double* count_sum, double* real_sum);
 /* Target (background) material of MCC: mass and node fields density, mean velocity and
  * temperature (Material.getDen / getUAve.. / getT), ni*nj each; u, v, w may be NULL (0). */
 int sf_mcc_set_target(sf_ctx* ctx, double mass, const double* den, const double* u, const double* v,

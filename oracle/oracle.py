@@ -101,6 +101,9 @@ def _declare(L):
     L.orc_dsmc.argtypes = [C.c_int, C.c_int, d, C.c_int, d, C.c_double, C.c_double, C.c_double,
                            C.c_double, C.c_double, C.c_double, C.c_double, d, d, C.c_int64]
     L.orc_dsmc.restype = C.c_long
+    L.orc_dsmc_pair.argtypes = [C.c_int, C.c_int, d, C.c_int, d, C.c_double, C.c_double, C.c_int, d, C.c_double,
+                                C.c_double] + [C.c_double] * 9 + [d, d, C.c_int64]
+    L.orc_dsmc_pair.restype = C.c_long
     L.orc_mcc.argtypes = [C.c_int, C.c_int, d, d, C.c_int, i8, i8, C.c_int, d, C.c_double,
                           C.c_double, d, d, d, d, d, C.c_double, C.c_double, C.c_int, C.c_int64]
     L.orc_mcc.restype = C.c_long
@@ -319,6 +322,18 @@ def dsmc(ni, nj, cell_vol, parts, mass, spwt, d_ref, T_ref, omega, vss_alpha, de
     return lib().orc_dsmc(ni, nj, _f64(cell_vol), parts.shape[0], parts.reshape(-1), mass, spwt,
                           d_ref, T_ref, omega, vss_alpha, delta_t, cell_state.reshape(-1),
                           counts.reshape(-1), int(seed))
+
+
+def dsmc_pair(ni, nj, cell_vol, parts1, mass1, spwt1, parts2, mass2, spwt2, mat1, mat2, delta_t,
+              cell_state, counts, seed):
+    """DSMC.collideCell for two materials; mat1/mat2: dicts of diam, T_ref, omega, vss_alpha."""
+    for a in (parts1, parts2, cell_state, counts):
+        assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return lib().orc_dsmc_pair(ni, nj, _f64(cell_vol), parts1.shape[0], parts1.reshape(-1), mass1, spwt1,
+                               parts2.shape[0], parts2.reshape(-1), mass2, spwt2, mat1["diam"], mat2["diam"],
+                               mat1["T_ref"], mat2["T_ref"], mat1["omega"], mat2["omega"],
+                               mat1.get("vss_alpha", 1.0), mat2.get("vss_alpha", 1.0), delta_t,
+                               cell_state.reshape(-1), counts.reshape(-1), int(seed))
 
 
 def mcc(m: OMesh, parts, src_mass, tgt_mass, tden, tu, tv, tw, tT, sigma, dt, model, seed):

@@ -1461,6 +1461,117 @@ long orc_dsmc(int ni, int nj, const double* cell_vol, int n, double* parts, doub
   return total;
 }
 
+// DSMC.collideCell for two different kinetic materials (DSMC.java:259-350 with
+// mat1 != mat2) and ModelElastic.perform with Boyd's variable-weight update
+// (:373-453); SigmaBird463.init for the pair (SigmaPlus.java:54-66).  Particles of each
+// species are binned by cell in array order, as the reference's iterators list them.
+long orc_dsmc_pair(int ni, int nj, const double* cell_vol, int n1, double* parts1, double mass1, double spwt1,
+                   int n2, double* parts2, double mass2, double spwt2, double d1, double d2, double T_ref1,
+                   double T_ref2, double omega1, double omega2, double alpha1, double alpha2, double delta_t,
+                   double* cell_state, double* counts, int64_t seed) {
+  JRandom rnd;
+  rnd.set_seed(seed);
+  int nc = (ni - 1) * (nj - 1);
+  std::vector<std::vector<int>> c1(nc), c2(nc);
+  Particle* P1 = reinterpret_cast<Particle*>(parts1);
+  Particle* P2 = reinterpret_cast<Particle*>(parts2);
+  for (int p = 0; p < n1; p++) {
+    if (P1[p].alive == 0) continue;
+    int i = (int)P1[p].lc[0], j = (int)P1[p].lc[1];
+    if (i >= ni - 1 || j >= nj - 1) continue;
+    c1[j * (ni - 1) + i].push_back(p);
+  }
+  for (int p = 0; p < n2; p++) {
+    if (P2[p].alive == 0) continue;
+    int i = (int)P2[p].lc[0], j = (int)P2[p].lc[1];
+    if (i >= ni - 1 || j >= nj - 1) continue;
+    c2[j * (ni - 1) + i].push_back(p);
+  }
+  const double dsum = d1 + d2;
+  const double sigma0 = 0.25 * PI * dsum * dsum;
+  const double T_ref = 0.5 * (T_ref1 + T_ref2), omega = 0.5 * (omega1 + omega2);
+  const double mr = mass1 * mass2 / (mass1 + mass2);
+  const double gam = bird_gamma(2.5 - omega);
+  const double vss_inv = 0.5 * (1.0 / alpha1 + 1.0 / alpha2);
+  long total = 0;
+  for (int i = 0; i < ni - 1; i++)
+    for (int j = 0; j < nj - 1; j++) {
+      int c = j * (ni - 1) + i;
+      auto& L1 = c1[c];
+      auto& L2 = c2[c];
+      double* st = cell_state + 2 * c;
+      double np1 = (double)L1.size(), np2 = (double)L2.size();
+      double Pab = spwt2 / spwt1, Pba = spwt1 / spwt2;
+      if (Pab > 1) Pab = 1;
+      if (Pba > 1) Pba = 1;
+      double nsel_f = ((np1 * spwt1 / cell_vol[c]) * np2 * delta_t * st[0]) / (Pab + (spwt2 / spwt1) * Pba);
+      nsel_f *= 2.0;
+      nsel_f += st[1];
+      int nsel = (int)nsel_f;
+      if (np1 < 1 || np2 < 1) continue;
+      st[1] = nsel_f - nsel;
+      if (nsel > np1 * np2) { nsel = (int)(np1 * np2); st[1] = 0; }
+      double sig_cr_max = 0;
+      for (int k = 0; k < nsel; k++) {
+        int p1 = (int)(rnd.nextDouble() * np1);
+        int p2 = (int)(rnd.nextDouble() * np2);
+        Particle& a = P1[L1[p1]];
+        Particle& b = P2[L2[p2]];
+        double cr[3] = {a.vel[0] - b.vel[0], a.vel[1] - b.vel[1], a.vel[2] - b.vel[2]};
+        double cr_mag = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+        double sigma = sigma0 * std::pow(2. * KB * T_ref / (mr * cr_mag * cr_mag), omega - 0.5) / gam;
+        double sigma_cr = cr_mag * sigma;
+        if (sigma_cr > sig_cr_max) sig_cr_max = sigma_cr;
+        if (rnd.nextDouble() < sigma_cr / st[0]) {
+          double rm1 = mass1 / (mass1 + mass2), rm2 = mass2 / (mass1 + mass2);
+          double g_mag = cr_mag;
+          double vc[3], vr[3];
+          for (int q = 0; q < 3; q++) vc[q] = rm1 * a.vel[q] + rm2 * b.vel[q];
+          if (std::fabs(vss_inv - 1.) < 1.e-4) {
+            double B = 2. * rnd.nextDouble() - 1.0;
+            double A = std::sqrt(1. - B * B);
+            vr[0] = B * g_mag;
+            double C = 2. * PI * rnd.nextDouble();
+            vr[1] = A * std::cos(C) * g_mag;
+            vr[2] = A * std::sin(C) * g_mag;
+          } else {
+            double B = 2. * (std::pow(rnd.nextDouble(), vss_inv)) - 1.;
+            double A = std::sqrt(1. - B * B);
+            double C = 2. * PI * rnd.nextDouble();
+            double OC = std::cos(C), SC = std::sin(C);
+            double D = std::sqrt(cr[1] * cr[1] + cr[2] * cr[2]);
+            if (D > 1.e-6) {
+              vr[0] = B * cr[0] + A * SC * D;
+              vr[1] = B * cr[1] + A * (g_mag * cr[2] * OC - cr[0] * cr[1] * SC) / D;
+              vr[2] = B * cr[2] - A * (g_mag * cr[1] * OC + cr[0] * cr[2] * SC) / D;
+            } else {
+              vr[0] = B * cr[1];
+              vr[1] = A * OC * cr[1];
+              vr[2] = A * SC * cr[1];
+            }
+          }
+          if (a.mpw == b.mpw) {
+            for (int q = 0; q < 3; q++) {
+              a.vel[q] = vc[q] + vr[q] * rm2;
+              b.vel[q] = vc[q] - vr[q] * rm1;
+            }
+          } else {
+            double pab = b.mpw / a.mpw, pba = a.mpw / b.mpw;
+            if (rnd.nextDouble() < pab)
+              for (int q = 0; q < 3; q++) a.vel[q] = vc[q] + rm2 * vr[q];
+            if (rnd.nextDouble() < pba)
+              for (int q = 0; q < 3; q++) b.vel[q] = vc[q] - rm1 * vr[q];
+          }
+          counts[2 * c] += 1.0;
+          counts[2 * c + 1] += 0.5 * (a.mpw + b.mpw);
+          total++;
+        }
+      }
+      if (sig_cr_max > 0) st[0] = sig_cr_max;
+    }
+  return total;
+}
+
 // --- MCC (collisions/MCC.java:167-285): MEX (elastic) or CEX against a Maxwellian
 // target described by node fields (den, u, v, w, T).  Constant cross-section sigma
 // (SigmaConst, Sigma.java:121-126).  model: 0 = MEX, 1 = CEX.  Returns collisions.

@@ -185,6 +185,9 @@ EXPORTS.update({
     "sf_dsmc": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Sigma), C.c_double, C.c_double,
                           C.POINTER(C.c_int64)]),
     "sf_dsmc_get_counts": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "sf_dsmc_pair": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(Sigma), C.POINTER(Sigma), C.c_double,
+                               C.c_double, C.POINTER(C.c_int64)]),
+    "sf_dsmc_pair_get_counts": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "sf_mcc_set_target": (C.c_int, [C.c_void_p, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_void_p, C.c_void_p]),
     "sf_mcc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(Sigma), C.c_double,

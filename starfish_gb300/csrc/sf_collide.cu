@@ -7,6 +7,7 @@
 // counter-based Philox streams keyed by (cell, step), so results match the reference in
 // distribution (its global java.util.Random stream cannot be reproduced in parallel).
 // Velocities are FP32 as stored; the selection count and cell state are FP64.
+#include <climits>
 #include <cmath>
 
 #include "sf_internal.h"
@@ -23,6 +24,8 @@ struct SigmaDev {
   float expo;      // omega - 1/2
   float inv_gamma; // 1 / Gamma(5/2 - omega) (Bird's gamma, Utils.gamma)
   float vss_inv;   // 0.5 (1/alpha1 + 1/alpha2)
+  float c_bird;    // BIRD463 sigma g = c_bird (g^2)^expo_cr: sigma0 (2 k T_ref / m_r)^(omega - 1/2) / Gamma
+  float expo_cr;   // 1/2 - (omega - 1/2)
 };
 
 // Sigma.eval (interactions/Sigma.java:121-195, SigmaPlus.java:54-76)
@@ -82,103 +85,213 @@ __device__ inline void elastic_vr(Philox& rng, float vss_inv, const float g[3], 
 constexpr int DSMC_HEAVY_NSEL = 1024;    // candidate pairs beyond which a cell gets a CTA
 constexpr int DSMC_HEAVY_THREADS = 512;
 
-// One candidate pair (a, b) of collideCell: sigma g, the NTC acceptance against the
-// cell's (sigma g)max, and ModelElastic.perform with equal masses and weights
-// (DSMC.java:373-415).  Returns whether the pair collided.
-__device__ inline bool collide_pair(ParticlesView& P, int64_t a, int64_t b, const SigmaDev& sg, float smax, Philox& rng,
+// Everything a DSMC launch needs for one material pair (DSMC.java:259-350).  For a
+// same-species pair P2/bins2 alias P1/bins1.
+struct DsmcArgs {
+  ParticlesView P1, P2;
+  const int* bins1;  // per sort key: first slot of the cell's particles (+1: the next cell's)
+  const int* bins2;
+  int ntx, nkeys;
+  const double* cell_vol;
+  double2* state;    // per cell (sigma g)max, remainder
+  double2* counts;   // per cell collision count, weight
+  SigmaDev sg;
+  double spwt1, spwt2;
+  double dt;         // frequency * dt of the reference
+  double nsel_den;   // Pab + (w2/w1) Pba (eq. 5 of Boyd's paper, DSMC.java:276-286)
+  double real_w;     // 0.5 (w1 + w2): the weight summed per collision (DSMC.java:344)
+  float rm1, rm2;    // m1/(m1+m2), m2/(m1+m2)
+  float pab, pba;    // ModelElastic's variable-weight update probabilities (w2/w1, w1/w2)
+  int boyd;          // the weights differ: Boyd's probabilistic velocity update
+  uint64_t seed;
+  uint32_t step;
+  unsigned long long* n_coll;
+  int* heavy;        // cells handed to k_dsmc_heavy (sort keys)
+  unsigned* n_heavy;
+  int heavy_cap;
+  unsigned* work;    // k_dsmc_heavy's cell counter
+};
+
+// sigma(g) g of Sigma.eval (interactions/Sigma.java:121-195, SigmaPlus.java:54-76) from
+// g^2.  Bird 4.63 is c g2^(1/2 - (omega - 1/2)) with c = sigma0 (2kT/m_r)^(omega - 1/2) /
+// Gamma: one MUFU pair and no square root.
+__device__ inline float sigma_cr_eval(const SigmaDev& s, float g2) {
+  if (s.model == SF_SIGMA_BIRD463) return g2 > 0.f ? s.c_bird * __powf(g2, s.expo_cr) : 0.f;
+  const float g = sqrtf(g2);
+  return g * sigma_eval(s, g);
+}
+
+// One candidate pair (a of P1, b of P2) of collideCell: sigma g, the NTC acceptance
+// sigma g / (sigma g)max, and ModelElastic.perform (DSMC.java:373-453) with the reduced
+// masses and, for different weights, Boyd's update probabilities.  Returns whether the
+// pair collided.
+__device__ inline bool collide_pair(const DsmcArgs& d, int64_t a, int64_t b, float smax, Philox& rng,
                                     float& smax_new) {
-  const float2 va = P.vxy[a], vb = P.vxy[b];
-  const float wa = P.vz[a], wb = P.vz[b];
+  const float2 va = d.P1.vxy[a], vb = d.P2.vxy[b];
+  const float wa = d.P1.vz[a], wb = d.P2.vz[b];
   const float g[3] = {va.x - vb.x, va.y - vb.y, wa - wb};
-  const float g_mag = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-  const float sigma_cr = g_mag * sigma_eval(sg, g_mag);
+  const float g2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+  const float sigma_cr = sigma_cr_eval(d.sg, g2);
   smax_new = fmaxf(smax_new, sigma_cr);
   if (!(rng.uniformf() < sigma_cr / smax)) return false;
-  const float vc[3] = {0.5f * (va.x + vb.x), 0.5f * (va.y + vb.y), 0.5f * (wa + wb)};
+  const float g_mag = sqrtf(g2);
+  const float vc[3] = {d.rm1 * va.x + d.rm2 * vb.x, d.rm1 * va.y + d.rm2 * vb.y, d.rm1 * wa + d.rm2 * wb};
   float vr[3];
-  elastic_vr(rng, sg.vss_inv, g, g_mag, vr);
-  P.vxy[a] = make_float2(vc[0] + 0.5f * vr[0], vc[1] + 0.5f * vr[1]);
-  P.vz[a] = vc[2] + 0.5f * vr[2];
-  P.vxy[b] = make_float2(vc[0] - 0.5f * vr[0], vc[1] - 0.5f * vr[1]);
-  P.vz[b] = vc[2] - 0.5f * vr[2];
+  elastic_vr(rng, d.sg.vss_inv, g, g_mag, vr);
+  const bool upd_a = !d.boyd || rng.uniformf() < d.pab;
+  const bool upd_b = !d.boyd || rng.uniformf() < d.pba;
+  if (upd_a) {
+    d.P1.vxy[a] = make_float2(vc[0] + d.rm2 * vr[0], vc[1] + d.rm2 * vr[1]);
+    d.P1.vz[a] = vc[2] + d.rm2 * vr[2];
+  }
+  if (upd_b) {
+    d.P2.vxy[b] = make_float2(vc[0] - d.rm1 * vr[0], vc[1] - d.rm1 * vr[1]);
+    d.P2.vz[b] = vc[2] - d.rm1 * vr[2];
+  }
   return true;
 }
 
-__device__ inline unsigned gcd_u(unsigned a, unsigned b) {
-  while (b) {
-    const unsigned t = a % b;
-    a = b;
-    b = t;
-  }
-  return a;
+__device__ inline bool is_prime(uint32_t x) {
+  if (x < 4u) return x >= 2u;
+  if ((x & 1u) == 0u) return false;
+  for (uint32_t f = 3u; (uint64_t)f * f <= x; f += 2u)
+    if (x % f == 0u) return false;
+  return true;
 }
 
-// DSMC.collideCell (DSMC.java:259-350) with one warp per cell, warps striding over the
-// cells; cells with more than DSMC_HEAVY_NSEL candidate pairs (dense cells of a jet hold
-// thousands of particles) are listed for k_dsmc_heavy instead.  The NTC
-// selection count and the acceptance sigma g / (sigma g)max are the reference's; the
-// nsel candidate pairs are drawn in rounds of up to 32 disjoint pairs, one per lane: a
-// round uses the cell's particles s + k t (mod np), k < 2 m, with random s and a random
-// stride t coprime to np, so its 2 m particles are distinct and the pairs can collide
-// in parallel.  Each pair is two distinct random particles of the cell, as in the
-// reference; only pairs within one round cannot share a particle.
-__global__ void __launch_bounds__(128) k_dsmc(MeshView m, ParticlesView P, const int* __restrict__ bins, int ntx,
-                                              int nkeys, const double* __restrict__ cell_vol,
-                                              double2* __restrict__ state, double2* __restrict__ counts,
-                                              SigmaDev sg, double spwt, double dt, uint64_t seed, uint32_t step,
-                                              unsigned long long* __restrict__ n_coll, int* __restrict__ heavy,
-                                              unsigned* __restrict__ n_heavy, int heavy_cap) {
+// Smallest prime >= n (n >= 2), the 32 lanes of a warp testing consecutive candidates.
+__device__ inline uint32_t warp_next_prime(uint32_t n) {
+  const unsigned FULL = 0xffffffffu;
+  for (uint32_t base = n;; base += 32u) {
+    const unsigned b = __ballot_sync(FULL, is_prime(base + (threadIdx.x & 31u)));
+    if (b) return base + (uint32_t)(__ffs(b) - 1);
+  }
+}
+
+// uniform in [0, q) (bias below q / 2^64)
+__device__ inline uint32_t rand_below(Philox& r, uint32_t q) {
+  const uint64_t x = ((uint64_t)r.next_u32() << 32) | r.next_u32();
+  return (uint32_t)__umul64hi(x, (uint64_t)q);
+}
+
+// Candidate pairs of a cell.  The reference draws each pair as p1 uniform and p2 != p1
+// uniform, independently (DSMC.java:314-320; for two species p1 and p2 each uniform in
+// their own list).  Here a round of pairs is collided in parallel, so its pairs must
+// not share a particle.  A round maps the fixed inputs x = 0, 1, 2, ... through a random
+// affine map s(x) = (a x + b) mod q of the prime field Z_q, q the smallest prime >= np,
+// with a uniform in [1, q) and b uniform in [0, q): the maps of Z_q are sharply
+// 2-transitive, so the images (s(x1), s(x2)) of two fixed distinct inputs are uniform
+// over all ordered pairs of distinct elements.  Input pair k of a same-species round is
+// (2k, 2k + 1); an image >= np is no particle and that candidate is not used (the
+// others, conditioned on being particles, stay uniform over the cell's ordered pairs).
+// Distinct inputs have distinct images, so the pairs of a round are disjoint.  For two
+// species lane k takes s1(k) and s2(k) from two independent maps.  Rounds continue
+// until nsel candidates have been used.
+struct AffineMap {
+  uint32_t q, a, b;
+  __device__ inline uint32_t operator()(uint32_t x) const {
+    if (q <= (1u << 22)) return (a * x + b) % q;  // a x + b < 2^32 for x < 1024
+    return (uint32_t)(((uint64_t)a * x + b) % q);
+  }
+  __device__ inline uint32_t next(uint32_t y) const {  // s(x + 1) from y = s(x)
+    const uint32_t z = y + a;
+    return z >= q ? z - q : z;
+  }
+  __device__ inline void draw(Philox& r) {
+    a = 1u + rand_below(r, q - 1u);
+    b = rand_below(r, q);
+  }
+};
+
+// Bound on the rounds of a cell: every round uses each considered candidate with
+// probability > 1/4, so this is never reached in practice; it only bounds the loop.
+__device__ inline int max_rounds(int nsel) { return nsel > (1 << 26) ? INT_MAX : 64 + 16 * nsel; }
+
+// NTC selection count of collideCell (DSMC.java:272-304): nsel and the new remainder;
+// false when the cell has too few particles (the reference returns before updating rem)
+template <bool PAIR>
+__device__ inline bool cell_nsel(const DsmcArgs& d, int np1, int np2, int c, double2 st, int& nsel, double& rem) {
+  if (PAIR ? (np1 < 1 || np2 < 1) : (np1 < 2)) return false;
+  double nsel_f = (((double)np1 * d.spwt1 / d.cell_vol[c]) * (double)np2 * d.dt * st.x) / d.nsel_den;
+  if (PAIR) nsel_f *= 2.0;  // "q-p" collisions are not done separately from "p-q"
+  nsel_f += st.y;
+  nsel = (int)nsel_f;
+  rem = nsel_f - nsel;
+  if ((double)nsel > (double)np1 * (double)np2) {
+    nsel = (int)((double)np1 * (double)np2);
+    rem = 0.0;
+  }
+  return true;
+}
+
+// DSMC.collideCell with one warp per cell, warps striding over the cells; cells with
+// more than DSMC_HEAVY_NSEL candidate pairs (the dense cells of a jet hold thousands of
+// particles) are listed for k_dsmc_heavy.  The NTC count, the acceptance and the
+// (sigma g)max update are the reference's; candidates come in rounds of up to 32
+// disjoint pairs (AffineMap), one per lane.
+template <bool PAIR>
+__global__ void __launch_bounds__(128) k_dsmc(MeshView m, DsmcArgs d) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int warps = (int)(gridDim.x * blockDim.x) >> 5;
-  for (int key = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); key < nkeys; key += warps) {
+  for (int key = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); key < d.nkeys; key += warps) {
     int i, j;
-    key_cell((uint32_t)key, ntx, i, j);
+    key_cell((uint32_t)key, d.ntx, i, j);
     if (i >= m.ni - 1 || j >= m.nj - 1) continue;
     const int c = j * (m.ni - 1) + i;
-    const int start = bins[key], np = bins[key + 1] - start;
-    if (np < 2) continue;  // the reference returns before updating rem (:293-296)
-    double2 st = state[c];  // x: (sigma g)max, y: remainder
-    const double npd = (double)np;
-    // equal weights: Pab = Pba = 1, denominator Pab + (w2/w1) Pba = 2 (DSMC.java:276-286)
-    const double nsel_f = ((npd * spwt / cell_vol[c]) * npd * dt * st.x) / 2.0 + st.y;
-    int nsel = (int)nsel_f;
-    if (nsel > DSMC_HEAVY_NSEL && np >= 128) {
+    const int s1 = d.bins1[key], np1 = d.bins1[key + 1] - s1;
+    const int s2 = PAIR ? d.bins2[key] : s1;
+    const int np2 = PAIR ? d.bins2[key + 1] - s2 : np1;
+    double2 st = d.state[c];  // x: (sigma g)max, y: remainder
+    int nsel;
+    double rem;
+    if (!cell_nsel<PAIR>(d, np1, np2, c, st, nsel, rem)) continue;
+    if (nsel > DSMC_HEAVY_NSEL && min(np1, np2) >= 128) {
       // many rounds: hand the cell to a whole CTA (k_dsmc_heavy), which recomputes nsel
       int slot = 0;
-      if (lane == 0) slot = (int)atomicAdd(n_heavy, 1u);
+      if (lane == 0) slot = (int)atomicAdd(d.n_heavy, 1u);
       slot = __shfl_sync(FULL, slot, 0);
-      if (slot < heavy_cap) {
-        if (lane == 0) heavy[slot] = key;
+      if (slot < d.heavy_cap) {
+        if (lane == 0) d.heavy[slot] = key;
         continue;
       }
     }
-    st.y = nsel_f - nsel;
-    if ((double)nsel > npd * npd) {
-      nsel = (int)(npd * npd);
-      st.y = 0.0;
-    }
-    Philox rng(seed, RNG_DSMC, (uint64_t)c * 32u + (uint64_t)lane, step);
+    st.y = rem;
+    Philox rng(d.seed, RNG_DSMC, (uint64_t)c * 32u + (uint64_t)lane, d.step);
+    AffineMap s1m, s2m;
+    s1m.q = warp_next_prime((uint32_t)np1);
+    s2m.q = PAIR ? warp_next_prime((uint32_t)np2) : s1m.q;
     float smax_new = 0.f;
     const float smax = (float)st.x;
     int ncol = 0;
-    const int per_round = min(32, np / 2);
-    for (int k0 = 0; k0 < nsel; k0 += per_round) {
-      const int mr = min(per_round, nsel - k0);
-      unsigned s0 = 0, t0 = 1;
+    const int per_round = PAIR ? min(32, min(np1, np2)) : min(32, np1 / 2);
+    int left = nsel;
+    for (int round = 0, cap = max_rounds(nsel); left > 0 && round < cap; round++) {
+      const int mr = min(per_round, left);
       if (lane == 0) {
-        s0 = (unsigned)min((int)(rng.uniform() * npd), np - 1);
-        t0 = 1u + (unsigned)min((int)(rng.uniform() * (npd - 1.0)), np - 2);
-        for (int tries = 0; tries < 64 && gcd_u(t0, (unsigned)np) != 1u; tries++) t0 = t0 % (unsigned)(np - 1) + 1u;
-        if (gcd_u(t0, (unsigned)np) != 1u) t0 = 1u;
+        s1m.draw(rng);
+        if (PAIR) s2m.draw(rng);
       }
-      s0 = __shfl_sync(FULL, s0, 0);
-      t0 = __shfl_sync(FULL, t0, 0);
+      s1m.a = __shfl_sync(FULL, s1m.a, 0);
+      s1m.b = __shfl_sync(FULL, s1m.b, 0);
+      if (PAIR) {
+        s2m.a = __shfl_sync(FULL, s2m.a, 0);
+        s2m.b = __shfl_sync(FULL, s2m.b, 0);
+      }
+      bool used = false;
       if (lane < mr) {
-        const int p1 = (int)((s0 + (uint64_t)(2 * lane) * t0) % (uint64_t)np);
-        const int p2 = (int)((s0 + (uint64_t)(2 * lane + 1) * t0) % (uint64_t)np);
-        if (collide_pair(P, start + p1, start + p2, sg, smax, rng, smax_new)) ncol++;
+        uint32_t p1, p2;
+        if (PAIR) {
+          p1 = s1m((uint32_t)lane);
+          p2 = s2m((uint32_t)lane);
+        } else {
+          p1 = s1m(2u * lane);
+          p2 = s1m.next(p1);
+        }
+        used = p1 < (uint32_t)np1 && p2 < (uint32_t)np2;
+        if (used && collide_pair(d, s1 + (int64_t)p1, s2 + (int64_t)p2, smax, rng, smax_new)) ncol++;
       }
+      left -= __popc(__ballot_sync(FULL, used));
       __syncwarp();  // this round's velocities are visible to the next round's lanes
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -187,74 +300,100 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, ParticlesView P, const
     }
     if (lane == 0) {
       if (smax_new > 0.f) st.x = (double)smax_new;
-      state[c] = st;
+      d.state[c] = st;
       if (ncol) {
-        double2 cs = counts[c];
+        double2 cs = d.counts[c];
         cs.x += ncol;
-        cs.y += ncol * spwt;  // 0.5 (w1 + w2) per collision
-        counts[c] = cs;
-        atomicAdd(n_coll, (unsigned long long)ncol);
+        cs.y += ncol * d.real_w;
+        d.counts[c] = cs;
+        atomicAdd(d.n_coll, (unsigned long long)ncol);
       }
     }
   }
 }
 
 // The cells handed over by k_dsmc, one CTA of DSMC_HEAVY_THREADS per cell: rounds of up
-// to DSMC_HEAVY_THREADS disjoint pairs (same selection as k_dsmc), the CTA synchronising
-// between rounds.
-__global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(
-    MeshView m, ParticlesView P, const int* __restrict__ bins, int ntx, const double* __restrict__ cell_vol,
-    double2* __restrict__ state, double2* __restrict__ counts, SigmaDev sg, double spwt, double dt, uint64_t seed,
-    uint32_t step, unsigned long long* __restrict__ n_coll, const int* __restrict__ heavy,
-    const unsigned* __restrict__ n_heavy, int heavy_cap, unsigned* __restrict__ work) {
+// to DSMC_HEAVY_THREADS disjoint pairs (the same AffineMap selection), the CTA
+// synchronising between rounds.
+template <bool PAIR>
+__global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, DsmcArgs d) {
   __shared__ int s_idx;
-  __shared__ unsigned s_s0, s_t0;
+  __shared__ uint32_t s_q[2], s_ab[4];
   __shared__ float s_max[DSMC_HEAVY_THREADS / 32];
   __shared__ int s_n[DSMC_HEAVY_THREADS / 32];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const int nh = min((int)*n_heavy, heavy_cap);
+  const int nh = min((int)*d.n_heavy, d.heavy_cap);
   for (;;) {
-    if (tid == 0) s_idx = (int)atomicAdd(work, 1u);
+    if (tid == 0) s_idx = (int)atomicAdd(d.work, 1u);
     __syncthreads();
     const int idx = s_idx;
     __syncthreads();
     if (idx >= nh) break;
-    const int key = heavy[idx];
+    const int key = d.heavy[idx];
     int i, j;
-    key_cell((uint32_t)key, ntx, i, j);
+    key_cell((uint32_t)key, d.ntx, i, j);
     const int c = j * (m.ni - 1) + i;
-    const int start = bins[key], np = bins[key + 1] - start;
-    double2 st = state[c];
-    const double npd = (double)np;
-    const double nsel_f = ((npd * spwt / cell_vol[c]) * npd * dt * st.x) / 2.0 + st.y;
-    int nsel = (int)nsel_f;
-    st.y = nsel_f - nsel;
-    if ((double)nsel > npd * npd) {
-      nsel = (int)(npd * npd);
-      st.y = 0.0;
+    const int s1 = d.bins1[key], np1 = d.bins1[key + 1] - s1;
+    const int s2 = PAIR ? d.bins2[key] : s1;
+    const int np2 = PAIR ? d.bins2[key + 1] - s2 : np1;
+    double2 st = d.state[c];
+    int nsel;
+    double rem;
+    cell_nsel<PAIR>(d, np1, np2, c, st, nsel, rem);  // true: k_dsmc listed the cell
+    st.y = rem;
+    if (wid == 0) {
+      const uint32_t q1 = warp_next_prime((uint32_t)np1);
+      const uint32_t q2 = PAIR ? warp_next_prime((uint32_t)np2) : q1;
+      if (lane == 0) {
+        s_q[0] = q1;
+        s_q[1] = q2;
+      }
     }
-    Philox rng(seed, RNG_DSMC_HEAVY, (uint64_t)c * DSMC_HEAVY_THREADS + (uint64_t)tid, step);
+    __syncthreads();
+    AffineMap s1m, s2m;
+    s1m.q = s_q[0];
+    s2m.q = s_q[1];
+    Philox rng(d.seed, RNG_DSMC_HEAVY, (uint64_t)c * DSMC_HEAVY_THREADS + (uint64_t)tid, d.step);
     float smax_new = 0.f;
     const float smax = (float)st.x;
     int ncol = 0;
-    const int per_round = min(DSMC_HEAVY_THREADS, np / 2);
-    for (int k0 = 0; k0 < nsel; k0 += per_round) {
-      const int mr = min(per_round, nsel - k0);
+    const int per_round = PAIR ? min(DSMC_HEAVY_THREADS, min(np1, np2)) : min(DSMC_HEAVY_THREADS, np1 / 2);
+    int left = nsel;
+    for (int round = 0, cap = max_rounds(nsel); left > 0 && round < cap; round++) {
+      const int mr = min(per_round, left);
       if (tid == 0) {
-        unsigned s0 = (unsigned)min((int)(rng.uniform() * npd), np - 1);
-        unsigned t0 = 1u + (unsigned)min((int)(rng.uniform() * (npd - 1.0)), np - 2);
-        for (int tries = 0; tries < 64 && gcd_u(t0, (unsigned)np) != 1u; tries++) t0 = t0 % (unsigned)(np - 1) + 1u;
-        if (gcd_u(t0, (unsigned)np) != 1u) t0 = 1u;
-        s_s0 = s0;
-        s_t0 = t0;
+        s1m.draw(rng);
+        s_ab[0] = s1m.a;
+        s_ab[1] = s1m.b;
+        if (PAIR) {
+          s2m.draw(rng);
+          s_ab[2] = s2m.a;
+          s_ab[3] = s2m.b;
+        }
       }
       __syncthreads();
-      if (tid < mr) {
-        const int p1 = (int)((s_s0 + (uint64_t)(2 * tid) * s_t0) % (uint64_t)np);
-        const int p2 = (int)((s_s0 + (uint64_t)(2 * tid + 1) * s_t0) % (uint64_t)np);
-        if (collide_pair(P, start + p1, start + p2, sg, smax, rng, smax_new)) ncol++;
+      s1m.a = s_ab[0];
+      s1m.b = s_ab[1];
+      if (PAIR) {
+        s2m.a = s_ab[2];
+        s2m.b = s_ab[3];
       }
-      __syncthreads();  // velocities and s_s0 / s_t0 of this round are done with
+      bool used = false;
+      if (tid < mr) {
+        uint32_t p1, p2;
+        if (PAIR) {
+          p1 = s1m((uint32_t)tid);
+          p2 = s2m((uint32_t)tid);
+        } else {
+          p1 = s1m(2u * tid);
+          p2 = s1m.next(p1);
+        }
+        used = p1 < (uint32_t)np1 && p2 < (uint32_t)np2;
+        if (used && collide_pair(d, s1 + (int64_t)p1, s2 + (int64_t)p2, smax, rng, smax_new)) ncol++;
+      }
+      // the count of used candidates; also orders this round's velocities and s_ab
+      // before the next round
+      left -= __syncthreads_count(used);
     }
     for (int o = 16; o > 0; o >>= 1) {
       smax_new = fmaxf(smax_new, __shfl_xor_sync(0xffffffffu, smax_new, o));
@@ -271,15 +410,16 @@ __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(
         ncol += s_n[w];
       }
       if (smax_new > 0.f) st.x = (double)smax_new;
-      state[c] = st;
+      d.state[c] = st;
       if (ncol) {
-        double2 cs = counts[c];
+        double2 cs = d.counts[c];
         cs.x += ncol;
-        cs.y += ncol * spwt;
-        counts[c] = cs;
-        atomicAdd(n_coll, (unsigned long long)ncol);
+        cs.y += ncol * d.real_w;
+        d.counts[c] = cs;
+        atomicAdd(d.n_coll, (unsigned long long)ncol);
       }
     }
+    __syncthreads();  // s_max / s_n are reused by the next cell
   }
 }
 
@@ -502,46 +642,67 @@ double bird_gamma(double X) {
               0.1010678 * Y * Y * Y * Y * Y);
 }
 
-SigmaDev make_sigma(const sf_sigma* s, double m1, double m2) {
+// Sigma.init for the pair (mat1, mat2) (SigmaPlus.java:54-66 for Bird 4.63) and the pair's
+// vss_inv (DSMC.java:81).  s2 carries the second material's diameter, reference
+// temperature, viscosity index and VSS alpha; null for a same-material pair.
+SigmaDev make_sigma(const sf_sigma* s, const sf_sigma* s2, double m1, double m2) {
   SF_REQUIRE(s, SF_ERR_ARG, "null sigma");
   SF_REQUIRE(s->model >= SF_SIGMA_CONST && s->model <= SF_SIGMA_BIRD463, SF_ERR_ARG, "bad sigma model");
+  if (!s2) s2 = s;
   SigmaDev d{};
   d.model = s->model;
   for (int k = 0; k < 4; k++) d.c[k] = (float)s->c[k];
   if (s->model == SF_SIGMA_BIRD463) {
-    SF_REQUIRE(s->diam > 0 && s->T_ref > 0, SF_ERR_ARG, "Bird 4.63 needs diam and T_ref");
-    // SigmaBird463.init (SigmaPlus.java:54-66) with mat1 == mat2
-    const double d_ref = s->diam + s->diam;
+    SF_REQUIRE(s->diam > 0 && s->T_ref > 0 && s2->diam > 0 && s2->T_ref > 0, SF_ERR_ARG,
+               "Bird 4.63 needs diam and T_ref");
+    const double d_ref = s->diam + s2->diam;
+    const double T_ref = 0.5 * (s->T_ref + s2->T_ref);
+    const double omega = 0.5 * (s->omega + s2->omega);
     const double mr = m1 * m2 / (m1 + m2);
-    d.sigma0 = (float)(0.25 * PI * d_ref * d_ref);
-    d.kT2_mr = (float)(2.0 * KB * s->T_ref / mr);
-    d.expo = (float)(s->omega - 0.5);
-    d.inv_gamma = (float)(1.0 / bird_gamma(2.5 - s->omega));
+    const double sigma0 = 0.25 * PI * d_ref * d_ref;
+    const double kT2_mr = 2.0 * KB * T_ref / mr;
+    const double inv_gamma = 1.0 / bird_gamma(2.5 - omega);
+    d.sigma0 = (float)sigma0;
+    d.kT2_mr = (float)kT2_mr;
+    d.expo = (float)(omega - 0.5);
+    d.inv_gamma = (float)inv_gamma;
+    d.c_bird = (float)(sigma0 * std::pow(kT2_mr, omega - 0.5) * inv_gamma);
+    d.expo_cr = (float)(0.5 - (omega - 0.5));
   }
-  const double a = s->vss_alpha > 0 ? s->vss_alpha : 1.0;
-  d.vss_inv = (float)(0.5 * (1.0 / a + 1.0 / a));
+  const double a1 = s->vss_alpha > 0 ? s->vss_alpha : 1.0;
+  const double a2 = s2->vss_alpha > 0 ? s2->vss_alpha : 1.0;
+  d.vss_inv = (float)(0.5 * (1.0 / a1 + 1.0 / a2));
   return d;
 }
 
 }  // namespace
 
 struct SfDsmcState {
+  int sid1 = -1, sid2 = -1;
   double2* state = nullptr;   // per cell (sigma g)max, remainder
   double2* counts = nullptr;  // per cell collision count, weight
   double* cell_vol = nullptr;
-  bool init = false;
+  int* bins1 = nullptr;       // two species: the first one's sort bins (the second uses ctx->bins)
 };
 
-// per-context, per-species DSMC state; freed with the context through the destroy hook
-static SfDsmcState* dsmc_state(sf_ctx* ctx, int sid, double sig_cr_max0) {
-  if ((int)ctx->dsmc.size() <= sid) ctx->dsmc.resize(sid + 1, nullptr);
-  SfDsmcState*& st = ctx->dsmc[sid];
-  if (st) return st;
-  st = new SfDsmcState();
+// per-context DSMC state of a material pair; freed with the context through the destroy hook
+static SfDsmcState* find_dsmc(sf_ctx* ctx, int sid1, int sid2) {
+  for (SfDsmcState* st : ctx->dsmc)
+    if (st->sid1 == sid1 && st->sid2 == sid2) return st;
+  return nullptr;
+}
+
+static SfDsmcState* dsmc_state(sf_ctx* ctx, int sid1, int sid2, double sig_cr_max0) {
+  if (SfDsmcState* st = find_dsmc(ctx, sid1, sid2)) return st;
+  SfDsmcState* st = new SfDsmcState();
+  ctx->dsmc.push_back(st);
+  st->sid1 = sid1;
+  st->sid2 = sid2;
   const int nc = ctx->ncells();
   SF_CUDA(cudaMalloc(&st->state, sizeof(double2) * nc));
   SF_CUDA(cudaMalloc(&st->counts, sizeof(double2) * nc));
   SF_CUDA(cudaMalloc(&st->cell_vol, sizeof(double) * nc));
+  if (sid1 != sid2) SF_CUDA(cudaMalloc(&st->bins1, sizeof(int) * ((size_t)ctx->nkeys + 1)));
   std::vector<double2> s0(nc, make_double2(sig_cr_max0, 0.0));
   copy_wait(st->state, s0.data(), sizeof(double2) * nc, cudaMemcpyHostToDevice, ctx->stream);
   zero_wait(st->counts, sizeof(double2) * nc, ctx->stream);
@@ -556,16 +717,15 @@ static SfDsmcState* dsmc_state(sf_ctx* ctx, int sid, double sig_cr_max0) {
       cv[(size_t)j * (ctx->ni - 1) + i] = v;
     }
   copy_wait(st->cell_vol, cv.data(), sizeof(double) * nc, cudaMemcpyHostToDevice, ctx->stream);
-  st->init = true;
   return st;
 }
 
 void sf_collide_destroy_internal(sf_ctx* ctx) {
   for (SfDsmcState* st : ctx->dsmc) {
-    if (!st) continue;
     cudaFree(st->state);
     cudaFree(st->counts);
     cudaFree(st->cell_vol);
+    cudaFree(st->bins1);
     delete st;
   }
   ctx->dsmc.clear();
@@ -583,32 +743,69 @@ void sf_collide_destroy_internal(sf_ctx* ctx) {
   }
 }
 
-extern "C" {
+namespace {
 
-int sf_dsmc(sf_ctx* ctx, int32_t sid, const sf_sigma* sigma, double dt, double sig_cr_max0, int64_t* n_coll) {
-  SF_API_BEGIN
-  SfSpecies* sp = get_species(ctx, sid);
+// DSMC.perform(mesh) for the pair (sid1, sid2): cell binning by the species' counting
+// sorts, then collideCell per cell (k_dsmc, k_dsmc_heavy).
+void dsmc_run(sf_ctx* ctx, int sid1, int sid2, const sf_sigma* sigma, const sf_sigma* sigma2, double dt,
+              double sig_cr_max0, int64_t* n_coll) {
+  SfSpecies* sp1 = get_species(ctx, sid1);
+  SfSpecies* sp2 = get_species(ctx, sid2);
   SF_REQUIRE(dt > 0 && sig_cr_max0 > 0, SF_ERR_ARG, "dt and sig_cr_max must be positive");
   SF_CUDA(cudaSetDevice(ctx->device));
-  const SigmaDev sg = make_sigma(sigma, sp->mass, sp->mass);
-  SfDsmcState* st = dsmc_state(ctx, sid, sig_cr_max0);
-  // DSMC.perform(mesh) bins particles by cell on every call: the counting sort
-  launch_sort(ctx, sp);
+  const bool pair = sid1 != sid2;
+  SfDsmcState* st = dsmc_state(ctx, sid1, sid2, sig_cr_max0);
+  DsmcArgs d{};
+  d.sg = make_sigma(sigma, pair ? sigma2 : nullptr, sp1->mass, sp2->mass);
+  // DSMC.perform(mesh) bins particles by cell on every call: the counting sort.  With two
+  // species the first one's bins are kept aside before the second sort reuses ctx->bins.
+  launch_sort(ctx, sp1);
+  if (pair) {
+    SF_CUDA(cudaMemcpyAsync(st->bins1, ctx->bins, sizeof(int) * ((size_t)ctx->nkeys + 1), cudaMemcpyDeviceToDevice,
+                            ctx->stream));
+    launch_sort(ctx, sp2);
+  }
+  d.P1 = sp1->cur;
+  d.P2 = sp2->cur;
+  d.bins1 = pair ? st->bins1 : ctx->bins;
+  d.bins2 = ctx->bins;
+  d.ntx = ctx->ntx;
+  d.nkeys = ctx->nkeys;
+  d.cell_vol = st->cell_vol;
+  d.state = st->state;
+  d.counts = st->counts;
+  d.spwt1 = sp1->spwt;
+  d.spwt2 = sp2->spwt;
+  d.dt = dt;
+  // eq. 5 of Boyd's paper (DSMC.java:276-286)
+  const double Pab = std::min(1.0, sp2->spwt / sp1->spwt), Pba = std::min(1.0, sp1->spwt / sp2->spwt);
+  d.nsel_den = Pab + (sp2->spwt / sp1->spwt) * Pba;
+  d.real_w = 0.5 * (sp1->spwt + sp2->spwt);
+  d.rm1 = (float)(sp1->mass / (sp1->mass + sp2->mass));
+  d.rm2 = (float)(sp2->mass / (sp1->mass + sp2->mass));
+  d.boyd = sp1->spwt != sp2->spwt;
+  d.pab = (float)(sp2->spwt / sp1->spwt);
+  d.pba = (float)(sp1->spwt / sp2->spwt);
+  d.seed = ctx->seed ^ 0xD5C0ULL;
+  d.step = ctx->rng_epoch++;
   // counters[6]: collisions; as unsigned: [3] the number of heavy cells, [4] the
-  // heavy-cell work counter.  The heavy-cell list lives
-  // in bins_tmp (the sort's write cursors, free once the particles are binned).
+  // heavy-cell work counter.  The heavy-cell list lives in bins_tmp (the sort's write
+  // cursors, free once the particles are binned).
   SF_CUDA(cudaMemsetAsync(ctx->counters + 3, 0, 4 * sizeof(unsigned long long), ctx->stream));
-  unsigned* n_heavy = reinterpret_cast<unsigned*>(ctx->counters + 3);
-  const uint32_t epoch = ctx->rng_epoch++;
-  const uint64_t seed = ctx->seed ^ 0xD5C0ULL;
+  d.n_coll = ctx->counters + 6;
+  d.heavy = ctx->bins_tmp;
+  d.n_heavy = reinterpret_cast<unsigned*>(ctx->counters + 3);
+  d.heavy_cap = ctx->nkeys;
+  d.work = reinterpret_cast<unsigned*>(ctx->counters + 4);
   {
     TimedScope ts(ctx, "dsmc");
-    k_dsmc<<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(
-        ctx->mesh_view(), sp->cur, ctx->bins, ctx->ntx, ctx->nkeys, st->cell_vol, st->state, st->counts, sg,
-        sp->spwt, dt, seed, epoch, ctx->counters + 6, ctx->bins_tmp, n_heavy, ctx->nkeys);
-    k_dsmc_heavy<<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(
-        ctx->mesh_view(), sp->cur, ctx->bins, ctx->ntx, st->cell_vol, st->state, st->counts, sg, sp->spwt, dt, seed,
-        epoch, ctx->counters + 6, ctx->bins_tmp, n_heavy, ctx->nkeys, reinterpret_cast<unsigned*>(ctx->counters + 4));
+    if (pair) {
+      k_dsmc<true><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc_heavy<true><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
+    } else {
+      k_dsmc<false><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc_heavy<false><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
+    }
     ctx->launches += 2;
   }
   SF_CUDA(cudaGetLastError());
@@ -617,21 +814,50 @@ int sf_dsmc(sf_ctx* ctx, int32_t sid, const sf_sigma* sigma, double dt, double s
   SF_CUDA(cudaStreamSynchronize(ctx->stream));
   timer_collect(ctx);
   if (n_coll) *n_coll = (int64_t)nc;
+}
+
+void dsmc_counts(sf_ctx* ctx, int sid1, int sid2, double* count_sum, double* real_sum) {
+  get_species(ctx, sid1);
+  get_species(ctx, sid2);
+  SfDsmcState* st = find_dsmc(ctx, sid1, sid2);
+  SF_REQUIRE(st, SF_ERR_STATE, "no DSMC performed for this pair");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const int nc = ctx->ncells();
+  std::vector<double2> h(nc);
+  copy_wait(h.data(), st->counts, sizeof(double2) * nc, cudaMemcpyDeviceToHost, ctx->stream);
+  for (int c = 0; c < nc; c++) {
+    if (count_sum) count_sum[c] = h[c].x;
+    if (real_sum) real_sum[c] = h[c].y;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int sf_dsmc(sf_ctx* ctx, int32_t sid, const sf_sigma* sigma, double dt, double sig_cr_max0, int64_t* n_coll) {
+  SF_API_BEGIN
+  dsmc_run(ctx, sid, sid, sigma, nullptr, dt, sig_cr_max0, n_coll);
+  SF_API_END(ctx)
+}
+
+int sf_dsmc_pair(sf_ctx* ctx, int32_t sid1, int32_t sid2, const sf_sigma* sigma1, const sf_sigma* sigma2, double dt,
+                 double sig_cr_max0, int64_t* n_coll) {
+  SF_API_BEGIN
+  SF_REQUIRE(sid1 == sid2 || sigma2, SF_ERR_ARG, "a pair of two species needs the second material's sigma data");
+  dsmc_run(ctx, sid1, sid2, sigma1, sigma2, dt, sig_cr_max0, n_coll);
   SF_API_END(ctx)
 }
 
 int sf_dsmc_get_counts(sf_ctx* ctx, int32_t sid, double* count_sum, double* real_sum) {
   SF_API_BEGIN
-  get_species(ctx, sid);
-  SF_REQUIRE(sid < (int)ctx->dsmc.size() && ctx->dsmc[sid], SF_ERR_STATE, "no DSMC performed for this species");
-  SF_CUDA(cudaSetDevice(ctx->device));
-  const int nc = ctx->ncells();
-  std::vector<double2> h(nc);
-  copy_wait(h.data(), ctx->dsmc[sid]->counts, sizeof(double2) * nc, cudaMemcpyDeviceToHost, ctx->stream);
-  for (int c = 0; c < nc; c++) {
-    if (count_sum) count_sum[c] = h[c].x;
-    if (real_sum) real_sum[c] = h[c].y;
-  }
+  dsmc_counts(ctx, sid, sid, count_sum, real_sum);
+  SF_API_END(ctx)
+}
+
+int sf_dsmc_pair_get_counts(sf_ctx* ctx, int32_t sid1, int32_t sid2, double* count_sum, double* real_sum) {
+  SF_API_BEGIN
+  dsmc_counts(ctx, sid1, sid2, count_sum, real_sum);
   SF_API_END(ctx)
 }
 
@@ -666,7 +892,7 @@ void mcc_run(sf_ctx* ctx, SfSpecies* sp, int model, const sf_sigma* sigma, doubl
   SF_REQUIRE(ctx->mcc_target, SF_ERR_STATE, "no MCC target (sf_mcc_set_target)");
   SF_REQUIRE(dt > 0, SF_ERR_ARG, "dt must be positive");
   SF_CUDA(cudaSetDevice(ctx->device));
-  const SigmaDev sg = make_sigma(sigma, sp->mass, ctx->mcc_mass);
+  const SigmaDev sg = make_sigma(sigma, nullptr, sp->mass, ctx->mcc_mass);
   const size_t nn = (size_t)ctx->ni * ctx->nj;
   TargetView tg;
   tg.den = ctx->mcc_target;

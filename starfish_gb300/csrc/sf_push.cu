@@ -1486,7 +1486,10 @@ std::mutex g_noalloc_mutex;
 unsigned char* g_noalloc_base[NOALLOC_MAX_DEVICES] = {};
 
 // Device address of g_push_scratch on ctx->device, looked up once per device (the
-// device must be current).
+// device must be current) and kept for the life of the process.  A host that resets a
+// device (cudaDeviceReset) discards the module and with it this array, so the kept
+// address is stale afterwards: such a host must not call sf_push_deposit_noalloc again
+// in the same process.
 unsigned char* noalloc_scratch(sf_ctx* ctx) {
   SF_REQUIRE(ctx->device >= 0 && ctx->device < NOALLOC_MAX_DEVICES, SF_ERR_ARG, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);

@@ -341,26 +341,37 @@ def _sigma(model, c=(0, 0, 0, 0), diam=0.0, T_ref=273.0, omega=0.5, vss_alpha=1.
 
 
 class DSMC:
-    """GPU DSMC pair interaction (collisions/DSMC.java) for one kinetic species."""
+    """GPU DSMC pair interaction (collisions/DSMC.java): pair="mat1,mat2" with mat2 the same
+    kinetic material (the default) or another one.  The cross-section model and
+    coefficients are the interaction's; diam, T_ref, omega and vss_alpha are mat1's, and
+    mat2's come in material2_params (a dict with those keys) for two materials."""
 
     def __init__(self, domain: GpuDomain, material: KineticMaterial, model=4, c=(0, 0, 0, 0), diam=0.0,
-                 T_ref=273.0, omega=0.5, vss_alpha=1.0, sig_cr_max=1e-16, frequency=1):
+                 T_ref=273.0, omega=0.5, vss_alpha=1.0, sig_cr_max=1e-16, frequency=1,
+                 material2: KineticMaterial = None, material2_params=None):
         self.d, self.km = domain, material
+        self.km2 = material2 if material2 is not None else material
         self.sigma = _sigma(model, c, diam, T_ref, omega, vss_alpha)
+        p2 = dict(diam=diam, T_ref=T_ref, omega=omega, vss_alpha=vss_alpha)
+        if material2_params:
+            p2.update(material2_params)
+        self.sigma2 = _sigma(model, c, **p2)
         self.sig_cr_max0 = sig_cr_max
         self.frequency = frequency
 
     def perform(self, dt):
         n = C.c_int64()
-        self.d.check(self.d.lib.sf_dsmc(self.d.ctx, self.km.sid, C.byref(self.sigma), dt * self.frequency,
-                                        self.sig_cr_max0, C.byref(n)))
+        self.d.check(self.d.lib.sf_dsmc_pair(self.d.ctx, self.km.sid, self.km2.sid, C.byref(self.sigma),
+                                             C.byref(self.sigma2), dt * self.frequency, self.sig_cr_max0,
+                                             C.byref(n)))
         return n.value
 
     def counts(self):
         nc = (self.d.ni - 1) * (self.d.nj - 1)
         cnt = np.zeros(nc)
         real = np.zeros(nc)
-        self.d.check(self.d.lib.sf_dsmc_get_counts(self.d.ctx, self.km.sid, abi.ptr(cnt), abi.ptr(real)))
+        self.d.check(self.d.lib.sf_dsmc_pair_get_counts(self.d.ctx, self.km.sid, self.km2.sid, abi.ptr(cnt),
+                                                        abi.ptr(real)))
         return cnt, real
 
 

@@ -396,6 +396,64 @@ def test_oracle_dsmc_collision_rate_matches_vhs_theory():
         assert (P[:, 3:6] ** 2).sum() == pytest.approx(e0, rel=1e-12)
 
 
+def test_oracle_dsmc_pair_rate_and_boyd_update():
+    """Two materials (argon and helium) in one equilibrium cell.  With equal weights the NTC
+    count of an unlike pair is N1 N2 w dt <sigma g> / V (nsel doubled for two species,
+    denominator Pab + Pba = 2), with <sigma g> for the reduced mass and the pair's mean
+    d, T_ref and omega (SigmaBird463.init), and elastic collisions keep the mass-weighted
+    momentum and the kinetic energy.  With weights w2 = w1 / 4 the count follows the
+    reference's expression 2 (N1 w1 / V) N2 dt <sigma g> / (Pab + (w2/w1) Pba) with Pab = 1/4,
+    Pba = 1 (DSMC.java:276-290; for unequal weights this is w1/w2 times N1 N2 w1 dt <sigma g>
+    / V, and parity keeps it), and a collision moves particle 1 with probability w2/w1 and
+    particle 2 always (Boyd's update, :431-452)."""
+    import math
+    KB, AMU = 1.3806503e-23, 1.66053886e-27
+    m1, m2 = 40 * AMU, 4 * AMU
+    mat1 = dict(diam=4.17e-10, T_ref=273.0, omega=0.81, vss_alpha=1.0)
+    mat2 = dict(diam=2.33e-10, T_ref=273.0, omega=0.66, vss_alpha=1.0)
+    mr = m1 * m2 / (m1 + m2)
+    d = 0.5 * (mat1["diam"] + mat2["diam"])
+    om = 0.5 * (mat1["omega"] + mat2["omega"])
+    T_ref = 273.0
+    V, dt, n1, n2, T = 1e-9, 1e-6, 1500, 1000, 500.0
+    sg = math.pi * d * d * (2 * KB * T_ref / mr) ** (om - 0.5) * (2 * KB * T / mr) ** (1 - om) / math.gamma(1.5)
+    for ratio, seed in ((1.0, 5), (0.25, 6)):
+        rng = np.random.default_rng(seed)
+        P1 = np.zeros((n1, 12))
+        P2 = np.zeros((n2, 12))
+        P1[:, 3:6] = rng.normal(0.0, math.sqrt(KB * T / m1), (n1, 3))
+        P2[:, 3:6] = rng.normal(0.0, math.sqrt(KB * T / m2), (n2, 3))
+        P1[:, 6:8] = P2[:, 6:8] = 0.5
+        P1[:, 10] = P2[:, 10] = 1
+        den = ratio + ratio * 1.0  # Pab + (w2/w1) Pba
+        w1 = 2e4 * V * den / (2 * n1 * n2 * dt * sg)  # about 2e4 collisions expected
+        w2 = w1 * ratio
+        P1[:, 9], P2[:, 9] = w1, w2
+        state = np.array([[6.0 * sg, 0.0]])
+        counts = np.zeros((1, 2))
+        v1, v2 = P1[:, 3:6].copy(), P2[:, 3:6].copy()
+        p0 = m1 * v1.sum(axis=0) + m2 * v2.sum(axis=0)
+        e0 = m1 * (v1 ** 2).sum() + m2 * (v2 ** 2).sum()
+        got = O.dsmc_pair(2, 2, np.array([V]), P1, m1, w1, P2, m2, w2, mat1, mat2, dt, state, counts, seed)
+        assert got == pytest.approx(2e4, rel=0.05)
+        assert counts[0, 0] == got
+        assert counts[0, 1] == pytest.approx(got * 0.5 * (w1 + w2), rel=1e-12)
+        moved1 = np.any(P1[:, 3:6] != v1, axis=1).sum()
+        moved2 = np.any(P2[:, 3:6] != v2, axis=1).sum()
+        if ratio == 1.0:
+            p1 = m1 * P1[:, 3:6].sum(axis=0) + m2 * P2[:, 3:6].sum(axis=0)
+            e1 = m1 * (P1[:, 3:6] ** 2).sum() + m2 * (P2[:, 3:6] ** 2).sum()
+            assert np.allclose(p1, p0, atol=1e-9 * (m1 * np.abs(v1).sum()))
+            assert e1 == pytest.approx(e0, rel=1e-12)
+        else:
+            # each collision moves particle 2, and particle 1 with probability 1/4: among
+            # 1500 argon and 1000 helium particles, nearly every helium particle and
+            # about 1 - exp(-got / 4 / n1) of the argon particles have moved
+            assert moved2 > 0.99 * n2
+            f1 = 1 - math.exp(-got * 0.25 / n1)
+            assert abs(moved1 / n1 - f1) < 0.05
+
+
 def test_oracle_poisson_boltzmann_debye_shielding():
     """Boltzmann electrons over a uniform ion background e n0, walls at phi_w << kTe on the
     left and right, Neumann top and bottom: the linearised equation phi'' = phi / lambda_D^2

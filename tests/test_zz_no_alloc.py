@@ -6,7 +6,9 @@ call runs on scratch that still holds the first call's contents.  After each cal
 densities, moments, ParticleMover totals, counters and particle states must agree to
 the push parity tolerances (densities 1e-6 of the field maximum, positions 1e-5 cells,
 velocities 1e-6 relative, totals 1e-5); the deposit is integer fixed point, so the
-densities agree exactly in practice.  The file sorts last so that it also runs after every other GPU test.
+densities agree exactly in practice.  The driver's free-memory figure must not move
+across any no-allocation call, including the first one, which also cell-sorts the freshly
+appended particles.  The file sorts last so that it also runs after every other GPU test.
 """
 import ctypes as C
 
@@ -68,7 +70,19 @@ def _compare(dom_a, km_a, st_a, dom_b, km_b, st_b):
     assert np.max(np.abs(pa[:, 2:] - pb[:, 2:]), initial=0.0) <= 1e-6 * np.max(np.abs(pa[:, 2:]))
 
 
+def _device_free_bytes():
+    """Free memory of the current device as the driver reports it (cudaMemGetInfo): any
+    cudaMalloc, by the library or anyone else in the process, lowers it."""
+    torch = pytest.importorskip("torch")
+    free, _ = torch.cuda.mem_get_info()
+    return free
+
+
 def test_noalloc_push_matches_push_two_calls(gpulib):
+    """Also checks that no call of the no-allocation entry point changes the device's free
+    memory: the first one, which runs the automatic cell sort of the freshly appended
+    species, and the second.  The ordinary entry point runs first on its own context, so
+    the kernels both use are already loaded when the no-allocation calls are measured."""
     from starfish_gb300.plugin import GpuDomain
     cfg = W.config0()
     spec, ion = cfg.mesh, cfg.ion
@@ -80,9 +94,13 @@ def test_noalloc_push_matches_push_two_calls(gpulib):
             d.set_efield(efi, efj)
         km_a = _species(dom_a, ion, pos, vel, cfg.dt)
         km_b = _species(dom_b, ion, pos, vel, cfg.dt)
+        _device_free_bytes()  # the query's own set-up happens before the first reading
         for call in range(2):
             st_a = _step(dom_a, km_a, cfg.dt, noalloc=False)
+            free0 = _device_free_bytes()
             st_b = _step(dom_b, km_b, cfg.dt, noalloc=True)
+            free1 = _device_free_bytes()
+            assert free1 == free0, f"call {call}: free device memory changed by {free0 - free1} bytes"
             assert st_a["n_slow"] > 0 and st_a["n_removed"] > 0, "the case must exercise the slow path"
             _compare(dom_a, km_a, st_a, dom_b, km_b, st_b)
     finally:

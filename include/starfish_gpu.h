@@ -140,6 +140,10 @@ typedef struct {
  * (UniformMesh.java:55-72, Mesh.initNodes 364-402, Solver.init 153-189). */
 int sf_ctx_create(const sf_mesh_desc* mesh, int device, sf_ctx** out);
 int sf_ctx_destroy(sf_ctx* ctx);
+/* Seed of all random streams of the context (Starfish.random, core/common/Starfish.java:238,
+ * which <starfish randomize="true"> reseeds at :647); restarts the stream counters.  The
+ * default seed is fixed, so runs repeat unless a seed is set. */
+int sf_ctx_set_seed(sf_ctx* ctx, uint64_t seed);
 /* Last error message of a context (or of the last failed sf_ctx_create when ctx is NULL). */
 const char* sf_last_error(const sf_ctx* ctx);
 /* Library version string. */

@@ -82,6 +82,7 @@ EXPORTS = {
     "sf_last_error": (C.c_char_p, [C.c_void_p]),
     "sf_ctx_create": (C.c_int, [C.POINTER(MeshDesc), C.c_int, C.POINTER(C.c_void_p)]),
     "sf_ctx_destroy": (C.c_int, [C.c_void_p]),
+    "sf_ctx_set_seed": (C.c_int, [C.c_void_p, C.c_uint64]),
     "sf_build_node_segments": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
                                          C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
     "sf_species_add": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int64,

@@ -655,6 +655,17 @@ int sf_ctx_create(const sf_mesh_desc* md, int device, sf_ctx** out) {
   }
 }
 
+// Starfish.random (core/common/Starfish.java:238, reseeded by <starfish randomize> at
+// :647): the seed of every random stream of the context (sources, surfaces, DSMC, MCC).
+int sf_ctx_set_seed(sf_ctx* ctx, uint64_t seed) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx, SF_ERR_ARG, "null context");
+  ctx->seed = seed;
+  ctx->rng_epoch = 0;
+  for (SfSpecies* sp : ctx->species) sp->step = 0;
+  SF_API_END(ctx)
+}
+
 int sf_ctx_destroy(sf_ctx* ctx) {
   if (!ctx) return SF_OK;
   cudaSetDevice(ctx->device);

@@ -34,9 +34,12 @@ constexpr int TILE = PB * PPT;     // particles per block tile
 constexpr int SBOX = 4096;         // shared-memory deposit box (nodes)
 
 
-__device__ __forceinline__ unsigned quant(float w) {
-  // S in [0,1] -> round(S * 2^31); S = 1 gives 2^31 which fits in 32 bits
-  return __float2uint_rn(w * 2147483648.0f);
+// Deposit quantisation of every path: S in [0,1] -> round(S * 2^22), at most 2^22 - 1, so
+// that the 32-bit shared-memory sum over the TILE = 1024 particles of a tile cannot wrap;
+// the values are scaled by 2^9 into the 2^31 fixed point of the global counts (DEP_SCALE).
+constexpr int TILE_SHIFT = 9;
+__device__ __forceinline__ unsigned quant22(float w) {
+  return min(__float2uint_rn(w * 4194304.0f), 4194303u);
 }
 
 // Bilinear weights of the scatter (Field2D.scatter, core/domain/Field2D.java:244-295):
@@ -83,12 +86,12 @@ struct Kahan {
 // ---------------------------------------------------------------------------------
 // fused push + deposit
 // ---------------------------------------------------------------------------------
-// Deposit accumulation: each particle adds round(S * 2^31) to its four corner nodes.
-// Inside a block the tile's box of nodes is accumulated in shared memory as two 32-bit
-// halves (low/high 16 bits of the fixed-point value), so that plain 32-bit shared
-// atomics cannot overflow (<= 1024 particles per tile), then flushed with one 64-bit
-// global atomic per touched node.  Tiles whose box does not fit (unsorted input) fall
-// back to 64-bit global atomics per corner.
+// Deposit accumulation: each particle adds round(S * 2^22) (quant22) to its four corner
+// nodes.  Inside a block the tile's box of nodes is accumulated in shared memory with one
+// 32-bit atomic per corner (1024 particles of at most 2^22 - 1 cannot overflow), then
+// flushed with one 64-bit global atomic per touched node, scaled by 2^9 into the global
+// 2^31 fixed point.  Tiles whose box does not fit (unsorted input) add the same scaled
+// values with 64-bit global atomics per corner, so both routes give the same integers.
 __device__ bool may_hit_fp32(const MeshView& m, int i, int j, float fx, float fy, float gx, float gy);
 
 // One tile (TILE particles from t0) of the fused push + deposit: load, push, fast-path
@@ -101,7 +104,7 @@ template <int DOM, bool STATS, bool MOM, bool PRE = false>
 __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView& P, const PushArgs& a, int64_t t0,
                                           unsigned long long* __restrict__ count, long long* __restrict__ mom,
                                           int* __restrict__ slow_idx, unsigned long long* __restrict__ counters,
-                                          const SampleView& smp, unsigned* acc_lo, unsigned* acc_hi,
+                                          const SampleView& smp, unsigned* acc,
                                           int (*sred)[PB / 32], Kahan& st_px, Kahan& st_py, Kahan& st_pz, Kahan& st_e,
                                           unsigned& st_n) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -118,26 +121,32 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
   uint32_t lcell[PPT];
   float2 lfrac[PPT], lvxy[PPT];
   float lvz[PPT];
+  // the tile's arrays from its first particle: 32-bit indices inside the tile
+  uint32_t* __restrict__ tcell = P.cell + t0;
+  float2* __restrict__ tfrac = P.frac + t0;
+  float2* __restrict__ tvxy = P.vxy + t0;
+  float* __restrict__ tvz = P.vz + t0;
+  const int nrem = (int)min(P.n - t0, (int64_t)TILE);
 #pragma unroll
   for (int k = 0; k < PPT; k++) {
-    const int64_t p = t0 + k * PB + threadIdx.x;
+    const int q = k * PB + (int)threadIdx.x;
     lcell[k] = DEAD;
     lvz[k] = 0.f;
-    if (p < P.n) {
-      lcell[k] = __ldcs(&P.cell[p]);
-      lfrac[k] = __ldcs(&P.frac[p]);
-      lvxy[k] = __ldcs(&P.vxy[p]);
-      if (DOM != SF_DOMAIN_XY || STATS || MOM) lvz[k] = __ldcs(&P.vz[p]);
+    if (q < nrem) {
+      lcell[k] = __ldcs(tcell + q);
+      lfrac[k] = __ldcs(tfrac + q);
+      lvxy[k] = __ldcs(tvxy + q);
+      if (DOM != SF_DOMAIN_XY || STATS || MOM) lvz[k] = __ldcs(tvz + q);
     }
   }
 #pragma unroll
   for (int k = 0; k < PPT; k++) {
-    const int64_t p = t0 + k * PB + threadIdx.x;
+    const int q = k * PB + (int)threadIdx.x;
     dep[k] = false;
     pi[k] = pj[k] = 0;
     pfx[k] = pfy[k] = 0.f;
     int status = 0;  // 1 finished here, 2 exact path, 3 removed at a domain face
-    if (p < P.n) {
+    if (q < nrem) {
       const uint32_t c = lcell[k];
       if (c != DEAD) {
         const int i = cell_i(c), j = cell_j(c);
@@ -198,10 +207,10 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
         if (PRE && DOM == SF_DOMAIN_XY && !clear)
           clear = !may_hit_fp32(m, i, j, f.x, f.y, gx, gy);
         if (inside && clear) {
-          __stcs(&P.cell[p], pack_cell(i2, j2));
-          __stcs(&P.frac[p], make_float2(nfx, nfy));
-          __stcs(&P.vxy[p], make_float2(nvx, nvy));
-          if (DOM != SF_DOMAIN_XY) __stcs(&P.vz[p], nvz);
+          __stcs(tcell + q, pack_cell(i2, j2));
+          __stcs(tfrac + q, make_float2(nfx, nfy));
+          __stcs(tvxy + q, make_float2(nvx, nvy));
+          if (DOM != SF_DOMAIN_XY) __stcs(tvz + q, nvz);
           status = 1;
           dep[k] = true;
           pi[k] = i2;
@@ -225,11 +234,11 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
         } else if (!inside && clear && m.all_delete) {
           // no candidate segment on the way and every domain face removes particles
           // (KineticMaterial.java:614-746: OPEN/DIRICHLET/... return false)
-          P.cell[p] = DEAD;
+          tcell[q] = DEAD;
           status = 3;
         } else {
           // exact path later: keep the old position, store the updated velocity
-          P.vxy[p] = v;
+          tvxy[q] = v;
           status = 2;
         }
       }
@@ -240,7 +249,7 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
       unsigned long long base = 0;
       if (lane == leader) base = atomicAdd(&counters[0], (unsigned long long)__popc(ms));
       base = __shfl_sync(FULL, base, leader);
-      if (status == 2) slow_idx[base + __popc(ms & ((1u << lane) - 1u))] = (int)p;
+      if (status == 2) slow_idx[base + __popc(ms & ((1u << lane) - 1u))] = (int)t0 + q;
     }
     const unsigned md = __ballot_sync(FULL, status == 3);
     if (md && lane == __ffs(md) - 1) atomicAdd(&counters[1], (unsigned long long)__popc(md));
@@ -272,10 +281,7 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
   const bool any = imax >= 0;
   const bool use_smem = any && (bw * bh <= SBOX);
   if (use_smem) {
-    for (int q = threadIdx.x; q < bw * bh; q += PB) {
-      acc_lo[q] = 0u;
-      acc_hi[q] = 0u;
-    }
+    for (int q = threadIdx.x; q < bw * bh; q += PB) acc[q] = 0u;
   }
   __syncthreads();
   if (any) {
@@ -289,8 +295,8 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
       if (!d) continue;
       float wx, wy;
       scatter_weights<DOM>(pfx[k], pfy[k], pi[k], pj[k], a, wx, wy);
-      const unsigned q[4] = {quant((1.f - wx) * (1.f - wy)), quant(wx * (1.f - wy)), quant(wx * wy),
-                             quant((1.f - wx) * wy)};
+      const unsigned q[4] = {quant22((1.f - wx) * (1.f - wy)), quant22(wx * (1.f - wy)), quant22(wx * wy),
+                             quant22((1.f - wx) * wy)};
       if (MOM) {
         const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
         const int base = pj[k] * m.ni + pi[k];
@@ -314,21 +320,20 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
         const int off[4] = {0, 1, bw + 1, bw};
 #pragma unroll
         for (int cc = 0; cc < 4; cc++) {
-          atomicAdd(&acc_lo[l + off[cc]], q[cc] & 0xFFFFu);
-          atomicAdd(&acc_hi[l + off[cc]], q[cc] >> 16);
+          atomicAdd(&acc[l + off[cc]], q[cc]);
         }
       } else {
         const size_t u = (size_t)pj[k] * m.ni + pi[k];
         const size_t off[4] = {0, 1, (size_t)m.ni + 1, (size_t)m.ni};
 #pragma unroll
-        for (int cc = 0; cc < 4; cc++) atomicAdd(&count[u + off[cc]], (unsigned long long)q[cc]);
+        for (int cc = 0; cc < 4; cc++) atomicAdd(&count[u + off[cc]], (unsigned long long)q[cc] << TILE_SHIFT);
       }
     }
   }
   __syncthreads();
   if (use_smem) {
     for (int q = threadIdx.x; q < bw * bh; q += PB) {
-      const unsigned long long v = ((unsigned long long)acc_hi[q] << 16) + acc_lo[q];
+      const unsigned long long v = (unsigned long long)acc[q] << TILE_SHIFT;
       if (v) atomicAdd(&count[(size_t)(jmin + q / bw) * m.ni + imin + q % bw], v);
     }
   }
@@ -341,8 +346,7 @@ __global__ void __launch_bounds__(PB, 4) k_push(MeshView m, ParticlesView P, Pus
                                               long long* __restrict__ mom, int* __restrict__ slow_idx,
                                               unsigned long long* __restrict__ counters,
                                               double* __restrict__ stats_partial, SampleView smp) {
-  __shared__ unsigned acc_lo[SBOX];
-  __shared__ unsigned acc_hi[SBOX];
+  __shared__ unsigned acc[SBOX];
   __shared__ int sred[4][PB / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
@@ -351,7 +355,7 @@ __global__ void __launch_bounds__(PB, 4) k_push(MeshView m, ParticlesView P, Pus
   unsigned st_n = 0;
 
   for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < P.n; t0 += (int64_t)gridDim.x * TILE) {
-    push_tile<DOM, STATS, MOM>(m, P, a, t0, count, mom, slow_idx, counters, smp, acc_lo, acc_hi, sred, st_px, st_py,
+    push_tile<DOM, STATS, MOM>(m, P, a, t0, count, mom, slow_idx, counters, smp, acc, sred, st_px, st_py,
                                st_pz, st_e, st_n);
   }
   if (STATS) {
@@ -694,7 +698,9 @@ __device__ inline void deposit_global_t(const MeshView& m, unsigned long long* c
   const size_t u = (size_t)j * m.ni + i;
   const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
   const size_t off[4] = {0, 1, (size_t)m.ni + 1, (size_t)m.ni};
-  for (int cc = 0; cc < 4; cc++) atomicAdd(&count[u + off[cc]], (unsigned long long)quant(s[cc]));
+  // the tile deposit's quantisation, so that a particle adds the same integers whichever
+  // path finishes it
+  for (int cc = 0; cc < 4; cc++) atomicAdd(&count[u + off[cc]], (unsigned long long)quant22(s[cc]) << TILE_SHIFT);
   if (mom_on) {
     const float vv[3] = {vx, vy, vz};
     for (int cc = 0; cc < 4; cc++)
@@ -1209,8 +1215,7 @@ __global__ void k_batch_zero(BatchDev b) {
 
 template <int DOM>
 __global__ void __launch_bounds__(PB, 2) k_push_batch(BatchDev b) {
-  __shared__ unsigned acc_lo[SBOX];
-  __shared__ unsigned acc_hi[SBOX];
+  __shared__ unsigned acc[SBOX];
   __shared__ int sred[4][PB / 32];
   Kahan st_px, st_py, st_pz, st_e;
   unsigned st_n = 0;
@@ -1221,7 +1226,7 @@ __global__ void __launch_bounds__(PB, 2) k_push_batch(BatchDev b) {
     ParticlesView P = I.P;
     P.n = b.n_dev[i];
     push_tile<DOM, false, false, true>(I.m, P, I.a, (gt - b.tile_start[i]) * TILE, I.count, nullptr, I.slow_idx,
-                                 I.sa.counters, SampleView{nullptr, nullptr}, acc_lo, acc_hi, sred, st_px, st_py,
+                                 I.sa.counters, SampleView{nullptr, nullptr}, acc, sred, st_px, st_py,
                                  st_pz, st_e, st_n);
   }
 }

@@ -31,6 +31,10 @@ class GpuDomain:
     def check(self, rc):
         abi.check(rc, self.ctx)
 
+    def set_seed(self, seed):
+        """Starfish.random's seed for every random stream of this domain."""
+        self.check(self.lib.sf_ctx_set_seed(self.ctx, int(seed)))
+
     def set_efield(self, efi, efj):
         efi = np.ascontiguousarray(efi, np.float64)
         efj = np.ascontiguousarray(efj, np.float64)

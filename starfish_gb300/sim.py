@@ -15,9 +15,11 @@ from .plugin import GpuDomain, KineticMaterial, PoissonSolver
 
 class EsPicSimulation:
     def __init__(self, cfg: W.EsPicConfig, device=0, capacity=None, inlet=True, seed_particles=None,
-                 poisson_tol=1e-6):
+                 poisson_tol=1e-6, seed=None):
         self.cfg = cfg
         self.dom = GpuDomain(cfg.mesh, device=device)
+        if seed is not None:
+            self.dom.set_seed(seed)
         ion = cfg.ion
         cap = capacity or max(4 * cfg.n_particles, 1 << 20)
         self.ions = KineticMaterial(self.dom, ion.mass, ion.charge, ion.spwt, capacity=cap)
@@ -38,13 +40,15 @@ class EsPicSimulation:
             pos, vel = seed_particles
             self.ions.add_particles(pos, vel, rewind=True, dt=cfg.dt)
 
-    def step(self):
+    def step(self, sample=False):
+        """One time step; sample=True also adds the ions to the velocity samples
+        (KineticMaterial.updateSamples, after clear_samples)."""
         cfg = self.cfg
         t0 = time.perf_counter()
         if self.inlet is not None:
             self.ions.sample_maxwellian_source(self.inlet, cfg.ion.den, cfg.ion.v_drift, cfg.ion.temp, cfg.dt)
         t1 = time.perf_counter()
-        st = self.ions.update_fields(cfg.dt, stats=True)
+        st = self.ions.update_fields(cfg.dt, stats=True, sample=sample)
         t2 = time.perf_counter()
         self.solver.update_rho()
         _, sst = self.solver.solve()

@@ -1,0 +1,318 @@
+"""Parity at the benchmarked configurations, against the oracle.
+
+- One push + scatter on the 2049x1025 mesh of the 64M-ion workload (dx 0.05 mm, dt 2.5e-8 s,
+  electrode field) on a 2M-particle sample, in storage order and after the cell sort
+  (KineticMaterial.updateFields, KineticMaterial.java:117-197, 299-750).
+- One push of an RZ domain (radius along x) with diffuse walls (rotateToRZ,
+  KineticMaterial.java:424-442; SurfaceInteraction.java:153-213).
+- A short axisymmetric DSMC jet (source + push + DSMC.perform every step) over three seeds:
+  collision counts, density and temperature in coarse regions against the oracle's loop
+  over the same steps (DSMC.java:194-454), within bounds from the seed-to-seed spread.
+Tolerances of the single pushes are those of the push parity tests: positions 1e-5 cells,
+velocities 1e-6 relative, densities 1e-6 of the field maximum.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from starfish_gb300 import abi
+from starfish_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+KB = 1.3806503e-23
+AMU = 1.66053886e-27
+
+
+def _omesh(spec):
+    return O.OMesh(spec.ni, spec.nj, spec.x0, spec.dh, spec.domain, spec.node_type, spec.face_type)
+
+
+def _exact_state(spec, lc, vel):
+    """(int cell, FP32 fraction) positions and FP32 velocities, as the device holds them."""
+    i = np.minimum(np.floor(lc[:, 0]), spec.ni - 2)
+    j = np.minimum(np.floor(lc[:, 1]), spec.nj - 2)
+    lc = np.column_stack([i + (lc[:, 0] - i).astype(np.float32).astype(np.float64),
+                          j + (lc[:, 1] - j).astype(np.float32).astype(np.float64)])
+    return lc, vel.astype(np.float32).astype(np.float64)
+
+
+def _parts(spec, lc, vel, w):
+    P = np.zeros((lc.shape[0], 12))
+    P[:, 0] = spec.x0[0] + lc[:, 0] * spec.dh[0]
+    P[:, 1] = spec.x0[1] + lc[:, 1] * spec.dh[1]
+    P[:, 3:6] = vel
+    P[:, 6:8] = lc
+    P[:, 9] = w
+    P[:, 10] = 1
+    return P
+
+
+def _match(glc, gvel, olc, ovel):
+    """Pairs every GPU particle with its oracle twin when the storage orders differ: the
+    nearest oracle row in (position in cells, velocity / 1 km/s); the pairing must be one
+    to one."""
+    from scipy.spatial import cKDTree
+    g = np.hstack([glc, gvel / 1e3])
+    o = np.hstack([olc, ovel / 1e3])
+    _, idx = cKDTree(o).query(g)
+    assert np.unique(idx).size == idx.size, "particles of the two sets do not pair up"
+    return olc[idx], ovel[idx]
+
+
+@pytest.mark.parametrize("sorted_first", [False, True])
+def test_push_2049x1025_sample_matches_oracle(gpulib, sorted_first):
+    """2M ions of the 64M workload's distribution (uniform over the gas, Maxwellian 1000 K
+    + 7 km/s drift, 5 % of them 2-6x faster) on its mesh and time step: about one ion per
+    node, so that the densest nodes hold several ions (a node of one ion would show the
+    FP32 rounding of a 20-cell move, 2e-6 cells, as 2e-6 of the field maximum).  In storage
+    order each particle is compared with its oracle twin; after the cell sort (the
+    shared-memory tile deposit) each GPU particle is paired with its nearest oracle twin."""
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    n = 2_000_000
+    cfg = W.config1(n)
+    spec, ion, dt = cfg.mesh, cfg.ion, cfg.dt
+    _, efi, efj = W.electrode_efield(spec)
+    pos, vel = W.uniform_maxwellian(spec, ion, n, 17)
+    rng = np.random.default_rng(18)
+    k = n // 20
+    vel[:k] *= rng.uniform(2, 6, (k, 1))
+    lc = np.column_stack([(pos[:, 0] - spec.x0[0]) / spec.dh[0], (pos[:, 1] - spec.x0[1]) / spec.dh[1]])
+    lc, vel = _exact_state(spec, lc, vel)
+    dom = GpuDomain(spec)
+    try:
+        dom.set_efield(efi, efj)
+        km = KineticMaterial(dom, ion.mass, ion.charge, ion.spwt, capacity=lc.shape[0] + 16)
+        km.set_sort_interval(1 if sorted_first else 0)
+        km.add_particles_lc(lc, vel)
+        st = km.update_fields(dt, stats=True)
+        glc, gvel = km.download()
+        gden = km.get_den()
+        gflux, gdep = km.surface_flux()
+    finally:
+        dom.close()
+    m = _omesh(spec)
+    e32i = efi.astype(np.float32).astype(np.float64)
+    e32j = efj.astype(np.float32).astype(np.float64)
+    segs = O.seg_table(spec.seg_xy, spec.seg_btype, O.SURF_ABSORB)
+    P = _parts(spec, lc, vel, ion.spwt)
+    alive, ost, oflux, odep = O.push(m, e32i, e32j, ion.charge, ion.mass, dt, segs, spec.node_seg_ptr,
+                                     spec.node_seg_idx, P)
+    oden = O.update_fields(m, O.node_volumes(m), P)
+    keep = P[:, 10] == 1
+    assert st["np"] == keep.sum() == glc.shape[0]
+    assert st["n_removed"] > 0  # ions reach the electrode and the walls
+    olc, ovel = P[keep, 6:8], P[keep, 3:6]
+    if sorted_first:
+        olc, ovel = _match(glc, gvel, olc, ovel)
+    assert np.max(np.abs(glc - olc)) < 1e-5
+    vs = np.linalg.norm(ovel, axis=1, keepdims=True)
+    assert np.max(np.abs(gvel - ovel) / vs) < 1e-6
+    assert np.max(np.abs(gden - oden)) <= 1e-6 * np.abs(oden).max()
+    # the oracle sums 2M weights one by one in FP64 (rounding ~1e-16 per add)
+    assert st["n_sum"] == pytest.approx(ost[0], rel=1e-9)
+    assert st["e_sum"] == pytest.approx(ost[4], rel=1e-5)
+    seg_g = gdep.reshape(-1, 2).sum(axis=1)
+    seg_o = odep.reshape(-1, 2).sum(axis=1)
+    assert np.allclose(seg_g, seg_o, rtol=1e-12)
+    assert np.allclose(gdep, odep, rtol=1e-6)
+
+
+def rz_jet(ni=33, nj=65, Lr=0.032, Lz=0.064, r_inlet=4e-3):
+    """The small jet with the axes exchanged: radius along x (i), z along y (j); the axis
+    is the LEFT face (symmetry).  Segments are swapped and reversed so that their normals
+    still point into the gas."""
+    zr = W.jet_mesh(ni=nj, nj=ni, Lz=Lz, Lr=Lr, r_inlet=r_inlet)
+    nmax = max(ni, nj)
+    face = np.full((4, nmax), abi.DB_OPEN, np.int8)
+    face[abi.FACE_LEFT, :] = abi.DB_SYMMETRY
+    segs = zr.seg_xy[:, [3, 2, 1, 0]].copy()  # (x1, y1, x2, y2) -> (y2, x2, y1, x1)
+    return W.MeshSpec(ni, nj, (0.0, 0.0), (Lr / (ni - 1), Lz / (nj - 1)), abi.DOMAIN_RZ,
+                      np.full(ni * nj, abi.NODE_OPEN, np.int8), face, np.zeros(ni * nj), segs,
+                      zr.seg_btype.copy())
+
+
+def test_rz_push_with_diffuse_walls_matches_oracle(gpulib):
+    """rotateToRZ, the Ruyten radial weights along x and the axis at i = 0 on the device,
+    against the oracle: particles that meet no wall match one by one, and so does the
+    density away from the re-emitted ones; diffusely re-emitted particles carry the wall
+    temperature."""
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    spec = rz_jet()
+    mass, w = 40 * AMU, 1e10
+    vth = np.sqrt(2 * KB * 300.0 / mass)
+    rng = np.random.default_rng(4)
+    n = 40000
+    lc = np.column_stack([rng.uniform(0, spec.ni - 1.001, n), rng.uniform(0, spec.nj - 1.001, n)])
+    vel = rng.standard_normal((n, 3)) * 600.0
+    lc, vel = _exact_state(spec, lc, vel)
+    dt = 2e-6
+    dom = GpuDomain(spec)
+    try:
+        dom.set_efield(np.zeros(spec.nn), np.zeros(spec.nn))
+        km = KineticMaterial(dom, mass, 0.0, w, capacity=n + 16)
+        for s in range(spec.seg_xy.shape[0]):
+            km.set_surface(s, abi.SURF_DIFFUSE, vth=vth, c_rest=1.0, c_accom=1.0)
+        km.set_sort_interval(0)
+        km.add_particles_lc(lc, vel)
+        km.update_fields(dt)
+        glc, gvel = km.download()
+        gden = km.get_den()
+        gflux, _ = km.surface_flux()
+    finally:
+        dom.close()
+    m = _omesh(spec)
+    ptr, idx = O.node_segments(m, spec.seg_xy)
+    segs = O.seg_table(spec.seg_xy, spec.seg_btype, O.SURF_DIFFUSE, vth=vth, c_rest=1.0, c_accom=1.0)
+    P = _parts(spec, lc, vel, w)
+    speed0 = np.linalg.norm(vel, axis=1)
+    O.push(m, np.zeros(spec.nn), np.zeros(spec.nn), 0.0, mass, dt, segs, ptr, idx, P, seed=5)
+    keep = P[:, 10] == 1
+    assert glc.shape[0] == keep.sum()
+    speed1 = np.linalg.norm(P[:, 3:6], axis=1)
+    plain = np.abs(speed1 - speed0) <= 1e-9 * speed0
+    sel = plain[keep]
+    assert sel.sum() > 0.9 * keep.sum()
+    assert np.max(np.abs(glc[sel] - P[keep][sel, 6:8])) < 1e-5
+    assert np.max(np.abs(gvel[sel] - P[keep][sel, 3:6]) / speed0[keep][sel, None]) < 1e-5
+    # the radial scatter of the particles that met no wall, away from the re-emitted ones
+    vol = O.node_volumes(m)
+    oden = O.update_fields(m, vol, np.ascontiguousarray(P[keep][sel]))
+    hit_lc = glc[~sel]
+    near = np.zeros((spec.nj, spec.ni), bool)
+    hi, hj = np.floor(hit_lc[:, 0]).astype(int), np.floor(hit_lc[:, 1]).astype(int)
+    for di in (0, 1):
+        for dj in (0, 1):
+            near[np.clip(hj + dj, 0, spec.nj - 1), np.clip(hi + di, 0, spec.ni - 1)] = True
+    far = ~near.reshape(-1)
+    assert far.sum() > 0.5 * spec.nn
+    assert np.max(np.abs(gden[far] - oden[far])) <= 1e-6 * np.abs(oden).max()
+    hit = ~sel
+    assert hit.sum() > 100
+    gspeed = np.linalg.norm(gvel, axis=1)
+    assert gspeed[hit].mean() == pytest.approx(2 * vth / np.sqrt(np.pi), rel=0.1)
+    assert gflux.sum() > 0
+
+
+def _jet_cfg():
+    spec = W.jet_mesh(ni=65, nj=33, Lz=0.064, Lr=0.032, r_inlet=4e-3)
+    return dict(spec=spec, mass=40 * AMU, spwt=2.5e11, inlet=np.array([0.0, 4e-3, 0.0, 0.0]), den=1e22,
+                temp=300.0, v_drift=500.0, wall_temp=300.0, diam=4.17e-10, T_ref=273.0, omega=0.81, dt=1e-6)
+
+
+def _blocks(field_cells, ni, nj, bi=8, bj=8):
+    """Sums of a per-cell field over blocks of bi x bj cells."""
+    f = field_cells.reshape(nj - 1, ni - 1)
+    return f.reshape((nj - 1) // bj, bj, (ni - 1) // bi, bi).sum(axis=(1, 3))
+
+
+def _node_blocks(field_nodes, weight, ni, nj, bi=8, bj=8):
+    """Weighted node averages over blocks (the last node row / column dropped)."""
+    f = (field_nodes * weight).reshape(nj, ni)[:-1, :-1]
+    w = weight.reshape(nj, ni)[:-1, :-1]
+    fs = f.reshape((nj - 1) // bj, bj, (ni - 1) // bi, bi).sum(axis=(1, 3))
+    ws = w.reshape((nj - 1) // bj, bj, (ni - 1) // bi, bi).sum(axis=(1, 3))
+    return fs / np.maximum(ws, 1e-300)
+
+
+def _gpu_jet(c, steps, sample_from, seed):
+    from starfish_gb300.plugin import DSMC, GpuDomain, KineticMaterial
+    spec = c["spec"]
+    dom = GpuDomain(spec)
+    try:
+        dom.set_seed(seed)
+        dom.set_efield(np.zeros(spec.nn), np.zeros(spec.nn))
+        km = KineticMaterial(dom, c["mass"], 0.0, c["spwt"], capacity=1 << 20)
+        vth = np.sqrt(2 * KB * c["wall_temp"] / c["mass"])
+        for s in range(spec.seg_xy.shape[0]):
+            km.set_surface(s, abi.SURF_DIFFUSE, vth=vth, c_rest=1.0, c_accom=1.0)
+        ds = DSMC(dom, km, model=abi.SIGMA_BIRD463, diam=c["diam"], T_ref=c["T_ref"], omega=c["omega"])
+        km.clear_samples()
+        for t in range(steps):
+            km.sample_maxwellian_source(c["inlet"], c["den"], c["v_drift"], c["temp"], c["dt"])
+            km.update_fields(c["dt"], stats=False, sample=t >= sample_from)
+            ds.perform(c["dt"])
+        cnt, _ = ds.counts()
+        gas = km.compute_fields(c["temp"])
+        out = {"count": cnt, "nd": gas["nd-ave"], "T": gas["T"], "np": km.get_np()}
+    finally:
+        dom.close()
+    return out
+
+
+def _oracle_jet(c, steps, sample_from, seed):
+    spec = c["spec"]
+    m = _omesh(spec)
+    ptr, idx = O.node_segments(m, spec.seg_xy)
+    vol = O.node_volumes(m)
+    cv = O.cell_volumes(m)
+    vth = np.sqrt(2 * KB * c["wall_temp"] / c["mass"])
+    segs = O.seg_table(spec.seg_xy, spec.seg_btype, O.SURF_DIFFUSE, vth=vth, c_rest=1.0, c_accom=1.0)
+    zero = np.zeros(spec.nn)
+    nc = (spec.ni - 1) * (spec.nj - 1)
+    state = np.zeros((nc, 2))
+    state[:, 0] = 1e-16
+    counts = np.zeros((nc, 2))
+    P = np.zeros((0, 12))
+    rem = 0.0
+    sums = None
+    ns = 0
+    for t in range(steps):
+        new, rem = O.maxwellian_source(seed * 1000003 + t, c["inlet"], c["den"], c["v_drift"], c["temp"], c["mass"],
+                                       c["spwt"], c["dt"], rem, domain=spec.domain)
+        O.add_particles(m, zero, zero, 0.0, c["mass"], c["dt"], new)
+        P = np.ascontiguousarray(np.vstack([P, new]))
+        O.push(m, zero, zero, 0.0, c["mass"], c["dt"], segs, ptr, idx, P, seed=seed * 7919 + t)
+        P = np.ascontiguousarray(P[P[:, 10] == 1])
+        if t >= sample_from:
+            sums = O.update_samples(m, P, sums)
+            ns += 1
+        O.dsmc(spec.ni, spec.nj, cv, P, c["mass"], c["spwt"], c["diam"], c["T_ref"], c["omega"], 1.0, c["dt"],
+               state, counts, seed * 104729 + t)
+    gas = O.compute_fields(sums, ns, vol, c["mass"], c["temp"])
+    return {"count": counts[:, 0].copy(), "nd": gas["nd-ave"], "T": gas["T"], "np": P.shape[0]}
+
+
+def _agree(ga, oa, mask, rel):
+    """Seed means within 4 standard errors of the difference plus rel of |oracle|."""
+    gm, om = ga.mean(axis=0), oa.mean(axis=0)
+    se = np.sqrt(ga.var(axis=0, ddof=1) / ga.shape[0] + oa.var(axis=0, ddof=1) / oa.shape[0])
+    bad = mask & (np.abs(gm - om) > 4 * se + rel * np.abs(om))
+    return int(bad.sum()), gm[mask], om[mask]
+
+
+def test_dsmc_jet_matches_oracle_over_seeds(gpulib):
+    """The axisymmetric argon jet on a 65x33 mesh (inlet r < 4 mm at 1e22 m^-3, 300 K,
+    500 m/s; diffuse walls at 300 K; VHS argon; dt 1 us), 120 steps, three seeds on each
+    side: per-block collision counts, sampled density and temperature (last 40 steps)
+    agree within 4 standard errors of the seed means plus 3 % (FP32 velocities and the
+    parallel rounds of disjoint pairs)."""
+    c = _jet_cfg()
+    spec = c["spec"]
+    steps, sample_from = 120, 80
+    seeds = (1, 2, 3)
+    g = [_gpu_jet(c, steps, sample_from, s) for s in seeds]
+    o = [_oracle_jet(c, steps, sample_from, s) for s in seeds]
+    ni, nj = spec.ni, spec.nj
+    gn = np.array([x["np"] for x in g], float)
+    on = np.array([x["np"] for x in o], float)
+    assert gn.mean() == pytest.approx(on.mean(), rel=0.02)
+    gc = np.array([_blocks(x["count"], ni, nj) for x in g])
+    oc = np.array([_blocks(x["count"], ni, nj) for x in o])
+    assert oc.sum() > 1e4  # collisional
+    busy = oc.mean(axis=0) > 200
+    nbad, gm, om = _agree(gc, oc, busy, 0.03)
+    assert busy.sum() >= 4 and nbad == 0, (gm, om)
+    assert gc.sum(axis=(1, 2)).mean() == pytest.approx(oc.sum(axis=(1, 2)).mean(), rel=0.03)
+    # sampled density and temperature over blocks, the temperature weighted by the
+    # oracle's mean sampled density
+    w_mean = np.mean([np.maximum(x["nd"], 0) for x in o], axis=0)
+    gnd = np.array([_node_blocks(x["nd"], np.ones(spec.nn), ni, nj) for x in g])
+    ond = np.array([_node_blocks(x["nd"], np.ones(spec.nn), ni, nj) for x in o])
+    dense = ond.mean(axis=0) > 0.02 * ond.mean(axis=0).max()
+    nbad, gm, om = _agree(gnd, ond, dense, 0.03)
+    assert dense.sum() >= 4 and nbad == 0, (gm, om)
+    gT = np.array([_node_blocks(x["T"], w_mean, ni, nj) for x in g])
+    oT = np.array([_node_blocks(x["T"], w_mean, ni, nj) for x in o])
+    nbad, gm, om = _agree(gT, oT, dense, 0.03)
+    assert nbad == 0, (gm, om)

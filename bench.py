@@ -195,6 +195,83 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
             "mesh": [spec.ni, spec.nj], "tol": tol, "particles_end": km.get_np(), "wall_s": wall}
 
 
+def l2_copy_gbs(mb=24, reps=200):
+    """Copy bandwidth of a buffer that stays in L2 (two 24 MB buffers, 129 MB of L2): the
+    reference for kernels whose grids are L2-resident (torch copy on the device)."""
+    import torch
+    n = mb * 1024 * 1024 // 4
+    a = torch.ones(n, dtype=torch.float32, device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(10):
+        b.copy_(a)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        b.copy_(a)
+    e1.record()
+    e1.synchronize()
+    return 2 * 4 * n * reps / (e0.elapsed_time(e1) / 1e3) / 1e9
+
+
+def poisson_roofline(cfg, dom, solves=4, tol=1e-6):
+    """Per-kernel roofline of the plain solve on this mesh: the solve's launches run with
+    per-kernel CUDA events (outside the CUDA graph the timed solves use; the kernels are
+    the same) over `solves` warm solves, each after a 20 V step of the electrode.
+    Algorithmic bytes per launch: multigrid level l going down reads r, P (FP32) and the
+    node class (1 B) and writes y per fine node, and writes the restricted residual per
+    coarse node (13 + 4 N_{l+1}/N_l B per node); going up it reads the coarse correction,
+    y, r, P and the class and writes y (17 + 4 N_{l+1}/N_l B); the FP64 Newton residual
+    reads phi, b0 (FP64) and the class and writes F and P (FP32): 25 B per node, and runs
+    the FP64 exponential per node (FP64-pipe-bound)."""
+    from starfish_gb300.plugin import PoissonSolver
+    ps = PoissonSolver(dom, n0=cfg.n0, Te0=cfg.Te0, phi0=cfg.phi0, tol=tol, max_it=60, cycles=4)
+    ni, nj = cfg.mesh.ni, cfg.mesh.nj
+    levels = [(ni, nj)]
+    while levels[-1][0] * levels[-1][1] > 2200 and (levels[-1][0] - 1) % 2 == 0 and (levels[-1][1] - 1) % 2 == 0:
+        a, b = levels[-1]
+        levels.append(((a - 1) // 2 + 1, (b - 1) // 2 + 1))
+    bc = cfg.mesh.bc_value.copy()
+    electrode = bc != 0
+    ps.set_bc_values(bc)
+    ps.solve()  # settle
+    dom.timing(True)
+    dom.timing_reset()
+    for k in range(solves):
+        # warm solves that have work to do: the electrode moves by 20 V between them
+        bc[electrode] = -100.0 - 20.0 * ((k % 2) + 1)
+        ps.set_bc_values(bc)
+        ps.solve()
+    peak, kind = measured_peaks()
+    l2 = l2_copy_gbs()
+    out = {"kernels": {}, "hbm_peak_gbs": peak, "peak_kind": kind, "l2_copy_gbs": l2,
+           "how": "per-kernel CUDA events over warm plain solves on the 2049x1025 mesh"}
+    for l in range(len(levels) - 1):
+        nf = levels[l][0] * levels[l][1]
+        nc = levels[l + 1][0] * levels[l + 1][1]
+        for name, per_node in ((f"mg_down_L{l}", 13), (f"mg_up_L{l}", 17)):
+            ms, cnt = dom.kernel_time(name)
+            if cnt == 0:
+                continue
+            b = per_node * nf + 4 * nc
+            gbs = b / (ms / cnt / 1e3) / 1e9
+            out["kernels"][name] = {"nodes": nf, "ms": ms / cnt, "launches": cnt, "alg_bytes": b, "gbs": gbs,
+                                    "frac_hbm": gbs / peak, "frac_l2": gbs / l2}
+    ms, cnt = dom.kernel_time("nl_residual")
+    if cnt:
+        b = 25 * ni * nj
+        gbs = b / (ms / cnt / 1e3) / 1e9
+        out["kernels"]["nl_residual"] = {"nodes": ni * nj, "ms": ms / cnt, "launches": cnt, "alg_bytes": b,
+                                         "gbs": gbs, "frac_hbm": gbs / peak, "frac_l2": gbs / l2,
+                                         "bound": "FP64 pipe (the FP64 exponential per node)"}
+    for name in ("mg_coarse", "cg_matvec"):
+        ms, cnt = dom.kernel_time(name)
+        if cnt:
+            out["kernels"][name] = {"ms": ms / cnt, "launches": cnt}
+    dom.timing(False)
+    return out
+
+
 def dsmc_jet_bench(steps=20, warmup=3, n_particles=16 * 1024 * 1024, seed=0):
     """The DSMC expanding-jet workload: Argon on the 513x257 axisymmetric (ZR) mesh, inlet
     r < 5 mm at 1e22 m^-3 / 300 K / 500 m/s sampled on the device every step, diffuse
@@ -646,6 +723,7 @@ def main():
     if args.poisson_steps > 0:
         line["poisson"] = learned_poisson_bench(cfg, dom, km, steps=args.poisson_steps,
                                                 train_steps=min(500, args.poisson_steps // 4))
+        line["roofline_poisson"] = poisson_roofline(cfg, dom)
     if args.poisson_pair:
         # the same solve as the reference arm's `poisson` (257x129 from phi = 0)
         line["poisson_257x129"] = gpu_poisson_solve()

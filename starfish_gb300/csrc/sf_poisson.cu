@@ -947,11 +947,31 @@ static void level_up(cudaStream_t s, const LevelView& F, const LevelView& C) {
     k_level_up<32, 8><<<dim3((F.ni + 31) / 32, (F.nj + 7) / 8), TILE_NT, 0, s>>>(F, C);
 }
 
+// Names of the per-kernel timers of the solve (sf_timing_enable): the level kernels per
+// level, so that each level's bytes can be divided by its own time.
+static const char* level_timer(bool down, int l) {
+  static const char* dn[] = {"mg_down_L0", "mg_down_L1", "mg_down_L2", "mg_down_L3", "mg_down_L4", "mg_down_L5",
+                             "mg_down_L6", "mg_down_L7"};
+  static const char* up[] = {"mg_up_L0", "mg_up_L1", "mg_up_L2", "mg_up_L3", "mg_up_L4", "mg_up_L5",
+                             "mg_up_L6", "mg_up_L7"};
+  if (l > 7) return down ? "mg_down_L8+" : "mg_up_L8+";
+  return down ? dn[l] : up[l];
+}
+
 static void vcycle(sf_ctx* ctx, SfPoisson* ps) {
   cudaStream_t s = ctx->stream;
-  for (int l = 0; l < ps->cs; l++) level_down(s, ps->lv[l], ps->lv[l + 1]);
-  k_coarse_vcycle<<<1, 1024, ps->coarse_smem, s>>>(ps->cd, ps->lv[ps->cs], 2, 2);
-  for (int l = ps->cs - 1; l >= 0; l--) level_up(s, ps->lv[l], ps->lv[l + 1]);
+  for (int l = 0; l < ps->cs; l++) {
+    TimedScope ts(ctx, level_timer(true, l));
+    level_down(s, ps->lv[l], ps->lv[l + 1]);
+  }
+  {
+    TimedScope ts(ctx, "mg_coarse");
+    k_coarse_vcycle<<<1, 1024, ps->coarse_smem, s>>>(ps->cd, ps->lv[ps->cs], 2, 2);
+  }
+  for (int l = ps->cs - 1; l >= 0; l--) {
+    TimedScope ts(ctx, level_timer(false, l));
+    level_up(s, ps->lv[l], ps->lv[l + 1]);
+  }
   ctx->launches += 2 * ps->cs + 1;
 }
 
@@ -976,7 +996,10 @@ static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters) {
   k_cg_pupdate<<<g, 256, 0, s>>>(n, ps->sc, 1, L0.y, ps->cg_p);
   ctx->launches += 3;
   for (int k = 0; k < iters; k++) {
-    k_cg_matvec<<<ps->red_blocks, RB, 0, s>>>(L0, ps->cg_p, ps->cg_q, ps->partial);
+    {
+      TimedScope ts(ctx, "cg_matvec");
+      k_cg_matvec<<<ps->red_blocks, RB, 0, s>>>(L0, ps->cg_p, ps->cg_q, ps->partial);
+    }
     reduce(ctx, ps, ps->sc + SC_RED, 0);
     k_cg_scalars<<<1, 32, 0, s>>>(ps->sc, 1);
     k_cg_axpy<<<g, 256, 0, s>>>(n, ps->sc, ps->cg_p, ps->cg_q, ps->cg_x, L0.r, L0.y, ps->cg_zo);
@@ -994,9 +1017,18 @@ static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters) {
 // The inner work of one Newton step -- restriction of P, `iters` PCG iterations with
 // their V-cycles, phi -= correction -- is ~70 launches of mostly small kernels; it is
 // captured once as a CUDA graph and replayed, re-captured when its parameters change.
+// With per-kernel timing on, the same launches run directly on the stream, each
+// bracketed by its timer's events.
 static void newton_step(sf_ctx* ctx, SfPoisson* ps, int iters, double max_step) {
   cudaStream_t s = ctx->stream;
   const int nn = ps->ni * ps->nj;
+  if (ctx->timer.on) {
+    restrict_P(ctx, ps);
+    pcg(ctx, ps, iters);
+    k_update_phi<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, s>>>(nn, ps->phi, ps->cg_x, max_step);
+    ctx->launches++;
+    return;
+  }
   if (!ps->step_graph || ps->graph_iters != iters || ps->graph_max_step != max_step) {
     if (ps->step_graph) {
       SF_CUDA(cudaGraphExecDestroy(ps->step_graph));
@@ -1134,8 +1166,11 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
   // most h[2] / sqrt(nn) to ||R||_2 / N; past 1 % of tol the solve continues in FP64.
   auto residual = [&](double* r2, double* rinf) {
     for (;;) {
-      k_nl_residual<<<ps->red_blocks, RB, 0, s>>>(a, ps->phi, ps->b0, ps->type0, ps->lv[0].r, ps->lv[0].P,
-                                                  ps->partial);
+      {
+        TimedScope ts(ctx, "nl_residual");
+        k_nl_residual<<<ps->red_blocks, RB, 0, s>>>(a, ps->phi, ps->b0, ps->type0, ps->lv[0].r, ps->lv[0].P,
+                                                    ps->partial);
+      }
       k_reduce_partials3<<<1, 256, 0, s>>>(ps->partial, ps->red_blocks, ps->red);
       ctx->launches += 2;
       SF_CUDA(cudaMemcpyAsync(h, ps->red, 24, cudaMemcpyDeviceToHost, s));
@@ -1489,6 +1524,16 @@ __global__ void kb_newton_control(BPInst* I, int n, const BPParams* __restrict__
   s.live = 0;
 }
 
+// End of one Newton round of the batched solve, inside the WHILE node of the field-phase
+// graph: another round runs while some instance took a Newton step in this one (an
+// instance stops stepping once it converges, fails or reaches max_it, so the loop ends
+// after at most max_it + 1 rounds; the count is a second bound).
+__global__ void kb_round_done(const int* __restrict__ run, int* rounds, const BPParams* __restrict__ pr,
+                              cudaGraphConditionalHandle loop) {
+  const int k = ++*rounds;
+  cudaGraphSetConditional(loop, (*run > 0 && k <= pr->max_it) ? 1u : 0u);
+}
+
 // level kernels: grid level l of the live instances with l < cs
 __global__ void kb_restrict_P(BPInst* I, BPWork w, int l, int kmin) {
   const int tot = *w.total, cnt = *w.cnt;
@@ -1693,6 +1738,7 @@ struct BatchPoisson {
   int* d_order = nullptr;  // instances by decreasing coarse-cycle size
   int* d_iters = nullptr;
   int* d_run = nullptr;
+  int* d_rounds = nullptr;  // Newton rounds of the current field phase
   BPParams* d_prm = nullptr;
   BPStat* d_stat = nullptr;
   // the live list and its per-kind prefixes
@@ -1705,7 +1751,8 @@ struct BatchPoisson {
   int max_cs = 0;
   size_t coarse_smem = 0;
   cudaStream_t stream = nullptr;
-  std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // Newton round by max PCG iterations
+  cudaStream_t body_stream = nullptr;  // captures the Newton round into the WHILE node's body
+  std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // field phase by max PCG iterations
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
@@ -1808,19 +1855,65 @@ static void bp_table(std::vector<int>& tab, int n, F blocks, int& off, int& tot)
   tot = acc;
 }
 
+// The whole field phase as one CUDA graph: the instances' start state, rho and b0, the
+// live list, then a WHILE node whose body is one Newton round of every live instance
+// (bp_round) followed by kb_round_done, which decides on the device whether another round
+// runs; then E and the per-instance results.  The host reads nothing until the phase is
+// done.  Graphs are kept per number of PCG iterations (the round's launch sequence).
 static cudaGraphExec_t bp_graph(BatchPoisson* bp, int max_iters) {
   for (auto& g : bp->graphs)
     if (g.first == max_iters) return g.second;
+  cudaStream_t s = bp->stream;
+  const int n = bp->n, tg = (n + 127) / 128;
   cudaGraph_t graph = nullptr;
-  SF_CUDA(cudaStreamBeginCapture(bp->stream, cudaStreamCaptureModeThreadLocal));
+  SF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  cudaGraphConditionalHandle loop{};
+  cudaGraph_t body = nullptr;
   try {
-    bp_round(bp, bp->stream, max_iters);
+    kb_init<<<tg, 128, 0, s>>>(bp->d_inst, n, bp->d_iters);
+    kb_rho_b0<<<bp->ktot[BK_FINE], ET, 0, s>>>(bp->d_inst, n, bp->d_tab + bp->koff[BK_FINE], bp->d_prm);
+    bp_compact(bp, s);  // every instance is live
+    SF_CUDA(cudaMemsetAsync(bp->d_rounds, 0, sizeof(int), s));
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    SF_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+    SF_CUDA(cudaGraphConditionalHandleCreate(&loop, g, 1u, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    SF_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp));
+    body = cp.conditional.phGraph_out[0];
+    SF_CUDA(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    kb_efield<<<bp->ktot[BK_FINE], ET, 0, s>>>(bp->d_inst, n, bp->d_tab + bp->koff[BK_FINE]);
+    kb_collect<<<tg, 128, 0, s>>>(bp->d_inst, n, bp->d_stat);
+    SF_CUDA(cudaGetLastError());
   } catch (...) {
-    cudaStreamEndCapture(bp->stream, &graph);
+    cudaStreamEndCapture(s, &graph);
     if (graph) cudaGraphDestroy(graph);
     throw;
   }
-  SF_CUDA(cudaStreamEndCapture(bp->stream, &graph));
+  SF_CUDA(cudaStreamEndCapture(s, &graph));
+  try {
+    SF_CUDA(cudaStreamBeginCaptureToGraph(bp->body_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    try {
+      bp_round(bp, bp->body_stream, max_iters);
+      kb_round_done<<<1, 1, 0, bp->body_stream>>>(bp->d_run, bp->d_rounds, bp->d_prm, loop);
+      SF_CUDA(cudaGetLastError());
+    } catch (...) {
+      cudaGraph_t b2 = nullptr;
+      cudaStreamEndCapture(bp->body_stream, &b2);
+      throw;
+    }
+    SF_CUDA(cudaStreamEndCapture(bp->body_stream, &body));
+  } catch (...) {
+    cudaGraphDestroy(graph);
+    throw;
+  }
   cudaGraphExec_t ex = nullptr;
   const cudaError_t e = cudaGraphInstantiate(&ex, graph, 0);
   cudaGraphDestroy(graph);
@@ -1934,6 +2027,8 @@ BatchPoisson* batch_poisson_create(sf_ctx* const* ctxs, int n, int num_sms, cuda
     SF_CUDA(cudaMalloc(&bp->d_iters, sizeof(int) * 2 * n));
     SF_CUDA(cudaFuncSetAttribute(kb_coarse_vcycle, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)COARSE_SMEM_MAX));
     SF_CUDA(cudaMalloc(&bp->d_run, sizeof(int)));
+    SF_CUDA(cudaMalloc(&bp->d_rounds, sizeof(int)));
+    SF_CUDA(cudaStreamCreateWithFlags(&bp->body_stream, cudaStreamNonBlocking));
     SF_CUDA(cudaMalloc(&bp->d_prm, sizeof(BPParams)));
     SF_CUDA(cudaMalloc(&bp->d_stat, sizeof(BPStat) * n));
     SF_CUDA(cudaEventCreate(&bp->ev0));
@@ -1952,9 +2047,10 @@ void batch_poisson_destroy(BatchPoisson* bp) {
   for (auto& g : bp->graphs) cudaGraphExecDestroy(g.second);
   void* ptrs[] = {bp->d_inst,      bp->d_tab,       bp->d_koff,      bp->d_order,     bp->d_iters,
                   bp->d_run,       bp->d_prm,       bp->d_stat,      bp->d_act_pos,   bp->d_act_list,
-                  bp->d_act_cnt,   bp->d_act_start, bp->d_act_total};
+                  bp->d_act_cnt,   bp->d_act_start, bp->d_act_total, bp->d_rounds};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (bp->body_stream) cudaStreamDestroy(bp->body_stream);
   if (bp->ev0) cudaEventDestroy(bp->ev0);
   if (bp->ev1) cudaEventDestroy(bp->ev1);
   delete bp;
@@ -1988,25 +2084,11 @@ float batch_poisson_step(BatchPoisson* bp, const sf_poisson_params& prm, const i
     init[i] = iters[i];
     init[bp->n + i] = bp->ctx[i]->poisson->fp64_exp ? 1 : 0;  // the contexts hold the sticky choice
   }
+  cudaGraphExec_t g = bp_graph(bp, max_iters);
   SF_CUDA(cudaEventRecord(bp->ev0, s));
   SF_CUDA(cudaMemcpyAsync(bp->d_prm, &h, sizeof(h), cudaMemcpyHostToDevice, s));
   SF_CUDA(cudaMemcpyAsync(bp->d_iters, init.data(), sizeof(int) * 2 * bp->n, cudaMemcpyHostToDevice, s));
-  const int tg = (bp->n + 127) / 128;
-  kb_init<<<tg, 128, 0, s>>>(bp->d_inst, bp->n, bp->d_iters);
-  kb_rho_b0<<<bp->ktot[BK_FINE], ET, 0, s>>>(bp->d_inst, bp->n, bp->d_tab + bp->koff[BK_FINE], bp->d_prm);
-  bp_compact(bp, s);  // every instance is live
-  SF_CUDA(cudaGetLastError());
-  cudaGraphExec_t g = bp_graph(bp, max_iters);
-  for (int r = 0; r <= prm.max_it; r++) {
-    SF_CUDA(cudaGraphLaunch(g, s));
-    int run = 0;
-    SF_CUDA(cudaMemcpyAsync(&run, bp->d_run, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SF_CUDA(cudaStreamSynchronize(s));
-    if (run == 0) break;
-  }
-  kb_efield<<<bp->ktot[BK_FINE], ET, 0, s>>>(bp->d_inst, bp->n, bp->d_tab + bp->koff[BK_FINE]);
-  kb_collect<<<tg, 128, 0, s>>>(bp->d_inst, bp->n, bp->d_stat);
-  SF_CUDA(cudaGetLastError());
+  SF_CUDA(cudaGraphLaunch(g, s));  // the whole field phase, Newton loop included
   SF_CUDA(cudaEventRecord(bp->ev1, s));
   std::vector<BPStat> hs(bp->n);
   SF_CUDA(cudaMemcpyAsync(hs.data(), bp->d_stat, sizeof(BPStat) * bp->n, cudaMemcpyDeviceToHost, s));

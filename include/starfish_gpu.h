@@ -355,6 +355,14 @@ int sf_unet_stats(sf_ctx* ctx, double* last_loss, int64_t* samples, double* trai
 int sf_unet_debug(sf_ctx* ctx, const float* x, const float* dpred, float* pred, float* grads, int64_t* nparams);
 /* Reads (get) and/or replaces (set) the FP32 master parameters, same flattening. */
 int sf_unet_params(sf_ctx* ctx, float* get, const float* set);
+/* The network's 3x3 convolutions (forward and backward-data) run on the tcgen05 tensor
+ * cores (TMA loads, accumulators in tensor memory) wherever the grid rows are 16, 32, 64
+ * or a multiple of 128 nodes; on = 0 runs them all on the mma.sync kernels instead (the
+ * two paths are compared in the tests).  A tensor-core pipeline that stalls gives up
+ * after 2 s and the next call returns SF_ERR_TIMEOUT.  *tc_convs: convolutions run on
+ * the tcgen05 path so far. */
+int sf_unet_set_tensor_cores(sf_ctx* ctx, int32_t on);
+int sf_unet_tensor_core_stats(sf_ctx* ctx, int64_t* tc_convs);
 
 /* ---- batches of independent instances (no reference counterpart) --------------- */
 /* Many independent cases (contexts of different mesh sizes and particle counts, one

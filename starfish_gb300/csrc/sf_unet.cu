@@ -26,6 +26,13 @@
 using namespace sf;
 typedef __nv_bfloat16 bf16;
 
+namespace sf {
+// the tensor-core (tcgen05) convolution, sf_conv_tc.cu
+bool conv3x3_tc_supported(int H, int W, int Cin, int Cout, int out_C, int out_c0);
+void conv3x3_tc(cudaStream_t s, const bf16* in, int H, int W, int Cin, const bf16* w, const float* bias, int Cout,
+                bf16* out, int out_C, int out_c0, bool relu, int* err);
+}  // namespace sf
+
 namespace {
 
 constexpr int CONV_THREADS = 128;
@@ -500,6 +507,9 @@ struct SfUnet {
   bool have_prev = false;
   int adam_t = 0;
   double train_ms = 0, infer_ms = 0;
+  bool use_tc = true;         // tcgen05 convolutions where the shape allows
+  int* tc_err = nullptr;      // device flag: a tensor-core convolution timed out
+  int64_t tc_convs = 0;       // convolutions run on the tcgen05 path
 };
 
 static void* ualloc(SfUnet* u, size_t bytes) {
@@ -545,9 +555,19 @@ static UConv make_conv(SfUnet* u, int cin, int cout, std::mt19937& rng) {
 
 static int ew_grid(sf_ctx* ctx, size_t n) { return grid_for((int64_t)std::min<size_t>(n, 1u << 30), 256, ctx->num_sms * 8); }
 
+// Forward (and backward-data) 3x3 convolution: on the tcgen05 tensor cores for the
+// shapes sf_conv_tc.cu takes (grid rows of 16, 32, 64 or a multiple of 128 nodes), else on
+// mma.sync.
 static void conv_fwd(sf_ctx* ctx, const bf16* in, int H, int W, int Cin, const bf16* w16, const float* bias, int Cout,
                      bf16* out, int out_C, int out_c0, bool relu) {
   SF_REQUIRE(Cin % 16 == 0 && Cout % 16 == 0, SF_ERR_ARG, "U-Net channels must be multiples of 16");
+  SfUnet* u = ctx->unet;
+  if (u && u->use_tc && conv3x3_tc_supported(H, W, Cin, Cout, out_C, out_c0)) {
+    conv3x3_tc(ctx->stream, in, H, W, Cin, w16, bias, Cout, out, out_C, out_c0, relu, u->tc_err);
+    ctx->launches++;
+    u->tc_convs++;
+    return;
+  }
   const int NT = Cout % 64 == 0 ? 64 : (Cout % 32 == 0 ? 32 : 16);  // must divide Cout
   const bool ci32 = Cin % 32 == 0;
   dim3 grid((W + SEG - 1) / SEG, H, Cout / NT);
@@ -563,6 +583,17 @@ static void conv_fwd(sf_ctx* ctx, const bf16* in, int H, int W, int Cin, const b
   }
 #undef CONV
   ctx->launches++;
+}
+
+// After a stream synchronisation: a tensor-core convolution whose pipeline wait ran out
+// left its output incomplete; report it (and clear the flag for the next call).
+static void check_tc(sf_ctx* ctx, SfUnet* u) {
+  int e = 0;
+  copy_wait(&e, u->tc_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e) {
+    zero_wait(u->tc_err, sizeof(int), ctx->stream);
+    SF_REQUIRE(false, SF_ERR_TIMEOUT, "a tensor-core convolution of the U-Net timed out");
+  }
 }
 
 static void conv_wgrad(sf_ctx* ctx, const bf16* gout, const bf16* in, int H, int W, int Cin, int Cout, float* dW) {
@@ -852,6 +883,7 @@ void sf_unet_after_solve(sf_ctx* ctx, const double* phi, const double* rho, cons
     u->train_ms += ms;
     u->last_loss = l;
     u->samples++;
+    check_tc(ctx, u);
   }
   SF_CUDA(cudaMemcpyAsync(u->phi_prev, phi, 8 * nn, cudaMemcpyDeviceToDevice, s));
   SF_CUDA(cudaMemcpyAsync(u->rho_prev, rho, 8 * nn, cudaMemcpyDeviceToDevice, s));
@@ -909,6 +941,7 @@ int sf_unet_init(sf_ctx* ctx, int32_t base_channels, int32_t down, uint64_t seed
   u->sum2 = (double*)ualloc(u, sizeof(double));
   u->rho_prev = (double*)ualloc(u, 8 * nn);
   u->bc_prev = (double*)ualloc(u, 8 * nn);
+  u->tc_err = (int*)ualloc(u, sizeof(int));
   SF_API_END(ctx)
 }
 
@@ -971,6 +1004,21 @@ int sf_unet_debug(sf_ctx* ctx, const float* x, const float* dpred, float* pred, 
   }
   SF_CUDA(cudaGetLastError());
   SF_CUDA(cudaStreamSynchronize(s));
+  check_tc(ctx, u);
+  SF_API_END(ctx)
+}
+
+int sf_unet_set_tensor_cores(sf_ctx* ctx, int32_t on) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx && ctx->unet, SF_ERR_STATE, "no U-Net (sf_unet_init)");
+  ctx->unet->use_tc = on != 0;
+  SF_API_END(ctx)
+}
+
+int sf_unet_tensor_core_stats(sf_ctx* ctx, int64_t* tc_convs) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx && ctx->unet, SF_ERR_STATE, "no U-Net (sf_unet_init)");
+  if (tc_convs) *tc_convs = ctx->unet->tc_convs;
   SF_API_END(ctx)
 }
 

@@ -304,6 +304,15 @@ class LearnedWarmStart:
         return {"loss": loss.value, "samples": n.value, "train_ms": ms.value, "used": used.value,
                 "rejected": rej.value}
 
+    def tensor_cores(self, on=True):
+        """3x3 convolutions on the tcgen05 tensor cores (the default) or on mma.sync."""
+        self.d.check(self.d.lib.sf_unet_set_tensor_cores(self.d.ctx, int(on)))
+
+    def tensor_core_convs(self):
+        n = C.c_int64()
+        self.d.check(self.d.lib.sf_unet_tensor_core_stats(self.d.ctx, C.byref(n)))
+        return n.value
+
     def nparams(self):
         n = C.c_int64()
         self.d.check(self.d.lib.sf_unet_debug(self.d.ctx, None, None, None, None, C.byref(n)))

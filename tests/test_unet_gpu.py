@@ -197,6 +197,56 @@ def test_unet_matches_torch_random(gpulib):
         dom.close()
 
 
+@pytest.mark.parametrize("base", [16, 32])
+def test_unet_tensor_core_path_matches_mma_sync(gpulib, base):
+    """The tcgen05 convolutions (TMA loads, tensor-memory accumulators) against the
+    mma.sync kernels on the same parameters and inputs.  The 64x32 network grid puts every
+    level but the 8x4 one on the tensor-core path (rows of 64, 32 and 16 pixels).  On
+    dyadic values both paths are exact, so prediction and gradients must be identical;
+    the conv counter shows that the tensor-core path ran."""
+    dom, net = _net(base)
+    try:
+        shapes = _param_shapes(base)
+        rng = np.random.default_rng(base + 11)
+        parts = []
+        for sh in shapes[:-2]:
+            if len(sh) == 4:
+                nz = rng.random(sh) < 2.0 / (9 * sh[3])
+                parts.append(np.where(nz, rng.choice([-1.0, 1.0], sh), 0.0))
+            else:
+                parts.append(rng.integers(-1, 2, sh).astype(np.float64))
+        parts += [np.ones(shapes[-2]), np.zeros(1)]
+        p = np.concatenate([a.reshape(-1) for a in parts]).astype(np.float32)
+        x = rng.integers(-4, 5, (net.Hn, net.Wn, 16)).astype(np.float32)
+        dpred = rng.integers(-3, 4, (net.Hn, net.Wn)).astype(np.float32)
+        net.params(set_to=p)
+        n0 = net.tensor_core_convs()
+        net.tensor_cores(True)
+        pred_tc, g_tc = net.forward_backward(x, dpred)
+        n1 = net.tensor_core_convs()
+        net.tensor_cores(False)
+        pred_ms, g_ms = net.forward_backward(x, dpred)
+        assert net.tensor_core_convs() == n1
+        # forward: 3 levels x 2 encoder convs + 3 decoder levels x 2; backward-data: the same
+        assert n1 - n0 >= 12, (n0, n1)
+        assert np.array_equal(pred_tc, pred_ms)
+        assert np.array_equal(g_tc, g_ms)
+        # random values: the two accumulation orders agree to BF16 level
+        q = net.params().copy()
+        for k, (a, sh) in enumerate(zip(_split(q, shapes), shapes)):
+            if len(sh) == 1 and k < len(shapes) - 2:
+                a[:] = rng.normal(0, 0.05, sh)
+        net.params(set_to=q)
+        xr = rng.normal(0, 1, (net.Hn, net.Wn, 16)).astype(np.float32)
+        net.tensor_cores(True)
+        a_tc, _ = net.forward_backward(xr)
+        net.tensor_cores(False)
+        a_ms, _ = net.forward_backward(xr)
+        assert np.linalg.norm(a_tc - a_ms) <= 1e-2 * np.linalg.norm(a_ms)
+    finally:
+        dom.close()
+
+
 def _rho(spec, t, rng):
     """Quasi-neutral ion charge with a slow central modulation and 1 % noise."""
     x = np.arange(spec.ni) * spec.dh[0]

@@ -121,7 +121,7 @@ def electrode_potential(step, period=2000):
 
 
 def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_every=10, tol=1e-6,
-                          base=32, down=8, keep_training_every=0):
+                          base=32, down=8, keep_training_every=0, mode=1):
     """Learned-warm-start workload on the 2049x1025 mesh: the full ES-PIC step (Maxwellian
     inlet at x = 0, push + scatter of the ions, rho, Poisson-Boltzmann solve, E) with the
     electrode potential following -100 - 100 cos(2 pi t / 2000) V.  The U-Net trains online
@@ -131,7 +131,11 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
     residual ||R||_2/N < tol.  Solve times are CUDA-event device times of sf_poisson_nl
     (the learned one includes the network's inference and the residual of the previous
     potential it is checked against).  keep_training_every > 0 keeps training online
-    after the training phase on one pair every that many solves (outside the timing)."""
+    after the training phase on one pair every that many solves (outside the timing).
+    mode 2 uses the network as the coarse correction inside the PCG instead of as the
+    start: it trains on the first residual of each converged solve (use_learned = 2 from
+    the first step, the correction switching on once trained), and the compared solves
+    start from the same previous potential with and without the correction."""
     from starfish_gb300 import abi
     from starfish_gb300.plugin import LearnedWarmStart, PoissonSolver
     spec = cfg.mesh
@@ -144,6 +148,8 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
     ion = cfg.ion
     cold = None
     plain, learned, learned_all = [], [], []
+    if mode == 2:
+        ps.use_learned(True, mode=2)  # trains on every converged solve until train_steps
     t_start = time.perf_counter()
     for t in range(steps):
         bc[electrode] = electrode_potential(t)
@@ -156,7 +162,7 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
                 net.train(True, lr=1e-3, every=keep_training_every)
             else:
                 net.train(False)
-            ps.use_learned(True)
+            ps.use_learned(True, mode=mode)
         compare = t >= train_steps and (t - train_steps) % compare_every == 0
         phi_prev = dom.get_field(abi.FIELD_PHI) if compare else None
         _, st = ps.solve()
@@ -168,7 +174,7 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
             learned.append(st)
             ps.use_learned(False)
             _, sp = ps.solve(phi=phi_prev)
-            ps.use_learned(True)
+            ps.use_learned(True, mode=mode)
             plain.append(sp)
         ps.update_gradient_field()
     wall = time.perf_counter() - t_start
@@ -178,7 +184,10 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
         return float(np.mean([x[k] for x in lst])) if lst else None
 
     pm, lm = mean(plain, "ms"), mean(learned, "ms")
-    return {"metric": "Poisson ms/solve to ||R||_2/N < 1e-6 (FP64), learned vs plain warm start",
+    return {"metric": "Poisson ms/solve to ||R||_2/N < 1e-6 (FP64), learned vs plain " +
+                      ("warm start" if mode == 1 else "preconditioner (no learned coarse correction)"),
+            "mode": "warm start" if mode == 1 else "coarse correction inside the PCG",
+            "tensor_core_convs": net.tensor_core_convs(),
             "plain_ms": pm, "learned_ms": lm, "speedup": (pm / lm) if pm and lm else None,
             "plain_newton_it": mean(plain, "newton_it"), "learned_newton_it": mean(learned, "newton_it"),
             "plain_initial_residual": mean(plain, "initial_residual"),
@@ -188,7 +197,8 @@ def learned_poisson_bench(cfg, dom, km, steps=2000, train_steps=500, compare_eve
             "cold_start_ms": cold["ms"], "cold_start_newton_it": cold["newton_it"],
             "training": {"solves": ns["samples"], "ms_per_solve": ns["train_ms"] / max(ns["samples"], 1),
                          "final_loss": ns["loss"], "network": f"U-Net 4 levels, base {base}, "
-                         f"grid {net.Wn}x{net.Hn} (mesh / {down}), BF16 mma.sync, Adam lr 1e-3",
+                         f"grid {net.Wn}x{net.Hn} (mesh / {down}), BF16 3x3 convolutions on tcgen05 "
+                         f"(mma.sync where the grid row is not 16/32/64/128k), Adam lr 1e-3",
                          "keep_training_every": keep_training_every},
             "predictions_used": ns["used"], "predictions_rejected": ns["rejected"],
             "steps": steps, "train_steps": train_steps, "electrode": "-100 - 100 cos(2 pi t / 2000) V",
@@ -589,6 +599,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--poisson-steps", type=int, default=2000)
     ap.add_argument("--dsmc-steps", type=int, default=20)
+    ap.add_argument("--precond-steps", type=int, default=1000,
+                    help="steps of the learned coarse-correction leg (0: skip)")
     ap.add_argument("--no-poisson-pair", dest="poisson_pair", action="store_false",
                     help="skip the 257x129 solve that the reference arm also times")
     ap.add_argument("--batch-steps", type=int, default=16)
@@ -723,6 +735,10 @@ def main():
     if args.poisson_steps > 0:
         line["poisson"] = learned_poisson_bench(cfg, dom, km, steps=args.poisson_steps,
                                                 train_steps=min(500, args.poisson_steps // 4))
+        if args.precond_steps > 0:
+            line["poisson_precond"] = learned_poisson_bench(cfg, dom, km, steps=args.precond_steps,
+                                                            train_steps=min(300, args.precond_steps // 3),
+                                                            mode=2)
         line["roofline_poisson"] = poisson_roofline(cfg, dom)
     if args.poisson_pair:
         # the same solve as the reference arm's `poisson` (257x129 from phi = 0)

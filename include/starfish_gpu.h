@@ -290,7 +290,11 @@ typedef struct {
   double tol;       /* target FP64 residual ||R||_2 / N (LinearSolverGS metric, :111-125) */
   int32_t max_it;   /* cap on Newton / refinement iterations                            */
   int32_t cycles;   /* PCG iterations (one V-cycle each) per Newton step; <= 0: 4       */
-  int32_t use_learned; /* 1: start from the learned predictor when it is trained       */
+  int32_t use_learned; /* 1: start from the learned predictor when it is trained;
+                          2: the network as a coarse correction inside the PCG: the first
+                          preconditioner application of each Newton step is
+                          e + V(r - J e), e the network's estimate of J^-1 r; every
+                          converged solve in this mode trains it on its first residual */
   int32_t linear;   /* 1: linear Poisson (no electron term), PoissonSolver linear_mode  */
 } sf_poisson_params;
 

@@ -34,6 +34,7 @@ namespace {
 constexpr int TC_THREADS = 128;
 constexpr int TC_M = 128;
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // a wait longer than 2 s counts as failed
+constexpr int TC_SMEM_LIMIT = 210 * 1024;  // dynamic shared memory of every launch: <= 200 KB of stages + 1 KB
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -351,7 +352,20 @@ void conv3x3_tc(cudaStream_t s, const bf16* in, int H, int W, int Cin, const bf1
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     SF_REQUIRE(r == CUDA_SUCCESS, SF_ERR_CUDA, "cuTensorMapEncodeTiled (weights) failed");
   }
-  SF_CUDA(cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // the shared-memory limit is set once per device, to a bound above every launch's need,
+  // so that launches captured into CUDA graphs make no attribute call
+  {
+    static std::mutex m;
+    static bool set[64] = {};
+    int dev = 0;
+    SF_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(m);
+    if (dev < 0 || dev >= 64 || !set[dev]) {
+      SF_CUDA(cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_LIMIT));
+      if (dev >= 0 && dev < 64) set[dev] = true;
+    }
+  }
+  SF_REQUIRE(smem <= (size_t)TC_SMEM_LIMIT, SF_ERR_ARG, "tensor-core convolution stages exceed the shared memory");
   const dim3 grid((W + a.BW - 1) / a.BW, (H + a.BH - 1) / a.BH, Cout / a.N);
   k_conv3x3_tc<<<grid, TC_THREADS, smem, s>>>(ma, mb, a);
   SF_CUDA(cudaGetLastError());

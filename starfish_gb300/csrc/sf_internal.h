@@ -415,6 +415,14 @@ void sf_unet_after_solve(sf_ctx* ctx, const double* phi, const double* rho, cons
                          const uint8_t* type, double eps);
 // the prediction made the start worse: phi <- phi_prev (counted as rejected)
 void sf_unet_reject(sf_ctx* ctx, double* phi);
+// Coarse-correction mode of the network (sf_unet.cu): launches of the correction e of a
+// linear residual r (returns the device buffer of e); the start of a solve (first
+// residual, Newton diagonal, potential) kept for training; the training step after a
+// converged solve; whether the network has been trained at all.
+float* sf_unet_coarse_correction(sf_ctx* ctx, const float* r, const float* P, const uint8_t* type);
+void sf_unet_coarse_start(sf_ctx* ctx, const float* r0, const float* P0, const double* phi0);
+void sf_unet_coarse_train(sf_ctx* ctx, const double* phi_end, const uint8_t* type);
+bool sf_unet_coarse_ready(const sf_ctx* ctx);
 namespace sf {
 void launch_sort(sf_ctx* ctx, SfSpecies* sp);
 void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments);

@@ -625,6 +625,25 @@ __global__ void __launch_bounds__(RB) k_cg_matvec(LevelView L, const float* __re
   cg_matvec_body(L, p, q, partial, blockIdx.x, gridDim.x);
 }
 
+// Coarse correction by the network inside the first preconditioner application of a
+// Newton step: keep r, then r <- r - J e (e: the network's correction).
+__global__ void k_pc_residual(LevelView L, const float* __restrict__ e, float* __restrict__ keep) {
+  const int n = L.ni * L.nj;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    const float ru = L.r[u];
+    keep[u] = ru;
+    L.r[u] = ru - apply_J(L.type[u], e, L.P[u], u, L.ni, L.cx, L.cy);
+  }
+}
+// ... after the V-cycle on r - J e: z <- V(r - J e) + e, r restored
+__global__ void k_pc_finish(LevelView L, const float* __restrict__ e, const float* __restrict__ keep) {
+  const int n = L.ni * L.nj;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    L.y[u] += e[u];
+    L.r[u] = keep[u];
+  }
+}
+
 // x += alpha p, r -= alpha q, zo = z
 __device__ __forceinline__ void cg_axpy_node(int u, float al, const float* __restrict__ p, const float* __restrict__ q,
                                              float* __restrict__ x, float* __restrict__ r, const float* __restrict__ z,
@@ -788,6 +807,7 @@ struct SfPoisson {
   cudaGraphExec_t step_graph = nullptr;
   int graph_iters = -1;
   double graph_max_step = 0;
+  bool graph_coarse = false;  // the captured step applies the network's coarse correction
   int64_t graph_launches = 0;
 };
 
@@ -982,13 +1002,24 @@ static void reduce(sf_ctx* ctx, SfPoisson* ps, double* out, int max2) {
 
 // iters steps of flexible PCG on J y = F (F = lv[0].r, overwritten as the CG residual);
 // the correction is left in cg_x
-static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters) {
+static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters, bool coarse) {
   cudaStream_t s = ctx->stream;
   const LevelView& L0 = ps->lv[0];
   const int n = L0.ni * L0.nj;
   const int g = grid_for(n, 256, ctx->num_sms * 8);
   SF_CUDA(cudaMemsetAsync(ps->cg_x, 0, 4 * (size_t)n, s));
-  vcycle(ctx, ps);  // z0
+  if (coarse) {
+    // z0 = e + V(r - J e), e the network's coarse correction of r (cg_p holds r meanwhile;
+    // it is first written by the p update below)
+    TimedScope ts(ctx, "learned_coarse");
+    const float* e = sf_unet_coarse_correction(ctx, L0.r, L0.P, L0.type);
+    k_pc_residual<<<g, 256, 0, s>>>(L0, e, ps->cg_p);
+    vcycle(ctx, ps);
+    k_pc_finish<<<g, 256, 0, s>>>(L0, e, ps->cg_p);
+    ctx->launches += 2;
+  } else {
+    vcycle(ctx, ps);  // z0
+  }
   SF_CUDA(cudaMemsetAsync(ps->cg_zo, 0, 4 * (size_t)n, s));
   k_cg_dots<<<ps->red_blocks, RB, 0, s>>>(n, L0.r, L0.y, ps->cg_zo, ps->partial);
   reduce(ctx, ps, ps->sc + SC_RED, 0);
@@ -1019,17 +1050,17 @@ static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters) {
 // captured once as a CUDA graph and replayed, re-captured when its parameters change.
 // With per-kernel timing on, the same launches run directly on the stream, each
 // bracketed by its timer's events.
-static void newton_step(sf_ctx* ctx, SfPoisson* ps, int iters, double max_step) {
+static void newton_step(sf_ctx* ctx, SfPoisson* ps, int iters, double max_step, bool coarse) {
   cudaStream_t s = ctx->stream;
   const int nn = ps->ni * ps->nj;
   if (ctx->timer.on) {
     restrict_P(ctx, ps);
-    pcg(ctx, ps, iters);
+    pcg(ctx, ps, iters, coarse);
     k_update_phi<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, s>>>(nn, ps->phi, ps->cg_x, max_step);
     ctx->launches++;
     return;
   }
-  if (!ps->step_graph || ps->graph_iters != iters || ps->graph_max_step != max_step) {
+  if (!ps->step_graph || ps->graph_iters != iters || ps->graph_max_step != max_step || ps->graph_coarse != coarse) {
     if (ps->step_graph) {
       SF_CUDA(cudaGraphExecDestroy(ps->step_graph));
       ps->step_graph = nullptr;
@@ -1039,7 +1070,7 @@ static void newton_step(sf_ctx* ctx, SfPoisson* ps, int iters, double max_step) 
     SF_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     try {
       restrict_P(ctx, ps);
-      pcg(ctx, ps, iters);
+      pcg(ctx, ps, iters, coarse);
       k_update_phi<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, s>>>(nn, ps->phi, ps->cg_x, max_step);
       ctx->launches++;
     } catch (...) {
@@ -1053,6 +1084,7 @@ static void newton_step(sf_ctx* ctx, SfPoisson* ps, int iters, double max_step) 
     SF_CUDA(e);
     ps->graph_iters = iters;
     ps->graph_max_step = max_step;
+    ps->graph_coarse = coarse;
     ps->graph_launches = ctx->launches - l0;
     ctx->launches = l0;
   }
@@ -1187,7 +1219,7 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
   // learned warm start (inside the timed region): phi <- phi_prev + U-Net prediction of
   // the change, kept only if its FP64 residual is below that of phi_prev itself
   double res = 0, res_inf = 0, res0 = -1;
-  if (prm->use_learned && !phi && ctx->unet) {
+  if (prm->use_learned == 1 && !phi && ctx->unet) {
     double r_prev, rinf_prev;
     residual(&r_prev, &rinf_prev);
     if (sf_unet_warm_start(ctx, ps->phi, ps->rho, ps->bc, ps->type0)) {
@@ -1206,6 +1238,11 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
     }
     res0 = res;
   }
+  // coarse-correction mode (use_learned = 2): the network corrects the first
+  // preconditioner application of every Newton step once it has been trained; every
+  // converged solve in this mode trains it on its own first residual
+  const bool coarse_mode = prm->use_learned == 2 && ctx->unet;
+  const bool coarse = coarse_mode && sf_unet_coarse_ready(ctx);
   int it = 0, vcount = 0;
   bool conv = false, diverged = false;
   for (it = 0; it <= prm->max_it; it++) {
@@ -1220,7 +1257,8 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
       break;
     }
     if (it == prm->max_it) break;
-    newton_step(ctx, ps, iters, prm->linear ? 1e300 : 10.0 * prm->kTe0);
+    if (it == 0 && coarse_mode) sf_unet_coarse_start(ctx, ps->lv[0].r, ps->lv[0].P, ps->phi);
+    newton_step(ctx, ps, iters, prm->linear ? 1e300 : 10.0 * prm->kTe0, coarse);
     vcount += iters;
   }
   ps->fp64_exp = a.fp64_exp != 0;
@@ -1231,7 +1269,8 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
   SF_CUDA(cudaGetLastError());
   // every converged solve is a training pair for the warm-start network (outside the
   // timed region; its cost is reported by sf_unet_stats)
-  if (conv && ctx->unet) sf_unet_after_solve(ctx, ps->phi, ps->rho, ps->bc, ps->type0, prm->eps);
+  if (conv && coarse_mode) sf_unet_coarse_train(ctx, ps->phi, ps->type0);
+  else if (conv && ctx->unet) sf_unet_after_solve(ctx, ps->phi, ps->rho, ps->bc, ps->type0, prm->eps);
   if (phi) {
     SF_CUDA(cudaMemcpyAsync(phi, ps->phi, 8 * (size_t)nn, cudaMemcpyDeviceToHost, s));
     SF_CUDA(cudaStreamSynchronize(s));

@@ -455,6 +455,93 @@ __global__ void k_unet_apply(InputArgs a, const float* __restrict__ sigma, const
   }
 }
 
+// ---- the network as a coarse correction inside the Poisson solve's PCG ------------
+// Input of the correction for a linear residual r (FP32, the Newton system J e = r) and
+// the Newton diagonal P, per network pixel covering down x down fine nodes:
+//   0  r block mean / RMS(r)        1  fraction of fixed nodes        2  (L/4)^2 P block mean
+// The network predicts e / s with s = (L/4)^2 RMS(r); the correction is s bilinear(pred)
+// on the free nodes and zero on fixed ones.  RMS(r) comes from sum2 (sum of r^2 over the
+// fine nodes).
+struct PcArgs {
+  int ni, nj, Hn, Wn, down;
+  float L4sq;  // (L / 4)^2
+};
+
+__global__ void k_pc_sum2(size_t n, const float* __restrict__ r, double* __restrict__ sum2) {
+  double s2 = 0.0;
+  for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < n; u += (size_t)gridDim.x * blockDim.x) {
+    const double v = r[u];
+    s2 += v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) s2 += __shfl_down_sync(0xffffffffu, s2, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(sum2, s2);
+}
+
+__global__ void k_pc_inputs(PcArgs a, const double* __restrict__ sum2, const float* __restrict__ r,
+                            const float* __restrict__ P, const uint8_t* __restrict__ type, bf16* __restrict__ x) {
+  const size_t n = (size_t)a.Hn * a.Wn;
+  const float rms = (float)sqrt(*sum2 / ((double)a.ni * a.nj));
+  const float inv = rms > 0.f ? 1.f / rms : 0.f;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    const int X = p % a.Wn, Y = p / a.Wn;
+    float rs = 0.f, ps = 0.f;
+    int nfix = 0, cnt = 0;
+    for (int dj = 0; dj < a.down; dj++) {
+      const int j = a.down * Y + dj;
+      if (j >= a.nj) break;
+      for (int di = 0; di < a.down; di++) {
+        const int i = a.down * X + di;
+        if (i >= a.ni) break;
+        const size_t u = (size_t)j * a.ni + i;
+        rs += r[u];
+        ps += P[u];
+        nfix += type[u] == NODE_FIXED;
+        cnt++;
+      }
+    }
+    bf16* xp = x + p * 16;
+    xp[0] = __float2bfloat16(rs / cnt * inv);
+    xp[1] = __float2bfloat16((float)nfix / (float)cnt);
+    xp[2] = __float2bfloat16(a.L4sq * ps / cnt);
+    for (int c = 3; c < 16; c++) xp[c] = __float2bfloat16(0.f);
+  }
+}
+
+// e = s bilinear(pred) on free nodes, 0 on fixed nodes
+__global__ void k_pc_apply(PcArgs a, const double* __restrict__ sum2, const float* __restrict__ pred,
+                           const uint8_t* __restrict__ type, float* __restrict__ e) {
+  const size_t n = (size_t)a.ni * a.nj;
+  const float s = a.L4sq * (float)sqrt(*sum2 / (double)n);
+  for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < n; u += (size_t)gridDim.x * blockDim.x) {
+    if (type[u] == NODE_FIXED) {
+      e[u] = 0.f;
+      continue;
+    }
+    const int i = u % a.ni, j = u / a.ni;
+    const float fx = (float)i / a.down, fy = (float)j / a.down;
+    const int X = min((int)fx, a.Wn - 1), Y = min((int)fy, a.Hn - 1);
+    const int X1 = min(X + 1, a.Wn - 1), Y1 = min(Y + 1, a.Hn - 1);
+    const float wx = fminf(fx - X, 1.f), wy = fminf(fy - Y, 1.f);
+    const float v = (1 - wx) * (1 - wy) * pred[(size_t)Y * a.Wn + X] + wx * (1 - wy) * pred[(size_t)Y * a.Wn + X1] +
+                    wx * wy * pred[(size_t)Y1 * a.Wn + X1] + (1 - wx) * wy * pred[(size_t)Y1 * a.Wn + X];
+    e[u] = s * v;
+  }
+}
+
+// training target of the correction: (phi_start - phi_end) / s at node (down X, down Y):
+// the Newton correction the whole solve applied to its first residual
+__global__ void k_pc_target(PcArgs a, const double* __restrict__ sum2, const double* __restrict__ phi_start,
+                            const double* __restrict__ phi_end, float* __restrict__ target) {
+  const size_t n = (size_t)a.Hn * a.Wn;
+  const double s = (double)a.L4sq * sqrt(*sum2 / ((double)a.ni * a.nj));
+  const double inv = s > 0 ? 1.0 / s : 0.0;
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+    const int X = p % a.Wn, Y = p / a.Wn;
+    const size_t u0 = (size_t)(a.down * Y) * a.ni + a.down * X;
+    target[p] = (float)((phi_start[u0] - phi_end[u0]) * inv);
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------------------------
@@ -507,6 +594,12 @@ struct SfUnet {
   bool have_prev = false;
   int adam_t = 0;
   double train_ms = 0, infer_ms = 0;
+  // coarse-correction mode: the first residual and Newton diagonal of the last solve and
+  // its start potential (the training pair once it has converged), and the correction
+  float *pc_r0 = nullptr, *pc_P0 = nullptr, *pc_e = nullptr;
+  double* pc_phi0 = nullptr;
+  double* pc_sum2 = nullptr;  // [0] sum r^2 of the current correction input, [1] of the saved r0
+  bool pc_have = false;       // pc_r0 / pc_P0 / pc_phi0 hold the start of the last solve
   bool use_tc = true;         // tcgen05 convolutions where the shape allows
   int* tc_err = nullptr;      // device flag: a tensor-core convolution timed out
   int64_t tc_convs = 0;       // convolutions run on the tcgen05 path
@@ -906,6 +999,95 @@ bool sf_unet_warm_start(sf_ctx* ctx, double* phi, const double* rho, const doubl
   u->used++;
   return true;
 }
+
+static PcArgs pc_args(sf_ctx* ctx, SfUnet* u) {
+  PcArgs a;
+  a.ni = ctx->ni;
+  a.nj = ctx->nj;
+  a.Hn = u->Hn;
+  a.Wn = u->Wn;
+  a.down = u->down;
+  const double L = std::min((ctx->ni - 1) * ctx->dh[0], (ctx->nj - 1) * ctx->dh[1]) / 4;
+  a.L4sq = (float)(L * L);
+  return a;
+}
+
+static void pc_buffers(sf_ctx* ctx, SfUnet* u) {
+  if (u->pc_e) return;
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  u->pc_r0 = (float*)ualloc(u, 4 * nn);
+  u->pc_P0 = (float*)ualloc(u, 4 * nn);
+  u->pc_e = (float*)ualloc(u, 4 * nn);
+  u->pc_phi0 = (double*)ualloc(u, 8 * nn);
+  u->pc_sum2 = (double*)ualloc(u, 2 * sizeof(double));
+}
+
+// Launches the network's correction e for the residual r (only launches: the Newton step
+// that calls it is captured as a CUDA graph).  e lives in the network's buffer, which the
+// first use allocates: that first use happens at the start of a solve in this mode
+// (sf_unet_coarse_start), before any capture.
+float* sf_unet_coarse_correction(sf_ctx* ctx, const float* r, const float* P, const uint8_t* type) {
+  SfUnet* u = ctx->unet;
+  pc_buffers(ctx, u);
+  cudaStream_t s = ctx->stream;
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  const PcArgs a = pc_args(ctx, u);
+  SF_CUDA(cudaMemsetAsync(u->pc_sum2, 0, sizeof(double), s));
+  k_pc_sum2<<<ew_grid(ctx, nn), 256, 0, s>>>(nn, r, u->pc_sum2);
+  k_pc_inputs<<<ew_grid(ctx, (size_t)u->Hn * u->Wn), 256, 0, s>>>(a, u->pc_sum2, r, P, type, u->x.p);
+  unet_forward(ctx, u);
+  k_pc_apply<<<ew_grid(ctx, nn), 256, 0, s>>>(a, u->pc_sum2, u->pred, type, u->pc_e);
+  ctx->launches += 3;
+  return u->pc_e;
+}
+
+// The start of a solve in coarse-correction mode: its first residual, Newton diagonal and
+// potential, kept for the training pair the converged solve makes.
+void sf_unet_coarse_start(sf_ctx* ctx, const float* r0, const float* P0, const double* phi0) {
+  SfUnet* u = ctx->unet;
+  pc_buffers(ctx, u);
+  cudaStream_t s = ctx->stream;
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  SF_CUDA(cudaMemcpyAsync(u->pc_r0, r0, 4 * nn, cudaMemcpyDeviceToDevice, s));
+  SF_CUDA(cudaMemcpyAsync(u->pc_P0, P0, 4 * nn, cudaMemcpyDeviceToDevice, s));
+  SF_CUDA(cudaMemcpyAsync(u->pc_phi0, phi0, 8 * nn, cudaMemcpyDeviceToDevice, s));
+  u->pc_have = true;
+}
+
+// After a converged solve in coarse-correction mode (outside the solve's timing): one
+// training step on (first residual, first Newton diagonal) -> the whole correction the
+// solve applied, phi_start - phi_end.
+void sf_unet_coarse_train(sf_ctx* ctx, const double* phi_end, const uint8_t* type) {
+  SfUnet* u = ctx->unet;
+  if (!u || !u->pc_have || !u->training) return;
+  u->pc_have = false;
+  cudaStream_t s = ctx->stream;
+  const size_t nn = (size_t)ctx->ni * ctx->nj;
+  const PcArgs a = pc_args(ctx, u);
+  cudaEvent_t e0, e1;
+  SF_CUDA(cudaEventCreate(&e0));
+  SF_CUDA(cudaEventCreate(&e1));
+  SF_CUDA(cudaEventRecord(e0, s));
+  SF_CUDA(cudaMemsetAsync(u->pc_sum2 + 1, 0, sizeof(double), s));
+  k_pc_sum2<<<ew_grid(ctx, nn), 256, 0, s>>>(nn, u->pc_r0, u->pc_sum2 + 1);
+  k_pc_inputs<<<ew_grid(ctx, (size_t)u->Hn * u->Wn), 256, 0, s>>>(a, u->pc_sum2 + 1, u->pc_r0, u->pc_P0, type, u->x.p);
+  k_pc_target<<<ew_grid(ctx, (size_t)u->Hn * u->Wn), 256, 0, s>>>(a, u->pc_sum2 + 1, u->pc_phi0, phi_end, u->target);
+  ctx->launches += 3;
+  double l = 0;
+  for (int k = 0; k < u->iters_per_sample; k++) l = unet_train_step(ctx, u);
+  SF_CUDA(cudaEventRecord(e1, s));
+  SF_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  u->train_ms += ms;
+  u->last_loss = l;
+  u->samples++;
+  check_tc(ctx, u);
+}
+
+bool sf_unet_coarse_ready(const sf_ctx* ctx) { return ctx->unet && ctx->unet->samples > 0; }
 
 void sf_unet_reject(sf_ctx* ctx, double* phi) {
   SfUnet* u = ctx->unet;

@@ -271,9 +271,11 @@ class PoissonSolver:
         self.d.check(self.d.lib.sf_boltzmann(self.d.ctx, abi.ptr(ne)))
         return ne
 
-    def use_learned(self, on=True):
-        """Start each solve from the learned warm start (LearnedWarmStart must exist)."""
-        self.prm.use_learned = 1 if on else 0
+    def use_learned(self, on=True, mode=1):
+        """Use the domain's network (LearnedWarmStart must exist): mode 1 starts each solve
+        from its predicted potential; mode 2 uses it as a coarse correction inside the
+        PCG and trains it on each converged solve's first residual."""
+        self.prm.use_learned = int(mode) if on else 0
 
 
 class LearnedWarmStart:

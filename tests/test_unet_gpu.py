@@ -313,6 +313,46 @@ def test_learned_warm_start_gain(gpulib):
         dom.close()
 
 
+def test_learned_coarse_correction_in_pcg(gpulib):
+    """use_learned = 2: the network, trained online on each converged solve's first
+    residual, corrects the first preconditioner application of every Newton step inside
+    the PCG.  The solves still reach the FP64 tolerance and the same potential as plain
+    solves from the same start; the 64x32 network grid runs on the tensor-core path."""
+    from starfish_gb300.plugin import GpuDomain, LearnedWarmStart, PoissonSolver
+    spec = W.es_pic_mesh(65, 33, 1e-3, electrode_halfwidth=4e-3)
+    electrode = spec.bc_value != 0
+    dom = GpuDomain(spec)
+    try:
+        ps = PoissonSolver(dom, n0=1e12, Te0=2.0, tol=1e-6, max_it=60)
+        net = LearnedWarmStart(dom, base=16, down=1, seed=2, lr=2e-3, iters_per_sample=2)
+        ps.use_learned(True, mode=2)
+        rng = np.random.default_rng(5)
+        bc = spec.bc_value.copy()
+        period = 300
+        for t in range(150):
+            bc[electrode] = -100 - 100 * np.cos(2 * np.pi * t / period)
+            ps.set_bc_values(bc)
+            _, st = ps.solve(rho=_rho(spec, t, rng))
+            assert st["residual"] < 1e-6
+        assert net.stats()["samples"] >= 100
+        assert net.tensor_core_convs() > 0
+        net.train(False)
+        for t in range(150, 170):
+            phi_prev = dom.get_field(abi.FIELD_PHI)
+            rho = _rho(spec, t, rng)
+            bc[electrode] = -100 - 100 * np.cos(2 * np.pi * t / period)
+            ps.set_bc_values(bc)
+            ps.use_learned(True, mode=2)
+            _, sl = ps.solve(rho=rho)
+            phi_l = dom.get_field(abi.FIELD_PHI)
+            ps.use_learned(False)
+            phi_p, sp = ps.solve(rho=rho, phi=phi_prev)
+            assert sl["residual"] < 1e-6 and sp["residual"] < 1e-6, (sl, sp)
+            assert np.max(np.abs(phi_l - phi_p)) < 1e-6 * np.max(np.abs(phi_p))
+    finally:
+        dom.close()
+
+
 def test_rejected_prediction_still_converges(gpulib):
     """A prediction worse than the previous potential is rejected (phi reverts to the
     previous solution) and the solve converges from there to the same potential."""

@@ -257,7 +257,27 @@ __device__ inline unsigned hash_insert(unsigned* hkey, unsigned key) {
   return SORT_HSIZE;  // unreachable: the table has more slots than a chunk has keys
 }
 
-__global__ void __launch_bounds__(SORT_B) k_sort_hist(ParticlesView p, int ntx, int* bins) {
+// Sort key of a particle: its cell's key, or with a look-ahead the key of the cell it will
+// reach in tau steps moving straight on (ax = tau dt / dx cells per m/s), clamped to the
+// mesh.  The look-ahead only orders particles for locality: a species sorted at the middle
+// of the interval between two sorts stays twice as compact on average as one sorted by its
+// current cells, since its particles spread from their predicted cell both before and
+// after.  Binning that needs the exact cells (DSMC) sorts with no look-ahead.
+struct SortLook {
+  float ax, ay;
+  int imax, jmax;  // ni - 2, nj - 2
+};
+__device__ __forceinline__ unsigned sort_key(uint32_t c, float2 f, float2 v, int ntx, const SortLook& L) {
+  int i = cell_i(c), j = cell_j(c);
+  if (L.ax != 0.f || L.ay != 0.f) {
+    const float di = fminf(fmaxf(f.x + v.x * L.ax, -1e6f), 1e6f), dj = fminf(fmaxf(f.y + v.y * L.ay, -1e6f), 1e6f);
+    i = min(max(i + (int)floorf(di), 0), L.imax);
+    j = min(max(j + (int)floorf(dj), 0), L.jmax);
+  }
+  return cell_key(i, j, ntx);
+}
+
+__global__ void __launch_bounds__(SORT_B) k_sort_hist(ParticlesView p, int ntx, int* bins, SortLook L) {
   __shared__ unsigned hkey[SORT_HSIZE];
   __shared__ unsigned hcnt[SORT_HSIZE];
   for (int64_t base = (int64_t)blockIdx.x * SORT_CHUNK; base < p.n; base += (int64_t)gridDim.x * SORT_CHUNK) {
@@ -271,7 +291,10 @@ __global__ void __launch_bounds__(SORT_B) k_sort_hist(ParticlesView p, int ntx, 
       const int64_t q = base + k * SORT_B + threadIdx.x;
       const uint32_t c = (q < p.n) ? p.cell[q] : DEAD;
       if (c == DEAD) continue;
-      const unsigned slot = hash_insert(hkey, cell_key(cell_i(c), cell_j(c), ntx));
+      const bool look = L.ax != 0.f || L.ay != 0.f;
+      const float2 f = look ? p.frac[q] : make_float2(0.f, 0.f);
+      const float2 v = look ? p.vxy[q] : make_float2(0.f, 0.f);
+      const unsigned slot = hash_insert(hkey, sort_key(c, f, v, ntx, L));
       if (slot < SORT_HSIZE) atomicAdd(&hcnt[slot], 1u);
     }
     __syncthreads();
@@ -289,7 +312,8 @@ constexpr size_t SORT_SCATTER_SMEM =
     (size_t)SORT_HSIZE * 3 * sizeof(unsigned) +
     (size_t)SORT_CHUNK * (sizeof(uint32_t) + sizeof(float2) + sizeof(float2) + sizeof(float) + sizeof(int));
 
-__global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, ParticlesView dst, int ntx, int* cursor) {
+__global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, ParticlesView dst, int ntx, int* cursor,
+                                                         SortLook L) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* s_frac = reinterpret_cast<float2*>(smem_raw);
   float2* s_vxy = s_frac + SORT_CHUNK;
@@ -330,7 +354,7 @@ __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, Part
       const uint32_t c = r_cell[k];
       slot[k] = SORT_HSIZE;
       if (c == DEAD) continue;
-      slot[k] = hash_insert(hkey, cell_key(cell_i(c), cell_j(c), ntx));
+      slot[k] = hash_insert(hkey, sort_key(c, r_frac[k], r_vxy[k], ntx, L));
       if (slot[k] < SORT_HSIZE) rank[k] = atomicAdd(&hcnt[slot[k]], 1u);
     }
     __syncthreads();
@@ -482,14 +506,15 @@ static void exclusive_scan(sf_ctx* ctx, int* data, int n) {
                           ctx->stream));
 }
 
-void launch_sort(sf_ctx* ctx, SfSpecies* sp) {
+void launch_sort(sf_ctx* ctx, SfSpecies* sp, float look_x, float look_y) {
   const int nk = ctx->nkeys;
+  const SortLook L{look_x, look_y, ctx->ni - 2, ctx->nj - 2};
   TimedScope ts(ctx, "sort");
   SF_CUDA(cudaMemsetAsync(ctx->bins, 0, sizeof(int) * (size_t)(nk + 1), ctx->stream));
   if (sp->n > 0) {
     ctx->launches += 5;
     int g = grid_for((sp->n + SORT_CHUNK - 1) / SORT_CHUNK, 1, ctx->num_sms * 6);
-    k_sort_hist<<<g, SORT_B, 0, ctx->stream>>>(sp->cur, ctx->ntx, ctx->bins);
+    k_sort_hist<<<g, SORT_B, 0, ctx->stream>>>(sp->cur, ctx->ntx, ctx->bins, L);
     exclusive_scan(ctx, ctx->bins, nk + 1);  // bins[key] = first slot of the cell, bins[nk] = total
     SF_CUDA(cudaMemcpyAsync(ctx->bins_tmp, ctx->bins, sizeof(int) * (size_t)(nk + 1),
                             cudaMemcpyDeviceToDevice, ctx->stream));
@@ -500,7 +525,7 @@ void launch_sort(sf_ctx* ctx, SfSpecies* sp) {
                                  (int)SORT_SCATTER_SMEM));
     // 52 KB of shared memory and 64 registers per block: 4 blocks per SM
     const int gs = grid_for((sp->n + SORT_CHUNK - 1) / SORT_CHUNK, 1, ctx->num_sms * 4);
-    k_sort_scatter<<<gs, SORT_B, SORT_SCATTER_SMEM, ctx->stream>>>(sp->cur, dst, ctx->ntx, ctx->bins_tmp);
+    k_sort_scatter<<<gs, SORT_B, SORT_SCATTER_SMEM, ctx->stream>>>(sp->cur, dst, ctx->ntx, ctx->bins_tmp, L);
     SF_CUDA(cudaGetLastError());
     int total = 0;
     SF_CUDA(cudaMemcpyAsync(&total, ctx->bins + nk, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

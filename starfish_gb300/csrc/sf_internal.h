@@ -424,7 +424,9 @@ void sf_unet_coarse_start(sf_ctx* ctx, const float* r0, const float* P0, const d
 void sf_unet_coarse_train(sf_ctx* ctx, const double* phi_end, const uint8_t* type);
 bool sf_unet_coarse_ready(const sf_ctx* ctx);
 namespace sf {
-void launch_sort(sf_ctx* ctx, SfSpecies* sp);
+// Counting sort of a species by cell key (sf_context.cu); with a look-ahead (cells per
+// m/s in x and y) by the cell each particle reaches moving straight on, for locality only.
+void launch_sort(sf_ctx* ctx, SfSpecies* sp, float look_x = 0.f, float look_y = 0.f);
 void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments);
 SfSpecies* get_species(sf_ctx* ctx, int sid);
 void ensure_scratch(sf_ctx* ctx, int64_t particles);

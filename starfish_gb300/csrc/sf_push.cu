@@ -1310,9 +1310,13 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   const bool mom = sample || (flags & SF_PUSH_MOMENTS) != 0;
   SF_REQUIRE(!sample || sp->samp, SF_ERR_STATE, "velocity sampling not set up (sf_samples_clear)");
   const SampleView smp = sample ? sp->smp : SampleView{nullptr, nullptr};
-  // automatic cell sort every sort_interval pushes (the counter starts at the interval,
-  // so the first push of a species sorts)
-  if (sp->sort_interval > 0 && sp->pushes_since_sort >= sp->sort_interval) launch_sort(ctx, sp);
+  // automatic cell sort every sort_interval pushes (the counter starts at the interval, so
+  // the first push of a species sorts); the key looks half an interval ahead, so that the
+  // tiles are most compact in the middle of the interval (locality only)
+  if (sp->sort_interval > 0 && sp->pushes_since_sort >= sp->sort_interval) {
+    const double tau = 0.5 * sp->sort_interval * dt;
+    launch_sort(ctx, sp, (float)(tau / ctx->dh[0]), (float)(tau / ctx->dh[1]));
+  }
   const size_t nn = (size_t)ctx->ni * ctx->nj;
   cudaStream_t s = ctx->stream;
   SF_CUDA(cudaMemsetAsync(sp->count, 0, sizeof(unsigned long long) * nn, s));

@@ -111,7 +111,8 @@ def setup_workload(n_particles, seed=0):
         m = min(chunk, n_particles - c0)
         pos, vel = W.uniform_maxwellian(spec, cfg.ion, m, seed + c0)
         km.add_particles(pos, vel, rewind=True, dt=cfg.dt)
-    km.sort()
+    # no explicit sort: the first push sorts (automatically, with the look-ahead key of
+    # the steps that follow), so the timed steps see the steady-state sort cycle
     return cfg, dom, km, efi, efj
 
 

@@ -292,7 +292,7 @@ typedef struct {
   int32_t cycles;   /* PCG iterations (one V-cycle each) per Newton step; <= 0: 4       */
   int32_t use_learned; /* 1: start from the learned predictor when it is trained;
                           2: the network as a coarse correction inside the PCG: the first
-                          preconditioner application of each Newton step is
+                          preconditioner application of the first Newton step is
                           e + V(r - J e), e the network's estimate of J^-1 r; every
                           converged solve in this mode trains it on its first residual */
   int32_t linear;   /* 1: linear Poisson (no electron term), PoissonSolver linear_mode  */

@@ -803,12 +803,12 @@ struct SfPoisson {
   sf_poisson_params prm{};
   bool have_prm = false;
   bool fp64_exp = false;  // a previous solve needed the FP64 exponential: start there
-  // the inner work of one Newton step (restrict P, PCG, update) as a CUDA graph
-  cudaGraphExec_t step_graph = nullptr;
-  int graph_iters = -1;
-  double graph_max_step = 0;
-  bool graph_coarse = false;  // the captured step applies the network's coarse correction
-  int64_t graph_launches = 0;
+  // the inner work of one Newton step (restrict P, PCG, update) as a CUDA graph; [1] the
+  // step that applies the network's coarse correction, [0] the plain one
+  cudaGraphExec_t step_graph[2] = {nullptr, nullptr};
+  int graph_iters[2] = {-1, -1};
+  double graph_max_step[2] = {0, 0};
+  int64_t graph_launches[2] = {0, 0};
 };
 
 // zeroed: the first solve without a host phi starts from phi = 0, and no buffer holds
@@ -1060,10 +1060,11 @@ static void newton_step(sf_ctx* ctx, SfPoisson* ps, int iters, double max_step, 
     ctx->launches++;
     return;
   }
-  if (!ps->step_graph || ps->graph_iters != iters || ps->graph_max_step != max_step || ps->graph_coarse != coarse) {
-    if (ps->step_graph) {
-      SF_CUDA(cudaGraphExecDestroy(ps->step_graph));
-      ps->step_graph = nullptr;
+  const int gi = coarse ? 1 : 0;
+  if (!ps->step_graph[gi] || ps->graph_iters[gi] != iters || ps->graph_max_step[gi] != max_step) {
+    if (ps->step_graph[gi]) {
+      SF_CUDA(cudaGraphExecDestroy(ps->step_graph[gi]));
+      ps->step_graph[gi] = nullptr;
     }
     const int64_t l0 = ctx->launches;
     cudaGraph_t graph = nullptr;
@@ -1079,17 +1080,16 @@ static void newton_step(sf_ctx* ctx, SfPoisson* ps, int iters, double max_step, 
       throw;
     }
     SF_CUDA(cudaStreamEndCapture(s, &graph));
-    const cudaError_t e = cudaGraphInstantiate(&ps->step_graph, graph, 0);
+    const cudaError_t e = cudaGraphInstantiate(&ps->step_graph[gi], graph, 0);
     cudaGraphDestroy(graph);
     SF_CUDA(e);
-    ps->graph_iters = iters;
-    ps->graph_max_step = max_step;
-    ps->graph_coarse = coarse;
-    ps->graph_launches = ctx->launches - l0;
+    ps->graph_iters[gi] = iters;
+    ps->graph_max_step[gi] = max_step;
+    ps->graph_launches[gi] = ctx->launches - l0;
     ctx->launches = l0;
   }
-  SF_CUDA(cudaGraphLaunch(ps->step_graph, s));
-  ctx->launches += ps->graph_launches;
+  SF_CUDA(cudaGraphLaunch(ps->step_graph[gi], s));
+  ctx->launches += ps->graph_launches[gi];
 }
 
 void sf_poisson_destroy_internal(sf_ctx* ctx) {
@@ -1098,7 +1098,8 @@ void sf_poisson_destroy_internal(sf_ctx* ctx) {
   for (void* p : ps->allocs) cudaFree(p);
   if (ps->ev0) cudaEventDestroy(ps->ev0);
   if (ps->ev1) cudaEventDestroy(ps->ev1);
-  if (ps->step_graph) cudaGraphExecDestroy(ps->step_graph);
+  for (cudaGraphExec_t g : ps->step_graph)
+    if (g) cudaGraphExecDestroy(g);
   delete ps;
   ctx->poisson = nullptr;
 }
@@ -1238,9 +1239,11 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
     }
     res0 = res;
   }
-  // coarse-correction mode (use_learned = 2): the network corrects the first
-  // preconditioner application of every Newton step once it has been trained; every
-  // converged solve in this mode trains it on its own first residual
+  // coarse-correction mode (use_learned = 2): once trained, the network corrects the first
+  // preconditioner application of the solve's first Newton step -- the residual it is
+  // trained on (later steps' residuals are orders of magnitude smaller and dominated by
+  // the particle noise of rho); every converged solve in this mode trains it on its own
+  // first residual
   const bool coarse_mode = prm->use_learned == 2 && ctx->unet;
   const bool coarse = coarse_mode && sf_unet_coarse_ready(ctx);
   int it = 0, vcount = 0;
@@ -1258,7 +1261,7 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
     }
     if (it == prm->max_it) break;
     if (it == 0 && coarse_mode) sf_unet_coarse_start(ctx, ps->lv[0].r, ps->lv[0].P, ps->phi);
-    newton_step(ctx, ps, iters, prm->linear ? 1e300 : 10.0 * prm->kTe0, coarse);
+    newton_step(ctx, ps, iters, prm->linear ? 1e300 : 10.0 * prm->kTe0, coarse && it == 0);
     vcount += iters;
   }
   ps->fp64_exp = a.fp64_exp != 0;

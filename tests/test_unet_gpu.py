@@ -315,8 +315,8 @@ def test_learned_warm_start_gain(gpulib):
 
 def test_learned_coarse_correction_in_pcg(gpulib):
     """use_learned = 2: the network, trained online on each converged solve's first
-    residual, corrects the first preconditioner application of every Newton step inside
-    the PCG.  The solves still reach the FP64 tolerance and the same potential as plain
+    residual, corrects the first preconditioner application of the first Newton step
+    inside the PCG.  The solves still reach the FP64 tolerance and the same potential as plain
     solves from the same start; the 64x32 network grid runs on the tensor-core path."""
     from starfish_gb300.plugin import GpuDomain, LearnedWarmStart, PoissonSolver
     spec = W.es_pic_mesh(65, 33, 1e-3, electrode_halfwidth=4e-3)

@@ -414,7 +414,10 @@ int sf_batch_step(sf_batch* b, double dt, const sf_poisson_params* prm, sf_batch
           for (int i = w; i < b->n; i += T) {
             try {
               SF_CUDA(cudaSetDevice(b->device));
-              launch_sort(b->ctx[i], get_species(b->ctx[i], b->sid[i]));
+              // keys half a sort interval ahead, as the single-context automatic sort
+              sf_ctx* c = b->ctx[i];
+              const double tau = 0.5 * b->sort_interval * dt;
+              launch_sort(c, get_species(c, b->sid[i]), (float)(tau / c->dh[0]), (float)(tau / c->dh[1]));
             } catch (const std::exception& e) {
               fail(i, e.what());
             }

@@ -417,7 +417,8 @@ int sf_batch_step(sf_batch* b, double dt, const sf_poisson_params* prm, sf_batch
               // keys half a sort interval ahead, as the single-context automatic sort
               sf_ctx* c = b->ctx[i];
               const double tau = 0.5 * b->sort_interval * dt;
-              launch_sort(c, get_species(c, b->sid[i]), (float)(tau / c->dh[0]), (float)(tau / c->dh[1]));
+              SfSpecies* si = get_species(c, b->sid[i]);
+              launch_sort(c, si, (float)(tau / c->dh[0]), (float)(tau / c->dh[1]), si->sort_qb);
             } catch (const std::exception& e) {
               fail(i, e.what());
             }

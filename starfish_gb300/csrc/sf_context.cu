@@ -262,10 +262,15 @@ __device__ inline unsigned hash_insert(unsigned* hkey, unsigned key) {
 // mesh.  The look-ahead only orders particles for locality: a species sorted at the middle
 // of the interval between two sorts stays twice as compact on average as one sorted by its
 // current cells, since its particles spread from their predicted cell both before and
-// after.  Binning that needs the exact cells (DSMC) sorts with no look-ahead.
+// after.  With qb > 0 the key is that of the 2^qb x 2^qb block of cells holding the cell
+// (tile-major, then row-major blocks inside the 16x16 tile): a coarser key gives the
+// scatter long runs per key (particles of one old block land in few new blocks) while a
+// run of sorted particles stays as compact as with exact cells.  Binning that needs the
+// exact cells (DSMC) sorts with qb = 0 and no look-ahead.
 struct SortLook {
   float ax, ay;
   int imax, jmax;  // ni - 2, nj - 2
+  int qb;          // log2 of the key block edge in cells (0..4)
 };
 __device__ __forceinline__ unsigned sort_key(uint32_t c, float2 f, float2 v, int ntx, const SortLook& L) {
   int i = cell_i(c), j = cell_j(c);
@@ -274,7 +279,10 @@ __device__ __forceinline__ unsigned sort_key(uint32_t c, float2 f, float2 v, int
     i = min(max(i + (int)floorf(di), 0), L.imax);
     j = min(max(j + (int)floorf(dj), 0), L.jmax);
   }
-  return cell_key(i, j, ntx);
+  if (L.qb == 0) return cell_key(i, j, ntx);
+  const int s = 4 - L.qb;
+  const unsigned tile = (unsigned)((j >> 4) * ntx + (i >> 4));
+  return (tile << (2 * s)) | ((unsigned)((j & 15) >> L.qb) << s) | (unsigned)((i & 15) >> L.qb);
 }
 
 __global__ void __launch_bounds__(SORT_B) k_sort_hist(ParticlesView p, int ntx, int* bins, SortLook L) {
@@ -506,16 +514,17 @@ static void exclusive_scan(sf_ctx* ctx, int* data, int n) {
                           ctx->stream));
 }
 
-void launch_sort(sf_ctx* ctx, SfSpecies* sp, float look_x, float look_y) {
-  const int nk = ctx->nkeys;
-  const SortLook L{look_x, look_y, ctx->ni - 2, ctx->nj - 2};
+void launch_sort(sf_ctx* ctx, SfSpecies* sp, float look_x, float look_y, int qb) {
+  SF_REQUIRE(qb >= 0 && qb <= 4, SF_ERR_ARG, "sort key block out of range");
+  const int nk = ctx->nkeys >> (2 * qb);  // keys of 2^qb x 2^qb-cell blocks
+  const SortLook L{look_x, look_y, ctx->ni - 2, ctx->nj - 2, qb};
   TimedScope ts(ctx, "sort");
   SF_CUDA(cudaMemsetAsync(ctx->bins, 0, sizeof(int) * (size_t)(nk + 1), ctx->stream));
   if (sp->n > 0) {
     ctx->launches += 5;
     int g = grid_for((sp->n + SORT_CHUNK - 1) / SORT_CHUNK, 1, ctx->num_sms * 6);
     k_sort_hist<<<g, SORT_B, 0, ctx->stream>>>(sp->cur, ctx->ntx, ctx->bins, L);
-    exclusive_scan(ctx, ctx->bins, nk + 1);  // bins[key] = first slot of the cell, bins[nk] = total
+    exclusive_scan(ctx, ctx->bins, nk + 1);  // bins[key] = first slot of the key, bins[nk] = total
     SF_CUDA(cudaMemcpyAsync(ctx->bins_tmp, ctx->bins, sizeof(int) * (size_t)(nk + 1),
                             cudaMemcpyDeviceToDevice, ctx->stream));
     ParticlesView dst = sp->alt;

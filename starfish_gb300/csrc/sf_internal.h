@@ -267,6 +267,7 @@ struct SfSpecies {
   double* deposit = nullptr;  // 2*nseg
   uint32_t step = 0;          // pushes done (RNG counter)
   int sort_interval = 16;     // automatic sort every N pushes (0 = never)
+  int sort_qb = 2;            // automatic sort key: blocks of 2^sort_qb x 2^sort_qb cells
   int pushes_since_sort = 1 << 30;
   // velocity sampling (allocated by sf_samples_clear)
   SampleView smp{nullptr, nullptr};
@@ -426,7 +427,11 @@ bool sf_unet_coarse_ready(const sf_ctx* ctx);
 namespace sf {
 // Counting sort of a species by cell key (sf_context.cu); with a look-ahead (cells per
 // m/s in x and y) by the cell each particle reaches moving straight on, for locality only.
-void launch_sort(sf_ctx* ctx, SfSpecies* sp, float look_x = 0.f, float look_y = 0.f);
+// Counting sort of a species' particles.  look_x/y: look-ahead in cells per (m/s) (0: the
+// particles' current cells); qb: key blocks of 2^qb x 2^qb cells inside each 16x16-cell
+// tile (0: exact cells, which binning by cell needs).  The automatic sort of the push passes
+// the species' look-ahead and sort_qb.
+void launch_sort(sf_ctx* ctx, SfSpecies* sp, float look_x = 0.f, float look_y = 0.f, int qb = 0);
 void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments);
 SfSpecies* get_species(sf_ctx* ctx, int sid);
 void ensure_scratch(sf_ctx* ctx, int64_t particles);

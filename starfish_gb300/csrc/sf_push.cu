@@ -1310,12 +1310,13 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   const bool mom = sample || (flags & SF_PUSH_MOMENTS) != 0;
   SF_REQUIRE(!sample || sp->samp, SF_ERR_STATE, "velocity sampling not set up (sf_samples_clear)");
   const SampleView smp = sample ? sp->smp : SampleView{nullptr, nullptr};
-  // automatic cell sort every sort_interval pushes (the counter starts at the interval, so
-  // the first push of a species sorts); the key looks half an interval ahead, so that the
-  // tiles are most compact in the middle of the interval (locality only)
+  // automatic sort every sort_interval pushes (the counter starts at the interval, so the
+  // first push of a species sorts); the key looks half an interval ahead, so that the
+  // tiles are most compact in the middle of the interval, and is that of the species'
+  // sort block of cells (locality only)
   if (sp->sort_interval > 0 && sp->pushes_since_sort >= sp->sort_interval) {
     const double tau = 0.5 * sp->sort_interval * dt;
-    launch_sort(ctx, sp, (float)(tau / ctx->dh[0]), (float)(tau / ctx->dh[1]));
+    launch_sort(ctx, sp, (float)(tau / ctx->dh[0]), (float)(tau / ctx->dh[1]), sp->sort_qb);
   }
   const size_t nn = (size_t)ctx->ni * ctx->nj;
   cudaStream_t s = ctx->stream;
@@ -1553,6 +1554,17 @@ extern "C" int sf_species_set_sort_interval(sf_ctx* ctx, int32_t sid, int32_t in
   SfSpecies* sp = get_species(ctx, sid);
   SF_REQUIRE(interval >= 0, SF_ERR_ARG, "interval must be >= 0");
   sp->sort_interval = interval;
+  SF_API_END(ctx)
+}
+
+extern "C" int sf_species_set_sort_block(sf_ctx* ctx, int32_t sid, int32_t cells) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  int qb = -1;
+  for (int q = 0; q <= 4; q++)
+    if (cells == (1 << q)) qb = q;
+  SF_REQUIRE(qb >= 0, SF_ERR_ARG, "sort block must be 1, 2, 4, 8 or 16 cells");
+  sp->sort_qb = qb;
   SF_API_END(ctx)
 }
 

@@ -151,6 +151,10 @@ class KineticMaterial:
     def set_sort_interval(self, k):
         self.d.check(self.d.lib.sf_species_set_sort_interval(self.d.ctx, self.sid, int(k)))
 
+    def set_sort_block(self, cells):
+        """Key of the automatic sort: blocks of cells x cells cells (1, 2, 4, 8, 16)."""
+        self.d.check(self.d.lib.sf_species_set_sort_block(self.d.ctx, self.sid, int(cells)))
+
     def sort(self):
         self.d.check(self.d.lib.sf_particles_sort(self.d.ctx, self.sid))
 

@@ -210,3 +210,49 @@ def test_cell_sort_orders_and_keeps_particles(gpulib):
         assert np.all(np.diff(k) >= 0)
         b = np.lexsort(np.column_stack([lc, v]).T)
         assert np.array_equal(np.column_stack([lc1, v1])[a], np.column_stack([lc, v])[b])
+
+
+@pytest.mark.parametrize("cells", [2, 4, 16])
+def test_sort_block_changes_order_only(gpulib, cells):
+    """The automatic sort's key block (sf_species_set_sort_block) only reorders: pushes
+    with sorts by 1-cell and by coarser key blocks (look-ahead keys, a sort every other
+    push) give bit-identical node counts and the same surviving particles."""
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    spec = W.es_pic_mesh(257, 129, 2.5e-4, electrode_halfwidth=4.5e-3)
+    ion = W.IonSpecies()
+    _, efi, efj = W.electrode_efield(spec)
+    pos, vel = W.uniform_maxwellian(spec, ion, 300000, 5)
+    outs = []
+    for b in (1, cells):
+        dom = GpuDomain(spec)
+        dom.set_efield(efi, efj)
+        km = KineticMaterial(dom, ion.mass, ion.charge, ion.spwt, capacity=400000)
+        km.set_sort_interval(2)
+        km.set_sort_block(b)
+        km.add_particles(pos, vel, rewind=True, dt=1.25e-7)
+        counts = []
+        for _ in range(5):
+            km.update_fields(1.25e-7)
+            counts.append(km.get_count())
+        lc, v = km.download()
+        outs.append((counts, lc, v))
+        dom.close()
+    for c0, c1 in zip(outs[0][0], outs[1][0]):
+        assert np.array_equal(c0, c1)
+    (_, lc0, v0), (_, lc1, v1) = outs
+    assert lc0.shape == lc1.shape
+    a = np.lexsort(np.column_stack([lc0, v0]).T)
+    b_ = np.lexsort(np.column_stack([lc1, v1]).T)
+    assert np.array_equal(np.column_stack([lc0, v0])[a], np.column_stack([lc1, v1])[b_])
+
+
+def test_sort_block_rejects_bad_sizes(gpulib):
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    ion = W.IonSpecies()
+    dom = GpuDomain(spec)
+    km = KineticMaterial(dom, ion.mass, ion.charge, ion.spwt, capacity=100)
+    for bad in (0, 3, 32, -1):
+        with pytest.raises(abi.SfError):
+            km.set_sort_block(bad)
+    dom.close()

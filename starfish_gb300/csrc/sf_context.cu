@@ -288,21 +288,34 @@ __device__ __forceinline__ unsigned sort_key(uint32_t c, float2 f, float2 v, int
 __global__ void __launch_bounds__(SORT_B) k_sort_hist(ParticlesView p, int ntx, int* bins, SortLook L) {
   __shared__ unsigned hkey[SORT_HSIZE];
   __shared__ unsigned hcnt[SORT_HSIZE];
+  const bool look = L.ax != 0.f || L.ay != 0.f;
   for (int64_t base = (int64_t)blockIdx.x * SORT_CHUNK; base < p.n; base += (int64_t)gridDim.x * SORT_CHUNK) {
     for (int q = threadIdx.x; q < SORT_HSIZE; q += SORT_B) {
       hkey[q] = EMPTY_KEY;
       hcnt[q] = 0u;
     }
-    __syncthreads();
+    // all of a thread's loads are issued before the first is used (no load waits on the
+    // cell word of another: removed slots read their fraction and velocity too)
+    uint32_t c[SORT_IPT];
+    float2 f[SORT_IPT], v[SORT_IPT];
 #pragma unroll
     for (int k = 0; k < SORT_IPT; k++) {
       const int64_t q = base + k * SORT_B + threadIdx.x;
-      const uint32_t c = (q < p.n) ? p.cell[q] : DEAD;
-      if (c == DEAD) continue;
-      const bool look = L.ax != 0.f || L.ay != 0.f;
-      const float2 f = look ? p.frac[q] : make_float2(0.f, 0.f);
-      const float2 v = look ? p.vxy[q] : make_float2(0.f, 0.f);
-      const unsigned slot = hash_insert(hkey, sort_key(c, f, v, ntx, L));
+      c[k] = DEAD;
+      f[k] = v[k] = make_float2(0.f, 0.f);
+      if (q < p.n) {
+        c[k] = __ldcs(&p.cell[q]);
+        if (look) {
+          f[k] = __ldcs(&p.frac[q]);
+          v[k] = __ldcs(&p.vxy[q]);
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SORT_IPT; k++) {
+      if (c[k] == DEAD) continue;
+      const unsigned slot = hash_insert(hkey, sort_key(c[k], f[k], v[k], ntx, L));
       if (slot < SORT_HSIZE) atomicAdd(&hcnt[slot], 1u);
     }
     __syncthreads();

@@ -166,9 +166,9 @@ int sf_species_add(sf_ctx* ctx, double charge, double mass, double spwt, int64_t
 /* Automatic cell sort every `interval` pushes (default 16; 0 = only explicit sorts).
  * Sorting keeps the deposit's shared-memory tiles compact and drops removed slots. */
 int sf_species_set_sort_interval(sf_ctx* ctx, int32_t sid, int32_t interval);
-/* Key of the automatic sort: blocks of `cells` x `cells` cells (1, 2, 4, 8 or 16; default 4)
+/* Key of the automatic sort: blocks of `cells` x `cells` cells (1, 2, 4, 8 or 16; default 8)
  * inside 16x16-cell tiles.  Coarser blocks make the sort cheaper; the push's locality is
- * that of a run of sorted particles, about the same for blocks up to 4 cells.  Explicit
+ * that of a run of sorted particles, about the same for blocks up to 8 cells.  Explicit
  * sorts (sf_particles_sort) and the DSMC binning always sort by exact cell.  No reference
  * counterpart (the reference keeps per-cell particle lists). */
 int sf_species_set_sort_block(sf_ctx* ctx, int32_t sid, int32_t cells);

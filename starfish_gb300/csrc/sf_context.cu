@@ -379,13 +379,19 @@ __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, Part
       if (slot[k] < SORT_HSIZE) rank[k] = atomicAdd(&hcnt[slot[k]], 1u);
     }
     __syncthreads();
-    // exclusive scan of the counts over the table -> chunk-local offsets
-    unsigned loc[SPT];
+    // chunk-local offsets by an exclusive scan of the key counts, and each key's run in the
+    // output reserved at the same time.  Thread t owns slots t, t + SORT_B, ...: consecutive
+    // lanes touch consecutive slots (no bank conflicts).  The runs of different keys may sit
+    // in any order in the staging buffer; only a key's particles have to be contiguous.
+    unsigned cnt[SPT], run[SPT];
     unsigned tsum = 0;
 #pragma unroll
     for (int q = 0; q < SPT; q++) {
-      loc[q] = tsum;
-      tsum += hcnt[threadIdx.x * SPT + q];
+      const int sidx = threadIdx.x + q * SORT_B;
+      cnt[q] = hcnt[sidx];
+      run[q] = 0u;
+      if (cnt[q]) run[q] = (unsigned)atomicAdd(&cursor[hkey[sidx]], (int)cnt[q]);
+      tsum += cnt[q];
     }
     unsigned x = tsum;
 #pragma unroll
@@ -397,13 +403,14 @@ __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, Part
     __syncthreads();
     unsigned wpre = 0;
     for (int w = 0; w < wid; w++) wpre += (unsigned)warp_tot[w];
-    const unsigned tpre = wpre + x - tsum;
+    unsigned off = wpre + x - tsum;
 #pragma unroll
-    for (int q = 0; q < SPT; q++) hoff[threadIdx.x * SPT + q] = tpre + loc[q];
-    __syncthreads();
-    // reserve each key's run in the output; hcnt becomes the run's first slot
-    for (int q = threadIdx.x; q < SORT_HSIZE; q += SORT_B)
-      if (hcnt[q]) hcnt[q] = (unsigned)atomicAdd(&cursor[hkey[q]], (int)hcnt[q]);
+    for (int q = 0; q < SPT; q++) {
+      const int sidx = threadIdx.x + q * SORT_B;
+      hoff[sidx] = off;
+      off += cnt[q];
+      if (cnt[q]) hcnt[sidx] = run[q];  // hcnt becomes the run's first output slot
+    }
     __syncthreads();
     // stage the chunk in key order
 #pragma unroll

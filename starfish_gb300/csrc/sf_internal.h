@@ -267,7 +267,7 @@ struct SfSpecies {
   double* deposit = nullptr;  // 2*nseg
   uint32_t step = 0;          // pushes done (RNG counter)
   int sort_interval = 16;     // automatic sort every N pushes (0 = never)
-  int sort_qb = 2;            // automatic sort key: blocks of 2^sort_qb x 2^sort_qb cells
+  int sort_qb = 3;            // automatic sort key: blocks of 2^sort_qb x 2^sort_qb cells
   int pushes_since_sort = 1 << 30;
   // velocity sampling (allocated by sf_samples_clear)
   SampleView smp{nullptr, nullptr};

@@ -373,6 +373,12 @@ int sf_unet_params(sf_ctx* ctx, float* get, const float* set);
  * the tcgen05 path so far. */
 int sf_unet_set_tensor_cores(sf_ctx* ctx, int32_t on);
 int sf_unet_tensor_core_stats(sf_ctx* ctx, int64_t* tc_convs);
+/* Failure-detection check of the tensor-core pipeline: runs one small convolution whose
+ * copies are never issued, so that its first wait runs out (after 20 ms); the CTAs record
+ * the failure, free their tensor memory and return.  Returns SF_ERR_TIMEOUT when that
+ * happened (the context stays usable), SF_ERR_STATE if the timeout was not reported.
+ * Needs no U-Net. */
+int sf_unet_tensor_core_wait_test(sf_ctx* ctx);
 
 /* ---- batches of independent instances (no reference counterpart) --------------- */
 /* Many independent cases (contexts of different mesh sizes and particle counts, one

@@ -203,6 +203,7 @@ EXPORTS.update({
     "sf_unet_init": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64]),
     "sf_unet_set_tensor_cores": (C.c_int, [C.c_void_p, C.c_int32]),
     "sf_unet_tensor_core_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "sf_unet_tensor_core_wait_test": (C.c_int, [C.c_void_p]),
     "sf_unet_set_training": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_int32, C.c_int32]),
     "sf_unet_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                 C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),

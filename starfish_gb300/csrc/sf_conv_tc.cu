@@ -16,7 +16,8 @@
 // thread 32 issues the MMAs, and all four warps read the accumulator back (warp w holds
 // tensor-memory lanes 32w..32w+31, i.e. pixels 32w..32w+31) and write bias + ReLU as
 // BF16.  Every wait on an mbarrier is bounded (2 s): on timeout the CTA records an error,
-// stops issuing, and still frees its tensor memory.
+// stops issuing, waits (bounded again) for the copies and MMAs it has in flight, and still
+// frees its tensor memory.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -49,8 +50,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
   return t;
 }
-// bounded wait for the phase with the given parity; false after WAIT_NS
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+// bounded wait for the phase with the given parity; false after limit_ns
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned long long limit_ns) {
   const uint32_t a = smem_u32(bar);
   const unsigned long long t0 = global_ns();
   for (unsigned k = 0;; k++) {
@@ -61,7 +62,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
         : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
-    if ((k & 63) == 63 && global_ns() - t0 > WAIT_NS) return false;
+    if ((k & 63) == 63 && global_ns() - t0 > limit_ns) return false;
   }
 }
 
@@ -126,6 +127,8 @@ struct TcArgs {
   int tmem_cols;  // power of two >= max(32, N)
   int stages;
   int* err;
+  unsigned long long wait_ns;  // limit of each mbarrier wait (WAIT_NS)
+  int stall;                   // wait test: no copy is issued, so the first wait runs out
 };
 
 // One CTA: output pixels of box (blockIdx.x, blockIdx.y), channels [blockIdx.z N, +N).
@@ -165,12 +168,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3x3_tc(const __grid_const
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
+  int last_load = -1, last_mma = -1;  // the last step whose copies / MMAs this thread issued
 
-  if (tid == 0) {
+  if (tid == 0 && !a.stall) {
     // producer: the A box of the step's tap and channel chunk, and the B box of weights
     for (int k = 0; k < ksteps; k++) {
       const int s = k % a.stages, use = k / a.stages;
-      if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1)) {
+      if (use > 0 && !mbar_wait(&empty_bar[s], (use - 1) & 1, a.wait_ns)) {
         atomicExch(&failed, 1);
         break;
       }
@@ -181,6 +185,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3x3_tc(const __grid_const
       mbar_expect_tx(&full_bar[s], (unsigned)(a_bytes + b_bytes));
       tma_load_3d(st, &map_a, ci0, x0 + kx - 1, y0 + ky - 1, &full_bar[s]);
       tma_load_2d(st + a_bytes, &map_b, tap * a.Cin + ci0, co0, &full_bar[s]);
+      last_load = k;
     }
   } else if (tid == 32) {
     // MMA issuer
@@ -188,7 +193,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3x3_tc(const __grid_const
     bool ok = true;
     for (int k = 0; k < ksteps; k++) {
       const int s = k % a.stages, use = k / a.stages;
-      if (!mbar_wait(&full_bar[s], use & 1)) {
+      if (!mbar_wait(&full_bar[s], use & 1, a.wait_ns)) {
         atomicExch(&failed, 1);
         ok = false;
         break;
@@ -206,6 +211,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3x3_tc(const __grid_const
         mma_bf16_tmem(tmem, da, db, idesc, (k > 0 || kk > 0) ? 1u : 0u);
       }
       mma_commit(&empty_bar[s]);  // frees the stage once these MMAs have read it
+      last_mma = k;
     }
     if (ok) mma_commit(&done_bar);
     else mbar_expect_tx(&done_bar, 0);  // release the epilogue without a result
@@ -213,7 +219,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3x3_tc(const __grid_const
   __syncwarp();
 
   // epilogue: every warp waits for the accumulator, then reads its 32 lanes (pixels)
-  const bool have = mbar_wait(&done_bar, 0) && !*(volatile int*)&failed;
+  // (longer than the MMA issuer's own waits, which end by releasing this barrier)
+  const bool done = mbar_wait(&done_bar, 0, 4 * a.wait_ns);
+  if (!done) atomicExch(&failed, 1);  // a wait that ran out here is an error too
+  const bool have = done && !*(volatile int*)&failed;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (have) {
     const int p = 32 * warp + lane;
@@ -249,6 +258,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3x3_tc(const __grid_const
       dst[0] = reinterpret_cast<const uint4*>(v)[0];
       dst[1] = reinterpret_cast<const uint4*>(v)[1];
     }
+  }
+  // after a timeout, nothing this CTA started may still be running when it frees its tensor
+  // memory and exits: the producer waits (bounded) for the copies of its last stages, the
+  // MMA issuer for its last commit (which covers every MMA it issued before)
+  if (*(volatile int*)&failed) {
+    if (tid == 0)
+      for (int k = max(0, last_load - a.stages + 1); k <= last_load; k++)
+        mbar_wait(&full_bar[k % a.stages], (unsigned)(k / a.stages) & 1u, a.wait_ns);
+    if (tid == 32 && last_mma >= 0)
+      mbar_wait(&empty_bar[last_mma % a.stages], (unsigned)(last_mma / a.stages) & 1u, a.wait_ns);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -296,10 +315,13 @@ bool conv3x3_tc_supported(int H, int W, int Cin, int Cout, int out_C, int out_c0
 // out[y][x][out_c0 + co] = act(bias[co] + sum w[co][ky][kx][ci] in[y+ky-1][x+kx-1][ci]) on
 // the tensor cores.  in: H x W x Cin BF16 (NHWC), w: Cout x 9 x Cin BF16.  err: device int
 // set to 1 if a CTA's pipeline timed out (the output is then incomplete).
-void conv3x3_tc(cudaStream_t s, const bf16* in, int H, int W, int Cin, const bf16* w, const float* bias, int Cout,
-                bf16* out, int out_C, int out_c0, bool relu, int* err) {
+static void conv3x3_tc_launch(cudaStream_t s, const bf16* in, int H, int W, int Cin, const bf16* w,
+                              const float* bias, int Cout, bf16* out, int out_C, int out_c0, bool relu, int* err,
+                              unsigned long long wait_ns, bool stall) {
   SF_REQUIRE(conv3x3_tc_supported(H, W, Cin, Cout, out_C, out_c0), SF_ERR_ARG, "shape not on the tensor-core path");
   TcArgs a{};
+  a.wait_ns = wait_ns;
+  a.stall = stall ? 1 : 0;
   a.bias = bias;
   a.out = out;
   a.H = H;
@@ -369,6 +391,42 @@ void conv3x3_tc(cudaStream_t s, const bf16* in, int H, int W, int Cin, const bf1
   const dim3 grid((W + a.BW - 1) / a.BW, (H + a.BH - 1) / a.BH, Cout / a.N);
   k_conv3x3_tc<<<grid, TC_THREADS, smem, s>>>(ma, mb, a);
   SF_CUDA(cudaGetLastError());
+}
+
+void conv3x3_tc(cudaStream_t s, const bf16* in, int H, int W, int Cin, const bf16* w, const float* bias, int Cout,
+                bf16* out, int out_C, int out_c0, bool relu, int* err) {
+  conv3x3_tc_launch(s, in, H, W, Cin, w, bias, Cout, out, out_C, out_c0, relu, err, WAIT_NS, false);
+}
+
+// One 16x16x16 -> 16 convolution in which no copy is issued, so that the MMA issuer's first
+// wait runs out (after 20 ms): the CTA has to record the failure, release its epilogue, free
+// its tensor memory and return.  Returns the kernel's error flag (1 when the wait ran out).
+int conv3x3_tc_wait_test(cudaStream_t s) {
+  const int H = 16, W = 16, C = 16;
+  bf16 *in = nullptr, *w = nullptr, *out = nullptr;
+  int* err = nullptr;
+  int herr = -1;
+  SF_CUDA(cudaMalloc(&in, sizeof(bf16) * H * W * C));
+  SF_CUDA(cudaMalloc(&w, sizeof(bf16) * C * 9 * C));
+  SF_CUDA(cudaMalloc(&out, sizeof(bf16) * H * W * C));
+  SF_CUDA(cudaMalloc(&err, sizeof(int)));
+  try {
+    SF_CUDA(cudaMemsetAsync(in, 0, sizeof(bf16) * H * W * C, s));
+    SF_CUDA(cudaMemsetAsync(w, 0, sizeof(bf16) * C * 9 * C, s));
+    SF_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    conv3x3_tc_launch(s, in, H, W, C, w, nullptr, C, out, C, 0, false, err, 20000000ull, true);
+    SF_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SF_CUDA(cudaStreamSynchronize(s));
+  } catch (...) {
+    cudaStreamSynchronize(s);
+    cudaFree(in); cudaFree(w); cudaFree(out); cudaFree(err);
+    throw;
+  }
+  SF_CUDA(cudaFree(in));
+  SF_CUDA(cudaFree(w));
+  SF_CUDA(cudaFree(out));
+  SF_CUDA(cudaFree(err));
+  return herr;
 }
 
 }  // namespace sf

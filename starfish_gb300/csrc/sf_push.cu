@@ -410,33 +410,44 @@ __device__ float sample_maxw_speed(Philox& r, float v_th) {
 
 
 // Conservative FP32 test of one segment (a, b) against the straight path f -> g, all in
-// cells: false means the two cannot intersect within the reference's tolerances
-// (LinearSegment.intersect accepts parameters within 1e-7 outside [0, 1]; this test's
-// margin is far wider than FP32 rounding of coordinates up to a few thousand cells).
-// Near-parallel or near-touching cases answer true.
-// Also classifies (seg_class_fp32): 0 cannot intersect; 1 intersects with both parameters
-// at least the same margin inside (0, 1): *tseg, *tpart = the segment and path parameters,
-// each within *marg of the exact values; 2 undecided.
+// cells relative to the particle's node: 0 means the two cannot intersect by the rule of
+// LinearSegment.intersect (both parameters within [-1e-7, 1 + 1e-7], Segment.java and
+// KineticMaterial.java:480-515); 1 means they intersect with both parameters inside (0, 1)
+// by more than the error bound, so the exact path takes this crossing with *tseg, *tpart
+// (the segment and path parameters) within *marg of its values; 2 is undecided.
+// The bound is a forward error bound of the FP32 cross products.  With u = 2^-24,
+// A = 1 + the largest endpoint coordinate and G = 1 + the largest path coordinate: the
+// endpoints carry u A (one rounding of integer cell + fraction), the path end 9 u G (the
+// FP32 move against the FP64 one), so the denominator r x s is off by at most 64 u G A, the
+// path numerator q x s by 24 u A^2 and the segment numerator q x r by 26 u A G (each
+// including the products' own roundings).  Near-parallel paths are undecided.
 __device__ __forceinline__ int seg_class_fp32(float ax, float ay, float bx, float by, float fx, float fy, float gx,
                                               float gy, float* tseg, float* tpart = nullptr, float* marg = nullptr) {
   const float rx = gx - fx, ry = gy - fy;
-  const float rl = fabsf(rx) + fabsf(ry);
   const float sx = bx - ax, sy = by - ay;
-  const float sl = fabsf(sx) + fabsf(sy);
   const float den = rx * sy - ry * sx;
   const float qx = ax - fx, qy = ay - fy;
   const float tn = qx * sy - qy * sx;  // t_part * den
   const float un = qx * ry - qy * rx;  // t_seg * den
   const float lim = fabsf(den);
-  const float tol = 1e-3f * lim + 1e-4f * (rl + 1.f) * (sl + 1.f) * (1.f + fabsf(qx) + fabsf(qy));
-  if (lim <= tol) return 2;  // (near) parallel
+  const float U = 5.9604645e-8f;  // 2^-24
+  const float A1 = fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fmaxf(fabsf(bx), fabsf(by))) + 1.f;
+  const float G1 = fmaxf(fmaxf(fabsf(gx), fabsf(gy)), fmaxf(fabsf(fx), fabsf(fy))) + 1.f;
+  const float d_den = 64.f * U * G1 * A1;
+  const float rs = (fabsf(rx) + fabsf(ry)) * (fabsf(sx) + fabsf(sy));
+  if (lim <= 2.f * d_den || lim <= 1e-5f * rs) return 2;  // (near) parallel
+  // the reference's acceptance window (1e-7 of each parameter range), with room for its own
+  // FP64 rounding
+  const float win = 1.02e-7f * lim;
+  const float tol_p = win + 24.f * U * A1 * A1 + d_den;
+  const float tol_s = win + 26.f * U * A1 * G1 + d_den;
   const float sgn = den > 0.f ? 1.f : -1.f;
   const float t1 = tn * sgn, t0 = un * sgn;
-  if (!(t1 >= -tol && t1 <= lim + tol && t0 >= -tol && t0 <= lim + tol)) return 0;
-  if (t1 >= tol && t1 <= lim - tol && t0 >= tol && t0 <= lim - tol) {
+  if (!(t1 >= -tol_p && t1 <= lim + tol_p && t0 >= -tol_s && t0 <= lim + tol_s)) return 0;
+  if (t1 >= tol_p && t1 <= lim - tol_p && t0 >= tol_s && t0 <= lim - tol_s) {
     *tseg = t0 / lim;
     if (tpart) *tpart = t1 / lim;
-    if (marg) *marg = tol / lim;
+    if (marg) *marg = fmaxf(tol_p, tol_s) / lim;
     return 1;
   }
   return 2;

@@ -31,6 +31,7 @@ namespace sf {
 bool conv3x3_tc_supported(int H, int W, int Cin, int Cout, int out_C, int out_c0);
 void conv3x3_tc(cudaStream_t s, const bf16* in, int H, int W, int Cin, const bf16* w, const float* bias, int Cout,
                 bf16* out, int out_C, int out_c0, bool relu, int* err);
+int conv3x3_tc_wait_test(cudaStream_t s);
 }  // namespace sf
 
 namespace {
@@ -1201,6 +1202,16 @@ int sf_unet_tensor_core_stats(sf_ctx* ctx, int64_t* tc_convs) {
   SF_API_BEGIN
   SF_REQUIRE(ctx && ctx->unet, SF_ERR_STATE, "no U-Net (sf_unet_init)");
   if (tc_convs) *tc_convs = ctx->unet->tc_convs;
+  SF_API_END(ctx)
+}
+
+int sf_unet_tensor_core_wait_test(sf_ctx* ctx) {
+  SF_API_BEGIN
+  SF_REQUIRE(ctx, SF_ERR_ARG, "null context");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  const int flag = sf::conv3x3_tc_wait_test(ctx->stream);
+  SF_REQUIRE(flag == 1, SF_ERR_STATE, "the stalled tensor-core pipeline did not report its timeout");
+  SF_REQUIRE(false, SF_ERR_TIMEOUT, "tensor-core pipeline wait ran out (as the test intends); the context stays usable");
   SF_API_END(ctx)
 }
 

@@ -388,3 +388,27 @@ def test_rejected_prediction_still_converges(gpulib):
         assert np.max(np.abs(phi_l - phi_p)) < 1e-6 * np.max(np.abs(phi_p))
     finally:
         dom.close()
+
+
+def test_tensor_core_wait_runs_out_cleanly(gpulib):
+    """Failure detection of the tcgen05 pipeline without a fault: a convolution whose
+    copies are never issued makes its first mbarrier wait run out (20 ms bound); the CTAs
+    must record the timeout, free their tensor memory and return, so that the call reports
+    SF_ERR_TIMEOUT and the context keeps working (a tensor-core forward pass afterwards
+    matches the mma.sync one)."""
+    from starfish_gb300 import abi
+    dom, net = _net(16)
+    try:
+        rc = dom.lib.sf_unet_tensor_core_wait_test(dom.ctx)
+        assert rc == abi.SF_ERR_TIMEOUT, rc
+        rng = np.random.default_rng(3)
+        x = rng.normal(0, 1, (net.Hn, net.Wn, 16)).astype(np.float32)
+        n0 = net.tensor_core_convs()
+        net.tensor_cores(True)
+        a_tc, _ = net.forward_backward(x)
+        assert net.tensor_core_convs() > n0
+        net.tensor_cores(False)
+        a_ms, _ = net.forward_backward(x)
+        assert np.linalg.norm(a_tc - a_ms) <= 1e-2 * np.linalg.norm(a_ms)
+    finally:
+        dom.close()

@@ -32,6 +32,7 @@ constexpr int PB = 256;            // threads per block
 constexpr int PPT = 4;             // particles per thread per tile
 constexpr int TILE = PB * PPT;     // particles per block tile
 constexpr int SBOX = 4096;         // shared-memory deposit box (nodes)
+constexpr int SLOW_THREADS = 128;  // threads per block of the exact-path kernels
 
 
 // Deposit quantisation of every path: S in [0,1] -> round(S * 2^22), at most 2^22 - 1, so
@@ -843,12 +844,17 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
   // in fixed point (2^-24, split in 12-bit halves: a block sees at most 2^31 / 2432
   // entries, whose sums stay below 2^32)
   __shared__ unsigned s_ahit[SMALL_NSEG], s_atlo[SMALL_NSEG], s_athi[SMALL_NSEG];
+  // slow-queue entries waiting for the exact path (at most two blocks' worth: below one
+  // before an iteration adds at most one)
+  __shared__ int s_exact[2 * SLOW_THREADS];
+  __shared__ int s_nex;
   const bool seg_local = m.nseg <= SMALL_NSEG;
   __syncthreads();  // a block calling this again: the previous call's flush has read everything
   for (int q = threadIdx.x; q < 8; q += blockDim.x) s_stats[q] = 0.0;
   for (int q = threadIdx.x; q < 4 * SMALL_NSEG; q += blockDim.x) s_seg[q] = 0.0;
   for (int q = threadIdx.x; q < SMALL_NSEG; q += blockDim.x) s_ahit[q] = s_atlo[q] = s_athi[q] = 0u;
   if (threadIdx.x < 4) s_cnt[threadIdx.x] = 0ULL;
+  if (threadIdx.x == 0) s_nex = 0;
   __syncthreads();
   SlowArgs sa = sg;
   sa.stats_slow = s_stats;
@@ -864,80 +870,11 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
   unsigned long long ldone = 0;
   unsigned nabs = 0;  // absorptions decided in FP32 (boundary charge)
   const bool want = sg.stats != 0;
-  for (unsigned long long t = t_first; t < t_end; t += t_stride) {
-    const int64_t p = slow_idx[t];
+  // The exact FP64 path, for one particle.
+  auto exact_one = [&](int64_t p) {
     const uint32_t c = P.cell[p];
     const float2 f = P.frac[p];
     const float2 v = P.vxy[p];
-    {
-      // FP32 pre-filter: a particle whose (logical, straight) path certainly misses every
-      // candidate segment and stays in the mesh finishes exactly like the fast path
-      const int i = cell_i(c), j = cell_j(c);
-      float gx, gy, nv[3] = {v.x, v.y, P.vz[p]};
-      move_fp32<DOM>(i, j, f, a, gx, gy, nv);
-      if (!may_hit_fp32(m, i, j, f.x, f.y, gx, gy)) {
-        float fdi = floorf(gx), fdj = floorf(gy);
-        float nfx = gx - fdi, nfy = gy - fdj;
-        if (nfx >= 1.f) { nfx -= 1.f; fdi += 1.f; }
-        if (nfy >= 1.f) { nfy -= 1.f; fdj += 1.f; }
-        const int i2 = i + (int)fdi, j2 = j + (int)fdj;
-        const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
-        if (inside) {
-          P.cell[p] = pack_cell(i2, j2);
-          P.frac[p] = make_float2(nfx, nfy);
-          if (DOM != SF_DOMAIN_XY) {  // the rotation changed the velocity
-            P.vxy[p] = make_float2(nv[0], nv[1]);
-            P.vz[p] = nv[2];
-          }
-          ldone++;
-          if (want) {
-            lst[0] += 1.0;
-            lst[1] += (double)nv[0];
-            lst[2] += (double)nv[1];
-            lst[3] += (double)nv[2];
-            lst[4] += (double)sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
-          }
-          float wx, wy;
-          scatter_weights<DOM>(nfx, nfy, i2, j2, a, wx, wy);
-          deposit_global(m, count, mom, mom_on, smp, i2, j2, nfx, nfy, wx, wy, nv[0], nv[1], nv[2], nn);
-          continue;
-        }
-        if (m.all_delete) {
-          P.cell[p] = DEAD;
-          atomicAdd(&sa.counters[1], 1ULL);
-          atomicAdd(&sa.counters[3], 1ULL);
-          continue;
-        }
-      } else {
-        // a clear first hit of an absorbing segment (the common case of ions striking an
-        // electrode): the exact path would take the same segment and remove the
-        // particle there; only the flux and deposit shares need the hit point
-        int hs;
-        float ht;
-        if (first_hit_fp32(m, i, j, f.x, f.y, gx, gy, &hs, &ht)) {
-          const int model = sa.sv.model[hs];
-          if (model != SF_SURF_PASS && model != SF_SURF_NONE && model != SF_SURF_SPECULAR &&
-              model != SF_SURF_DIFFUSE) {
-            nabs++;
-            if (seg_local) {
-              const unsigned qt = __float2uint_rn(ht * 16777216.f);
-              atomicAdd(&s_ahit[hs], 1u);
-              atomicAdd(&s_atlo[hs], qt & 0xFFFu);
-              atomicAdd(&s_athi[hs], qt >> 12);
-            } else {
-              const double w1 = a.spwt * (1 - (double)ht), w2 = a.spwt * (double)ht;
-              atomicAdd(&sa.sv.flux[2 * hs], w1);
-              atomicAdd(&sa.sv.flux[2 * hs + 1], w2);
-              atomicAdd(&sa.sv.deposit[2 * hs], w1);
-              atomicAdd(&sa.sv.deposit[2 * hs + 1], w2);
-            }
-            P.cell[p] = DEAD;
-            atomicAdd(&sa.counters[1], 1ULL);
-            continue;
-          }
-        }
-      }
-    }
     double lc[2] = {cell_i(c) + (double)f.x, cell_j(c) + (double)f.y};
     double pos[2] = {m.x0[0] + lc[0] * m.dh[0], m.x0[1] + lc[1] * m.dh[1]};
     double vel[3] = {v.x, v.y, (double)P.vz[p]};
@@ -978,7 +915,7 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
     if (!alive) {
       P.cell[p] = DEAD;
       atomicAdd(&sa.counters[1], 1ULL);
-      continue;
+      return;
     }
     if (pdt > 0) atomicAdd(&sa.counters[2], 1ULL);  // remaining time is dropped
     if (periodic) {
@@ -1005,6 +942,110 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
     float wx, wy;
     scatter_weights<DOM>(fx, fy, i, j, a, wx, wy);
     deposit_global(m, count, mom, mom_on, smp, i, j, fx, fy, wx, wy, (float)vel[0], (float)vel[1], (float)vel[2], nn);
+  };
+  // The FP32 pre-filter, for one particle: true when it has to take the exact path.
+  auto prefilter = [&](int64_t p) -> bool {
+    const uint32_t c = P.cell[p];
+    const float2 f = P.frac[p];
+    const float2 v = P.vxy[p];
+    // a particle whose (logical, straight) path certainly misses every candidate segment
+    // and stays in the mesh finishes exactly like the fast path
+    const int i = cell_i(c), j = cell_j(c);
+    float gx, gy, nv[3] = {v.x, v.y, P.vz[p]};
+    move_fp32<DOM>(i, j, f, a, gx, gy, nv);
+    if (!may_hit_fp32(m, i, j, f.x, f.y, gx, gy)) {
+      float fdi = floorf(gx), fdj = floorf(gy);
+      float nfx = gx - fdi, nfy = gy - fdj;
+      if (nfx >= 1.f) { nfx -= 1.f; fdi += 1.f; }
+      if (nfy >= 1.f) { nfy -= 1.f; fdj += 1.f; }
+      const int i2 = i + (int)fdi, j2 = j + (int)fdj;
+      const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
+      if (inside) {
+        P.cell[p] = pack_cell(i2, j2);
+        P.frac[p] = make_float2(nfx, nfy);
+        if (DOM != SF_DOMAIN_XY) {  // the rotation changed the velocity
+          P.vxy[p] = make_float2(nv[0], nv[1]);
+          P.vz[p] = nv[2];
+        }
+        ldone++;
+        if (want) {
+          lst[0] += 1.0;
+          lst[1] += (double)nv[0];
+          lst[2] += (double)nv[1];
+          lst[3] += (double)nv[2];
+          lst[4] += (double)sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+        }
+        float wx, wy;
+        scatter_weights<DOM>(nfx, nfy, i2, j2, a, wx, wy);
+        deposit_global(m, count, mom, mom_on, smp, i2, j2, nfx, nfy, wx, wy, nv[0], nv[1], nv[2], nn);
+        return false;
+      }
+      if (m.all_delete) {
+        P.cell[p] = DEAD;
+        atomicAdd(&sa.counters[1], 1ULL);
+        atomicAdd(&sa.counters[3], 1ULL);
+        return false;
+      }
+      return true;
+    }
+    // a clear first hit of an absorbing segment (the common case of ions striking an
+    // electrode): the exact path would take the same segment and remove the particle
+    // there; only the flux and deposit shares need the hit point
+    int hs;
+    float ht;
+    if (first_hit_fp32(m, i, j, f.x, f.y, gx, gy, &hs, &ht)) {
+      const int model = sa.sv.model[hs];
+      if (model != SF_SURF_PASS && model != SF_SURF_NONE && model != SF_SURF_SPECULAR &&
+          model != SF_SURF_DIFFUSE) {
+        nabs++;
+        if (seg_local) {
+          const unsigned qt = __float2uint_rn(ht * 16777216.f);
+          atomicAdd(&s_ahit[hs], 1u);
+          atomicAdd(&s_atlo[hs], qt & 0xFFFu);
+          atomicAdd(&s_athi[hs], qt >> 12);
+        } else {
+          const double w1 = a.spwt * (1 - (double)ht), w2 = a.spwt * (double)ht;
+          atomicAdd(&sa.sv.flux[2 * hs], w1);
+          atomicAdd(&sa.sv.flux[2 * hs + 1], w2);
+          atomicAdd(&sa.sv.deposit[2 * hs], w1);
+          atomicAdd(&sa.sv.deposit[2 * hs + 1], w2);
+        }
+        P.cell[p] = DEAD;
+        atomicAdd(&sa.counters[1], 1ULL);
+        return false;
+      }
+    }
+    return true;
+  };
+  // Particles that need the exact path are gathered in a block-local list and run by
+  // consecutive threads once a block's worth is there (and at the end), so that the FP64
+  // work runs in full warps instead of one or two lanes of every warp.  The entries
+  // t_first - threadIdx.x + k t_stride are the same for the whole block.
+  const int nb = blockDim.x;
+  for (unsigned long long t0 = t_first - threadIdx.x; t0 < t_end; t0 += t_stride) {
+    const unsigned long long t = t0 + threadIdx.x;
+    const bool ex = t < t_end && prefilter(slow_idx[t]);
+    const unsigned mex = __ballot_sync(0xffffffffu, ex);
+    if (mex) {
+      const int leader = __ffs(mex) - 1;
+      int base = 0;
+      if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(&s_nex, __popc(mex));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (ex) s_exact[base + __popc(mex & ((1u << (threadIdx.x & 31)) - 1u))] = (int)slow_idx[t];
+    }
+    __syncthreads();
+    const int nex = s_nex;
+    if (nex >= nb) {
+      const int q = s_exact[nex - nb + threadIdx.x];
+      __syncthreads();  // every entry read before the list shrinks and refills
+      if (threadIdx.x == 0) s_nex = nex - nb;
+      exact_one(q);
+      __syncthreads();
+    }
+  }
+  {
+    const int nex = s_nex;
+    if ((int)threadIdx.x < nex) exact_one(s_exact[threadIdx.x]);
   }
   for (int o = 16; o > 0; o >>= 1) {
     if (want)
@@ -1047,7 +1088,7 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
 }
 
 template <int DOM>
-__global__ void __launch_bounds__(128) k_push_slow(MeshView m, ParticlesView P, PushArgs a, SlowArgs sg,
+__global__ void __launch_bounds__(SLOW_THREADS) k_push_slow(MeshView m, ParticlesView P, PushArgs a, SlowArgs sg,
                                                    const int* __restrict__ slow_idx,
                                                    unsigned long long* __restrict__ count,
                                                    long long* __restrict__ mom, int mom_on, SampleView smp) {
@@ -1245,7 +1286,7 @@ __global__ void __launch_bounds__(PB, 2) k_push_batch(BatchDev b) {
 // The exact path over the chunks of all instances' slow queues: every block takes chunks
 // in turn, so an instance with a long queue is spread over the whole GPU.
 template <int DOM>
-__global__ void __launch_bounds__(128) k_push_slow_batch(BatchDev b) {
+__global__ void __launch_bounds__(SLOW_THREADS) k_push_slow_batch(BatchDev b) {
   const int64_t total = b.chunk_start[b.n];
   for (int64_t c = blockIdx.x; c < total; c += gridDim.x) {
     const int i = batch_find(b.chunk_start, b.n, c);
@@ -1296,7 +1337,7 @@ void batch_push(const BatchDev& b, cudaStream_t stream, int num_sms, int blocks_
   k_batch_zero<<<dim3(8, b.n), 256, 0, stream>>>(b);
   k_push_batch<SF_DOMAIN_XY><<<num_sms * blocks_per_sm, PB, 0, stream>>>(b);
   k_slow_plan<<<1, 1024, 0, stream>>>(b);
-  k_push_slow_batch<SF_DOMAIN_XY><<<num_sms * slow_blocks_per_sm, 128, 0, stream>>>(b);
+  k_push_slow_batch<SF_DOMAIN_XY><<<num_sms * slow_blocks_per_sm, SLOW_THREADS, 0, stream>>>(b);
   k_finalize_batch<<<dim3(4, b.n), 256, 0, stream>>>(b);
   SF_CUDA(cudaGetLastError());
 }
@@ -1404,15 +1445,15 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
     ctx->launches++;
     switch (ctx->domain) {
       case SF_DOMAIN_XY:
-        k_push_slow<SF_DOMAIN_XY><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom,
+        k_push_slow<SF_DOMAIN_XY><<<sgrid, SLOW_THREADS, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom,
                                                         smp);
         break;
       case SF_DOMAIN_RZ:
-        k_push_slow<SF_DOMAIN_RZ><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom,
+        k_push_slow<SF_DOMAIN_RZ><<<sgrid, SLOW_THREADS, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom,
                                                         smp);
         break;
       default:
-        k_push_slow<SF_DOMAIN_ZR><<<sgrid, 128, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom,
+        k_push_slow<SF_DOMAIN_ZR><<<sgrid, SLOW_THREADS, 0, s>>>(ctx->mesh_view(), sp->cur, a, sa, sc.slow_idx, sp->count, sp->mom, mom,
                                                         smp);
         break;
     }

@@ -327,7 +327,9 @@ int sf_set_bc_values(sf_ctx* ctx, const double* bc);
  * density (ni*nj) or NULL to use the device rho (sf_update_rho).  phi: host initial
  * guess and result, or NULL to keep the potential on the device (the previous solution
  * is then the initial guess).  Returns SF_ERR_NOT_CONVERGED / SF_ERR_DIVERGED as
- * Solver.java:384-385 and :437-439 report them. */
+ * Solver.java:384-385 and :437-439 report them.  XY, RZ and ZR meshes: on RZ/ZR, A is
+ * the reference's axisymmetric FVM operator (face fluxes weighted by the face radius over
+ * the node volume 2 pi r dA); the learned modes (use_learned) take XY meshes only. */
 int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, double* phi,
                   sf_solve_stats* stats);
 /* PotentialSolver.updateGradientField (pic/PotentialSolver.java:56-70): E = -grad(phi)

@@ -50,6 +50,15 @@ struct LevelView {
   const uint8_t* type;
 };
 
+// Axisymmetric meshes (RZ: radius along i, ZR: along j): the inner FP32 system is the
+// reference's Jacobian with every row multiplied by a radius, which makes it symmetric:
+// interior rows by 2 pi r (the node's radius; Ax is the cylindrical Laplacian / 2 pi),
+// open-face rows by the radius of the face that joins them to the interior.
+struct AxiView {
+  int axi;       // 1 = RZ, 2 = ZR
+  float r0, dr;  // radius of the first node column (RZ) / row (ZR), and the spacing
+};
+
 struct CoarseDesc {  // levels [0, n) of the single-CTA solve; level 0 is read from global memory
   int n;
   int ni[MAX_LEVELS], nj[MAX_LEVELS];
@@ -423,6 +432,10 @@ struct NlArgs {
   double inv_kTe, phi0;
   int linear;
   int fp64_exp;  // 0: Boltzmann exponential in FP32 (with an error bound), 1: FP64
+  // axisymmetric meshes: 1 = RZ (radius along i), 2 = ZR (radius along j), 0 = XY;
+  // r0, dr: radius of the first node column / row and its spacing
+  int axi = 0;
+  double r0 = 0.0, dr = 0.0;
 };
 
 constexpr int RB = 256;
@@ -505,14 +518,34 @@ __device__ __forceinline__ void nl_residual_body(const NlArgs& a, const double* 
     const double xc = x[u];
     double F, Fs;
     float P = 0.f;
+    // axisymmetric: the radius of the node's row (ZR) or column (RZ) and of the faces
+    // half a cell below / above it; the inner system's row weights (symmetric form)
+    double rc = 1.0, rm = 1.0, rp = 1.0;
+    if (a.axi) {
+      const int k = a.axi == 1 ? u % a.ni : u / a.ni;
+      rc = a.r0 + k * a.dr;
+      rm = rc - 0.5 * a.dr;
+      rp = rc + 0.5 * a.dr;
+    }
     switch (t) {
       case NC_FIXED: F = Fs = xc - b0[u]; break;
-      case NC_NLEFT: F = (x[u + 1] - xc) / a.dx; Fs = F / a.dx; break;
-      case NC_NRIGHT: F = (xc - x[u - 1]) / a.dx; Fs = -F / a.dx; break;
-      case NC_NBOTTOM: F = (x[u + a.ni] - xc) / a.dy; Fs = F / a.dy; break;
-      case NC_NTOP: F = (xc - x[u - a.ni]) / a.dy; Fs = -F / a.dy; break;
+      case NC_NLEFT: F = (x[u + 1] - xc) / a.dx; Fs = F / a.dx * (a.axi == 1 ? rp : rc); break;
+      case NC_NRIGHT: F = (xc - x[u - 1]) / a.dx; Fs = -F / a.dx * (a.axi == 1 ? rm : rc); break;
+      case NC_NBOTTOM: F = (x[u + a.ni] - xc) / a.dy; Fs = F / a.dy * (a.axi == 2 ? rp : rc); break;
+      case NC_NTOP: F = (xc - x[u - a.ni]) / a.dy; Fs = -F / a.dy * (a.axi == 2 ? rm : rc); break;
       default: {
-        const double Ax = a.cx * (x[u - 1] + x[u + 1] - 2.0 * xc) + a.cy * (x[u - a.ni] + x[u + a.ni] - 2.0 * xc);
+        // XY: the 5-point operator.  RZ / ZR: the reference's FVM row on the uniform mesh
+        // (Solver.java:451-553: face fluxes weighted by the face radius, divided by the
+        // node volume 2 pi r dA), i.e. the cylindrical Laplacian / 2 pi
+        double Ax;
+        if (a.axi == 2)
+          Ax = (rc * a.cx * (x[u - 1] + x[u + 1] - 2.0 * xc) +
+                a.cy * (rp * (x[u + a.ni] - xc) + rm * (x[u - a.ni] - xc))) / (2.0 * PI * rc);
+        else if (a.axi == 1)
+          Ax = (a.cx * (rp * (x[u + 1] - xc) + rm * (x[u - 1] - xc)) +
+                rc * a.cy * (x[u - a.ni] + x[u + a.ni] - 2.0 * xc)) / (2.0 * PI * rc);
+        else
+          Ax = a.cx * (x[u - 1] + x[u + 1] - 2.0 * xc) + a.cy * (x[u - a.ni] + x[u + a.ni] - 2.0 * xc);
         double ex = 0.0;
         if (!a.linear) {
           const double arg = (xc - a.phi0) * a.inv_kTe;
@@ -528,6 +561,11 @@ __device__ __forceinline__ void nl_residual_body(const NlArgs& a, const double* 
           }
         }
         F = Fs = Ax - (b0[u] + ex);
+        if (a.axi) {
+          // the symmetric inner system: this row times 2 pi r, and P likewise (per unit r)
+          Fs = 2.0 * PI * rc * F;
+          P *= (float)(2.0 * PI);
+        }
       }
     }
     F32[u] = (float)Fs;
@@ -623,6 +661,62 @@ __device__ __forceinline__ void cg_matvec_body(const LevelView& L, const float* 
 __global__ void __launch_bounds__(RB) k_cg_matvec(LevelView L, const float* __restrict__ p, float* __restrict__ q,
                                                   double* __restrict__ partial) {
   cg_matvec_body(L, p, q, partial, blockIdx.x, gridDim.x);
+}
+
+// row-weighted J of an axisymmetric mesh (see AxiView); P is stored as 2 pi P
+__device__ __forceinline__ float apply_Jw(uint8_t t, const float* y, float P, int u, int ni, float cx, float cy,
+                                          const AxiView& X) {
+  const float yc = y[u];
+  const int k = X.axi == 1 ? u % ni : u / ni;
+  const float rc = X.r0 + (float)k * X.dr, rm = rc - 0.5f * X.dr, rp = rc + 0.5f * X.dr;
+  switch (t) {
+    case NC_FIXED: return yc;
+    case NC_NLEFT: return (X.axi == 1 ? rp : rc) * cx * (y[u + 1] - yc);
+    case NC_NRIGHT: return (X.axi == 1 ? rm : rc) * cx * (y[u - 1] - yc);
+    case NC_NBOTTOM: return (X.axi == 2 ? rp : rc) * cy * (y[u + ni] - yc);
+    case NC_NTOP: return (X.axi == 2 ? rm : rc) * cy * (y[u - ni] - yc);
+    default:
+      if (X.axi == 2)
+        return rc * cx * (y[u - 1] + y[u + 1] - 2.f * yc) + cy * (rp * (y[u + ni] - yc) + rm * (y[u - ni] - yc)) -
+               rc * P * yc;
+      return cx * (rp * (y[u + 1] - yc) + rm * (y[u - 1] - yc)) + rc * cy * (y[u - ni] + y[u + ni] - 2.f * yc) -
+             rc * P * yc;
+  }
+}
+
+__global__ void __launch_bounds__(RB) k_cg_matvec_axi(LevelView L, AxiView X, const float* __restrict__ p,
+                                                      float* __restrict__ q, double* __restrict__ partial) {
+  const int n = L.ni * L.nj;
+  float s = 0.f;
+  for (int u = blockIdx.x * RB + threadIdx.x; u < n; u += gridDim.x * RB) {
+    const float qu = apply_Jw(L.type[u], p, L.P[u], u, L.ni, L.cx, L.cy, X);
+    q[u] = qu;
+    s = fmaf(p[u], qu, s);
+  }
+  block_sum2((double)s, 0.0, partial, false, blockIdx.x);
+}
+
+// The preconditioner of the row-weighted system: z = D^-1/2 V(D^-1/2 r) with D the row
+// radii (a quarter cell on the axis) and V the XY multigrid cycle on the level-0 P (which
+// holds 2 pi P): D^-1/2 J_w D^-1/2 is the XY operator up to terms of order (dr / r)^2.
+__device__ __forceinline__ float axi_scale(const AxiView& X, int u, int ni) {
+  const int k = X.axi == 1 ? u % ni : u / ni;
+  return rsqrtf(fmaxf(X.r0 + (float)k * X.dr, 0.25f * X.dr));
+}
+__global__ void k_axi_pre(LevelView L, AxiView X, float* __restrict__ keep) {
+  const int n = L.ni * L.nj;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    const float ru = L.r[u];
+    keep[u] = ru;
+    L.r[u] = axi_scale(X, u, L.ni) * ru;
+  }
+}
+__global__ void k_axi_post(LevelView L, AxiView X, const float* __restrict__ keep) {
+  const int n = L.ni * L.nj;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+    L.y[u] *= axi_scale(X, u, L.ni);
+    L.r[u] = keep[u];
+  }
 }
 
 // Coarse correction by the network inside the first preconditioner application of a
@@ -809,6 +903,11 @@ struct SfPoisson {
   int graph_iters[2] = {-1, -1};
   double graph_max_step[2] = {0, 0};
   int64_t graph_launches[2] = {0, 0};
+  // axisymmetric meshes (0 for XY)
+  int axi = 0;
+  AxiView axv{};
+  double r0 = 0.0, dr = 0.0;
+  float* axi_keep = nullptr;
 };
 
 // zeroed: the first solve without a host phi starts from phi = 0, and no buffer holds
@@ -823,10 +922,16 @@ static void* dalloc(sf_ctx* ctx, SfPoisson* ps, size_t bytes) {
 
 static SfPoisson* poisson_get(sf_ctx* ctx) {
   if (ctx->poisson) return ctx->poisson;
-  SF_REQUIRE(ctx->domain == SF_DOMAIN_XY, SF_ERR_ARG,
-             "the Poisson solve supports XY meshes (axisymmetric meshes use a given field)");
+  const int axi = ctx->domain == SF_DOMAIN_RZ ? 1 : (ctx->domain == SF_DOMAIN_ZR ? 2 : 0);
+  SF_REQUIRE(!axi || ctx->x0[axi - 1] >= 0.0, SF_ERR_ARG, "axisymmetric mesh with negative radii");
   SfPoisson* ps = new SfPoisson();
   ctx->poisson = ps;
+  ps->axi = axi;
+  if (axi) {
+    ps->r0 = ctx->x0[axi - 1];
+    ps->dr = ctx->dh[axi - 1];
+    ps->axv = AxiView{axi, (float)ps->r0, (float)ps->dr};
+  }
   const int ni = ctx->ni, nj = ctx->nj;
   const size_t nn = (size_t)ni * nj;
   ps->ni = ni;
@@ -842,6 +947,7 @@ static SfPoisson* poisson_get(sf_ctx* ctx) {
   ps->cg_p = (float*)dalloc(ctx, ps, 4 * nn);
   ps->cg_q = (float*)dalloc(ctx, ps, 4 * nn);
   ps->cg_zo = (float*)dalloc(ctx, ps, 4 * nn);
+  if (axi) ps->axi_keep = (float*)dalloc(ctx, ps, 4 * nn);
   ps->type0 = (uint8_t*)dalloc(ctx, ps, nn);
   // the partition of every reduction depends on the mesh alone (a batched solve of the
   // same mesh reproduces the sums bit for bit)
@@ -1002,6 +1108,19 @@ static void reduce(sf_ctx* ctx, SfPoisson* ps, double* out, int max2) {
 
 // iters steps of flexible PCG on J y = F (F = lv[0].r, overwritten as the CG residual);
 // the correction is left in cg_x
+// z = M^-1 r on level 0 (r = lv[0].r, z -> lv[0].y): the V-cycle, for an axisymmetric
+// mesh between the radius scalings of the row-weighted system
+static void precond(sf_ctx* ctx, SfPoisson* ps, int g) {
+  if (!ps->axi) {
+    vcycle(ctx, ps);
+    return;
+  }
+  k_axi_pre<<<g, 256, 0, ctx->stream>>>(ps->lv[0], ps->axv, ps->axi_keep);
+  vcycle(ctx, ps);
+  k_axi_post<<<g, 256, 0, ctx->stream>>>(ps->lv[0], ps->axv, ps->axi_keep);
+  ctx->launches += 2;
+}
+
 static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters, bool coarse) {
   cudaStream_t s = ctx->stream;
   const LevelView& L0 = ps->lv[0];
@@ -1018,7 +1137,7 @@ static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters, bool coarse) {
     k_pc_finish<<<g, 256, 0, s>>>(L0, e, ps->cg_p);
     ctx->launches += 2;
   } else {
-    vcycle(ctx, ps);  // z0
+    precond(ctx, ps, g);  // z0
   }
   SF_CUDA(cudaMemsetAsync(ps->cg_zo, 0, 4 * (size_t)n, s));
   k_cg_dots<<<ps->red_blocks, RB, 0, s>>>(n, L0.r, L0.y, ps->cg_zo, ps->partial);
@@ -1029,14 +1148,17 @@ static void pcg(sf_ctx* ctx, SfPoisson* ps, int iters, bool coarse) {
   for (int k = 0; k < iters; k++) {
     {
       TimedScope ts(ctx, "cg_matvec");
-      k_cg_matvec<<<ps->red_blocks, RB, 0, s>>>(L0, ps->cg_p, ps->cg_q, ps->partial);
+      if (ps->axi)
+        k_cg_matvec_axi<<<ps->red_blocks, RB, 0, s>>>(L0, ps->axv, ps->cg_p, ps->cg_q, ps->partial);
+      else
+        k_cg_matvec<<<ps->red_blocks, RB, 0, s>>>(L0, ps->cg_p, ps->cg_q, ps->partial);
     }
     reduce(ctx, ps, ps->sc + SC_RED, 0);
     k_cg_scalars<<<1, 32, 0, s>>>(ps->sc, 1);
     k_cg_axpy<<<g, 256, 0, s>>>(n, ps->sc, ps->cg_p, ps->cg_q, ps->cg_x, L0.r, L0.y, ps->cg_zo);
     ctx->launches += 3;
     if (k == iters - 1) break;
-    vcycle(ctx, ps);
+    precond(ctx, ps, g);
     k_cg_dots<<<ps->red_blocks, RB, 0, s>>>(n, L0.r, L0.y, ps->cg_zo, ps->partial);
     reduce(ctx, ps, ps->sc + SC_RED, 0);
     k_cg_scalars<<<1, 32, 0, s>>>(ps->sc, 2);
@@ -1191,7 +1313,12 @@ int sf_poisson_nl(sf_ctx* ctx, const sf_poisson_params* prm, const double* rho, 
   a.phi0 = prm->phi0;
   a.linear = prm->linear ? 1 : 0;
   a.fp64_exp = ps->fp64_exp ? 1 : 0;
-  const int iters = prm->cycles > 0 ? prm->cycles : 4;
+  a.axi = ps->axi;
+  a.r0 = ps->r0;
+  a.dr = ps->dr;
+  SF_REQUIRE(!ps->axi || prm->use_learned == 0, SF_ERR_ARG, "the learned modes take XY meshes");
+  // the radius-scaled preconditioner is weaker near the axis: more PCG steps per Newton step
+  const int iters = prm->cycles > 0 ? prm->cycles : (ps->axi ? 6 : 4);
   SF_CUDA(cudaEventRecord(ps->ev0, s));
   double h[3];
   // FP64 residual of the current phi into level 0 (F, P) and its norms.  The FP32

@@ -715,3 +715,47 @@ def test_oracle_xy_maxwellian_source_known_answer():
     assert parts[:, 4].std() == pytest.approx(1.2 * sig, rel=0.01)
     assert parts[:, 1].mean() == pytest.approx(0.02, abs=6 * 0.04 / np.sqrt(12 * parts.shape[0]))
     assert parts[:, 1].min() >= 0.0 and parts[:, 1].max() <= 0.04
+
+
+@pytest.mark.parametrize("domain,x0", [(2, (0.0, 0.0)), (1, (0.0, 0.0)), (2, (0.0, 2e-3))])
+def test_oracle_axisymmetric_rows_are_the_closed_form(domain, x0):
+    """The device's closed-form axisymmetric operator: on a uniform RZ / ZR mesh every
+    interior row of the reference's FVM assembly (Solver.java:451-553, face fluxes weighted
+    by the face radius over the node volume 2 pi r dA, Mesh.java:998-1020) is
+    [r c_a (axial neighbours) + c_r (r+ (radial up) + r- (radial down))] / (2 pi r), and the
+    open-face rows are plain one-sided gradients."""
+    from starfish_gb300 import abi
+    ni, nj = 17, 9
+    dh = (1e-3, 5e-4) if domain == abi.DOMAIN_ZR else (5e-4, 1e-3)
+    nt = np.full(ni * nj, abi.NODE_OPEN, np.int8)
+    face = np.full((4, max(ni, nj)), abi.DB_OPEN, np.int8)
+    face[abi.FACE_BOTTOM if domain == abi.DOMAIN_ZR else abi.FACE_LEFT, :] = abi.DB_SYMMETRY
+    nt[5 * ni + 8] = abi.NODE_DIRICHLET
+    m = O.OMesh(ni, nj, x0, dh, domain, nt, face)
+    ptr, col, val = O.assemble(m)["A"]
+    cx, cy = 1 / dh[0] ** 2, 1 / dh[1] ** 2
+    for j in range(nj):
+        for i in range(ni):
+            u = j * ni + i
+            row = dict(zip(col[ptr[u]:ptr[u + 1]], val[ptr[u]:ptr[u + 1]]))
+            if nt[u] == abi.NODE_DIRICHLET:
+                assert row == {u: 1.0}
+                continue
+            if i in (0, ni - 1) or j in (0, nj - 1):
+                # one-sided gradient rows (radius-free)
+                h = dh[0] if i in (0, ni - 1) else dh[1]
+                assert sorted(abs(v) for v in row.values()) == pytest.approx([1 / h, 1 / h], rel=1e-12)
+                continue
+            if domain == abi.DOMAIN_ZR:
+                r = x0[1] + j * dh[1]
+                exp = {u - 1: cx / (2 * np.pi), u + 1: cx / (2 * np.pi),
+                       u + ni: cy * (r + dh[1] / 2) / (2 * np.pi * r), u - ni: cy * (r - dh[1] / 2) / (2 * np.pi * r)}
+            else:
+                r = x0[0] + i * dh[0]
+                exp = {u + 1: cx * (r + dh[0] / 2) / (2 * np.pi * r), u - 1: cx * (r - dh[0] / 2) / (2 * np.pi * r),
+                       u - ni: cy / (2 * np.pi), u + ni: cy / (2 * np.pi)}
+            exp[u] = -sum(exp.values())
+            for k, v in row.items():
+                assert v == pytest.approx(exp.get(k, 0.0), rel=1e-12, abs=1e-9 * abs(exp[u]))
+            for k, v in exp.items():
+                assert row.get(k, 0.0) == pytest.approx(v, rel=1e-12)

@@ -606,9 +606,6 @@ int sf_ctx_create(const sf_mesh_desc* md, int device, sf_ctx** out) {
     ctx->device = device;
     SF_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
     SF_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-    SF_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
-    SF_CUDA(cudaEventCreateWithFlags(&ctx->copy_fork, cudaEventDisableTiming));
-    SF_CUDA(cudaEventCreateWithFlags(&ctx->copy_join, cudaEventDisableTiming));
     ctx->ni = md->ni;
     ctx->nj = md->nj;
     ctx->nmax = std::max(md->ni, md->nj);
@@ -752,9 +749,6 @@ int sf_ctx_destroy(sf_ctx* ctx) {
     cudaEventDestroy(p.second.second);
   }
   for (cudaEvent_t e : ctx->timer.pool) cudaEventDestroy(e);
-  if (ctx->copy_fork) cudaEventDestroy(ctx->copy_fork);
-  if (ctx->copy_join) cudaEventDestroy(ctx->copy_join);
-  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return SF_OK;
@@ -993,14 +987,8 @@ int sf_set_efield(sf_ctx* ctx, const double* efi, const double* efj) {
   SF_REQUIRE(ctx && efi && efj, SF_ERR_ARG, "null argument");
   SF_CUDA(cudaSetDevice(ctx->device));
   size_t nn = (size_t)ctx->ni * ctx->nj;
-  // the two components cross the host link side by side (one on the copy stream, forked
-  // after the main stream's earlier work and joined before the packing)
-  SF_CUDA(cudaEventRecord(ctx->copy_fork, ctx->stream));
-  SF_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_fork, 0));
-  SF_CUDA(cudaMemcpyAsync(ctx->dscratch + nn, efj, sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->copy_stream));
-  SF_CUDA(cudaEventRecord(ctx->copy_join, ctx->copy_stream));
   SF_CUDA(cudaMemcpyAsync(ctx->dscratch, efi, sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->stream));
-  SF_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->copy_join, 0));
+  SF_CUDA(cudaMemcpyAsync(ctx->dscratch + nn, efj, sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->stream));
   k_pack_efield<<<grid_for((int64_t)nn, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
       (int)nn, ctx->dscratch, ctx->dscratch + nn, ctx->E);
   ctx->launches++;
@@ -1026,18 +1014,9 @@ int sf_get_field(sf_ctx* ctx, int32_t field, int32_t sid, double* out) {
   }
   SfSpecies* sp = get_species(ctx, sid);
   switch (field) {
-    case SF_FIELD_ND: {
-      // two halves side by side (the second on the copy stream, after the main stream's work)
-      const size_t h = nn / 2;
-      SF_CUDA(cudaEventRecord(ctx->copy_fork, ctx->stream));
-      SF_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->copy_fork, 0));
-      SF_CUDA(cudaMemcpyAsync(out + h, sp->nd + h, sizeof(double) * (nn - h), cudaMemcpyDeviceToHost,
-                              ctx->copy_stream));
-      SF_CUDA(cudaEventRecord(ctx->copy_join, ctx->copy_stream));
-      SF_CUDA(cudaMemcpyAsync(out, sp->nd, sizeof(double) * h, cudaMemcpyDeviceToHost, ctx->stream));
-      SF_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->copy_join, 0));
+    case SF_FIELD_ND:
+      SF_CUDA(cudaMemcpyAsync(out, sp->nd, sizeof(double) * nn, cudaMemcpyDeviceToHost, ctx->stream));
       break;
-    }
     case SF_FIELD_U:
     case SF_FIELD_V:
     case SF_FIELD_W:

@@ -347,10 +347,6 @@ struct SfTimer {
 struct sf_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
-  // second stream for host copies that can run beside the main stream's (E components,
-  // halves of a field read back), joined to it by the events below
-  cudaStream_t copy_stream = nullptr;
-  cudaEvent_t copy_fork = nullptr, copy_join = nullptr;
   int num_sms = 0;
   std::string err;
   // mesh (host copies)

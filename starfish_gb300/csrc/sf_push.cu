@@ -351,7 +351,6 @@ __global__ void __launch_bounds__(PB, 4) k_push(MeshView m, ParticlesView P, Pus
   __shared__ int sred[4][PB / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
-  const size_t nn = (size_t)m.ni * m.nj;
   Kahan st_px, st_py, st_pz, st_e;
   unsigned st_n = 0;
 
@@ -1266,7 +1265,9 @@ __global__ void k_batch_zero(BatchDev b) {
 }
 
 template <int DOM>
-__global__ void __launch_bounds__(PB, 2) k_push_batch(BatchDev b) {
+// 4 blocks of PB per SM (64 registers, with spills): in the batched step faster than 2
+// blocks (123 registers) or 3 (80)
+__global__ void __launch_bounds__(PB, 4) k_push_batch(BatchDev b) {
   __shared__ unsigned acc[SBOX];
   __shared__ int sred[4][PB / 32];
   Kahan st_px, st_py, st_pz, st_e;

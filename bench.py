@@ -234,7 +234,8 @@ def poisson_roofline(cfg, dom, solves=4, tol=1e-6):
     coarse node (13 + 4 N_{l+1}/N_l B per node); going up it reads the coarse correction,
     y, r, P and the class and writes y (17 + 4 N_{l+1}/N_l B); the FP64 Newton residual
     reads phi, b0 (FP64) and the class and writes F and P (FP32): 25 B per node, and runs
-    the FP64 exponential per node (FP64-pipe-bound)."""
+    about 20 FP64 instructions per node (FP64-pipe-bound), reported against the part's
+    nominal FP64 rate."""
     from starfish_gb300.plugin import PoissonSolver
     ps = PoissonSolver(dom, n0=cfg.n0, Te0=cfg.Te0, phi0=cfg.phi0, tol=tol, max_it=60, cycles=4)
     ni, nj = cfg.mesh.ni, cfg.mesh.nj
@@ -272,9 +273,19 @@ def poisson_roofline(cfg, dom, solves=4, tol=1e-6):
     if cnt:
         b = 25 * ni * nj
         gbs = b / (ms / cnt / 1e3) / 1e9
+        # FP64 arithmetic instructions per interior node, counted from the kernel's source
+        # (5-point operator 6, argument 2, table exponential and its range test 5, coefficient
+        # and P 2, F 2, the norm and max 2, the mode test 1); about 7 FP32/FP64 conversions
+        # per node come on top.  Against the nominal 1.25 TFLOP/s FP64 of the part (no
+        # measured FP64 peak): 0.625e12 FP64 lane-instructions per second.
+        fp64_per_node = 20
+        ginst = fp64_per_node * ni * nj / (ms / cnt / 1e3) / 1e9
         out["kernels"]["nl_residual"] = {"nodes": ni * nj, "ms": ms / cnt, "launches": cnt, "alg_bytes": b,
                                          "gbs": gbs, "frac_hbm": gbs / peak, "frac_l2": gbs / l2,
-                                         "bound": "FP64 pipe (the FP64 exponential per node)"}
+                                         "bound": "FP64 pipe",
+                                         "fp64_instr_per_node": fp64_per_node, "fp64_ginstr_s": ginst,
+                                         "frac_fp64_nominal": ginst / 625.0,
+                                         "fp64_peak": "nominal 1.25 TFLOP/s = 625 G FP64 lane-instructions/s"}
     for name in ("mg_coarse", "cg_matvec"):
         ms, cnt = dom.kernel_time(name)
         if cnt:

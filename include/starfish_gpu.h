@@ -192,9 +192,22 @@ int sf_species_set_surface_product(sf_ctx* ctx, int32_t sid, int32_t seg, int32_
 /* Appends particles from physical positions (KineticMaterial.addParticle, KineticMaterial.java:759-802):
  * lc = XtoL(pos), clamped to the mesh; if rewind != 0 the velocity is rewound by -dt/2
  * with the current electric field (needs sf_set_efield / a Poisson solve first).
- * pos, vel: n*3 doubles; mpw: n weights or NULL (= spwt; only uniform weights are held). */
+ * pos, vel: n*3 doubles; mpw: n weights (Particle.mpw) or NULL (= spwt).  A species of
+ * uniform weight takes only mpw = spwt; one switched to per-particle weights
+ * (sf_species_set_weighted) takes any 0 < mpw <= spwt. */
 int sf_particles_append(sf_ctx* ctx, int32_t sid, int64_t n, const double* pos, const double* vel,
                         const double* mpw, int32_t rewind, double dt);
+/* Per-particle weights (Particle.mpw, KineticMaterial.java:1207-1282) for a species:
+ * switched on before its first particle; the species weight spwt is then the largest
+ * weight a particle may carry.  The push deposits, moments, totals and surface sums scale
+ * by mpw / spwt; sources, surface products and MCC products enter at spwt.  DSMC, MCC and
+ * batched instances take species of uniform weight only (SF_ERR_ARG otherwise). */
+int sf_species_set_weighted(sf_ctx* ctx, int32_t sid, int32_t on);
+/* sf_particles_append_lc with per-particle weights mpw (n; a weighted species). */
+int sf_particles_append_lc_w(sf_ctx* ctx, int32_t sid, int64_t n, const double* lc, const double* vel,
+                             const double* mpw);
+/* The weights (mpw) of the particles sf_particles_download returns, in the same order. */
+int sf_particles_download_weights(sf_ctx* ctx, int32_t sid, int64_t cap, double* mpw, int64_t* n_out);
 /* Appends particles given logical coordinates (Particle.lc, n*2) instead of positions;
  * no rewind.  Used to load identical state into the GPU and the reference. */
 int sf_particles_append_lc(sf_ctx* ctx, int32_t sid, int64_t n, const double* lc,

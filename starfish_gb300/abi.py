@@ -92,6 +92,10 @@ EXPORTS = {
     "sf_species_set_surface_product": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double]),
     "sf_species_set_sort_interval": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "sf_species_set_sort_block": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "sf_species_set_weighted": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "sf_particles_append_lc_w": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sf_particles_download_weights": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p,
+                                                C.POINTER(C.c_int64)]),
     "sf_particles_append": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_int32, C.c_double]),
     "sf_particles_append_lc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p]),

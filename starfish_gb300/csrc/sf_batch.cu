@@ -152,6 +152,7 @@ T* balloc(sf_batch* b, size_t count) {
 BatchInst make_inst(sf_batch* b, int i) {
   sf_ctx* c = b->ctx[i];
   SfSpecies* sp = get_species(c, b->sid[i]);
+  SF_REQUIRE(!sp->weighted, SF_ERR_ARG, "batched instances take species of uniform weight");
   BatchInst I{};
   I.m = c->mesh_view();
   I.P = sp->cur;

@@ -525,6 +525,7 @@ __device__ bool mcc_append(const MeshView& m, const ParticlesView& Q, int64_t ca
   Q.frac[d] = f;
   Q.vxy[d] = make_float2((float)v[0] - qm_halfdt * e.x, (float)v[1] - qm_halfdt * e.y);
   Q.vz[d] = (float)v[2];
+  if (Q.w) Q.w[d] = 1.f;  // products at the species weight
   return true;
 }
 
@@ -752,6 +753,7 @@ void dsmc_run(sf_ctx* ctx, int sid1, int sid2, const sf_sigma* sigma, const sf_s
   SfSpecies* sp1 = get_species(ctx, sid1);
   SfSpecies* sp2 = get_species(ctx, sid2);
   SF_REQUIRE(dt > 0 && sig_cr_max0 > 0, SF_ERR_ARG, "dt and sig_cr_max must be positive");
+  SF_REQUIRE(!sp1->weighted && !sp2->weighted, SF_ERR_ARG, "DSMC takes species of uniform weight");
   SF_CUDA(cudaSetDevice(ctx->device));
   const bool pair = sid1 != sid2;
   SfDsmcState* st = dsmc_state(ctx, sid1, sid2, sig_cr_max0);
@@ -956,6 +958,7 @@ int sf_mcc(sf_ctx* ctx, int32_t sid, int32_t model, const sf_sigma* sigma, doubl
   SfSpecies* sp = get_species(ctx, sid);
   SF_REQUIRE(model == SF_MCC_MEX || model == SF_MCC_CEX, SF_ERR_ARG,
              "bad MCC model (ionization: sf_mcc_ionization)");
+  SF_REQUIRE(!sp->weighted, SF_ERR_ARG, "MCC takes species of uniform weight");
   unsigned long long h[3];
   mcc_run(ctx, sp, model, sigma, dt, nullptr, 0.0, h);
   if (n_coll) *n_coll = (int64_t)h[0];
@@ -968,6 +971,7 @@ int sf_mcc_ionization(sf_ctx* ctx, int32_t sid, int32_t product_sid, const sf_si
   SfSpecies* sp = get_species(ctx, sid);
   SfSpecies* prod = get_species(ctx, product_sid);
   SF_REQUIRE(product_sid != sid, SF_ERR_ARG, "the product (ion) species must differ from the source (electrons)");
+  SF_REQUIRE(!sp->weighted, SF_ERR_ARG, "MCC takes species of uniform weight");
   SF_REQUIRE(ionization_energy >= 0, SF_ERR_ARG, "ionization energy must be >= 0 eV");
   unsigned long long h[3];
   mcc_run(ctx, sp, SF_MCC_IONIZATION, sigma, dt, prod, ionization_energy, h);

@@ -333,6 +333,8 @@ constexpr size_t SORT_SCATTER_SMEM =
     (size_t)SORT_HSIZE * 3 * sizeof(unsigned) +
     (size_t)SORT_CHUNK * (sizeof(uint32_t) + sizeof(float2) + sizeof(float2) + sizeof(float) + sizeof(int));
 
+// W: the species holds per-particle weights (staged and moved as well)
+template <bool W>
 __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, ParticlesView dst, int ntx, int* cursor,
                                                          SortLook L) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -344,6 +346,7 @@ __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, Part
   uint32_t* s_cell = hoff + SORT_HSIZE;
   float* s_vz = reinterpret_cast<float*>(s_cell + SORT_CHUNK);
   int* s_dst = reinterpret_cast<int*>(s_vz + SORT_CHUNK);
+  float* s_w = reinterpret_cast<float*>(s_dst + SORT_CHUNK);  // weighted species only (larger launch)
   __shared__ int warp_tot[SORT_B / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   constexpr int SPT = SORT_HSIZE / SORT_B;  // slots per thread in the scan
@@ -358,16 +361,18 @@ __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, Part
     // to memory)
     uint32_t r_cell[SORT_IPT];
     float2 r_frac[SORT_IPT], r_vxy[SORT_IPT];
-    float r_vz[SORT_IPT];
+    float r_vz[SORT_IPT], r_w[SORT_IPT];
 #pragma unroll
     for (int k = 0; k < SORT_IPT; k++) {
       const int64_t q = base + k * SORT_B + threadIdx.x;
       r_cell[k] = DEAD;
+      r_w[k] = 1.f;
       if (q < src.n) {
         r_cell[k] = __ldcs(&src.cell[q]);
         r_frac[k] = __ldcs(&src.frac[q]);
         r_vxy[k] = __ldcs(&src.vxy[q]);
         r_vz[k] = __ldcs(&src.vz[q]);
+        if (W) r_w[k] = __ldcs(&src.w[q]);
       }
     }
 #pragma unroll
@@ -421,6 +426,7 @@ __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, Part
       s_frac[l] = r_frac[k];
       s_vxy[l] = r_vxy[k];
       s_vz[l] = r_vz[k];
+      if (W) s_w[l] = r_w[k];
       s_dst[l] = (int)(hcnt[slot[k]] + rank[k]);
     }
     __syncthreads();
@@ -433,6 +439,7 @@ __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, Part
       dst.frac[d] = s_frac[l];
       dst.vxy[d] = s_vxy[l];
       dst.vz[d] = s_vz[l];
+      if (W) dst.w[d] = s_w[l];
     }
     __syncthreads();
   }
@@ -550,11 +557,17 @@ void launch_sort(sf_ctx* ctx, SfSpecies* sp, float look_x, float look_y, int qb)
     ParticlesView dst = sp->alt;
     dst.n = sp->n;
     // per device and the same for every context (set-up threads may sort concurrently)
-    SF_CUDA(cudaFuncSetAttribute(k_sort_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    SF_CUDA(cudaFuncSetAttribute(k_sort_scatter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)SORT_SCATTER_SMEM));
+    SF_CUDA(cudaFuncSetAttribute(k_sort_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(SORT_SCATTER_SMEM + sizeof(float) * SORT_CHUNK)));
     // 52 KB of shared memory and 64 registers per block: 4 blocks per SM
     const int gs = grid_for((sp->n + SORT_CHUNK - 1) / SORT_CHUNK, 1, ctx->num_sms * 4);
-    k_sort_scatter<<<gs, SORT_B, SORT_SCATTER_SMEM, ctx->stream>>>(sp->cur, dst, ctx->ntx, ctx->bins_tmp, L);
+    if (sp->cur.w)
+      k_sort_scatter<true><<<gs, SORT_B, SORT_SCATTER_SMEM + sizeof(float) * SORT_CHUNK, ctx->stream>>>(
+          sp->cur, dst, ctx->ntx, ctx->bins_tmp, L);
+    else
+      k_sort_scatter<false><<<gs, SORT_B, SORT_SCATTER_SMEM, ctx->stream>>>(sp->cur, dst, ctx->ntx, ctx->bins_tmp, L);
     SF_CUDA(cudaGetLastError());
     int total = 0;
     SF_CUDA(cudaMemcpyAsync(&total, ctx->bins + nk, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -731,7 +744,7 @@ int sf_ctx_destroy(sf_ctx* ctx) {
     void* ptrs[] = {sp->cur.cell, sp->cur.frac, sp->cur.vxy,  sp->cur.vz,     sp->alt.cell,  sp->alt.frac,
                     sp->alt.vxy,  sp->alt.vz,   sp->count,    sp->mom,        sp->nd,        sp->uvw,
                     sp->seg_model, sp->seg_param, sp->flux,   sp->deposit,    sp->smp.mom2,  sp->smp.mpc,
-                    sp->samp,     sp->gas,      sp->seg_product};
+                    sp->samp,     sp->gas,      sp->seg_product, sp->cur.w,   sp->alt.w};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     delete sp;
@@ -843,9 +856,20 @@ int sf_species_set_surface_product(sf_ctx* ctx, int32_t sid, int32_t seg, int32_
 }
 
 // Shared body of the two append entry points: lc (n*2) and vel (n*3) on the host.
+// mpw: per-particle weights (weighted species), or null for the species weight
 static void append_lc_impl(sf_ctx* ctx, SfSpecies* sp, int64_t n, const double* lc, const double* vel,
-                           bool rewind, double dt) {
+                           bool rewind, double dt, const double* mpw = nullptr) {
   SF_REQUIRE(sp->n + n <= sp->cap, SF_ERR_OOM, "species capacity exceeded");
+  if (sp->weighted) {
+    // relative weights mpw / spwt in (0, 1]: the species weight bounds its particles'
+    std::vector<float> w((size_t)n, 1.f);
+    for (int64_t k = 0; mpw && k < n; k++) {
+      const double r = mpw[k] / sp->spwt;
+      SF_REQUIRE(r > 0.0 && r <= 1.0, SF_ERR_ARG, "particle weights must lie in (0, spwt]");
+      w[(size_t)k] = (float)r;
+    }
+    copy_wait(sp->cur.w + sp->n, w.data(), sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream);
+  }
   const int64_t CH = 1 << 22;
   double *dlc = nullptr, *dvel = nullptr;
   SF_CUDA(cudaMalloc(&dlc, sizeof(double) * 2 * (size_t)std::min(n, CH)));
@@ -883,14 +907,16 @@ int sf_particles_append(sf_ctx* ctx, int32_t sid, int64_t n, const double* pos, 
   SfSpecies* sp = get_species(ctx, sid);
   SF_REQUIRE(n >= 0 && (n == 0 || (pos && vel)), SF_ERR_ARG, "null particle arrays");
   SF_REQUIRE(!rewind || ctx->efield_set, SF_ERR_STATE, "rewind needs the electric field");
-  if (mpw)
+  if (mpw && !sp->weighted)
     for (int64_t k = 0; k < n; k++)
-      SF_REQUIRE(mpw[k] == sp->spwt, SF_ERR_ARG, "per-particle weights must equal the species spwt");
+      SF_REQUIRE(mpw[k] == sp->spwt, SF_ERR_ARG,
+                 "per-particle weights that differ from the species spwt need sf_species_set_weighted");
   SF_CUDA(cudaSetDevice(ctx->device));
   // XtoL (UniformMesh.java:154-161) and the edge clamp of addParticle (KineticMaterial.java:764-772);
   // positions outside the mesh are rejected like Starfish.domain_module.getMesh(pos) == null.
   std::vector<double> lc(2 * (size_t)n);
   std::vector<double> v(3 * (size_t)n);
+  std::vector<double> wk(mpw ? (size_t)n : 0);
   int64_t kept = 0;
   for (int64_t k = 0; k < n; k++) {
     double lx = (pos[3 * k] - ctx->x0[0]) / ctx->dh[0];
@@ -901,9 +927,10 @@ int sf_particles_append(sf_ctx* ctx, int32_t sid, int64_t n, const double* pos, 
     v[3 * kept] = vel[3 * k];
     v[3 * kept + 1] = vel[3 * k + 1];
     v[3 * kept + 2] = vel[3 * k + 2];
+    if (mpw) wk[(size_t)kept] = mpw[k];
     kept++;
   }
-  if (kept > 0) append_lc_impl(ctx, sp, kept, lc.data(), v.data(), rewind != 0, dt);
+  if (kept > 0) append_lc_impl(ctx, sp, kept, lc.data(), v.data(), rewind != 0, dt, mpw ? wk.data() : nullptr);
   SF_API_END(ctx)
 }
 
@@ -916,6 +943,61 @@ int sf_particles_append_lc(sf_ctx* ctx, int32_t sid, int64_t n, const double* lc
                SF_ERR_ARG, "logical coordinate outside the mesh");
   SF_CUDA(cudaSetDevice(ctx->device));
   if (n > 0) append_lc_impl(ctx, sp, n, lc, vel, false, 0.0);
+  SF_API_END(ctx)
+}
+
+int sf_particles_append_lc_w(sf_ctx* ctx, int32_t sid, int64_t n, const double* lc, const double* vel,
+                             const double* mpw) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(n >= 0 && (n == 0 || (lc && vel && mpw)), SF_ERR_ARG, "null particle arrays");
+  SF_REQUIRE(sp->weighted, SF_ERR_STATE, "the species holds no per-particle weights (sf_species_set_weighted)");
+  for (int64_t k = 0; k < n; k++)
+    SF_REQUIRE(lc[2 * k] >= 0 && lc[2 * k + 1] >= 0 && lc[2 * k] <= ctx->ni - 1 && lc[2 * k + 1] <= ctx->nj - 1,
+               SF_ERR_ARG, "logical coordinate outside the mesh");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  if (n > 0) append_lc_impl(ctx, sp, n, lc, vel, false, 0.0, mpw);
+  SF_API_END(ctx)
+}
+
+int sf_species_set_weighted(sf_ctx* ctx, int32_t sid, int32_t on) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(sp->n == 0, SF_ERR_STATE, "per-particle weights are switched before the first particle");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  if (on && !sp->weighted) {
+    SF_CUDA(cudaMalloc(&sp->cur.w, sizeof(float) * (size_t)std::max<int64_t>(sp->cap, 1)));
+    SF_CUDA(cudaMalloc(&sp->alt.w, sizeof(float) * (size_t)std::max<int64_t>(sp->cap, 1)));
+  } else if (!on && sp->weighted) {
+    SF_CUDA(cudaFree(sp->cur.w));
+    SF_CUDA(cudaFree(sp->alt.w));
+    sp->cur.w = sp->alt.w = nullptr;
+  }
+  sp->weighted = on != 0;
+  SF_API_END(ctx)
+}
+
+int sf_particles_download_weights(sf_ctx* ctx, int32_t sid, int64_t cap, double* mpw, int64_t* n_out) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(n_out, SF_ERR_ARG, "null argument");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  size_t n = (size_t)sp->n;
+  std::vector<uint32_t> cell(n);
+  std::vector<float> w(n, 1.f);
+  if (n) {
+    SF_CUDA(cudaMemcpyAsync(cell.data(), sp->cur.cell, 4 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (sp->weighted) SF_CUDA(cudaMemcpyAsync(w.data(), sp->cur.w, 4 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    SF_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  int64_t k2 = 0;
+  for (size_t k = 0; k < n; k++) {
+    if (cell[k] == DEAD) continue;
+    if (mpw && k2 < cap) mpw[k2] = (double)w[k] * sp->spwt;
+    k2++;
+  }
+  *n_out = std::min(k2, cap);
+  SF_REQUIRE(k2 <= cap, SF_ERR_ARG, "host arrays too small for the particle count");
   SF_API_END(ctx)
 }
 

@@ -113,6 +113,8 @@ struct ParticlesView {
   float2* vxy;
   float* vz;
   int64_t n;  // slots in use
+  float* w;   // per-slot weight as a fraction of the species weight (mpw / spwt, in (0, 1]);
+              // null: every particle carries the species weight
 };
 
 // A species that surface impacts turn particles into (the ParticleListSource of the
@@ -268,6 +270,7 @@ struct SfSpecies {
   uint32_t step = 0;          // pushes done (RNG counter)
   int sort_interval = 16;     // automatic sort every N pushes (0 = never)
   int sort_qb = 3;            // automatic sort key: blocks of 2^sort_qb x 2^sort_qb cells
+  bool weighted = false;      // per-particle weights held (cur.w / alt.w)
   int pushes_since_sort = 1 << 30;
   // velocity sampling (allocated by sf_samples_clear)
   SampleView smp{nullptr, nullptr};

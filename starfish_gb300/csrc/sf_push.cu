@@ -101,13 +101,15 @@ __device__ bool may_hit_fp32(const MeshView& m, int i, int j, float fx, float fy
 // particle that fails the distance test is given the exact path's FP32 pre-filter here,
 // and finishes here when no candidate segment can be on its path (moves of many cells,
 // as in small meshes at large dt, would otherwise mostly queue for the exact path).
-template <int DOM, bool STATS, bool MOM, bool PRE = false>
+// W: per-particle weights (P.w): each deposit, moment and total is scaled by the particle's
+// fraction of the species weight, and st_w sums the fractions (st_n counts particles).
+template <int DOM, bool STATS, bool MOM, bool PRE = false, bool W = false>
 __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView& P, const PushArgs& a, int64_t t0,
                                           unsigned long long* __restrict__ count, long long* __restrict__ mom,
                                           int* __restrict__ slow_idx, unsigned long long* __restrict__ counters,
                                           const SampleView& smp, unsigned* acc,
                                           int (*sred)[PB / 32], Kahan& st_px, Kahan& st_py, Kahan& st_pz, Kahan& st_e,
-                                          unsigned& st_n) {
+                                          unsigned& st_n, Kahan& st_w) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
   const size_t nn = (size_t)m.ni * m.nj;
@@ -122,6 +124,7 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
   uint32_t lcell[PPT];
   float2 lfrac[PPT], lvxy[PPT];
   float lvz[PPT];
+  float pw[PPT];  // weight fractions (W)
   // the tile's arrays from its first particle: 32-bit indices inside the tile
   uint32_t* __restrict__ tcell = P.cell + t0;
   float2* __restrict__ tfrac = P.frac + t0;
@@ -133,11 +136,13 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
     const int q = k * PB + (int)threadIdx.x;
     lcell[k] = DEAD;
     lvz[k] = 0.f;
+    pw[k] = 1.f;
     if (q < nrem) {
       lcell[k] = __ldcs(tcell + q);
       lfrac[k] = __ldcs(tfrac + q);
       lvxy[k] = __ldcs(tvxy + q);
       if (DOM != SF_DOMAIN_XY || STATS || MOM) lvz[k] = __ldcs(tvz + q);
+      if (W) pw[k] = __ldcs(P.w + t0 + q);
     }
   }
 #pragma unroll
@@ -227,10 +232,12 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
           jmax = max(jmax, j2);
           if (STATS) {
             st_n++;
-            st_px.add(nvx);
-            st_py.add(nvy);
-            st_pz.add(nvz);
-            st_e.add(sqrtf(nvx * nvx + nvy * nvy + nvz * nvz));
+            const float wk = pw[k];
+            if (W) st_w.add(wk);
+            st_px.add(W ? wk * nvx : nvx);
+            st_py.add(W ? wk * nvy : nvy);
+            st_pz.add(W ? wk * nvz : nvz);
+            st_e.add((W ? wk : 1.f) * sqrtf(nvx * nvx + nvy * nvy + nvz * nvz));
           }
         } else if (!inside && clear && m.all_delete) {
           // no candidate segment on the way and every domain face removes particles
@@ -296,10 +303,13 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
       if (!d) continue;
       float wx, wy;
       scatter_weights<DOM>(pfx[k], pfy[k], pi[k], pj[k], a, wx, wy);
-      const unsigned q[4] = {quant22((1.f - wx) * (1.f - wy)), quant22(wx * (1.f - wy)), quant22(wx * wy),
-                             quant22((1.f - wx) * wy)};
+      const float wk = pw[k];
+      const unsigned q[4] = {quant22((W ? wk : 1.f) * ((1.f - wx) * (1.f - wy))),
+                             quant22((W ? wk : 1.f) * (wx * (1.f - wy))), quant22((W ? wk : 1.f) * (wx * wy)),
+                             quant22((W ? wk : 1.f) * ((1.f - wx) * wy))};
       if (MOM) {
-        const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
+        const float s[4] = {(W ? wk : 1.f) * ((1.f - wx) * (1.f - wy)), (W ? wk : 1.f) * (wx * (1.f - wy)),
+                            (W ? wk : 1.f) * (wx * wy), (W ? wk : 1.f) * ((1.f - wx) * wy)};
         const int base = pj[k] * m.ni + pi[k];
         const int off[4] = {0, 1, m.ni + 1, m.ni};
 #pragma unroll
@@ -341,7 +351,7 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
   __syncthreads();
 }
 
-template <int DOM, bool STATS, bool MOM>
+template <int DOM, bool STATS, bool MOM, bool W>
 __global__ void __launch_bounds__(PB, 4) k_push(MeshView m, ParticlesView P, PushArgs a,
                                               unsigned long long* __restrict__ count,
                                               long long* __restrict__ mom, int* __restrict__ slow_idx,
@@ -351,16 +361,17 @@ __global__ void __launch_bounds__(PB, 4) k_push(MeshView m, ParticlesView P, Pus
   __shared__ int sred[4][PB / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned FULL = 0xffffffffu;
-  Kahan st_px, st_py, st_pz, st_e;
+  Kahan st_px, st_py, st_pz, st_e, st_w;
   unsigned st_n = 0;
 
   for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < P.n; t0 += (int64_t)gridDim.x * TILE) {
-    push_tile<DOM, STATS, MOM>(m, P, a, t0, count, mom, slow_idx, counters, smp, acc, sred, st_px, st_py,
-                               st_pz, st_e, st_n);
+    push_tile<DOM, STATS, MOM, false, W>(m, P, a, t0, count, mom, slow_idx, counters, smp, acc, sred, st_px, st_py,
+                                         st_pz, st_e, st_n, st_w);
   }
   if (STATS) {
-    // block reduction of the per-thread sums (FP64 from here on)
-    double vals[5] = {(double)st_n, (double)st_px.s - st_px.c, (double)st_py.s - st_py.c,
+    // block reduction of the per-thread sums (FP64 from here on); the first is the particle
+    // count, or with weights the sum of the weight fractions
+    double vals[5] = {W ? (double)st_w.s - st_w.c : (double)st_n, (double)st_px.s - st_px.c, (double)st_py.s - st_py.c,
                       (double)st_pz.s - st_pz.c, (double)st_e.s - st_e.c};
     __shared__ double sd[5][PB / 32];
 #pragma unroll
@@ -625,6 +636,7 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
           Q.P.frac[d] = make_float2(fx, fy);
           Q.P.vxy[d] = make_float2((float)v[0] - Q.qm_halfdt * e.x, (float)v[1] - Q.qm_halfdt * e.y);
           Q.P.vz[d] = (float)v[2];
+          if (Q.P.w) Q.P.w[d] = 1.f;  // products at their species weight
         }
         alive = false;
       }
@@ -702,12 +714,13 @@ __device__ bool process_boundary(const MeshView& m, const SlowArgs& sa, const Pu
 template <int DOM>
 __device__ inline void deposit_global_t(const MeshView& m, unsigned long long* count, long long* mom, int mom_on,
                                         const SampleView& smp, int i, int j, float fx, float fy, float wx, float wy,
-                                        float vx, float vy, float vz, size_t nn) {
+                                        float vx, float vy, float vz, size_t nn, float wt = 1.f) {
   // macroparticles per cell at (int) lc (KineticMaterial.updateSamples), before the skip
   if (mom_on && smp.mpc) atomicAdd(&smp.mpc[(size_t)(j + (fy >= 1.f)) * m.ni + i + (fx >= 1.f)], 1u);
   if ((fx >= 1.f && i == m.ni - 2) || (fy >= 1.f && j == m.nj - 2)) return;  // scatter skip rule
   const size_t u = (size_t)j * m.ni + i;
-  const float s[4] = {(1.f - wx) * (1.f - wy), wx * (1.f - wy), wx * wy, (1.f - wx) * wy};
+  // wt: the particle's fraction of the species weight (1 without per-particle weights)
+  const float s[4] = {wt * ((1.f - wx) * (1.f - wy)), wt * (wx * (1.f - wy)), wt * (wx * wy), wt * ((1.f - wx) * wy)};
   const size_t off[4] = {0, 1, (size_t)m.ni + 1, (size_t)m.ni};
   // the tile deposit's quantisation, so that a particle adds the same integers whichever
   // path finishes it
@@ -874,6 +887,9 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
     const uint32_t c = P.cell[p];
     const float2 f = P.frac[p];
     const float2 v = P.vxy[p];
+    const float wp = P.w ? P.w[p] : 1.f;  // fraction of the species weight
+    PushArgs ap = a;                       // the particle's own weight in the surface sums
+    ap.spwt = a.spwt * (double)wp;
     double lc[2] = {cell_i(c) + (double)f.x, cell_j(c) + (double)f.y};
     double pos[2] = {m.x0[0] + lc[0] * m.dh[0], m.x0[1] + lc[1] * m.dh[1]};
     double vel[3] = {v.x, v.y, (double)P.vz[p]};
@@ -908,7 +924,7 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
       lc[0] = (pos[0] - m.x0[0]) * m.inv_dh[0];
       lc[1] = (pos[1] - m.x0[1]) * m.inv_dh[1];
       periodic = false;
-      alive = process_boundary(m, sa, a, pos, vel, lc, pdt, old, lc_old, rng, periodic);
+      alive = process_boundary(m, sa, ap, pos, vel, lc, pdt, old, lc_old, rng, periodic);
       if (!alive) break;
     }
     if (!alive) {
@@ -932,21 +948,23 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
     P.vxy[p] = make_float2((float)vel[0], (float)vel[1]);
     P.vz[p] = (float)vel[2];
     if (want) {
-      lst[0] += 1.0;
-      lst[1] += vel[0];
-      lst[2] += vel[1];
-      lst[3] += vel[2];
-      lst[4] += sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+      lst[0] += (double)wp;
+      lst[1] += wp * vel[0];
+      lst[2] += wp * vel[1];
+      lst[3] += wp * vel[2];
+      lst[4] += wp * sqrt(vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
     }
     float wx, wy;
     scatter_weights<DOM>(fx, fy, i, j, a, wx, wy);
-    deposit_global(m, count, mom, mom_on, smp, i, j, fx, fy, wx, wy, (float)vel[0], (float)vel[1], (float)vel[2], nn);
+    deposit_global(m, count, mom, mom_on, smp, i, j, fx, fy, wx, wy, (float)vel[0], (float)vel[1], (float)vel[2], nn,
+                   wp);
   };
   // The FP32 pre-filter, for one particle: true when it has to take the exact path.
   auto prefilter = [&](int64_t p) -> bool {
     const uint32_t c = P.cell[p];
     const float2 f = P.frac[p];
     const float2 v = P.vxy[p];
+    const float wp = P.w ? P.w[p] : 1.f;
     // a particle whose (logical, straight) path certainly misses every candidate segment
     // and stays in the mesh finishes exactly like the fast path
     const int i = cell_i(c), j = cell_j(c);
@@ -968,15 +986,15 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
         }
         ldone++;
         if (want) {
-          lst[0] += 1.0;
-          lst[1] += (double)nv[0];
-          lst[2] += (double)nv[1];
-          lst[3] += (double)nv[2];
-          lst[4] += (double)sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+          lst[0] += (double)wp;
+          lst[1] += (double)(wp * nv[0]);
+          lst[2] += (double)(wp * nv[1]);
+          lst[3] += (double)(wp * nv[2]);
+          lst[4] += (double)(wp * sqrtf(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]));
         }
         float wx, wy;
         scatter_weights<DOM>(nfx, nfy, i2, j2, a, wx, wy);
-        deposit_global(m, count, mom, mom_on, smp, i2, j2, nfx, nfy, wx, wy, nv[0], nv[1], nv[2], nn);
+        deposit_global(m, count, mom, mom_on, smp, i2, j2, nfx, nfy, wx, wy, nv[0], nv[1], nv[2], nn, wp);
         return false;
       }
       if (m.all_delete) {
@@ -992,7 +1010,7 @@ __device__ __forceinline__ void push_slow_body(const MeshView& m, const Particle
     // there; only the flux and deposit shares need the hit point
     int hs;
     float ht;
-    if (first_hit_fp32(m, i, j, f.x, f.y, gx, gy, &hs, &ht)) {
+    if (!P.w && first_hit_fp32(m, i, j, f.x, f.y, gx, gy, &hs, &ht)) {
       const int model = sa.sv.model[hs];
       if (model != SF_SURF_PASS && model != SF_SURF_NONE && model != SF_SURF_SPECULAR &&
           model != SF_SURF_DIFFUSE) {
@@ -1280,7 +1298,7 @@ __global__ void __launch_bounds__(PB, 4) k_push_batch(BatchDev b) {
     P.n = b.n_dev[i];
     push_tile<DOM, false, false, true>(I.m, P, I.a, (gt - b.tile_start[i]) * TILE, I.count, nullptr, I.slow_idx,
                                  I.sa.counters, SampleView{nullptr, nullptr}, acc, sred, st_px, st_py,
-                                 st_pz, st_e, st_n);
+                                 st_pz, st_e, st_n, st_e);
   }
 }
 
@@ -1316,8 +1334,12 @@ __global__ void k_finalize_batch(BatchDev b) {
 template <int DOM, bool STATS, bool MOM>
 void launch_push_t(sf_ctx* ctx, SfSpecies* sp, const PushArgs& a, int grid, const PushScratch& sc,
                    const SampleView& smp) {
-  k_push<DOM, STATS, MOM><<<grid, PB, 0, ctx->stream>>>(ctx->mesh_view(), sp->cur, a, sp->count, sp->mom,
-                                                      sc.slow_idx, sc.counters, sc.stats_partial, smp);
+  if (sp->cur.w)
+    k_push<DOM, STATS, MOM, true><<<grid, PB, 0, ctx->stream>>>(ctx->mesh_view(), sp->cur, a, sp->count, sp->mom,
+                                                                sc.slow_idx, sc.counters, sc.stats_partial, smp);
+  else
+    k_push<DOM, STATS, MOM, false><<<grid, PB, 0, ctx->stream>>>(ctx->mesh_view(), sp->cur, a, sp->count, sp->mom,
+                                                                 sc.slow_idx, sc.counters, sc.stats_partial, smp);
 }
 
 template <int DOM>

@@ -87,6 +87,7 @@ __device__ __forceinline__ void inject_one(const MeshView& m, const ParticlesVie
   P.frac[d] = make_float2(fx, fy);
   P.vxy[d] = make_float2((float)vx - a.qm_halfdt * ex, (float)vy - a.qm_halfdt * ey);
   P.vz[d] = (float)vz;
+  if (P.w) P.w[d] = 1.f;  // sources emit at the species weight
 }
 
 __global__ void k_inject_maxwellian(MeshView m, ParticlesView P, InjectArgs a, int n, unsigned long long* counter) {
@@ -230,6 +231,7 @@ __global__ void k_preload(MeshView m, ParticlesView P, PreloadArgs a, const int6
       const int64_t d = a.base + k;
       if (point_internal(m, px, py)) {
         P.cell[d] = DEAD;
+        if (P.w) P.w[d] = 1.f;
         atomicAdd(n_internal, 1ULL);
         continue;
       }
@@ -251,6 +253,7 @@ __global__ void k_preload(MeshView m, ParticlesView P, PreloadArgs a, const int6
       P.frac[d] = make_float2(fx, fy);
       P.vxy[d] = make_float2((float)vx - a.qm_halfdt * ex, (float)vy - a.qm_halfdt * ey);
       P.vz[d] = (float)vz;
+      if (P.w) P.w[d] = 1.f;
     }
   }
 }

@@ -92,18 +92,28 @@ class KineticMaterial:
         self._src_rem = {}
 
     # KineticMaterial.addParticle(pos, vel) with the -dt/2 velocity rewind
-    def add_particles(self, pos, vel, rewind=True, dt=0.0):
+    def add_particles(self, pos, vel, rewind=True, dt=0.0, mpw=None):
         pos = np.ascontiguousarray(pos, np.float64)
         vel = np.ascontiguousarray(vel, np.float64)
+        w = None if mpw is None else np.ascontiguousarray(mpw, np.float64)
         n = pos.shape[0]
         self.d.check(self.d.lib.sf_particles_append(self.d.ctx, self.sid, n, abi.ptr(pos),
-                                                    abi.ptr(vel), None, int(rewind), float(dt)))
+                                                    abi.ptr(vel), abi.ptr(w), int(rewind), float(dt)))
 
-    def add_particles_lc(self, lc, vel):
+    def add_particles_lc(self, lc, vel, mpw=None):
         lc = np.ascontiguousarray(lc, np.float64)
         vel = np.ascontiguousarray(vel, np.float64)
+        if mpw is not None:
+            w = np.ascontiguousarray(mpw, np.float64)
+            self.d.check(self.d.lib.sf_particles_append_lc_w(self.d.ctx, self.sid, lc.shape[0], abi.ptr(lc),
+                                                             abi.ptr(vel), abi.ptr(w)))
+            return
         self.d.check(self.d.lib.sf_particles_append_lc(self.d.ctx, self.sid, lc.shape[0],
                                                        abi.ptr(lc), abi.ptr(vel)))
+
+    def set_weighted(self, on=True):
+        """Per-particle weights (Particle.mpw) for this species, before its first particle."""
+        self.d.check(self.d.lib.sf_species_set_weighted(self.d.ctx, self.sid, int(bool(on))))
 
     def sample_maxwellian_source(self, seg_xy, den, v_drift, temp, dt):
         """MaxwellianSource on one straight segment, sampled on the device; returns the
@@ -208,6 +218,14 @@ class KineticMaterial:
         self.d.check(self.d.lib.sf_particles_download(self.d.ctx, self.sid, n, abi.ptr(lc),
                                                       abi.ptr(vel), C.byref(got)))
         return lc[:got.value], vel[:got.value]
+
+    def download_weights(self):
+        """mpw of the particles download() returns, in the same order."""
+        n = self.get_np()
+        w = np.zeros(max(n, 1))
+        got = C.c_int64()
+        self.d.check(self.d.lib.sf_particles_download_weights(self.d.ctx, self.sid, n, abi.ptr(w), C.byref(got)))
+        return w[:got.value]
 
     def surface_flux(self):
         ns = self.d.spec.seg_xy.reshape(-1, 4).shape[0]

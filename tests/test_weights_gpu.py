@@ -1,0 +1,169 @@
+"""Per-particle weights (Particle.mpw, KineticMaterial.java:1207-1282): a species switched to
+weights (sf_species_set_weighted) pushes, scatters, sums and hits surfaces with each
+particle's own mpw, against the oracle, which carries mpw per particle as the reference
+does; the weights follow their particles through the sort and the restart path; sources
+on a weighted species emit at the species weight; the unsupported uses are refused."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from starfish_gb300 import abi
+from starfish_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+from test_push_gpu import make_state, oracle_parts  # noqa: E402
+
+
+def _omesh(spec):
+    return O.OMesh(spec.ni, spec.nj, spec.x0, spec.dh, spec.domain, spec.node_type, spec.face_type)
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_weighted_push_matches_oracle_c0(gpulib, seed):
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    ion = W.IonSpecies()
+    _, efi, efj = W.electrode_efield(spec)
+    n, dt = 20000, 5e-7
+    lc, vel = make_state(spec, ion, n, seed)
+    rng = np.random.default_rng(seed + 50)
+    # weights that FP32 holds exactly as fractions of spwt
+    frac = np.round(rng.uniform(0.25, 1.0, n) * 256) / 256
+    mpw = frac * ion.spwt
+    dom = GpuDomain(spec)
+    try:
+        dom.set_efield(efi, efj)
+        km = KineticMaterial(dom, ion.mass, ion.charge, ion.spwt, capacity=n + 16)
+        km.set_weighted(True)
+        km.set_sort_interval(0)
+        km.add_particles_lc(lc, vel, mpw=mpw)
+        st = km.update_fields(dt, stats=True)
+        glc, gvel = km.download()
+        gw = km.download_weights()
+        gden = km.get_den()
+        gflux, gdep = km.surface_flux()
+    finally:
+        dom.close()
+    m = _omesh(spec)
+    e32i = efi.astype(np.float32).astype(np.float64)
+    e32j = efj.astype(np.float32).astype(np.float64)
+    segs = O.seg_table(spec.seg_xy, spec.seg_btype, O.SURF_ABSORB)
+    P = oracle_parts(spec, lc, vel, ion.spwt)
+    P[:, 9] = mpw
+    alive, ost, oflux, odep = O.push(m, e32i, e32j, ion.charge, ion.mass, dt, segs,
+                                     spec.node_seg_ptr, spec.node_seg_idx, P)
+    oden = O.update_fields(m, O.node_volumes(m), P)
+    keep = P[:, 10] == 1
+    assert st["np"] == keep.sum() == glc.shape[0]
+    assert np.max(np.abs(glc - P[keep, 6:8])) < 1e-5
+    assert np.array_equal(gw, mpw[keep])
+    # the weighted density: each corner share quantised as 2^-22 of the species weight
+    assert np.max(np.abs(gden - oden)) <= 1e-6 * np.abs(oden).max()
+    assert st["n_sum"] == pytest.approx(ost[0], rel=1e-6)
+    assert st["e_sum"] == pytest.approx(ost[4], rel=1e-5)
+    seg_g = gdep.reshape(-1, 2).sum(axis=1)
+    seg_o = odep.reshape(-1, 2).sum(axis=1)
+    assert np.allclose(seg_g, seg_o, rtol=1e-12)
+    assert np.allclose(gdep, odep, rtol=1e-6)
+    assert st["n_removed"] > 0
+
+
+def test_weights_follow_particles_through_sort_and_restart(gpulib):
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    spec = W.es_pic_mesh(257, 129, 2.5e-4, electrode_halfwidth=4.5e-3)
+    ion = W.IonSpecies()
+    _, efi, efj = W.electrode_efield(spec)
+    pos, vel = W.uniform_maxwellian(spec, ion, 200000, 7)
+    rng = np.random.default_rng(8)
+    mpw = rng.uniform(0.1, 1.0, pos.shape[0]) * ion.spwt
+    outs = []
+    dom = GpuDomain(spec)
+    try:
+        dom.set_efield(efi, efj)
+        km = KineticMaterial(dom, ion.mass, ion.charge, ion.spwt, capacity=250000)
+        km.set_weighted(True)
+        km.set_sort_interval(2)
+        km.add_particles(pos, vel, rewind=True, dt=1.25e-7, mpw=mpw)
+        for _ in range(3):
+            km.update_fields(1.25e-7)
+        lc1, v1 = km.download()
+        w1 = km.download_weights()
+        km.sort()
+        lc2, v2 = km.download()
+        w2 = km.download_weights()
+        a = np.lexsort(np.column_stack([lc1, v1, w1]).T)
+        b = np.lexsort(np.column_stack([lc2, v2, w2]).T)
+        assert np.array_equal(np.column_stack([lc1, v1, w1])[a], np.column_stack([lc2, v2, w2])[b])
+        km.update_fields(1.25e-7)
+        outs.append(km.get_count())
+        # restart: the same particles and weights into a fresh context
+        dom2 = GpuDomain(spec)
+        try:
+            dom2.set_efield(efi, efj)
+            km2 = KineticMaterial(dom2, ion.mass, ion.charge, ion.spwt, capacity=250000)
+            km2.set_weighted(True)
+            km2.set_sort_interval(0)
+            km2.add_particles_lc(lc2, v2, mpw=w2)
+            km2.update_fields(1.25e-7)
+            outs.append(km2.get_count())
+        finally:
+            dom2.close()
+    finally:
+        dom.close()
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_weighted_species_sources_emit_at_the_species_weight(gpulib):
+    """A Maxwellian source on a weighted species gives the same particles and the same
+    deposit as on a species of uniform weight (weight fraction 1)."""
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    ion = W.IonSpecies()
+    _, efi, efj = W.electrode_efield(spec)
+    Ly = spec.lengths()[1]
+    counts = []
+    for weighted in (False, True):
+        dom = GpuDomain(spec)
+        try:
+            dom.set_seed(3)
+            dom.set_efield(efi, efj)
+            km = KineticMaterial(dom, ion.mass, ion.charge, ion.spwt, capacity=200000)
+            km.set_weighted(weighted)
+            for _ in range(3):
+                km.sample_maxwellian_source([0.0, Ly, 0.0, 0.0], ion.den, ion.v_drift, ion.temp, 5e-7)
+                km.update_fields(5e-7)
+            counts.append(km.get_count())
+            if weighted:
+                assert np.all(km.download_weights() == ion.spwt)
+        finally:
+            dom.close()
+    assert np.array_equal(counts[0], counts[1])
+
+
+def test_weight_rejections(gpulib):
+    from starfish_gb300.plugin import DSMC, GpuDomain, KineticMaterial
+    spec = W.es_pic_mesh(81, 41, 1e-3)
+    ion = W.IonSpecies()
+    dom = GpuDomain(spec)
+    try:
+        dom.set_efield(np.zeros(spec.nn), np.zeros(spec.nn))
+        km = KineticMaterial(dom, ion.mass, ion.charge, ion.spwt, capacity=100)
+        lc = np.array([[10.5, 10.5]])
+        v = np.zeros((1, 3))
+        # differing weights on a species of uniform weight
+        with pytest.raises(abi.SfError):
+            km.add_particles(lc * 1e-3, v, rewind=False, mpw=[0.5 * ion.spwt])
+        km.set_weighted(True)
+        # a weight above the species weight
+        with pytest.raises(abi.SfError):
+            km.add_particles_lc(lc, v, mpw=[2.0 * ion.spwt])
+        km.add_particles_lc(lc, v, mpw=[0.5 * ion.spwt])
+        # switching after the first particle
+        with pytest.raises(abi.SfError):
+            km.set_weighted(False)
+        # DSMC takes species of uniform weight
+        with pytest.raises(abi.SfError):
+            DSMC(dom, km, diam=4e-10).perform(1e-6)
+    finally:
+        dom.close()

@@ -152,7 +152,6 @@ T* balloc(sf_batch* b, size_t count) {
 BatchInst make_inst(sf_batch* b, int i) {
   sf_ctx* c = b->ctx[i];
   SfSpecies* sp = get_species(c, b->sid[i]);
-  SF_REQUIRE(!sp->weighted, SF_ERR_ARG, "batched instances take species of uniform weight");
   BatchInst I{};
   I.m = c->mesh_view();
   I.P = sp->cur;
@@ -295,7 +294,8 @@ int sf_batch_create(sf_ctx** ctxs, const int32_t* sids, int32_t n, int32_t threa
       SF_REQUIRE(ctxs[i]->device == b->device, SF_ERR_ARG, "all instances of a batch must be on one device");
       SF_REQUIRE(ctxs[i]->domain == SF_DOMAIN_XY, SF_ERR_ARG, "batched instances must be XY meshes");
       for (int k = 0; k < i; k++) SF_REQUIRE(ctxs[k] != ctxs[i], SF_ERR_ARG, "a context appears twice in the batch");
-      get_species(ctxs[i], sids[i]);
+      SF_REQUIRE(!get_species(ctxs[i], sids[i])->weighted, SF_ERR_ARG,
+                 "batched instances take species of uniform weight");
       b->ctx.push_back(ctxs[i]);
       b->sid.push_back(sids[i]);
     }

@@ -125,8 +125,9 @@ __device__ inline float sigma_cr_eval(const SigmaDev& s, float g2) {
 // sigma g / (sigma g)max, and ModelElastic.perform (DSMC.java:373-453) with the reduced
 // masses and, for different weights, Boyd's update probabilities.  Returns whether the
 // pair collided.
+template <bool W>
 __device__ inline bool collide_pair(const DsmcArgs& d, int64_t a, int64_t b, float smax, Philox& rng,
-                                    float& smax_new) {
+                                    float& smax_new, double& wsum) {
   const float2 va = d.P1.vxy[a], vb = d.P2.vxy[b];
   const float wa = d.P1.vz[a], wb = d.P2.vz[b];
   const float g[3] = {va.x - vb.x, va.y - vb.y, wa - wb};
@@ -138,8 +139,20 @@ __device__ inline bool collide_pair(const DsmcArgs& d, int64_t a, int64_t b, flo
   const float vc[3] = {d.rm1 * va.x + d.rm2 * vb.x, d.rm1 * va.y + d.rm2 * vb.y, d.rm1 * wa + d.rm2 * wb};
   float vr[3];
   elastic_vr(rng, d.sg.vss_inv, g, g_mag, vr);
-  const bool upd_a = !d.boyd || rng.uniformf() < d.pab;
-  const bool upd_b = !d.boyd || rng.uniformf() < d.pba;
+  bool boyd = d.boyd;
+  float pab = d.pab, pba = d.pba;
+  if (W) {
+    // per-particle weights: Boyd's probabilities from the two particles' own weights, and
+    // their mean in the collided-weight sum (DSMC.java:344, 431-452)
+    const double w1 = d.spwt1 * (d.P1.w ? (double)d.P1.w[a] : 1.0);
+    const double w2 = d.spwt2 * (d.P2.w ? (double)d.P2.w[b] : 1.0);
+    boyd = w1 != w2;
+    pab = (float)(w2 / w1);
+    pba = (float)(w1 / w2);
+    wsum += 0.5 * (w1 + w2);
+  }
+  const bool upd_a = !boyd || rng.uniformf() < pab;
+  const bool upd_b = !boyd || rng.uniformf() < pba;
   if (upd_a) {
     d.P1.vxy[a] = make_float2(vc[0] + d.rm2 * vr[0], vc[1] + d.rm2 * vr[1]);
     d.P1.vz[a] = vc[2] + d.rm2 * vr[2];
@@ -229,7 +242,8 @@ __device__ inline bool cell_nsel(const DsmcArgs& d, int np1, int np2, int c, dou
 // particles) are listed for k_dsmc_heavy.  The NTC count, the acceptance and the
 // (sigma g)max update are the reference's; candidates come in rounds of up to 32
 // disjoint pairs (AffineMap), one per lane.
-template <bool PAIR>
+// W: a species holds per-particle weights
+template <bool PAIR, bool W>
 __global__ void __launch_bounds__(128) k_dsmc(MeshView m, DsmcArgs d) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -264,6 +278,7 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, DsmcArgs d) {
     float smax_new = 0.f;
     const float smax = (float)st.x;
     int ncol = 0;
+    double wsum = 0.0;  // collided weight (per-particle weights)
     const int per_round = PAIR ? min(32, min(np1, np2)) : min(32, np1 / 2);
     int left = nsel;
     for (int round = 0, cap = max_rounds(nsel); left > 0 && round < cap; round++) {
@@ -289,7 +304,7 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, DsmcArgs d) {
           p2 = s1m.next(p1);
         }
         used = p1 < (uint32_t)np1 && p2 < (uint32_t)np2;
-        if (used && collide_pair(d, s1 + (int64_t)p1, s2 + (int64_t)p2, smax, rng, smax_new)) ncol++;
+        if (used && collide_pair<W>(d, s1 + (int64_t)p1, s2 + (int64_t)p2, smax, rng, smax_new, wsum)) ncol++;
       }
       left -= __popc(__ballot_sync(FULL, used));
       __syncwarp();  // this round's velocities are visible to the next round's lanes
@@ -297,6 +312,7 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, DsmcArgs d) {
     for (int o = 16; o > 0; o >>= 1) {
       smax_new = fmaxf(smax_new, __shfl_xor_sync(FULL, smax_new, o));
       ncol += __shfl_xor_sync(FULL, ncol, o);
+      if (W) wsum += __shfl_xor_sync(FULL, wsum, o);
     }
     if (lane == 0) {
       if (smax_new > 0.f) st.x = (double)smax_new;
@@ -304,7 +320,7 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, DsmcArgs d) {
       if (ncol) {
         double2 cs = d.counts[c];
         cs.x += ncol;
-        cs.y += ncol * d.real_w;
+        cs.y += W ? wsum : ncol * d.real_w;
         d.counts[c] = cs;
         atomicAdd(d.n_coll, (unsigned long long)ncol);
       }
@@ -315,12 +331,13 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, DsmcArgs d) {
 // The cells handed over by k_dsmc, one CTA of DSMC_HEAVY_THREADS per cell: rounds of up
 // to DSMC_HEAVY_THREADS disjoint pairs (the same AffineMap selection), the CTA
 // synchronising between rounds.
-template <bool PAIR>
+template <bool PAIR, bool W>
 __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, DsmcArgs d) {
   __shared__ int s_idx;
   __shared__ uint32_t s_q[2], s_ab[4];
   __shared__ float s_max[DSMC_HEAVY_THREADS / 32];
   __shared__ int s_n[DSMC_HEAVY_THREADS / 32];
+  __shared__ double s_ws[DSMC_HEAVY_THREADS / 32];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int nh = min((int)*d.n_heavy, d.heavy_cap);
   for (;;) {
@@ -357,6 +374,7 @@ __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, D
     float smax_new = 0.f;
     const float smax = (float)st.x;
     int ncol = 0;
+    double wsum = 0.0;
     const int per_round = PAIR ? min(DSMC_HEAVY_THREADS, min(np1, np2)) : min(DSMC_HEAVY_THREADS, np1 / 2);
     int left = nsel;
     for (int round = 0, cap = max_rounds(nsel); left > 0 && round < cap; round++) {
@@ -389,7 +407,7 @@ __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, D
           p2 = s1m.next(p1);
         }
         used = p1 < (uint32_t)np1 && p2 < (uint32_t)np2;
-        if (used && collide_pair(d, s1 + (int64_t)p1, s2 + (int64_t)p2, smax, rng, smax_new)) ncol++;
+        if (used && collide_pair<W>(d, s1 + (int64_t)p1, s2 + (int64_t)p2, smax, rng, smax_new, wsum)) ncol++;
       }
       // the count of used candidates; also orders this round's velocities and s_ab
       // before the next round
@@ -398,23 +416,26 @@ __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, D
     for (int o = 16; o > 0; o >>= 1) {
       smax_new = fmaxf(smax_new, __shfl_xor_sync(0xffffffffu, smax_new, o));
       ncol += __shfl_xor_sync(0xffffffffu, ncol, o);
+      if (W) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
     }
     if (lane == 0) {
       s_max[wid] = smax_new;
       s_n[wid] = ncol;
+      if (W) s_ws[wid] = wsum;
     }
     __syncthreads();
     if (tid == 0) {
       for (int w = 1; w < DSMC_HEAVY_THREADS / 32; w++) {
         smax_new = fmaxf(smax_new, s_max[w]);
         ncol += s_n[w];
+        if (W) wsum += s_ws[w];
       }
       if (smax_new > 0.f) st.x = (double)smax_new;
       d.state[c] = st;
       if (ncol) {
         double2 cs = d.counts[c];
         cs.x += ncol;
-        cs.y += ncol * d.real_w;
+        cs.y += W ? wsum : ncol * d.real_w;
         d.counts[c] = cs;
         atomicAdd(d.n_coll, (unsigned long long)ncol);
       }
@@ -512,7 +533,7 @@ __device__ inline void isotropic_vel(Philox& r, double mag, double v[3]) {
 // KineticMaterial.addParticle (KineticMaterial.java:776-796): the new particle at the
 // source particle's place with the -dt/2 velocity rewind; false past the capacity
 __device__ bool mcc_append(const MeshView& m, const ParticlesView& Q, int64_t cap, unsigned long long* ctr, uint32_t cell,
-                           float2 f, const double v[3], float qm_halfdt) {
+                           float2 f, const double v[3], float qm_halfdt, float wnew = 1.f) {
   const int64_t d = Q.n + (int64_t)atomicAdd(ctr, 1ULL);
   if (d >= cap) return false;
   const int i = cell_i(cell), j = cell_j(cell);
@@ -525,7 +546,7 @@ __device__ bool mcc_append(const MeshView& m, const ParticlesView& Q, int64_t ca
   Q.frac[d] = f;
   Q.vxy[d] = make_float2((float)v[0] - qm_halfdt * e.x, (float)v[1] - qm_halfdt * e.y);
   Q.vz[d] = (float)v[2];
-  if (Q.w) Q.w[d] = 1.f;  // products at the species weight
+  if (Q.w) Q.w[d] = wnew;  // fraction of the species weight
   return true;
 }
 
@@ -550,6 +571,7 @@ __global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, i
     const float Pc = 1.f - __expf(-sigma_eval(sg, g) * g * dt * den);
     Philox rng(seed, RNG_MCC, (uint64_t)p, step);
     if (Pc < rng.uniformf()) continue;
+    const float wp = P.w ? P.w[p] : 1.f;  // the particle's fraction of the species weight
     // Material.sampleMaxwellianVelocity (Material.java:880-896): mean + SampleMaxw3D(v_th)
     float T = gather_node(tg.T, m.ni, i, j, f.x, f.y);
     if (T < 0.f) T = 0.f;
@@ -579,8 +601,9 @@ __global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, i
         double Tt = (double)gather_node(tg.T, m.ni, i, j, f.x, f.y);
         if (Tt <= 0) Tt = 100;
         isotropic_vel(rng, speed2a, v2b);
-        if (!mcc_append(m, ex.Pe, ex.cap_e, &cnt[1], c, f, v2b, ex.qm_halfdt_src)) atomicAdd(&cnt[3], 1ULL);
-        const int mp_gen = (int)(ex.spwt_ratio + rng.uniform());
+        // the second electron carries the source electron's weight (MCC.java:335)
+        if (!mcc_append(m, ex.Pe, ex.cap_e, &cnt[1], c, f, v2b, ex.qm_halfdt_src, wp)) atomicAdd(&cnt[3], 1ULL);
+        const int mp_gen = (int)(ex.spwt_ratio * (double)wp + rng.uniform());
         if (mp_gen > 0) {
           const double v_th = sqrt(2 * KB * Tt / ex.prod_mass);
           for (int k = 0; k < mp_gen; k++) {
@@ -618,12 +641,12 @@ __global__ void k_mcc(MeshView m, ParticlesView P, TargetView tg, SigmaDev sg, i
     const double li = i + (double)f.x, lj = j + (double)f.y;
     if (ex.S) {
       const double E2 = 0.5 * (double)src_mass * sqrt((double)vxy.x * vxy.x + (double)vxy.y * vxy.y + (double)vz * vz);
-      scatter_fp64(m, ex.S, li, lj, ex.spwt * (E1 - E2) / (ex.dt * node_vol_at(m, li, lj)));
+      scatter_fp64(m, ex.S, li, lj, ex.spwt * (double)wp * (E1 - E2) / (ex.dt * node_vol_at(m, li, lj)));
     }
     if (ex.count_sum) {
       const int u = (j + (f.y >= 1.f)) * m.ni + i + (f.x >= 1.f);
       atomicAdd(&ex.count_sum[u], 1.0);
-      atomicAdd(&ex.real_sum[u], ex.spwt);
+      atomicAdd(&ex.real_sum[u], ex.spwt * (double)wp);
     }
   }
 }
@@ -753,7 +776,6 @@ void dsmc_run(sf_ctx* ctx, int sid1, int sid2, const sf_sigma* sigma, const sf_s
   SfSpecies* sp1 = get_species(ctx, sid1);
   SfSpecies* sp2 = get_species(ctx, sid2);
   SF_REQUIRE(dt > 0 && sig_cr_max0 > 0, SF_ERR_ARG, "dt and sig_cr_max must be positive");
-  SF_REQUIRE(!sp1->weighted && !sp2->weighted, SF_ERR_ARG, "DSMC takes species of uniform weight");
   SF_CUDA(cudaSetDevice(ctx->device));
   const bool pair = sid1 != sid2;
   SfDsmcState* st = dsmc_state(ctx, sid1, sid2, sig_cr_max0);
@@ -801,12 +823,19 @@ void dsmc_run(sf_ctx* ctx, int sid1, int sid2, const sf_sigma* sigma, const sf_s
   d.work = reinterpret_cast<unsigned*>(ctx->counters + 4);
   {
     TimedScope ts(ctx, "dsmc");
-    if (pair) {
-      k_dsmc<true><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
-      k_dsmc_heavy<true><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
+    const bool wt = sp1->weighted || sp2->weighted;
+    if (pair && wt) {
+      k_dsmc<true, true><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc_heavy<true, true><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
+    } else if (pair) {
+      k_dsmc<true, false><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc_heavy<true, false><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
+    } else if (wt) {
+      k_dsmc<false, true><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc_heavy<false, true><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
     } else {
-      k_dsmc<false><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
-      k_dsmc_heavy<false><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc<false, false><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc_heavy<false, false><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
     }
     ctx->launches += 2;
   }
@@ -958,7 +987,6 @@ int sf_mcc(sf_ctx* ctx, int32_t sid, int32_t model, const sf_sigma* sigma, doubl
   SfSpecies* sp = get_species(ctx, sid);
   SF_REQUIRE(model == SF_MCC_MEX || model == SF_MCC_CEX, SF_ERR_ARG,
              "bad MCC model (ionization: sf_mcc_ionization)");
-  SF_REQUIRE(!sp->weighted, SF_ERR_ARG, "MCC takes species of uniform weight");
   unsigned long long h[3];
   mcc_run(ctx, sp, model, sigma, dt, nullptr, 0.0, h);
   if (n_coll) *n_coll = (int64_t)h[0];
@@ -971,7 +999,6 @@ int sf_mcc_ionization(sf_ctx* ctx, int32_t sid, int32_t product_sid, const sf_si
   SfSpecies* sp = get_species(ctx, sid);
   SfSpecies* prod = get_species(ctx, product_sid);
   SF_REQUIRE(product_sid != sid, SF_ERR_ARG, "the product (ion) species must differ from the source (electrons)");
-  SF_REQUIRE(!sp->weighted, SF_ERR_ARG, "MCC takes species of uniform weight");
   SF_REQUIRE(ionization_energy >= 0, SF_ERR_ARG, "ionization energy must be >= 0 eV");
   unsigned long long h[3];
   mcc_run(ctx, sp, SF_MCC_IONIZATION, sigma, dt, prod, ionization_energy, h);

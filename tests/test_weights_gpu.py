@@ -2,7 +2,8 @@
 weights (sf_species_set_weighted) pushes, scatters, sums and hits surfaces with each
 particle's own mpw, against the oracle, which carries mpw per particle as the reference
 does; the weights follow their particles through the sort and the restart path; sources
-on a weighted species emit at the species weight; the unsupported uses are refused."""
+on a weighted species emit at the species weight; DSMC and MCC take each particle's
+weight; the batched instances refuse weighted species."""
 import numpy as np
 import pytest
 
@@ -141,8 +142,105 @@ def test_weighted_species_sources_emit_at_the_species_weight(gpulib):
     assert np.array_equal(counts[0], counts[1])
 
 
-def test_weight_rejections(gpulib):
+def _box():
+    spec = W.es_pic_mesh(21, 21, 1e-3, walls=abi.DB_SYMMETRY, electrode_halfwidth=1e-12)
+    spec.seg_xy = np.zeros((0, 4))
+    spec.seg_btype = np.zeros(0, np.int32)
+    spec.node_type[:] = abi.NODE_OPEN
+    spec.bc_value[:] = 0
+    return spec
+
+
+def test_weighted_mcc_ionization_equals_a_species_of_that_weight(gpulib):
+    """MCC ionization (MCC.java:167-221, 304-356) on a weighted species whose particles all
+    carry half the species weight gives the collisions, products, S, count and weight sums of
+    a uniform species of that half weight: S and the weight sum take each particle's mpw,
+    the second electron the source electron's, the ion count spwt_src mpw/spwt / spwt_ion."""
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial, MCC
+    spec = _box()
+    n, eV, e_ion = 100000, 50.0, 15.76
+    me, mi, QE = 9.10938e-31, 40 * 1.66053886e-27, 1.60217646e-19
+    spwt_e, spwt_i = 5e6, 1e6
+    rng = np.random.default_rng(21)
+    lc = rng.uniform(0.5, 19.5, (n, 2))
+    lc = np.floor(lc) + (lc - np.floor(lc)).astype(np.float32).astype(np.float64)
+    d = rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    vel = (d * np.sqrt(2 * eV * QE / me)).astype(np.float32).astype(np.float64)
+    nn = spec.nn
+    den, T = np.full(nn, 1e20), np.full(nn, 300.0)
+    out = []
+    for weighted in (False, True):
+        dom = GpuDomain(spec)
+        try:
+            dom.set_seed(4)
+            dom.set_efield(np.zeros(nn), np.zeros(nn))
+            ke = KineticMaterial(dom, me, -QE, spwt_e if weighted else 0.5 * spwt_e, capacity=2 * n)
+            ki = KineticMaterial(dom, mi, QE, spwt_i, capacity=2 * n)
+            if weighted:
+                ke.set_weighted(True)
+                ke.add_particles_lc(lc, vel, mpw=np.full(n, 0.5 * spwt_e))
+            else:
+                ke.add_particles_lc(lc, vel)
+            mcc = MCC(dom, ke, target_mass=mi, den=den, temp=T, model=abi.MCC_IONIZATION,
+                      sigma_model=abi.SIGMA_CONST, c=[1e-20, 0, 0, 0])
+            cols, n_e, n_i = mcc.perform(5e-8, product=ki, ionization_energy=e_ion)
+            sums = mcc.sums()
+            _, evel = ke.download()
+            w = ke.download_weights()
+            out.append((cols, n_e, n_i, sums, evel, w))
+        finally:
+            dom.close()
+    (c0, e0, i0, s0, v0, w0), (c1, e1, i1, s1, v1, w1) = out
+    assert (c0, e0, i0) == (c1, e1, i1) and c0 > 0
+    # the electrons collided in place are identical; the second electrons are appended in
+    # atomic order, so the sets are compared
+    assert np.array_equal(v0[:n], v1[:n])
+    assert np.array_equal(v0[np.lexsort(v0.T)], v1[np.lexsort(v1.T)])
+    assert np.allclose(w1, 0.5 * spwt_e) and np.allclose(w0, 0.5 * spwt_e)
+    for key in ("S", "count_sum", "real_sum", "delta_n"):
+        assert np.allclose(s0[key], s1[key], rtol=1e-12, atol=1e-12 * np.abs(s0[key]).max()), key
+
+
+def test_weighted_dsmc_at_the_species_weight_equals_uniform(gpulib):
+    """DSMC on a weighted species whose particles all carry the species weight collides as
+    the uniform species (Boyd's update only acts on unequal weights, DSMC.java:431-452):
+    the collision counts agree within their noise (the order the cell sort leaves inside a
+    cell is set by atomics, so the pairs differ run to run), and the collided-weight sum is
+    the count times the weight."""
     from starfish_gb300.plugin import DSMC, GpuDomain, KineticMaterial
+    spec = _box()
+    n, mass, spwt = 40000, 40 * 1.66053886e-27, 1e12
+    rng = np.random.default_rng(6)
+    lc = rng.uniform(0, 20, (n, 2))
+    lc = np.floor(lc) + (lc - np.floor(lc)).astype(np.float32).astype(np.float64)
+    vel = (rng.standard_normal((n, 3)) * 300.0).astype(np.float32).astype(np.float64)
+    out = []
+    for weighted in (False, True):
+        dom = GpuDomain(spec)
+        try:
+            dom.set_seed(5)
+            dom.set_efield(np.zeros(spec.nn), np.zeros(spec.nn))
+            km = KineticMaterial(dom, mass, 0.0, spwt, capacity=n + 16)
+            km.set_weighted(weighted)
+            km.add_particles_lc(lc, vel, mpw=np.full(n, spwt) if weighted else None)
+            ds = DSMC(dom, km, model=abi.SIGMA_BIRD463, diam=4.17e-10, T_ref=273.0, omega=0.81)
+            cols = [ds.perform(1e-5) for _ in range(3)]
+            cnt, real = ds.counts()
+            _, v = km.download()
+            out.append((cols, cnt, real, v))
+        finally:
+            dom.close()
+    (c0, n0, r0, v0), (c1, n1, r1, v1) = out
+    assert sum(c0) > 0
+    assert abs(sum(c0) - sum(c1)) <= 5 * np.sqrt(sum(c0))
+    assert np.allclose(r1, n1 * spwt, rtol=1e-12, atol=0)
+    assert np.allclose(r0, n0 * spwt, rtol=1e-12, atol=0)
+    assert n1.sum() == sum(c1)
+
+
+def test_weight_rejections(gpulib):
+    from starfish_gb300.plugin import GpuBatch, GpuDomain, KineticMaterial, PoissonSolver
     spec = W.es_pic_mesh(81, 41, 1e-3)
     ion = W.IonSpecies()
     dom = GpuDomain(spec)
@@ -162,8 +260,14 @@ def test_weight_rejections(gpulib):
         # switching after the first particle
         with pytest.raises(abi.SfError):
             km.set_weighted(False)
-        # DSMC takes species of uniform weight
+        # the batched instances take species of uniform weight
+        ps = PoissonSolver(dom, n0=1e12, Te0=2.0, tol=1e-6, max_it=40)
+        ps.solve(rho=np.zeros(spec.nn), phi=np.zeros(spec.nn))
         with pytest.raises(abi.SfError):
-            DSMC(dom, km, diam=4e-10).perform(1e-6)
+            b = GpuBatch([dom], [km], threads=1)
+            try:
+                b.step(5e-7, ps)
+            finally:
+                b.close()
     finally:
         dom.close()

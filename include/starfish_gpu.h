@@ -262,11 +262,25 @@ int sf_get_field(sf_ctx* ctx, int32_t field, int32_t sid, double* out);
  * scatter of updateFields(md) (:168-197) into a deterministic int64 fixed-point
  * grid and the density nd = sum(w S)/V + nd_back.
  * flags: SF_PUSH_STATS computes sf_push_stats (reads vz); SF_PUSH_MOMENTS also
- * deposits the u/v/w moments.  stats may be NULL. */
+ * deposits the u/v/w moments.  stats may be NULL.
+ * SF_PUSH_NOWAIT: return once the push is queued on the context's stream instead of
+ * waiting for it (ignored with SF_PUSH_STATS or when a surface of the species emits
+ * products, which need this push's results on the host).  The removed-particle count
+ * stays on the device until the next call on the species that needs it (any entry point
+ * but the push itself), which waits for the stream first; stats, if given, is zeroed
+ * with np, n_removed, n_slow and n_bounce_limited = -1.  Work queued after it on the
+ * context's stream (sf_poisson_nl, sf_get_field, the next push) sees its results.  A
+ * kernel error of a push that did not wait is reported by a later call. */
 #define SF_PUSH_STATS 1
 #define SF_PUSH_MOMENTS 2
 #define SF_PUSH_SAMPLE 4   /* also KineticMaterial.updateSamples after the push (implies MOMENTS) */
+#define SF_PUSH_NOWAIT 8
 int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_stats* stats);
+/* Particle-steps pushed for the species since it was created: the sum over its
+ * sf_push_deposit / sf_push_deposit_noalloc calls of the particles alive when the push
+ * began (batched steps not included).  Waits for the context's stream.  No counterpart
+ * in the reference (its step log prints np per step). */
+int sf_species_particle_steps(sf_ctx* ctx, int32_t sid, int64_t* particle_steps);
 /* Velocity sampling (KineticMaterial.updateGasProperties, KineticMaterial.java:1553-1671).
  * sf_samples_clear (clearSamples, :1509-1530) zeroes the running sums; its first call sets
  * up the species' sampling buffers (allocates).  Each sf_push_deposit with SF_PUSH_SAMPLE
@@ -282,6 +296,7 @@ int sf_samples_compute(sf_ctx* ctx, int32_t sid, double T_init, int64_t* num_sam
  * fixed at start-up): the push's per-call scratch -- slow-path queue, event counters,
  * partial sums -- lives in a static __device__ array of the library instead of the
  * context's buffers.  Same arguments, results and errors as sf_push_deposit, plus:
+ *  - every call waits for its work; SF_PUSH_NOWAIT is rejected with SF_ERR_ARG;
  *  - the species may hold at most 2^21 (2,097,152) particle slots (live + removed
  *    since the last sort); a larger species is rejected with SF_ERR_ARG;
  *  - the first call on a device looks up the array's device address

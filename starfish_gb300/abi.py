@@ -26,7 +26,7 @@ BT_DIRICHLET, BT_OPEN, BT_SINK, BT_VIRTUAL = 0, 1, 2, 3
 SURF_PASS, SURF_ABSORB, SURF_NONE, SURF_SPECULAR, SURF_DIFFUSE = -1, 0, 1, 2, 3
 FIELD_ND, FIELD_U, FIELD_V, FIELD_W, FIELD_COUNT, FIELD_NODE_VOL = 0, 1, 2, 3, 4, 5
 FIELD_PHI, FIELD_RHO, FIELD_EFI, FIELD_EFJ, FIELD_NE = 10, 11, 12, 13, 14
-PUSH_STATS, PUSH_MOMENTS, PUSH_SAMPLE = 1, 2, 4
+PUSH_STATS, PUSH_MOMENTS, PUSH_SAMPLE, PUSH_NOWAIT = 1, 2, 4, 8
 FIELD_ND_AVE, FIELD_U_AVE, FIELD_V_AVE, FIELD_W_AVE, FIELD_T = 20, 21, 22, 23, 24
 FIELD_T1, FIELD_T2, FIELD_T3, FIELD_P, FIELD_MPC = 25, 26, 27, 28, 29
 
@@ -92,6 +92,7 @@ EXPORTS = {
     "sf_species_set_surface_product": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double]),
     "sf_species_set_sort_interval": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "sf_species_set_sort_block": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "sf_species_particle_steps": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int64)]),
     "sf_species_set_weighted": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "sf_particles_append_lc_w": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sf_particles_download_weights": (C.c_int, [C.c_void_p, C.c_int32, C.c_int64, C.c_void_p,

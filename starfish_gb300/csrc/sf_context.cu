@@ -46,10 +46,27 @@ sf::MeshView sf_ctx::mesh_view() const {
 
 namespace sf {
 
-SfSpecies* get_species(sf_ctx* ctx, int sid) {
+SfSpecies* get_species_nowait(sf_ctx* ctx, int sid) {
   SF_REQUIRE(ctx != nullptr, SF_ERR_ARG, "null context");
   SF_REQUIRE(sid >= 0 && sid < (int)ctx->species.size(), SF_ERR_ARG, "bad species id");
   return ctx->species[sid];
+}
+
+void settle_species(sf_ctx* ctx, SfSpecies* sp) {
+  if (!sp->acc_pending) return;
+  unsigned long long removed = 0;
+  copy_wait(&removed, sp->acc, sizeof(removed), cudaMemcpyDeviceToHost, ctx->stream);
+  SF_CUDA(cudaMemsetAsync(sp->acc, 0, sizeof(unsigned long long), ctx->stream));
+  sp->n_dead += (int64_t)removed;
+  if (removed > 0) sp->sorted = false;
+  sp->acc_pending = false;
+  timer_collect(ctx);
+}
+
+SfSpecies* get_species(sf_ctx* ctx, int sid) {
+  SfSpecies* sp = get_species_nowait(ctx, sid);
+  settle_species(ctx, sp);
+  return sp;
 }
 
 // Node volumes of a uniform mesh with clipped control volumes (Mesh.nodeVol,
@@ -578,6 +595,9 @@ void launch_sort(sf_ctx* ctx, SfSpecies* sp, float look_x, float look_y, int qb)
     sp->n = total;
   }
   sp->n_dead = 0;
+  // the compaction dropped every removed slot, including those of pushes not yet read
+  SF_CUDA(cudaMemsetAsync(sp->acc, 0, sizeof(unsigned long long), ctx->stream));
+  sp->acc_pending = false;
   sp->sorted = true;
   sp->pushes_since_sort = 0;
 }
@@ -696,6 +716,12 @@ int sf_ctx_create(const sf_mesh_desc* md, int device, sf_ctx** out) {
     copy_wait(ctx->d_face_type, ctx->face_type.data(), 4 * (size_t)ctx->nmax, cudaMemcpyHostToDevice, ctx->stream);
     SF_CUDA(cudaMalloc(&ctx->d_node_vol, sizeof(double) * nn));
     copy_wait(ctx->d_node_vol, ctx->node_vol.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->stream);
+    {
+      std::vector<double> iv(nn);
+      for (int u = 0; u < nn; u++) iv[u] = 1.0 / ctx->node_vol[u];
+      SF_CUDA(cudaMalloc(&ctx->d_node_ivol, sizeof(double) * nn));
+      copy_wait(ctx->d_node_ivol, iv.data(), sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->stream);
+    }
     SF_CUDA(cudaMalloc(&ctx->counters, sizeof(unsigned long long) * 8));
     ctx->stats_blocks = ctx->num_sms * 8;
     SF_CUDA(cudaMalloc(&ctx->stats_partial, sizeof(double) * 8 * (size_t)ctx->stats_blocks));
@@ -744,13 +770,14 @@ int sf_ctx_destroy(sf_ctx* ctx) {
     void* ptrs[] = {sp->cur.cell, sp->cur.frac, sp->cur.vxy,  sp->cur.vz,     sp->alt.cell,  sp->alt.frac,
                     sp->alt.vxy,  sp->alt.vz,   sp->count,    sp->mom,        sp->nd,        sp->uvw,
                     sp->seg_model, sp->seg_param, sp->flux,   sp->deposit,    sp->smp.mom2,  sp->smp.mpc,
-                    sp->samp,     sp->gas,      sp->seg_product, sp->cur.w,   sp->alt.w};
+                    sp->samp,     sp->gas,      sp->seg_product, sp->cur.w,   sp->alt.w,
+                    sp->acc};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     delete sp;
   }
   void* ptrs[] = {ctx->E, ctx->seg_dist, ctx->node_seg_ptr, ctx->node_seg_idx, ctx->d_seg_xy, ctx->d_seg_lc,
-                  ctx->d_seg_btype, ctx->d_face_type, ctx->d_node_vol, ctx->slow_idx, ctx->counters,
+                  ctx->d_seg_btype, ctx->d_face_type, ctx->d_node_vol, ctx->d_node_ivol, ctx->slow_idx, ctx->counters,
                   ctx->stats_partial, ctx->bins, ctx->bins_tmp, ctx->scan_blocks, ctx->dscratch};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -791,6 +818,8 @@ int sf_species_add(sf_ctx* ctx, double charge, double mass, double spwt, int64_t
   }
   SF_CUDA(cudaMalloc(&sp->count, sizeof(unsigned long long) * nn));
   SF_CUDA(cudaMemsetAsync(sp->count, 0, sizeof(unsigned long long) * nn, ctx->stream));
+  SF_CUDA(cudaMalloc(&sp->acc, sizeof(unsigned long long) * 2));
+  SF_CUDA(cudaMemsetAsync(sp->acc, 0, sizeof(unsigned long long) * 2, ctx->stream));
   SF_CUDA(cudaMalloc(&sp->mom, sizeof(long long) * 3 * nn));
   SF_CUDA(cudaMalloc(&sp->nd, sizeof(double) * nn));
   SF_CUDA(cudaMemsetAsync(sp->nd, 0, sizeof(double) * nn, ctx->stream));

@@ -254,6 +254,11 @@ struct SfSpecies {
   int64_t cap = 0;
   int64_t n = 0;         // slots in use (alive + removed, until the next sort)
   int64_t n_dead = 0;    // removed slots among n
+  // Device counters kept by the density epilogue of every push: [0] slots removed by
+  // pushes whose counts the host has not read yet (folded into n_dead by settle_species),
+  // [1] particle-steps pushed since the species was created.
+  unsigned long long* acc = nullptr;
+  bool acc_pending = false;  // a push that did not wait may have added to acc[0]
   bool sorted = false;   // slots are in cell order with no removed slots
   sf::ParticlesView cur{}, alt{};
   unsigned long long* count = nullptr;  // ni*nj fixed-point deposit
@@ -290,7 +295,7 @@ struct BatchInst {
   unsigned long long* count;   // species deposit (fixed point)
   int* slow_idx;
   double* nd;
-  const double* vol;
+  const double* ivol;              // 1 / node volume
   double w_scale, nd_back;
   // Maxwellian inlet (MaxwellianSource on one segment); src_on = 0: no source
   double sx1, sy1, sx2, sy2, snx, sny, v_th, v_drift, src_dt, mp_step;
@@ -374,6 +379,7 @@ struct sf_ctx {
   int* d_seg_btype = nullptr;
   int8_t* d_face_type = nullptr;
   double* d_node_vol = nullptr;
+  double* d_node_ivol = nullptr;  // 1 / node volume, for the density epilogues
   // scratch
   int* slow_idx = nullptr;        // capacity = max species capacity
   int64_t slow_cap = 0;
@@ -435,8 +441,13 @@ namespace sf {
 // tile (0: exact cells, which binning by cell needs).  The automatic sort of the push passes
 // the species' look-ahead and sort_qb.
 void launch_sort(sf_ctx* ctx, SfSpecies* sp, float look_x = 0.f, float look_y = 0.f, int qb = 0);
-void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments);
+void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments, const unsigned long long* counters);
+// The species, with the removed-slot counts of pushes that did not wait folded into
+// n_dead (waits for the context stream when there are any).
 SfSpecies* get_species(sf_ctx* ctx, int sid);
+// The species as it stands, without waiting (the push entry points).
+SfSpecies* get_species_nowait(sf_ctx* ctx, int sid);
+void settle_species(sf_ctx* ctx, SfSpecies* sp);
 void ensure_scratch(sf_ctx* ctx, int64_t particles);
 // Timing scope: brackets the kernels launched inside with events when timing is on.
 struct TimedScope {

@@ -1114,14 +1114,30 @@ __global__ void __launch_bounds__(SLOW_THREADS) k_push_slow(MeshView m, Particle
                      (unsigned long long)gridDim.x * blockDim.x);
 }
 
+// Node density from the fixed-point count.  Multiplies by the node's reciprocal volume
+// (computed once on the host) instead of dividing: an FP64 divide is a dozen FP64-pipe
+// instructions, which made this epilogue FP64-bound rather than bandwidth-bound.
+__device__ __forceinline__ double node_density(unsigned long long c, double w_scale, double ivol, double nd_back) {
+  return fma((double)c, w_scale * ivol, nd_back);
+}
+
 // int64 fixed point -> density (Field2D.scaleByVol, Field2D.java:418-431) and mean
 // velocities (Field2D.divideByField, :403-414)
+// Thread 0 also keeps the species' push counters: live_base = slots - removed slots
+// the host knows of, so live_base - acc[0] particles were alive when this push began.
 __global__ void k_finalize(int nn, const unsigned long long* __restrict__ count, const long long* __restrict__ mom,
-                           const double* __restrict__ vol, double w_scale, double nd_back,
-                           double* __restrict__ nd, double* __restrict__ uvw, int mom_on) {
+                           const double* __restrict__ ivol, double w_scale, double nd_back,
+                           double* __restrict__ nd, double* __restrict__ uvw, int mom_on,
+                           unsigned long long* __restrict__ acc, const unsigned long long* __restrict__ counters,
+                           long long live_base) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const unsigned long long removed_before = acc[0];
+    acc[1] += (unsigned long long)(live_base - (long long)removed_before);
+    acc[0] = removed_before + counters[1];
+  }
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x) {
     const unsigned long long c = count[u];
-    nd[u] = (double)c * w_scale / vol[u] + nd_back;
+    nd[u] = node_density(c, w_scale, ivol[u], nd_back);
     if (mom_on) {
       for (int d = 0; d < 3; d++)
         uvw[(size_t)d * nn + u] = c ? ((double)mom[(size_t)d * nn + u] / MOM_SCALE) / ((double)c / DEP_SCALE) : 0.0;
@@ -1323,7 +1339,7 @@ __global__ void k_finalize_batch(BatchDev b) {
   BatchInst& I = b.insts[blockIdx.y];
   const int nn = I.m.ni * I.m.nj;
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x)
-    I.nd[u] = (double)I.count[u] * I.w_scale / I.vol[u] + I.nd_back;
+    I.nd[u] = node_density(I.count[u], I.w_scale, I.ivol[u], I.nd_back);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     b.dead_dev[blockIdx.y] += (int64_t)I.sa.counters[1];
     I.a.step++;
@@ -1365,11 +1381,12 @@ void batch_push(const BatchDev& b, cudaStream_t stream, int num_sms, int blocks_
   SF_CUDA(cudaGetLastError());
 }
 
-void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments) {
+void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments, const unsigned long long* counters) {
   int nn = ctx->ni * ctx->nj;
   ctx->launches++;
   k_finalize<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
-      nn, sp->count, sp->mom, ctx->d_node_vol, sp->spwt / DEP_SCALE, sp->nd_back, sp->nd, sp->uvw, moments ? 1 : 0);
+      nn, sp->count, sp->mom, ctx->d_node_ivol, sp->spwt / DEP_SCALE, sp->nd_back, sp->nd, sp->uvw, moments ? 1 : 0,
+      sp->acc, counters, (long long)(sp->n - sp->n_dead));
 }
 
 }  // namespace sf
@@ -1383,6 +1400,8 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   const bool want_stats = (flags & SF_PUSH_STATS) != 0;
   const bool sample = (flags & SF_PUSH_SAMPLE) != 0;
   const bool mom = sample || (flags & SF_PUSH_MOMENTS) != 0;
+  // totals and surface products need the host to read this push's results
+  const bool nowait = (flags & SF_PUSH_NOWAIT) != 0 && !want_stats && !sp->has_products;
   SF_REQUIRE(!sample || sp->samp, SF_ERR_STATE, "velocity sampling not set up (sf_samples_clear)");
   const SampleView smp = sample ? sp->smp : SampleView{nullptr, nullptr};
   // automatic sort every sort_interval pushes (the counter starts at the interval, so the
@@ -1484,7 +1503,7 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   }
   {
     TimedScope ts(ctx, "finalize");
-    launch_finalize(ctx, sp, mom);
+    launch_finalize(ctx, sp, mom, sc.counters);
   }
   if (sample) {
     // KineticMaterial.updateSamples: this step's deposits into the running sums
@@ -1495,9 +1514,23 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
     sp->num_samples++;
   }
   SF_CUDA(cudaGetLastError());
+  if (nowait) {
+    // the removed-slot count stays on the device (acc[0]) until a call needs it
+    sp->acc_pending = true;
+    sp->step++;
+    sp->pushes_since_sort++;
+    sp->moments_valid = mom;
+    if (stats) {
+      memset(stats, 0, sizeof(*stats));
+      stats->np = stats->n_removed = stats->n_slow = stats->n_bounce_limited = -1;
+    }
+    return;
+  }
   double* h = ctx->host_pinned;
-  unsigned long long hc[4];
+  unsigned long long hc[4], removed = 0;
   SF_CUDA(cudaMemcpyAsync(hc, sc.counters, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  SF_CUDA(cudaMemcpyAsync(&removed, sp->acc, sizeof(removed), cudaMemcpyDeviceToHost, s));
+  SF_CUDA(cudaMemsetAsync(sp->acc, 0, sizeof(unsigned long long), s));
   if (want_stats) {
     k_sum_partials<<<1, 160, 0, s>>>(sc.stats_partial, grid, sc.sums);
     ctx->launches++;
@@ -1506,7 +1539,9 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   }
   SF_CUDA(cudaStreamSynchronize(s));
   timer_collect(ctx);
-  sp->n_dead += (int64_t)hc[1];
+  // this push's removals and those of earlier pushes that did not wait
+  sp->n_dead += (int64_t)removed;
+  sp->acc_pending = false;
   if (sp->has_products) {
     // product particles appended by surface impacts
     std::vector<unsigned long long> added(ctx->species.size());
@@ -1528,7 +1563,7 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   sp->step++;
   sp->pushes_since_sort++;
   sp->moments_valid = mom;
-  if (hc[1] > 0) sp->sorted = false;
+  if (removed > 0) sp->sorted = false;
   if (stats) {
     memset(stats, 0, sizeof(*stats));
     if (want_stats) {
@@ -1593,7 +1628,7 @@ unsigned char* noalloc_scratch(sf_ctx* ctx) {
 
 extern "C" int sf_push_deposit(sf_ctx* ctx, int32_t sid, double dt, int32_t flags, sf_push_stats* stats) {
   SF_API_BEGIN
-  SfSpecies* sp = get_species(ctx, sid);
+  SfSpecies* sp = get_species_nowait(ctx, sid);
   SF_REQUIRE(dt > 0, SF_ERR_ARG, "dt must be positive");
   SF_REQUIRE(ctx->efield_set, SF_ERR_STATE, "electric field not set (sf_set_efield or a Poisson solve)");
   SF_CUDA(cudaSetDevice(ctx->device));
@@ -1607,6 +1642,8 @@ extern "C" int sf_push_deposit_noalloc(sf_ctx* ctx, int32_t sid, double dt, int3
   SfSpecies* sp = get_species(ctx, sid);
   SF_REQUIRE(dt > 0, SF_ERR_ARG, "dt must be positive");
   SF_REQUIRE(ctx->efield_set, SF_ERR_STATE, "electric field not set (sf_set_efield or a Poisson solve)");
+  SF_REQUIRE(!(flags & SF_PUSH_NOWAIT), SF_ERR_ARG,
+             "sf_push_deposit_noalloc waits for every call: its scratch is shared by all contexts on the device");
   SF_REQUIRE(sp->n <= NOALLOC_MAX_PARTICLES, SF_ERR_ARG,
              "sf_push_deposit_noalloc: species holds " + std::to_string(sp->n) + " particle slots, more than its " +
                  std::to_string(NOALLOC_MAX_PARTICLES) + "-particle static scratch; use sf_push_deposit");
@@ -1621,6 +1658,17 @@ extern "C" int sf_push_deposit_noalloc(sf_ctx* ctx, int32_t sid, double dt, int3
                        reinterpret_cast<double*>(base + NOALLOC_OFF_PARTIAL), ctx->stats_blocks,
                        reinterpret_cast<double*>(base + NOALLOC_OFF_SUMS)};
   push_deposit_impl(ctx, sp, dt, flags, stats, sc);
+  SF_API_END(ctx)
+}
+
+extern "C" int sf_species_particle_steps(sf_ctx* ctx, int32_t sid, int64_t* particle_steps) {
+  SF_API_BEGIN
+  SfSpecies* sp = get_species(ctx, sid);
+  SF_REQUIRE(particle_steps, SF_ERR_ARG, "null argument");
+  SF_CUDA(cudaSetDevice(ctx->device));
+  unsigned long long v = 0;
+  copy_wait(&v, sp->acc + 1, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream);
+  *particle_steps = (int64_t)v;
   SF_API_END(ctx)
 }
 

@@ -172,10 +172,12 @@ class KineticMaterial:
         self.d.check(self.d.lib.sf_particles_clear(self.d.ctx, self.sid))
 
     # KineticMaterial.updateFields(): push + scatter (+ updateSamples with sample=True)
-    def update_fields(self, dt, stats=True, moments=False, sample=False):
+    def update_fields(self, dt, stats=True, moments=False, sample=False, wait=True):
+        """One push + scatter.  wait=False queues it and returns at once (SF_PUSH_NOWAIT;
+        without totals the returned counts are -1)."""
         st = abi.PushStats()
         flags = ((abi.PUSH_STATS if stats else 0) | (abi.PUSH_MOMENTS if moments else 0) |
-                 (abi.PUSH_SAMPLE if sample else 0))
+                 (abi.PUSH_SAMPLE if sample else 0) | (0 if wait else abi.PUSH_NOWAIT))
         self.d.check(self.d.lib.sf_push_deposit(self.d.ctx, self.sid, float(dt), flags,
                                                 C.byref(st)))
         return st.as_dict()
@@ -195,6 +197,12 @@ class KineticMaterial:
         out = {k: self.d.get_field(f, self.sid) for k, f in self.GAS_FIELDS.items()}
         out["num_samples"] = n.value
         return out
+
+    def particle_steps(self):
+        """Particle-steps pushed since the species was created."""
+        n = C.c_int64()
+        self.d.check(self.d.lib.sf_species_particle_steps(self.d.ctx, self.sid, C.byref(n)))
+        return n.value
 
     def get_np(self):
         n = C.c_int64()

@@ -288,10 +288,8 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
   const int bw = imax - imin + 2, bh = jmax - jmin + 2;
   const bool any = imax >= 0;
   const bool use_smem = any && (bw * bh <= SBOX);
-  if (use_smem) {
-    for (int q = threadIdx.x; q < bw * bh; q += PB) acc[q] = 0u;
-  }
-  __syncthreads();
+  // acc[] is all zero here: zeroed once by the kernel, and the flush below clears every
+  // node of the box it reads
   if (any) {
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
@@ -343,12 +341,37 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
   }
   __syncthreads();
   if (use_smem) {
+    // row = q / bw by a multiply-high with mg = ceil(2^32 / bw), exact while q * bw < 2^32
+    // (q < SBOX = 4096 and bw <= SBOX)
+    const uint32_t mg = 0xffffffffu / (uint32_t)bw + 1u;
     for (int q = threadIdx.x; q < bw * bh; q += PB) {
-      const unsigned long long v = (unsigned long long)acc[q] << TILE_SHIFT;
-      if (v) atomicAdd(&count[(size_t)(jmin + q / bw) * m.ni + imin + q % bw], v);
+      const unsigned a32 = acc[q];
+      if (a32) {
+        acc[q] = 0u;
+        const int r = (int)__umulhi((uint32_t)q, mg);
+        atomicAdd(&count[(size_t)(jmin + r) * m.ni + imin + (q - r * bw)], (unsigned long long)a32 << TILE_SHIFT);
+      }
     }
   }
   __syncthreads();
+}
+
+// L2 prefetch of a tile's particle arrays (one bulk prefetch per array, issued by one
+// thread): the block asks for its next tile while it pushes the current one, so that the
+// next tile's loads find their lines in L2.  Only whole 16-byte groups of the tile's
+// particles are requested, all inside [0, P.n).
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+  if (bytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+template <int DOM, bool STATS, bool MOM, bool W>
+__device__ __forceinline__ void prefetch_tile(const ParticlesView& P, int64_t t0) {
+  if (t0 >= P.n) return;
+  const uint32_t nrem = (uint32_t)min(P.n - t0, (int64_t)TILE);
+  prefetch_l2(P.cell + t0, (nrem * 4u) & ~15u);
+  prefetch_l2(P.frac + t0, (nrem * 8u) & ~15u);
+  prefetch_l2(P.vxy + t0, (nrem * 8u) & ~15u);
+  if (DOM != SF_DOMAIN_XY || STATS || MOM) prefetch_l2(P.vz + t0, (nrem * 4u) & ~15u);
+  if (W) prefetch_l2(P.w + t0, (nrem * 4u) & ~15u);
 }
 
 template <int DOM, bool STATS, bool MOM, bool W>
@@ -363,8 +386,12 @@ __global__ void __launch_bounds__(PB, 4) k_push(MeshView m, ParticlesView P, Pus
   const unsigned FULL = 0xffffffffu;
   Kahan st_px, st_py, st_pz, st_e, st_w;
   unsigned st_n = 0;
+  for (int q = threadIdx.x; q < SBOX; q += PB) acc[q] = 0u;
+  __syncthreads();
 
-  for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < P.n; t0 += (int64_t)gridDim.x * TILE) {
+  const int64_t stride = (int64_t)gridDim.x * TILE;
+  for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < P.n; t0 += stride) {
+    if (threadIdx.x == 0) prefetch_tile<DOM, STATS, MOM, W>(P, t0 + stride);
     push_tile<DOM, STATS, MOM, false, W>(m, P, a, t0, count, mom, slow_idx, counters, smp, acc, sred, st_px, st_py,
                                          st_pz, st_e, st_n, st_w);
   }
@@ -1306,6 +1333,8 @@ __global__ void __launch_bounds__(PB, 4) k_push_batch(BatchDev b) {
   __shared__ int sred[4][PB / 32];
   Kahan st_px, st_py, st_pz, st_e;
   unsigned st_n = 0;
+  for (int q = threadIdx.x; q < SBOX; q += PB) acc[q] = 0u;
+  __syncthreads();
   const int64_t total = b.tile_start[b.n];
   for (int64_t gt = blockIdx.x; gt < total; gt += gridDim.x) {
     const int i = batch_find(b.tile_start, b.n, gt);

@@ -536,12 +536,7 @@ __device__ bool mcc_append(const MeshView& m, const ParticlesView& Q, int64_t ca
                            float2 f, const double v[3], float qm_halfdt, float wnew = 1.f) {
   const int64_t d = Q.n + (int64_t)atomicAdd(ctr, 1ULL);
   if (d >= cap) return false;
-  const int i = cell_i(cell), j = cell_j(cell);
-  const int u = j * m.ni + i;
-  const float w00 = (1.f - f.x) * (1.f - f.y), w10 = f.x * (1.f - f.y), w11 = f.x * f.y, w01 = (1.f - f.x) * f.y;
-  const float2 e00 = m.E[u], e10 = m.E[u + 1], e11 = m.E[u + m.ni + 1], e01 = m.E[u + m.ni];
-  const float2 e = make_float2(w00 * e00.x + w10 * e10.x + w11 * e11.x + w01 * e01.x,
-                               w00 * e00.y + w10 * e10.y + w11 * e11.y + w01 * e01.y);
+  const float2 e = gather_efield(m.E, m.ni, cell_i(cell), cell_j(cell), f.x, f.y);
   Q.cell[d] = cell;
   Q.frac[d] = f;
   Q.vxy[d] = make_float2((float)v[0] - qm_halfdt * e.x, (float)v[1] - qm_halfdt * e.y);

@@ -228,21 +228,17 @@ __global__ void k_rewind(MeshView m, ParticlesView p, int64_t base, int n, float
   uint32_t c = p.cell[d];
   int i = cell_i(c), j = cell_j(c);
   float2 f = p.frac[d];
-  int u = j * m.ni + i;
-  float2 e00 = m.E[u], e10 = m.E[u + 1], e11 = m.E[u + m.ni + 1], e01 = m.E[u + m.ni];
-  float w00 = (1 - f.x) * (1 - f.y), w10 = f.x * (1 - f.y), w11 = f.x * f.y, w01 = (1 - f.x) * f.y;
-  float ex = w00 * e00.x + w10 * e10.x + w11 * e11.x + w01 * e01.x;
-  float ey = w00 * e00.y + w10 * e10.y + w11 * e11.y + w01 * e01.y;
+  const float2 e = gather_efield(m.E, m.ni, i, j, f.x, f.y);
   float2 v = p.vxy[d];
-  v.x -= qm_halfdt * ex;
-  v.y -= qm_halfdt * ey;
+  v.x -= qm_halfdt * e.x;
+  v.y -= qm_halfdt * e.y;
   p.vxy[d] = v;
 }
 
 __global__ void k_pack_efield(int nn, const double* __restrict__ efi, const double* __restrict__ efj,
-                              float2* __restrict__ E) {
+                              float4* __restrict__ E) {
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x)
-    E[u] = make_float2((float)efi[u], (float)efj[u]);
+    store_efield(E, u, make_float2((float)efi[u], (float)efj[u]));
 }
 
 // Counting sort by cell key.  Each block takes chunks of SORT_CHUNK particles and
@@ -683,8 +679,8 @@ int sf_ctx_create(const sf_mesh_desc* md, int device, sf_ctx** out) {
     }
     std::vector<uint8_t> sd = segment_distance(ctx, ptr, idx);
     // device mesh
-    SF_CUDA(cudaMalloc(&ctx->E, sizeof(float2) * nn));
-    SF_CUDA(cudaMemsetAsync(ctx->E, 0, sizeof(float2) * nn, ctx->stream));
+    SF_CUDA(cudaMalloc(&ctx->E, sizeof(float4) * nn));
+    SF_CUDA(cudaMemsetAsync(ctx->E, 0, sizeof(float4) * nn, ctx->stream));
     SF_CUDA(cudaMalloc(&ctx->seg_dist, nn));
     copy_wait(ctx->seg_dist, sd.data(), nn, cudaMemcpyHostToDevice, ctx->stream);
     SF_CUDA(cudaMalloc(&ctx->node_seg_ptr, sizeof(int) * (nn + 1)));

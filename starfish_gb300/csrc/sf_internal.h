@@ -63,6 +63,25 @@ struct alignas(16) SegLC {
 __host__ __device__ inline uint32_t pack_cell(int i, int j) { return ((uint32_t)j << 16) | (uint32_t)i; }
 __host__ __device__ inline int cell_i(uint32_t c) { return (int)(c & 0xFFFFu); }
 __host__ __device__ inline int cell_j(uint32_t c) { return (int)(c >> 16); }
+
+// The FP32 electric field is stored per node u as (E[u], E[u+1]), so that the four corners
+// of a cell are two 16-byte loads (u and u + ni) instead of four 8-byte ones.
+// Bilinear gather at (i + fx, j + fy) (Field2D.gather, core/domain/Field2D.java:318-350).
+__device__ __forceinline__ float2 gather_efield(const float4* __restrict__ E, int ni, int i, int j, float fx,
+                                                float fy) {
+  const int u = j * ni + i;
+  const float4 lo = __ldg(E + u), hi = __ldg(E + u + ni);
+  const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w11 = fx * fy, w01 = (1.f - fx) * fy;
+  float2 e;
+  e.x = w00 * lo.x + w10 * lo.z + w11 * hi.z + w01 * hi.x;
+  e.y = w00 * lo.y + w10 * lo.w + w11 * hi.w + w01 * hi.y;
+  return e;
+}
+// Writes node u's field into both of its places.
+__device__ __forceinline__ void store_efield(float4* E, int u, float2 e) {
+  reinterpret_cast<float2*>(E)[2 * (size_t)u] = e;
+  if (u > 0) reinterpret_cast<float2*>(E)[2 * (size_t)u - 1] = e;
+}
 // Sort key of a cell: 16x16-cell tiles in row-major tile order, row-major inside a tile,
 // so that a run of sorted particles is compact in both directions.
 __host__ __device__ inline uint32_t cell_key(int i, int j, int ntx) {
@@ -82,7 +101,7 @@ struct MeshView {
   double x0[2], dh[2];
   double inv_dh[2];             // 1 / dh (the exact path multiplies: an FP64 division is ~10x dearer)
   float inv_dx, inv_dy;
-  const float2* E;              // ni*nj (efi, efj) FP32
+  const float4* E;              // ni*nj: node u holds (efi, efj) of u and of u + 1, FP32
   const uint8_t* seg_dist;      // ni*nj Chebyshev distance to the nearest node listing a
                                 // DIRICHLET/SINK segment (255 = none within 255)
   const int* node_seg_ptr;      // ni*nj+1
@@ -366,7 +385,7 @@ struct sf_ctx {
   std::vector<double> seg_xy;
   std::vector<int> seg_btype;
   // device mesh
-  float2* E = nullptr;
+  float4* E = nullptr;  // see MeshView::E
   bool efield_set = false;
   bool all_delete = false;  // no SYMMETRY / PERIODIC face anywhere
   int ntx = 0, nty = 0;     // 16x16-cell tiles of the sort key

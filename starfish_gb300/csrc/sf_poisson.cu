@@ -876,7 +876,7 @@ __global__ void k_fix_phi(int n, double* __restrict__ x, const double* __restric
 // (the rows Solver.getNodeGradient assembles, Solver.java:559-611)
 __device__ __forceinline__ void efield_node(int u, int ni, int nj, double inv_dx, double inv_dy,
                                             const double* __restrict__ phi, double* __restrict__ efi,
-                                            double* __restrict__ efj, float2* __restrict__ E) {
+                                            double* __restrict__ efj, float4* __restrict__ E) {
   {
     const int j = u / ni, i = u - j * ni;
     double gi, gj;
@@ -888,12 +888,12 @@ __device__ __forceinline__ void efield_node(int u, int ni, int nj, double inv_dx
     else gj = (phi[u + ni] - phi[u - ni]) * (0.5 * inv_dy);
     efi[u] = -gi;
     efj[u] = -gj;
-    E[u] = make_float2((float)(-gi), (float)(-gj));
+    store_efield(E, u, make_float2((float)(-gi), (float)(-gj)));
   }
 }
 
 __global__ void k_efield(int ni, int nj, double inv_dx, double inv_dy, const double* __restrict__ phi,
-                         double* __restrict__ efi, double* __restrict__ efj, float2* __restrict__ E) {
+                         double* __restrict__ efi, double* __restrict__ efj, float4* __restrict__ E) {
   const int n = ni * nj;
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
     efield_node(u, ni, nj, inv_dx, inv_dy, phi, efi, efj, E);
@@ -1516,7 +1516,7 @@ struct BPInst {
   double *phi, *b0, *rho, *efi, *efj, *partial, *red, *sc;
   const double* bc;
   const uint8_t* type0;
-  float2* E;
+  float4* E;
   float *cg_x, *cg_p, *cg_q, *cg_zo;
   int nspecies;
   const double* nd[BP_MAX_SPECIES];

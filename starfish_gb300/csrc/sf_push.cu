@@ -64,14 +64,7 @@ __device__ __forceinline__ void scatter_weights(float fx, float fy, int i, int j
 __device__ __forceinline__ float2 gather_E(const MeshView& m, int i, int j, float fx, float fy) {
   // Field2D.gather (Field2D.java:318-350); at lc = n-1 the cell is n-2 with fraction 1,
   // which gives gather_safe's value (:371-390).
-  int u = j * m.ni + i;
-  float2 e00 = __ldg(&m.E[u]), e10 = __ldg(&m.E[u + 1]);
-  float2 e11 = __ldg(&m.E[u + m.ni + 1]), e01 = __ldg(&m.E[u + m.ni]);
-  float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w11 = fx * fy, w01 = (1.f - fx) * fy;
-  float2 e;
-  e.x = w00 * e00.x + w10 * e10.x + w11 * e11.x + w01 * e01.x;
-  e.y = w00 * e00.y + w10 * e10.y + w11 * e11.y + w01 * e01.y;
-  return e;
+  return gather_efield(m.E, m.ni, i, j, fx, fy);
 }
 
 struct Kahan {

@@ -77,11 +77,8 @@ __device__ __forceinline__ void inject_one(const MeshView& m, const ParticlesVie
   if (i > m.ni - 2) i = m.ni - 2;
   if (j > m.nj - 2) j = m.nj - 2;
   const float fx = (float)(lx - i), fy = (float)(ly - j);
-  const int u = j * m.ni + i;
-  const float2 e00 = m.E[u], e10 = m.E[u + 1], e11 = m.E[u + m.ni + 1], e01 = m.E[u + m.ni];
-  const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w11 = fx * fy, w01 = (1.f - fx) * fy;
-  const float ex = w00 * e00.x + w10 * e10.x + w11 * e11.x + w01 * e01.x;
-  const float ey = w00 * e00.y + w10 * e10.y + w11 * e11.y + w01 * e01.y;
+  const float2 eg = gather_efield(m.E, m.ni, i, j, fx, fy);
+  const float ex = eg.x, ey = eg.y;
   const int64_t d = a.base + (int64_t)atomicAdd(counter, 1ULL);
   P.cell[d] = pack_cell(i, j);
   P.frac[d] = make_float2(fx, fy);
@@ -244,11 +241,8 @@ __global__ void k_preload(MeshView m, ParticlesView P, PreloadArgs a, const int6
       if (i > m.ni - 2) i = m.ni - 2;
       if (j > m.nj - 2) j = m.nj - 2;
       const float fx = (float)(lx - i), fy = (float)(ly - j);
-      const int u = j * m.ni + i;
-      const float2 e00 = m.E[u], e10 = m.E[u + 1], e11 = m.E[u + m.ni + 1], e01 = m.E[u + m.ni];
-      const float w00 = (1.f - fx) * (1.f - fy), w10 = fx * (1.f - fy), w11 = fx * fy, w01 = (1.f - fx) * fy;
-      const float ex = w00 * e00.x + w10 * e10.x + w11 * e11.x + w01 * e01.x;
-      const float ey = w00 * e00.y + w10 * e10.y + w11 * e11.y + w01 * e01.y;
+      const float2 eg = gather_efield(m.E, m.ni, i, j, fx, fy);
+      const float ex = eg.x, ey = eg.y;
       P.cell[d] = pack_cell(i, j);
       P.frac[d] = make_float2(fx, fy);
       P.vxy[d] = make_float2((float)vx - a.qm_halfdt * ex, (float)vy - a.qm_halfdt * ey);

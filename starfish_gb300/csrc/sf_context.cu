@@ -63,6 +63,35 @@ void settle_species(sf_ctx* ctx, SfSpecies* sp) {
   timer_collect(ctx);
 }
 
+// The device address of a host buffer the GPU can read and write directly (pinned memory
+// from cudaHostAlloc or cudaHostRegister), or null for any other pointer.
+const void* mapped_host(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+__global__ void k_copy_f64(size_t n, const double* __restrict__ src, double* __restrict__ dst) {
+  for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < n; u += (size_t)gridDim.x * blockDim.x)
+    dst[u] = src[u];
+}
+
+// FP64 device array -> host (the caller waits for the stream): stored over the host link
+// by a kernel when the host buffer is pinned, else a copy.
+void copy_to_host(sf_ctx* ctx, double* out, const double* src, size_t n) {
+  double* m = static_cast<double*>(const_cast<void*>(mapped_host(out)));
+  if (m) {
+    k_copy_f64<<<grid_for((int64_t)n, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(n, src, m);
+    ctx->launches++;
+    SF_CUDA(cudaGetLastError());
+  } else {
+    SF_CUDA(cudaMemcpyAsync(out, src, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+}
+
 SfSpecies* get_species(sf_ctx* ctx, int sid) {
   SfSpecies* sp = get_species_nowait(ctx, sid);
   settle_species(ctx, sp);
@@ -235,6 +264,7 @@ __global__ void k_rewind(MeshView m, ParticlesView p, int64_t base, int n, float
   p.vxy[d] = v;
 }
 
+// efi / efj may be the caller's pinned host buffers, read over the host link
 __global__ void k_pack_efield(int nn, const double* __restrict__ efi, const double* __restrict__ efj,
                               float4* __restrict__ E) {
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x)
@@ -1094,10 +1124,15 @@ int sf_set_efield(sf_ctx* ctx, const double* efi, const double* efj) {
   SF_REQUIRE(ctx && efi && efj, SF_ERR_ARG, "null argument");
   SF_CUDA(cudaSetDevice(ctx->device));
   size_t nn = (size_t)ctx->ni * ctx->nj;
-  SF_CUDA(cudaMemcpyAsync(ctx->dscratch, efi, sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->stream));
-  SF_CUDA(cudaMemcpyAsync(ctx->dscratch + nn, efj, sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->stream));
-  k_pack_efield<<<grid_for((int64_t)nn, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
-      (int)nn, ctx->dscratch, ctx->dscratch + nn, ctx->E);
+  const double* mi = static_cast<const double*>(mapped_host(efi));
+  const double* mj = static_cast<const double*>(mapped_host(efj));
+  if (!(mi && mj)) {
+    SF_CUDA(cudaMemcpyAsync(ctx->dscratch, efi, sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->stream));
+    SF_CUDA(cudaMemcpyAsync(ctx->dscratch + nn, efj, sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->stream));
+    mi = ctx->dscratch;
+    mj = ctx->dscratch + nn;
+  }
+  k_pack_efield<<<grid_for((int64_t)nn, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>((int)nn, mi, mj, ctx->E);
   ctx->launches++;
   SF_CUDA(cudaGetLastError());
   SF_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1122,7 +1157,7 @@ int sf_get_field(sf_ctx* ctx, int32_t field, int32_t sid, double* out) {
   SfSpecies* sp = get_species(ctx, sid);
   switch (field) {
     case SF_FIELD_ND:
-      SF_CUDA(cudaMemcpyAsync(out, sp->nd, sizeof(double) * nn, cudaMemcpyDeviceToHost, ctx->stream));
+      copy_to_host(ctx, out, sp->nd, nn);
       break;
     case SF_FIELD_U:
     case SF_FIELD_V:

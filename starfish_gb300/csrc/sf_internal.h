@@ -467,6 +467,8 @@ SfSpecies* get_species(sf_ctx* ctx, int sid);
 // The species as it stands, without waiting (the push entry points).
 SfSpecies* get_species_nowait(sf_ctx* ctx, int sid);
 void settle_species(sf_ctx* ctx, SfSpecies* sp);
+const void* mapped_host(const void* p);
+void copy_to_host(sf_ctx* ctx, double* out, const double* src, size_t n);
 void ensure_scratch(sf_ctx* ctx, int64_t particles);
 // Timing scope: brackets the kernels launched inside with events when timing is on.
 struct TimedScope {

@@ -110,6 +110,9 @@ struct DsmcArgs {
   unsigned* n_heavy;
   int heavy_cap;
   unsigned* work;    // k_dsmc_heavy's cell counter
+  int* light;        // cells for k_dsmc (sort keys)
+  unsigned* n_light;
+  int* nsel;         // per cell: this call's candidate count (listed cells only)
 };
 
 // sigma(g) g of Sigma.eval (interactions/Sigma.java:121-195, SigmaPlus.java:54-76) from
@@ -134,7 +137,7 @@ __device__ inline bool collide_pair(const DsmcArgs& d, int64_t a, int64_t b, flo
   const float g2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
   const float sigma_cr = sigma_cr_eval(d.sg, g2);
   smax_new = fmaxf(smax_new, sigma_cr);
-  if (!(rng.uniformf() < sigma_cr / smax)) return false;
+  if (!(rng.uniformf() * smax < sigma_cr)) return false;  // sigma g / (sigma g)max > R
   const float g_mag = sqrtf(g2);
   const float vc[3] = {d.rm1 * va.x + d.rm2 * vb.x, d.rm1 * va.y + d.rm2 * vb.y, d.rm1 * wa + d.rm2 * wb};
   float vr[3];
@@ -237,46 +240,79 @@ __device__ inline bool cell_nsel(const DsmcArgs& d, int np1, int np2, int c, dou
   return true;
 }
 
-// DSMC.collideCell with one warp per cell, warps striding over the cells; cells with
-// more than DSMC_HEAVY_NSEL candidate pairs (the dense cells of a jet hold thousands of
-// particles) are listed for k_dsmc_heavy.  The NTC count, the acceptance and the
-// (sigma g)max update are the reference's; candidates come in rounds of up to 32
-// disjoint pairs (AffineMap), one per lane.
+// The NTC plan of every cell, one thread per cell: the selection count nsel and the new
+// remainder of collideCell (DSMC.java:272-304; the remainder is stored here), and the
+// cell's place in the list of k_dsmc (a warp per cell) or, beyond DSMC_HEAVY_NSEL
+// candidates with at least 128 particles on each side, of k_dsmc_heavy (a CTA per cell).
+// Cells with fewer particles than a pair, or no candidate this call, are in neither.  The
+// FP64 arithmetic of nsel runs once per cell instead of on every lane of a warp.
+template <bool PAIR>
+__global__ void k_dsmc_plan(MeshView m, DsmcArgs d) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int ncx = m.ni - 1, nc = ncx * (m.nj - 1);
+  const int stride = (int)(gridDim.x * blockDim.x);
+  for (int c0 = (int)(blockIdx.x * blockDim.x); c0 < nc; c0 += stride) {
+    const int c = c0 + (int)threadIdx.x;
+    int list = 0;  // 1 light, 2 heavy
+    int key = 0;
+    if (c < nc) {
+      const int j = c / ncx, i = c - j * ncx;
+      key = (int)cell_key(i, j, d.ntx);
+      const int s1 = d.bins1[key], np1 = d.bins1[key + 1] - s1;
+      const int np2 = PAIR ? d.bins2[key + 1] - d.bins2[key] : np1;
+      double2* stp = &d.state[c];
+      int nsel;
+      double rem;
+      if (cell_nsel<PAIR>(d, np1, np2, c, *stp, nsel, rem)) {
+        stp->y = rem;
+        if (nsel > 0) {
+          d.nsel[c] = nsel;
+          list = (nsel > DSMC_HEAVY_NSEL && min(np1, np2) >= 128) ? 2 : 1;
+        }
+      }
+    }
+    // warp-aggregated appends to the two lists
+#pragma unroll
+    for (int l = 1; l <= 2; l++) {
+      const unsigned mk = __ballot_sync(FULL, list == l);
+      if (!mk) continue;
+      const int leader = __ffs(mk) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(l == 1 ? d.n_light : d.n_heavy, (unsigned)__popc(mk));
+      base = __shfl_sync(FULL, base, leader);
+      if (list == l) (l == 1 ? d.light : d.heavy)[base + __popc(mk & ((1u << lane) - 1u))] = key;
+    }
+  }
+}
+
+// DSMC.collideCell for the cells of k_dsmc_plan's light list, one warp per cell, warps
+// striding over the list.  The acceptance and the (sigma g)max update are the
+// reference's; candidates come in rounds of up to 32 disjoint pairs (AffineMap), one per
+// lane.
 // W: a species holds per-particle weights
 template <bool PAIR, bool W>
 __global__ void __launch_bounds__(128) k_dsmc(MeshView m, DsmcArgs d) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int warps = (int)(gridDim.x * blockDim.x) >> 5;
-  for (int key = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); key < d.nkeys; key += warps) {
+  const int nl = (int)*d.n_light;
+  for (int e = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); e < nl; e += warps) {
+    const int key = d.light[e];
     int i, j;
     key_cell((uint32_t)key, d.ntx, i, j);
-    if (i >= m.ni - 1 || j >= m.nj - 1) continue;
     const int c = j * (m.ni - 1) + i;
     const int s1 = d.bins1[key], np1 = d.bins1[key + 1] - s1;
     const int s2 = PAIR ? d.bins2[key] : s1;
     const int np2 = PAIR ? d.bins2[key + 1] - s2 : np1;
-    double2 st = d.state[c];  // x: (sigma g)max, y: remainder
-    int nsel;
-    double rem;
-    if (!cell_nsel<PAIR>(d, np1, np2, c, st, nsel, rem)) continue;
-    if (nsel > DSMC_HEAVY_NSEL && min(np1, np2) >= 128) {
-      // many rounds: hand the cell to a whole CTA (k_dsmc_heavy), which recomputes nsel
-      int slot = 0;
-      if (lane == 0) slot = (int)atomicAdd(d.n_heavy, 1u);
-      slot = __shfl_sync(FULL, slot, 0);
-      if (slot < d.heavy_cap) {
-        if (lane == 0) d.heavy[slot] = key;
-        continue;
-      }
-    }
-    st.y = rem;
+    const int nsel = d.nsel[c];
+    const double smax_old = d.state[c].x;  // (sigma g)max
     Philox rng(d.seed, RNG_DSMC, (uint64_t)c * 32u + (uint64_t)lane, d.step);
     AffineMap s1m, s2m;
     s1m.q = warp_next_prime((uint32_t)np1);
     s2m.q = PAIR ? warp_next_prime((uint32_t)np2) : s1m.q;
     float smax_new = 0.f;
-    const float smax = (float)st.x;
+    const float smax = (float)smax_old;
     int ncol = 0;
     double wsum = 0.0;  // collided weight (per-particle weights)
     const int per_round = PAIR ? min(32, min(np1, np2)) : min(32, np1 / 2);
@@ -315,8 +351,7 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, DsmcArgs d) {
       if (W) wsum += __shfl_xor_sync(FULL, wsum, o);
     }
     if (lane == 0) {
-      if (smax_new > 0.f) st.x = (double)smax_new;
-      d.state[c] = st;
+      if (smax_new > 0.f) d.state[c].x = (double)smax_new;
       if (ncol) {
         double2 cs = d.counts[c];
         cs.x += ncol;
@@ -353,11 +388,8 @@ __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, D
     const int s1 = d.bins1[key], np1 = d.bins1[key + 1] - s1;
     const int s2 = PAIR ? d.bins2[key] : s1;
     const int np2 = PAIR ? d.bins2[key + 1] - s2 : np1;
-    double2 st = d.state[c];
-    int nsel;
-    double rem;
-    cell_nsel<PAIR>(d, np1, np2, c, st, nsel, rem);  // true: k_dsmc listed the cell
-    st.y = rem;
+    const int nsel = d.nsel[c];
+    const double smax_old = d.state[c].x;
     if (wid == 0) {
       const uint32_t q1 = warp_next_prime((uint32_t)np1);
       const uint32_t q2 = PAIR ? warp_next_prime((uint32_t)np2) : q1;
@@ -372,7 +404,7 @@ __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, D
     s2m.q = s_q[1];
     Philox rng(d.seed, RNG_DSMC_HEAVY, (uint64_t)c * DSMC_HEAVY_THREADS + (uint64_t)tid, d.step);
     float smax_new = 0.f;
-    const float smax = (float)st.x;
+    const float smax = (float)smax_old;
     int ncol = 0;
     double wsum = 0.0;
     const int per_round = PAIR ? min(DSMC_HEAVY_THREADS, min(np1, np2)) : min(DSMC_HEAVY_THREADS, np1 / 2);
@@ -430,8 +462,7 @@ __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, D
         ncol += s_n[w];
         if (W) wsum += s_ws[w];
       }
-      if (smax_new > 0.f) st.x = (double)smax_new;
-      d.state[c] = st;
+      if (smax_new > 0.f) d.state[c].x = (double)smax_new;
       if (ncol) {
         double2 cs = d.counts[c];
         cs.x += ncol;
@@ -702,6 +733,8 @@ struct SfDsmcState {
   double2* counts = nullptr;  // per cell collision count, weight
   double* cell_vol = nullptr;
   int* bins1 = nullptr;       // two species: the first one's sort bins (the second uses ctx->bins)
+  int* nsel = nullptr;        // per cell: candidate count of the current call (k_dsmc_plan)
+  int* light = nullptr;       // cells of k_dsmc (sort keys), up to one per cell
 };
 
 // per-context DSMC state of a material pair; freed with the context through the destroy hook
@@ -721,6 +754,8 @@ static SfDsmcState* dsmc_state(sf_ctx* ctx, int sid1, int sid2, double sig_cr_ma
   SF_CUDA(cudaMalloc(&st->state, sizeof(double2) * nc));
   SF_CUDA(cudaMalloc(&st->counts, sizeof(double2) * nc));
   SF_CUDA(cudaMalloc(&st->cell_vol, sizeof(double) * nc));
+  SF_CUDA(cudaMalloc(&st->nsel, sizeof(int) * nc));
+  SF_CUDA(cudaMalloc(&st->light, sizeof(int) * nc));
   if (sid1 != sid2) SF_CUDA(cudaMalloc(&st->bins1, sizeof(int) * ((size_t)ctx->nkeys + 1)));
   std::vector<double2> s0(nc, make_double2(sig_cr_max0, 0.0));
   copy_wait(st->state, s0.data(), sizeof(double2) * nc, cudaMemcpyHostToDevice, ctx->stream);
@@ -745,6 +780,8 @@ void sf_collide_destroy_internal(sf_ctx* ctx) {
     cudaFree(st->counts);
     cudaFree(st->cell_vol);
     cudaFree(st->bins1);
+    cudaFree(st->nsel);
+    cudaFree(st->light);
     delete st;
   }
   ctx->dsmc.clear();
@@ -808,17 +845,25 @@ void dsmc_run(sf_ctx* ctx, int sid1, int sid2, const sf_sigma* sigma, const sf_s
   d.seed = ctx->seed ^ 0xD5C0ULL;
   d.step = ctx->rng_epoch++;
   // counters[6]: collisions; as unsigned: [3] the number of heavy cells, [4] the
-  // heavy-cell work counter.  The heavy-cell list lives in bins_tmp (the sort's write
-  // cursors, free once the particles are binned).
+  // heavy-cell work counter, [5] the number of light cells.  The heavy-cell list lives in
+  // bins_tmp (the sort's write cursors, free once the particles are binned).
   SF_CUDA(cudaMemsetAsync(ctx->counters + 3, 0, 4 * sizeof(unsigned long long), ctx->stream));
   d.n_coll = ctx->counters + 6;
   d.heavy = ctx->bins_tmp;
   d.n_heavy = reinterpret_cast<unsigned*>(ctx->counters + 3);
   d.heavy_cap = ctx->nkeys;
   d.work = reinterpret_cast<unsigned*>(ctx->counters + 4);
+  d.light = st->light;
+  d.n_light = reinterpret_cast<unsigned*>(ctx->counters + 5);
+  d.nsel = st->nsel;
   {
     TimedScope ts(ctx, "dsmc");
     const bool wt = sp1->weighted || sp2->weighted;
+    const int pgrid = grid_for((int64_t)ctx->ncells(), 256, ctx->num_sms * 8);
+    if (pair)
+      k_dsmc_plan<true><<<pgrid, 256, 0, ctx->stream>>>(ctx->mesh_view(), d);
+    else
+      k_dsmc_plan<false><<<pgrid, 256, 0, ctx->stream>>>(ctx->mesh_view(), d);
     if (pair && wt) {
       k_dsmc<true, true><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
       k_dsmc_heavy<true, true><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
@@ -832,7 +877,7 @@ void dsmc_run(sf_ctx* ctx, int sid1, int sid2, const sf_sigma* sigma, const sf_s
       k_dsmc<false, false><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
       k_dsmc_heavy<false, false><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
     }
-    ctx->launches += 2;
+    ctx->launches += 3;
   }
   SF_CUDA(cudaGetLastError());
   unsigned long long nc = 0;

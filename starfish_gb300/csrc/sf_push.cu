@@ -1445,7 +1445,7 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
   SF_CUDA(cudaMemsetAsync(sc.counters, 0, sizeof(unsigned long long) * 8, s));
   // stats_partial tail (after the per-block area) holds the slow-path sums
   double* slow_stats = sc.stats_partial + (size_t)8 * (sc.stats_blocks - 1);
-  SF_CUDA(cudaMemsetAsync(sc.stats_partial, 0, sizeof(double) * 8 * (size_t)sc.stats_blocks, s));
+  if (want_stats) SF_CUDA(cudaMemsetAsync(sc.stats_partial, 0, sizeof(double) * 8 * (size_t)sc.stats_blocks, s));
 
   PushArgs a;
   a.qm_dt = (float)(sp->charge / sp->mass * dt);
@@ -1504,7 +1504,10 @@ void push_deposit_impl(sf_ctx* ctx, SfSpecies* sp, double dt, int32_t flags, sf_
       sa.sv.product = sp->seg_product;
       sa.sv.prod = ctx->d_prod;
     }
-    const int sgrid = ctx->num_sms * 16;
+    // 4 blocks of 128 per SM: the queue (0.2-0.5 M particles per step at 64 M ions) is
+    // spread over all SMs, and each block's set-up and flush are paid fewer times
+    // (0.044 -> 0.040 ms against 16 blocks per SM)
+    const int sgrid = ctx->num_sms * 4;
     TimedScope ts(ctx, "push_slow");
     ctx->launches++;
     switch (ctx->domain) {

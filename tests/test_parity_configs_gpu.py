@@ -283,14 +283,16 @@ def _agree(ga, oa, mask, rel):
 
 def test_dsmc_jet_matches_oracle_over_seeds(gpulib):
     """The axisymmetric argon jet on a 65x33 mesh (inlet r < 4 mm at 1e22 m^-3, 300 K,
-    500 m/s; diffuse walls at 300 K; VHS argon; dt 1 us), 120 steps, three seeds on each
+    500 m/s; diffuse walls at 300 K; VHS argon; dt 1 us), 120 steps, six seeds on each
     side: per-block collision counts, sampled density and temperature (last 40 steps)
     agree within 4 standard errors of the seed means plus 3 % (FP32 velocities and the
-    parallel rounds of disjoint pairs)."""
+    parallel rounds of disjoint pairs).  With three seeds a side the estimated standard
+    errors have heavy tails, and the same bound failed in two of three runs of unchanged
+    code; with eight seeds a side no block was beyond 3 standard errors or 3.3 %."""
     c = _jet_cfg()
     spec = c["spec"]
     steps, sample_from = 120, 80
-    seeds = (1, 2, 3)
+    seeds = (1, 2, 3, 4, 5, 6)
     g = [_gpu_jet(c, steps, sample_from, s) for s in seeds]
     o = [_oracle_jet(c, steps, sample_from, s) for s in seeds]
     ni, nj = spec.ni, spec.nj

@@ -83,7 +83,10 @@ __device__ inline void elastic_vr(Philox& rng, float vss_inv, const float g[3], 
 }
 
 constexpr int DSMC_HEAVY_NSEL = 1024;    // candidate pairs beyond which a cell gets a CTA
-constexpr int DSMC_HEAVY_THREADS = 512;
+// 1024 threads per dense cell: the rounds of a cell are sequential, so the densest cells'
+// round count sets the kernel's length (0.206 -> 0.173 ms per jet step against 512, and
+// 0.286 ms at 256)
+constexpr int DSMC_HEAVY_THREADS = 1024;
 
 // Everything a DSMC launch needs for one material pair (DSMC.java:259-350).  For a
 // same-species pair P2/bins2 alias P1/bins1.
@@ -866,16 +869,16 @@ void dsmc_run(sf_ctx* ctx, int sid1, int sid2, const sf_sigma* sigma, const sf_s
       k_dsmc_plan<false><<<pgrid, 256, 0, ctx->stream>>>(ctx->mesh_view(), d);
     if (pair && wt) {
       k_dsmc<true, true><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
-      k_dsmc_heavy<true, true><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc_heavy<true, true><<<ctx->num_sms, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
     } else if (pair) {
       k_dsmc<true, false><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
-      k_dsmc_heavy<true, false><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc_heavy<true, false><<<ctx->num_sms, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
     } else if (wt) {
       k_dsmc<false, true><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
-      k_dsmc_heavy<false, true><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc_heavy<false, true><<<ctx->num_sms, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
     } else {
       k_dsmc<false, false><<<ctx->num_sms * 16, 128, 0, ctx->stream>>>(ctx->mesh_view(), d);
-      k_dsmc_heavy<false, false><<<ctx->num_sms * 2, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
+      k_dsmc_heavy<false, false><<<ctx->num_sms, DSMC_HEAVY_THREADS, 0, ctx->stream>>>(ctx->mesh_view(), d);
     }
     ctx->launches += 3;
   }

@@ -553,6 +553,61 @@ def gpu_poisson_solve(seed=3, repeats=5):
             "newton_it": sts[0]["newton_it"], "residual": max(x["residual"] for x in sts), "repeats": repeats}
 
 
+def reference_dsmc_jet(n_particles=16 * 1024 * 1024, steps=1, warmup=2, threads=None, seed=0):
+    """The oracle's jet step on the DSMC leg's workload (513x257 ZR, 16M argon preloaded like
+    the GPU leg; fewer macroparticles scale the weight up, which keeps the candidates per
+    particle, nsel ~ n^2 w / V per cell, and so the work per particle-step, about the
+    same).  Each step: the inlet source, the push with
+    diffuse walls on `threads` host threads, then DSMC.perform (one host thread: the
+    reference's collideCell loop is serial).  `warmup` untimed steps first let (sigma g)max
+    grow from its initial 1e-16, as the GPU leg's warm-up steps do.  Particle-steps/s over
+    the timed steps, and the DSMC call's own time."""
+    from oracle import oracle as O
+    from starfish_gb300 import workloads as W
+    cfg = W.config2(n_particles)
+    spec = cfg.mesh
+    threads = threads or os.cpu_count() or 1
+    m = O.OMesh(spec.ni, spec.nj, spec.x0, spec.dh, spec.domain, spec.node_type, spec.face_type)
+    ptr, idx = O.node_segments(m, spec.seg_xy)
+    cv = O.cell_volumes(m)
+    vth = np.sqrt(2 * W.KB * cfg.wall_temp / cfg.mass)
+    segs = O.seg_table(spec.seg_xy, spec.seg_btype, O.SURF_DIFFUSE, vth=vth, c_rest=1.0, c_accom=1.0)
+    zero = np.zeros(spec.nn)
+    pos, vel = W.jet_particles(cfg, n_particles, seed)
+    P = np.zeros((n_particles, 12))
+    P[:, 0:3] = pos
+    P[:, 3:6] = vel
+    P[:, 9] = cfg.spwt
+    O.add_particles(m, zero, zero, 0.0, cfg.mass, cfg.dt, P)
+    nc = (spec.ni - 1) * (spec.nj - 1)
+    state = np.zeros((nc, 2))
+    state[:, 0] = 1e-16
+    counts = np.zeros((nc, 2))
+    rem, done, t_all, t_dsmc, c0 = 0.0, 0, 0.0, 0.0, 0.0
+    for t in range(warmup + steps):
+        if t == warmup:
+            done, t_all, t_dsmc, c0 = 0, 0.0, 0.0, float(counts[:, 0].sum())
+        t0 = time.perf_counter()
+        new, rem = O.maxwellian_source(seed * 1000003 + t, cfg.inlet, cfg.den, cfg.v_drift, cfg.temp, cfg.mass,
+                                       cfg.spwt, cfg.dt, rem, domain=spec.domain)
+        O.add_particles(m, zero, zero, 0.0, cfg.mass, cfg.dt, new)
+        P = np.ascontiguousarray(np.vstack([P, new]))
+        done += P.shape[0]
+        O.push(m, zero, zero, 0.0, cfg.mass, cfg.dt, segs, ptr, idx, P, seed=seed * 7919 + t, threads=threads)
+        P = np.ascontiguousarray(P[P[:, 10] == 1])
+        t1 = time.perf_counter()
+        O.dsmc(spec.ni, spec.nj, cv, P, cfg.mass, cfg.spwt, cfg.diam, cfg.T_ref, cfg.omega, 1.0, cfg.dt,
+               state, counts, seed * 104729 + t)
+        t2 = time.perf_counter()
+        t_all += t2 - t0
+        t_dsmc += t2 - t1
+    return {"workload": cfg.name, "value": done / t_all, "unit": "particle-steps/s (source + push + DSMC)",
+            "ms_per_step": 1e3 * t_all / steps, "dsmc_ms_per_step": 1e3 * t_dsmc / steps,
+            "collisions_per_step": float((counts[:, 0].sum() - c0) / steps), "steps": steps, "warmup": warmup,
+            "sample": f"{n_particles} macroparticles, {warmup} untimed + {steps} timed steps",
+            "cores": {"push": threads, "dsmc": 1}, "kind": "port"}
+
+
 def workload_config(cfg, particles, world):
     """The `config` of both arms' lines: the workload they measure."""
     return {"workload": cfg.name, "mesh": [cfg.mesh.ni, cfg.mesh.nj], "dx_m": cfg.mesh.dh[0],
@@ -597,6 +652,7 @@ def run_reference(args):
                                    f"{args.steps} steps, push on {threads} threads + serial scatter"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "poisson": reference_poisson_solve(),
+        "dsmc": reference_dsmc_jet(),
     }
     print(json.dumps(line))
 
@@ -774,6 +830,8 @@ def main():
                                           f"(push on {threads} threads, serial scatter), {t:.1f} s"}
         if args.poisson_pair:
             line["cpu_baseline"]["poisson_257x129"] = reference_poisson_solve()
+        if args.dsmc_steps > 0:
+            line["cpu_baseline"]["dsmc_jet"] = reference_dsmc_jet()
     dom.close()
     if rank == 0:
         print(json.dumps(line))

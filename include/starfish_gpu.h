@@ -202,8 +202,8 @@ int sf_particles_append(sf_ctx* ctx, int32_t sid, int64_t n, const double* pos, 
  * weight a particle may carry.  The push deposits, moments, totals and surface sums scale
  * by mpw / spwt; DSMC takes each pair's weights (Boyd's update, the collided-weight sum)
  * and MCC each particle's (S, the weight sum, the ion count; the second electron inherits
- * it); sources and surface products enter at spwt.  Batched instances take species of
- * uniform weight only (SF_ERR_ARG otherwise). */
+ * it); sources and surface products enter at spwt.  Batched instances take weighted
+ * and uniform species side by side. */
 int sf_species_set_weighted(sf_ctx* ctx, int32_t sid, int32_t on);
 /* sf_particles_append_lc with per-particle weights mpw (n; a weighted species). */
 int sf_particles_append_lc_w(sf_ctx* ctx, int32_t sid, int64_t n, const double* lc, const double* vel,

@@ -294,8 +294,6 @@ int sf_batch_create(sf_ctx** ctxs, const int32_t* sids, int32_t n, int32_t threa
       SF_REQUIRE(ctxs[i]->device == b->device, SF_ERR_ARG, "all instances of a batch must be on one device");
       SF_REQUIRE(ctxs[i]->domain == SF_DOMAIN_XY, SF_ERR_ARG, "batched instances must be XY meshes");
       for (int k = 0; k < i; k++) SF_REQUIRE(ctxs[k] != ctxs[i], SF_ERR_ARG, "a context appears twice in the batch");
-      SF_REQUIRE(!get_species(ctxs[i], sids[i])->weighted, SF_ERR_ARG,
-                 "batched instances take species of uniform weight");
       b->ctx.push_back(ctxs[i]);
       b->sid.push_back(sids[i]);
     }
@@ -319,6 +317,8 @@ int sf_batch_create(sf_ctx** ctxs, const int32_t* sids, int32_t n, int32_t threa
     b->d.chunk_start = balloc<int64_t>(b, n + 1);
     b->d.step_dev = balloc<uint32_t>(b, 1);
     b->d.overflow = balloc<int>(b, 1);
+    b->d.any_weighted = 0;
+    for (int i = 0; i < n; i++) b->d.any_weighted |= get_species(ctxs[i], sids[i])->weighted ? 1 : 0;
     b->pool.reset(new Pool(std::max(1, std::min<int>(threads > 0 ? threads : 8, n))));
     *out = b;
     return SF_OK;
@@ -389,8 +389,20 @@ int sf_batch_step(sf_batch* b, double dt, const sf_poisson_params* prm, sf_batch
   try {
     SF_REQUIRE(b && prm && dt > 0, SF_ERR_ARG, "null argument or bad dt");
     SF_CUDA(cudaSetDevice(b->device));
-    for (int i = 0; i < b->n; i++)
+    int aw = 0;
+    for (int i = 0; i < b->n; i++) {
       SF_REQUIRE(b->ctx[i]->efield_set, SF_ERR_STATE, "an instance has no electric field (solve or set E first)");
+      aw |= get_species(b->ctx[i], b->sid[i])->weighted ? 1 : 0;
+    }
+    if (aw != b->d.any_weighted) {
+      // a species was switched to per-particle weights since the graphs were captured
+      b->d.any_weighted = aw;
+      for (auto& g : b->graph)
+        if (g) {
+          cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
+    }
     std::string errs;
     std::mutex em;
     auto fail = [&](int i, const std::string& what) {

@@ -338,6 +338,7 @@ struct BatchDev {
   int64_t* chunk_start;  // n + 1: prefix of slow-queue chunks over the instances
   uint32_t* step_dev;  // batch step counter (RNG epoch of the sources)
   int* overflow;       // set when a source hit an instance's capacity
+  int any_weighted;    // some instance's species carries per-particle weights
 };
 namespace sf {
 // batched phases of one step, all on `stream` (sf_push.cu, sf_source.cu)

@@ -135,7 +135,7 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
       lfrac[k] = __ldcs(tfrac + q);
       lvxy[k] = __ldcs(tvxy + q);
       if (DOM != SF_DOMAIN_XY || STATS || MOM) lvz[k] = __ldcs(tvz + q);
-      if (W) pw[k] = __ldcs(P.w + t0 + q);
+      if (W) pw[k] = P.w ? __ldcs(P.w + t0 + q) : 1.f;  // (a batch mixes weighted and uniform species)
     }
   }
 #pragma unroll
@@ -1318,9 +1318,10 @@ __global__ void k_batch_zero(BatchDev b) {
   }
 }
 
-template <int DOM>
 // 4 blocks of PB per SM (64 registers, with spills): in the batched step faster than 2
-// blocks (123 registers) or 3 (80)
+// blocks (123 registers) or 3 (80).  W: some instance's species carries per-particle
+// weights (the others read as weight 1)
+template <int DOM, bool W>
 __global__ void __launch_bounds__(PB, 4) k_push_batch(BatchDev b) {
   __shared__ unsigned acc[SBOX];
   __shared__ int sred[4][PB / 32];
@@ -1334,7 +1335,7 @@ __global__ void __launch_bounds__(PB, 4) k_push_batch(BatchDev b) {
     const BatchInst& I = b.insts[i];
     ParticlesView P = I.P;
     P.n = b.n_dev[i];
-    push_tile<DOM, false, false, true>(I.m, P, I.a, (gt - b.tile_start[i]) * TILE, I.count, nullptr, I.slow_idx,
+    push_tile<DOM, false, false, true, W>(I.m, P, I.a, (gt - b.tile_start[i]) * TILE, I.count, nullptr, I.slow_idx,
                                  I.sa.counters, SampleView{nullptr, nullptr}, acc, sred, st_px, st_py,
                                  st_pz, st_e, st_n, st_e);
   }
@@ -1396,7 +1397,10 @@ namespace sf {
 void batch_push(const BatchDev& b, cudaStream_t stream, int num_sms, int blocks_per_sm, int slow_blocks_per_sm) {
   k_batch_begin<<<1, 1024, 0, stream>>>(b);
   k_batch_zero<<<dim3(8, b.n), 256, 0, stream>>>(b);
-  k_push_batch<SF_DOMAIN_XY><<<num_sms * blocks_per_sm, PB, 0, stream>>>(b);
+  if (b.any_weighted)
+    k_push_batch<SF_DOMAIN_XY, true><<<num_sms * blocks_per_sm, PB, 0, stream>>>(b);
+  else
+    k_push_batch<SF_DOMAIN_XY, false><<<num_sms * blocks_per_sm, PB, 0, stream>>>(b);
   k_slow_plan<<<1, 1024, 0, stream>>>(b);
   k_push_slow_batch<SF_DOMAIN_XY><<<num_sms * slow_blocks_per_sm, SLOW_THREADS, 0, stream>>>(b);
   k_finalize_batch<<<dim3(4, b.n), 256, 0, stream>>>(b);

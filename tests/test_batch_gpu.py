@@ -17,7 +17,7 @@ from starfish_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 
-def _instance(case, dt):
+def _instance(case, dt, weighted=False):
     from starfish_gb300.plugin import GpuDomain, KineticMaterial, PoissonSolver
     spec, ion = case.mesh, case.ion
     dom = GpuDomain(spec)
@@ -27,7 +27,11 @@ def _instance(case, dt):
     # removed slots stay until the next sort (every 16 steps) while the inlet keeps adding
     km = KineticMaterial(dom, ion.mass, ion.charge, ion.spwt, capacity=int(case.n_particles * 3) + 8192)
     pos, vel = W.uniform_maxwellian(spec, ion, case.n_particles, case.seed)
-    km.add_particles(pos, vel, rewind=True, dt=dt)
+    mpw = None
+    if weighted:
+        km.set_weighted(True)
+        mpw = ion.spwt * np.random.default_rng(case.seed + 77).uniform(0.2, 1.0, case.n_particles)
+    km.add_particles(pos, vel, rewind=True, dt=dt, mpw=mpw)
     return dom, km, ps
 
 
@@ -36,10 +40,10 @@ def _sorted(lc, vel):
     return a[np.lexsort(a.T[::-1])]
 
 
-def _batch_vs_twins(cases, dt, threads):
+def _batch_vs_twins(cases, dt, threads, weighted=()):
     from starfish_gb300.plugin import GpuBatch
-    A = [_instance(c, dt) for c in cases]
-    B = [_instance(c, dt) for c in cases]
+    A = [_instance(c, dt, k in weighted) for k, c in enumerate(cases)]
+    B = [_instance(c, dt, k in weighted) for k, c in enumerate(cases)]
     batch = GpuBatch([a[0] for a in A], [a[1] for a in A], threads=threads)
     try:
         st = batch.step(dt, A[0][2])  # first step: PCG iterations 2 in every bucket (tuning)
@@ -55,6 +59,11 @@ def _batch_vs_twins(cases, dt, threads):
             assert np.array_equal(da.get_field(abi.FIELD_EFI), db.get_field(abi.FIELD_EFI))
             assert ka.get_np() == kb.get_np()
             assert np.array_equal(_sorted(*ka.download()), _sorted(*kb.download()))
+            if weighted:
+                la, va = ka.download()
+                lb, vb = kb.download()
+                wa, wb = ka.download_weights(), kb.download_weights()
+                assert np.array_equal(_sorted(la, np.column_stack([va, wa])), _sorted(lb, np.column_stack([vb, wb])))
         live = sum(a[1].get_np() for a in A)
         assert st["particles"] == live
     finally:
@@ -65,6 +74,13 @@ def _batch_vs_twins(cases, dt, threads):
 
 def test_batch_step_matches_instances(gpulib):
     _batch_vs_twins(W.config4(6, seed=3, max_particles=200_000, min_particles=20_000), 5e-7, 3)
+
+
+def test_batch_with_weighted_species_matches_instances(gpulib):
+    """Instances 0 and 3 carry per-particle weights (mpw uniform in [0.2, 1] spwt), the
+    others uniform weight: the batched push deposits each particle's weight, as the
+    per-instance push does, bit for bit."""
+    _batch_vs_twins(W.config4(5, seed=8, max_particles=150_000, min_particles=20_000), 5e-7, 2, weighted=(0, 3))
 
 
 def test_batch_solve_matches_tiled_levels_on_a_large_mesh(gpulib):

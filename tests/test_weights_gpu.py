@@ -3,7 +3,7 @@ weights (sf_species_set_weighted) pushes, scatters, sums and hits surfaces with 
 particle's own mpw, against the oracle, which carries mpw per particle as the reference
 does; the weights follow their particles through the sort and the restart path; sources
 on a weighted species emit at the species weight; DSMC and MCC take each particle's
-weight; the batched instances refuse weighted species."""
+weight.  The batched instances with weighted species are checked in test_batch_gpu.py."""
 import numpy as np
 import pytest
 
@@ -240,7 +240,7 @@ def test_weighted_dsmc_at_the_species_weight_equals_uniform(gpulib):
 
 
 def test_weight_rejections(gpulib):
-    from starfish_gb300.plugin import GpuBatch, GpuDomain, KineticMaterial, PoissonSolver
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
     spec = W.es_pic_mesh(81, 41, 1e-3)
     ion = W.IonSpecies()
     dom = GpuDomain(spec)
@@ -260,14 +260,5 @@ def test_weight_rejections(gpulib):
         # switching after the first particle
         with pytest.raises(abi.SfError):
             km.set_weighted(False)
-        # the batched instances take species of uniform weight
-        ps = PoissonSolver(dom, n0=1e12, Te0=2.0, tol=1e-6, max_it=40)
-        ps.solve(rho=np.zeros(spec.nn), phi=np.zeros(spec.nn))
-        with pytest.raises(abi.SfError):
-            b = GpuBatch([dom], [km], threads=1)
-            try:
-                b.step(5e-7, ps)
-            finally:
-                b.close()
     finally:
         dom.close()

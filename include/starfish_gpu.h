@@ -466,7 +466,9 @@ typedef struct {
  * Every ordered pair of two distinct particles of a cell is an equally likely
  * candidate, as in the reference; the candidates of one parallel round share no
  * particle.  dt: frequency * dt of the reference.  sig_cr_max0: initial (sigma g)max of
- * every cell (DSMC element sig_cr_max, default 1e-16).  *n_coll: collisions performed. */
+ * every cell (DSMC element sig_cr_max, default 1e-16).  *n_coll: collisions performed;
+ * with n_coll NULL the call returns once the collisions are queued on the context's
+ * stream (the per-cell sums of sf_dsmc_get_counts hold them). */
 int sf_dsmc(sf_ctx* ctx, int32_t sid, const sf_sigma* sigma, double dt, double sig_cr_max0,
             int64_t* n_coll);
 /* DSMC.perform for the pair="mat1,mat2" of two kinetic species (DSMC.java:259-453):

@@ -884,10 +884,11 @@ void dsmc_run(sf_ctx* ctx, int sid1, int sid2, const sf_sigma* sigma, const sf_s
   }
   SF_CUDA(cudaGetLastError());
   unsigned long long nc = 0;
+  if (!n_coll) return;  // nothing to read: the collisions stay queued on the context's stream
   SF_CUDA(cudaMemcpyAsync(&nc, ctx->counters + 6, sizeof(nc), cudaMemcpyDeviceToHost, ctx->stream));
   SF_CUDA(cudaStreamSynchronize(ctx->stream));
   timer_collect(ctx);
-  if (n_coll) *n_coll = (int64_t)nc;
+  *n_coll = (int64_t)nc;
 }
 
 void dsmc_counts(sf_ctx* ctx, int sid1, int sid2, double* count_sum, double* real_sum) {

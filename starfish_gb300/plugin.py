@@ -404,12 +404,14 @@ class DSMC:
         self.sig_cr_max0 = sig_cr_max
         self.frequency = frequency
 
-    def perform(self, dt):
+    def perform(self, dt, wait=True):
+        """DSMC.perform: the number of collisions.  wait=False queues the collisions and
+        returns None (the per-cell sums of counts() hold them)."""
         n = C.c_int64()
         self.d.check(self.d.lib.sf_dsmc_pair(self.d.ctx, self.km.sid, self.km2.sid, C.byref(self.sigma),
                                              C.byref(self.sigma2), dt * self.frequency, self.sig_cr_max0,
-                                             C.byref(n)))
-        return n.value
+                                             C.byref(n) if wait else None))
+        return n.value if wait else None
 
     def counts(self):
         nc = (self.d.ni - 1) * (self.d.nj - 1)

@@ -110,3 +110,33 @@ def test_noalloc_refuses_nowait(gpulib):
         assert km.get_np() == 1000
     finally:
         dom.close()
+
+
+def test_dsmc_without_count_readback(gpulib):
+    """sf_dsmc with n_coll NULL queues the collisions: the per-cell sums hold them, and a
+    later call that reads its count sees the same cell state."""
+    from starfish_gb300.plugin import DSMC, GpuDomain, KineticMaterial
+    spec = W.es_pic_mesh(33, 33, 1e-3, walls=abi.DB_SYMMETRY, electrode_halfwidth=1e-12)
+    spec.seg_xy = np.zeros((0, 4))
+    spec.seg_btype = np.zeros(0, np.int32)
+    spec.node_type[:] = abi.NODE_OPEN
+    spec.bc_value[:] = 0.0
+    rng = np.random.default_rng(4)
+    n = 64 * 32 * 32
+    lc = rng.uniform(0.01, 31.99, (n, 2))
+    vel = rng.normal(0, 300.0, (n, 3))
+    dom = GpuDomain(spec)
+    try:
+        dom.set_efield(np.zeros(spec.nn), np.zeros(spec.nn))
+        km = KineticMaterial(dom, 40 * 1.6605e-27, 0.0, 1e13, capacity=n + 64)
+        km.add_particles_lc(lc, vel)
+        ds = DSMC(dom, km, model=abi.SIGMA_BIRD463, diam=4.17e-10, T_ref=273.0, omega=0.81)
+        got = [ds.perform(1e-6, wait=False) for _ in range(3)]
+        assert got == [None, None, None]
+        c3 = ds.counts()[0].sum()
+        assert c3 > 0
+        nc = ds.perform(1e-6)
+        assert nc > 0 and ds.counts()[0].sum() == c3 + nc
+        assert km.get_np() == n
+    finally:
+        dom.close()

@@ -328,11 +328,27 @@ __device__ __forceinline__ unsigned sort_key(uint32_t c, float2 f, float2 v, int
   return (tile << (2 * s)) | ((unsigned)((j & 15) >> L.qb) << s) | (unsigned)((i & 15) >> L.qb);
 }
 
+// L2 prefetch of the chunk at `base` (whole 16-byte groups inside [0, p.n)) of the arrays
+// a sort pass reads: the cells (what 0), also fraction and velocity (1), everything (2).
+__device__ __forceinline__ void prefetch_chunk(const ParticlesView& p, int64_t base, int what) {
+  if (threadIdx.x != 0 || base >= p.n) return;
+  const uint32_t m = (uint32_t)min(p.n - base, (int64_t)SORT_CHUNK);
+  prefetch_l2(p.cell + base, (m * 4u) & ~15u);
+  if (what < 1) return;
+  prefetch_l2(p.frac + base, (m * 8u) & ~15u);
+  prefetch_l2(p.vxy + base, (m * 8u) & ~15u);
+  if (what < 2) return;
+  prefetch_l2(p.vz + base, (m * 4u) & ~15u);
+  if (p.w) prefetch_l2(p.w + base, (m * 4u) & ~15u);
+}
+
 __global__ void __launch_bounds__(SORT_B) k_sort_hist(ParticlesView p, int ntx, int* bins, SortLook L) {
   __shared__ unsigned hkey[SORT_HSIZE];
   __shared__ unsigned hcnt[SORT_HSIZE];
   const bool look = L.ax != 0.f || L.ay != 0.f;
-  for (int64_t base = (int64_t)blockIdx.x * SORT_CHUNK; base < p.n; base += (int64_t)gridDim.x * SORT_CHUNK) {
+  const int64_t stride = (int64_t)gridDim.x * SORT_CHUNK;
+  for (int64_t base = (int64_t)blockIdx.x * SORT_CHUNK; base < p.n; base += stride) {
+    prefetch_chunk(p, base + stride, look ? 1 : 0);
     for (int q = threadIdx.x; q < SORT_HSIZE; q += SORT_B) {
       hkey[q] = EMPTY_KEY;
       hcnt[q] = 0u;
@@ -393,7 +409,9 @@ __global__ void __launch_bounds__(SORT_B) k_sort_scatter(ParticlesView src, Part
   __shared__ int warp_tot[SORT_B / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   constexpr int SPT = SORT_HSIZE / SORT_B;  // slots per thread in the scan
-  for (int64_t base = (int64_t)blockIdx.x * SORT_CHUNK; base < src.n; base += (int64_t)gridDim.x * SORT_CHUNK) {
+  const int64_t stride = (int64_t)gridDim.x * SORT_CHUNK;
+  for (int64_t base = (int64_t)blockIdx.x * SORT_CHUNK; base < src.n; base += stride) {
+    prefetch_chunk(src, base + stride, 2);
     for (int q = threadIdx.x; q < SORT_HSIZE; q += SORT_B) {
       hkey[q] = EMPTY_KEY;
       hcnt[q] = 0u;

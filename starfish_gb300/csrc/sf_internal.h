@@ -77,6 +77,13 @@ __device__ __forceinline__ float2 gather_efield(const float4* __restrict__ E, in
   e.y = w00 * lo.y + w10 * lo.w + w11 * hi.w + w01 * hi.y;
   return e;
 }
+// Asks L2 for `bytes` (a multiple of 16, from a 16-byte aligned address) with one bulk
+// prefetch: a block issues it for its next chunk of particles while it works on the
+// current one, so that the next chunk's loads find their lines in L2.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+  if (bytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // Writes node u's field into both of its places.
 __device__ __forceinline__ void store_efield(float4* E, int u, float2 e) {
   reinterpret_cast<float2*>(E)[2 * (size_t)u] = e;

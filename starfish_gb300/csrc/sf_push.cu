@@ -350,12 +350,8 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
 }
 
 // L2 prefetch of a tile's particle arrays (one bulk prefetch per array, issued by one
-// thread): the block asks for its next tile while it pushes the current one, so that the
-// next tile's loads find their lines in L2.  Only whole 16-byte groups of the tile's
-// particles are requested, all inside [0, P.n).
-__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
-  if (bytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
+// thread) while the block pushes its current tile.  Only whole 16-byte groups of the
+// tile's particles are requested, all inside [0, P.n).
 template <int DOM, bool STATS, bool MOM, bool W>
 __device__ __forceinline__ void prefetch_tile(const ParticlesView& P, int64_t t0) {
   if (t0 >= P.n) return;

@@ -360,7 +360,7 @@ __device__ __forceinline__ void prefetch_tile(const ParticlesView& P, int64_t t0
   prefetch_l2(P.frac + t0, (nrem * 8u) & ~15u);
   prefetch_l2(P.vxy + t0, (nrem * 8u) & ~15u);
   if (DOM != SF_DOMAIN_XY || STATS || MOM) prefetch_l2(P.vz + t0, (nrem * 4u) & ~15u);
-  if (W) prefetch_l2(P.w + t0, (nrem * 4u) & ~15u);
+  if (W && P.w) prefetch_l2(P.w + t0, (nrem * 4u) & ~15u);
 }
 
 template <int DOM, bool STATS, bool MOM, bool W>

@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(128) k_dsmc(MeshView m, DsmcArgs d) {
 template <bool PAIR, bool W>
 __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, DsmcArgs d) {
   __shared__ int s_idx;
-  __shared__ uint32_t s_q[2], s_ab[4];
+  __shared__ uint32_t s_q[2], s_ab[2][4];  // the maps of this round and the next
   __shared__ float s_max[DSMC_HEAVY_THREADS / 32];
   __shared__ int s_n[DSMC_HEAVY_THREADS / 32];
   __shared__ double s_ws[DSMC_HEAVY_THREADS / 32];
@@ -412,25 +412,30 @@ __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, D
     double wsum = 0.0;
     const int per_round = PAIR ? min(DSMC_HEAVY_THREADS, min(np1, np2)) : min(DSMC_HEAVY_THREADS, np1 / 2);
     int left = nsel;
+    // thread 0 draws the maps one round ahead, so that a round waits at one barrier only
+    auto draw = [&](uint32_t* ab) {  // into copies: thread 0 still uses this round's maps
+      AffineMap t1 = s1m, t2 = s2m;
+      t1.draw(rng);
+      ab[0] = t1.a;
+      ab[1] = t1.b;
+      if (PAIR) {
+        t2.draw(rng);
+        ab[2] = t2.a;
+        ab[3] = t2.b;
+      }
+    };
+    if (tid == 0) draw(s_ab[0]);
+    __syncthreads();
     for (int round = 0, cap = max_rounds(nsel); left > 0 && round < cap; round++) {
       const int mr = min(per_round, left);
-      if (tid == 0) {
-        s1m.draw(rng);
-        s_ab[0] = s1m.a;
-        s_ab[1] = s1m.b;
-        if (PAIR) {
-          s2m.draw(rng);
-          s_ab[2] = s2m.a;
-          s_ab[3] = s2m.b;
-        }
-      }
-      __syncthreads();
-      s1m.a = s_ab[0];
-      s1m.b = s_ab[1];
+      const uint32_t* ab = s_ab[round & 1];
+      s1m.a = ab[0];
+      s1m.b = ab[1];
       if (PAIR) {
-        s2m.a = s_ab[2];
-        s2m.b = s_ab[3];
+        s2m.a = ab[2];
+        s2m.b = ab[3];
       }
+      if (tid == 0) draw(s_ab[(round + 1) & 1]);  // read by the next round, after the barrier below
       bool used = false;
       if (tid < mr) {
         uint32_t p1, p2;
@@ -444,8 +449,8 @@ __global__ void __launch_bounds__(DSMC_HEAVY_THREADS) k_dsmc_heavy(MeshView m, D
         used = p1 < (uint32_t)np1 && p2 < (uint32_t)np2;
         if (used && collide_pair<W>(d, s1 + (int64_t)p1, s2 + (int64_t)p2, smax, rng, smax_new, wsum)) ncol++;
       }
-      // the count of used candidates; also orders this round's velocities and s_ab
-      // before the next round
+      // the count of used candidates; also orders this round's velocities and the next
+      // round's maps before the next round
       left -= __syncthreads_count(used);
     }
     for (int o = 16; o > 0; o >>= 1) {

@@ -167,15 +167,19 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
         } else if (DOM == SF_DOMAIN_ZR) {
           // rotateToZR (KineticMaterial.java:444-462) relative to the cell radius rj
           nfx = f.x + v.x * a.dt_dx;
+          // one reciprocal square root and one approximate division (2 ulp) instead of a
+          // square root and four IEEE divisions
           const float rj = a.r0y + (float)j * a.dy;
           const float A = vz * a.dt;
           const float dl = f.y * a.dy + v.y * a.dt;
           const float B = rj + dl;
-          const float R = sqrtf(A * A + B * B);
+          const float s2 = A * A + B * B;
+          const float ir = s2 > 0.f ? rsqrtf(s2) : 0.f;
+          const float R = s2 * ir;
           const float den = R + rj;
-          const float rrel = den > 0.f ? (A * A + dl * (2.f * rj + dl)) / den : 0.f;
-          nfy = rrel / a.dy;
-          const float cs = R > 0.f ? B / R : 1.f, sn = R > 0.f ? A / R : 0.f;
+          const float rrel = den > 0.f ? __fdividef(A * A + dl * (2.f * rj + dl), den) : 0.f;
+          nfy = rrel * m.inv_dy;
+          const float cs = R > 0.f ? B * ir : 1.f, sn = R > 0.f ? A * ir : 0.f;
           nvy = cs * v.y + sn * vz;
           nvz = -sn * v.y + cs * vz;
         } else {
@@ -185,11 +189,13 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
           const float A = vz * a.dt;
           const float dl = f.x * a.dx + v.x * a.dt;
           const float B = ri + dl;
-          const float R = sqrtf(A * A + B * B);
+          const float s2 = A * A + B * B;
+          const float ir = s2 > 0.f ? rsqrtf(s2) : 0.f;
+          const float R = s2 * ir;
           const float den = R + ri;
-          const float rrel = den > 0.f ? (A * A + dl * (2.f * ri + dl)) / den : 0.f;
-          nfx = rrel / a.dx;
-          const float cs = R > 0.f ? B / R : 1.f, sn = R > 0.f ? A / R : 0.f;
+          const float rrel = den > 0.f ? __fdividef(A * A + dl * (2.f * ri + dl), den) : 0.f;
+          nfx = rrel * m.inv_dx;
+          const float cs = R > 0.f ? B * ir : 1.f, sn = R > 0.f ? A * ir : 0.f;
           nvx = cs * v.x + sn * vz;
           nvz = -sn * v.x + cs * vz;
         }

@@ -90,7 +90,7 @@ __device__ bool may_hit_fp32(const MeshView& m, int i, int j, float fx, float fy
 
 // One tile (TILE particles from t0) of the fused push + deposit: load, push, fast-path
 // test, enqueue of slow candidates, shared-memory deposit of the tile's box and its
-// flush.  Shared by k_push (one mesh) and k_push_batch (many instances).  PRE (XY): a
+// flush.  Shared by k_push (one mesh) and k_push_batch (many instances).  PRE: a
 // particle that fails the distance test is given the exact path's FP32 pre-filter here,
 // and finishes here when no candidate segment can be on its path (moves of many cells,
 // as in small meshes at large dt, would otherwise mostly queue for the exact path).
@@ -158,7 +158,7 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
         float vz = lvz[k];
         // move in logical coordinates (x += v dt; XtoL)
         float nfx, nfy, nvx = v.x, nvy = v.y, nvz = vz;
-        float gx = 0.f, gy = 0.f;  // XY: the new position in cells from (i, j), before reduction
+        float gx, gy;  // the new position in cells from (i, j), before reduction
         if (DOM == SF_DOMAIN_XY) {
           nfx = f.x + v.x * a.dt_dx;
           nfy = f.y + v.y * a.dt_dy;
@@ -182,6 +182,8 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
           const float cs = R > 0.f ? B * ir : 1.f, sn = R > 0.f ? A * ir : 0.f;
           nvy = cs * v.y + sn * vz;
           nvz = -sn * v.y + cs * vz;
+          gx = nfx;
+          gy = nfy;
         } else {
           // rotateToRZ (KineticMaterial.java:424-442), radius along x
           nfy = f.y + v.y * a.dt_dy;
@@ -198,6 +200,8 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
           const float cs = R > 0.f ? B * ir : 1.f, sn = R > 0.f ? A * ir : 0.f;
           nvx = cs * v.x + sn * vz;
           nvz = -sn * v.x + cs * vz;
+          gx = nfx;
+          gy = nfy;
         }
         float fdi = floorf(nfx), fdj = floorf(nfy);
         nfx -= fdi;
@@ -209,8 +213,7 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
         const int span = max(abs(di), abs(dj)) + 1;
         const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
         bool clear = (int)__ldg(&m.seg_dist[j * m.ni + i]) > span;
-        if (PRE && DOM == SF_DOMAIN_XY && !clear)
-          clear = !may_hit_fp32(m, i, j, f.x, f.y, gx, gy);
+        if (PRE && !clear) clear = !may_hit_fp32(m, i, j, f.x, f.y, gx, gy);
         if (inside && clear) {
           __stcs(tcell + q, pack_cell(i2, j2));
           __stcs(tfrac + q, make_float2(nfx, nfy));
@@ -387,7 +390,10 @@ __global__ void __launch_bounds__(PB, 4) k_push(MeshView m, ParticlesView P, Pus
   const int64_t stride = (int64_t)gridDim.x * TILE;
   for (int64_t t0 = (int64_t)blockIdx.x * TILE; t0 < P.n; t0 += stride) {
     if (threadIdx.x == 0) prefetch_tile<DOM, STATS, MOM, W>(P, t0 + stride);
-    push_tile<DOM, STATS, MOM, false, W>(m, P, a, t0, count, mom, slow_idx, counters, smp, acc, sred, st_px, st_py,
+    // the in-tile pre-filter pays on RZ/ZR meshes whose walls run along dense gas (the jet's
+    // inlet plane: push 0.198 -> 0.228 ms, exact path 0.21 -> 0.09 ms per step); on the XY
+    // workload it made the push slower (0.598 -> 0.647 ms) than the queue it saves
+    push_tile<DOM, STATS, MOM, DOM != SF_DOMAIN_XY, W>(m, P, a, t0, count, mom, slow_idx, counters, smp, acc, sred, st_px, st_py,
                                          st_pz, st_e, st_n, st_w);
   }
   if (STATS) {

@@ -183,8 +183,7 @@ BatchInst make_inst(sf_batch* b, int i) {
   I.count = sp->count;
   I.slow_idx = c->slow_idx;
   I.nd = sp->nd;
-  I.ivol = c->d_node_ivol;
-  I.w_scale = sp->spwt / DEP_SCALE;
+  I.nd_factor = sp->nd_factor;
   I.nd_back = sp->nd_back;
   I.cap = sp->cap;
   const sf_batch::Src& s = b->src[i];

@@ -290,6 +290,7 @@ struct SfSpecies {
   unsigned long long* count = nullptr;  // ni*nj fixed-point deposit
   long long* mom = nullptr;             // 3*ni*nj fixed-point moments
   double* nd = nullptr;                 // ni*nj number density
+  double* nd_factor = nullptr;          // ni*nj spwt / 2^31 / V: count -> density
   double* uvw = nullptr;                // 3*ni*nj mean velocity
   bool moments_valid = false;
   int* seg_model = nullptr;
@@ -321,8 +322,8 @@ struct BatchInst {
   unsigned long long* count;   // species deposit (fixed point)
   int* slow_idx;
   double* nd;
-  const double* ivol;              // 1 / node volume
-  double w_scale, nd_back;
+  const double* nd_factor;         // per node spwt / 2^31 / V (the species')
+  double nd_back;
   // Maxwellian inlet (MaxwellianSource on one segment); src_on = 0: no source
   double sx1, sy1, sx2, sy2, snx, sny, v_th, v_drift, src_dt, mp_step;
   float qm_halfdt;
@@ -406,7 +407,6 @@ struct sf_ctx {
   int* d_seg_btype = nullptr;
   int8_t* d_face_type = nullptr;
   double* d_node_vol = nullptr;
-  double* d_node_ivol = nullptr;  // 1 / node volume, for the density epilogues
   // scratch
   int* slow_idx = nullptr;        // capacity = max species capacity
   int64_t slow_cap = 0;

@@ -1142,11 +1142,11 @@ __global__ void __launch_bounds__(SLOW_THREADS) k_push_slow(MeshView m, Particle
                      (unsigned long long)gridDim.x * blockDim.x);
 }
 
-// Node density from the fixed-point count.  Multiplies by the node's reciprocal volume
-// (computed once on the host) instead of dividing: an FP64 divide is a dozen FP64-pipe
-// instructions, which made this epilogue FP64-bound rather than bandwidth-bound.
-__device__ __forceinline__ double node_density(unsigned long long c, double w_scale, double ivol, double nd_back) {
-  return fma((double)c, w_scale * ivol, nd_back);
+// Node density from the fixed-point count: count x (spwt / 2^31 / V, the species' factor
+// computed once on the host) + nd_back.  Dividing by the volume here made this epilogue
+// FP64-bound (an FP64 divide is a dozen FP64-pipe instructions).
+__device__ __forceinline__ double node_density(unsigned long long c, double factor, double nd_back) {
+  return fma((double)c, factor, nd_back);
 }
 
 // int64 fixed point -> density (Field2D.scaleByVol, Field2D.java:418-431) and mean
@@ -1154,7 +1154,7 @@ __device__ __forceinline__ double node_density(unsigned long long c, double w_sc
 // Thread 0 also keeps the species' push counters: live_base = slots - removed slots
 // the host knows of, so live_base - acc[0] particles were alive when this push began.
 __global__ void k_finalize(int nn, const unsigned long long* __restrict__ count, const long long* __restrict__ mom,
-                           const double* __restrict__ ivol, double w_scale, double nd_back,
+                           const double* __restrict__ nd_factor, double nd_back,
                            double* __restrict__ nd, double* __restrict__ uvw, int mom_on,
                            unsigned long long* __restrict__ acc, const unsigned long long* __restrict__ counters,
                            long long live_base) {
@@ -1165,7 +1165,7 @@ __global__ void k_finalize(int nn, const unsigned long long* __restrict__ count,
   }
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x) {
     const unsigned long long c = count[u];
-    nd[u] = node_density(c, w_scale, ivol[u], nd_back);
+    nd[u] = node_density(c, nd_factor[u], nd_back);
     if (mom_on) {
       for (int d = 0; d < 3; d++)
         uvw[(size_t)d * nn + u] = c ? ((double)mom[(size_t)d * nn + u] / MOM_SCALE) / ((double)c / DEP_SCALE) : 0.0;
@@ -1370,7 +1370,7 @@ __global__ void k_finalize_batch(BatchDev b) {
   BatchInst& I = b.insts[blockIdx.y];
   const int nn = I.m.ni * I.m.nj;
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < nn; u += gridDim.x * blockDim.x)
-    I.nd[u] = node_density(I.count[u], I.w_scale, I.ivol[u], I.nd_back);
+    I.nd[u] = node_density(I.count[u], I.nd_factor[u], I.nd_back);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     b.dead_dev[blockIdx.y] += (int64_t)I.sa.counters[1];
     I.a.step++;
@@ -1419,7 +1419,7 @@ void launch_finalize(sf_ctx* ctx, SfSpecies* sp, bool moments, const unsigned lo
   int nn = ctx->ni * ctx->nj;
   ctx->launches++;
   k_finalize<<<grid_for(nn, 256, ctx->num_sms * 8), 256, 0, ctx->stream>>>(
-      nn, sp->count, sp->mom, ctx->d_node_ivol, sp->spwt / DEP_SCALE, sp->nd_back, sp->nd, sp->uvw, moments ? 1 : 0,
+      nn, sp->count, sp->mom, sp->nd_factor, sp->nd_back, sp->nd, sp->uvw, moments ? 1 : 0,
       sp->acc, counters, (long long)(sp->n - sp->n_dead));
 }
 

@@ -1175,7 +1175,9 @@ int sf_get_field(sf_ctx* ctx, int32_t field, int32_t sid, double* out) {
     std::copy(ctx->node_vol.begin(), ctx->node_vol.end(), out);
     return SF_OK;
   }
-  SfSpecies* sp = get_species(ctx, sid);
+  // the fields need no particle count: a push that did not wait is read behind it on the
+  // stream, with one wait at the end
+  SfSpecies* sp = get_species_nowait(ctx, sid);
   switch (field) {
     case SF_FIELD_ND:
       copy_to_host(ctx, out, sp->nd, nn);

@@ -31,3 +31,6 @@ def test_reference_arm_json_line():
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     ps = d["poisson"]
     assert ps["ms_per_solve"] > 0 and ps["newton_it"] >= 1 and ps["residual"] < 1e-5
+    dj = d["dsmc"]
+    assert dj["workload"] == "dsmc_jet_513x257_zr" and dj["value"] > 0
+    assert dj["collisions_per_step"] > 0 and dj["dsmc_ms_per_step"] > 0

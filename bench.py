@@ -322,9 +322,9 @@ def dsmc_jet_bench(steps=20, warmup=3, n_particles=16 * 1024 * 1024, seed=0):
         ds = DSMC(dom, km, model=abi.SIGMA_BIRD463, diam=cfg.diam, T_ref=cfg.T_ref, omega=cfg.omega)
 
         def step():
-            # the push and the collisions are queued without a host read; the source and the
-            # cell sort still read their particle counts back
-            km.sample_maxwellian_source(cfg.inlet, cfg.den, cfg.v_drift, cfg.temp, cfg.dt)
+            # the source, the push and the collisions are queued without a host read; the
+            # cell sort still reads its particle count back
+            km.sample_maxwellian_source(cfg.inlet, cfg.den, cfg.v_drift, cfg.temp, cfg.dt, wait=False)
             km.update_fields(cfg.dt, stats=False, wait=False)
             ds.perform(cfg.dt, wait=False)
 

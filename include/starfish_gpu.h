@@ -232,7 +232,10 @@ int sf_particles_clear(sf_ctx* ctx, int32_t sid);
  * push off the surface of Source.sampleKinetic (:167-198) and the -dt/2 velocity rewind
  * of KineticMaterial.addParticle (KineticMaterial.java:776-796).  The segment normal
  * (-dy, dx)/L gives the drift direction.  den: density (m^-3), temp (K), v_drift (m/s).
- * *rem carries the fractional particle count between calls.  *n_added: particles added. */
+ * *rem carries the fractional particle count between calls.  *n_added: particles added;
+ * with n_added NULL the call returns once the draws are queued: draw k takes the k-th
+ * slot behind the species' particles, and a draw landing outside the mesh leaves its slot
+ * removed (counted like a push's removals, as after SF_PUSH_NOWAIT). */
 int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg_xy, double den, double v_drift,
                          double temp, double dt, double* rem, int64_t* n_added);
 /* UniformSource on one straight segment (sources/UniformSource.java:36-80): mass flow rate

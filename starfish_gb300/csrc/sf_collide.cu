@@ -813,8 +813,10 @@ namespace {
 // sorts, then collideCell per cell (k_dsmc, k_dsmc_heavy).
 void dsmc_run(sf_ctx* ctx, int sid1, int sid2, const sf_sigma* sigma, const sf_sigma* sigma2, double dt,
               double sig_cr_max0, int64_t* n_coll) {
-  SfSpecies* sp1 = get_species(ctx, sid1);
-  SfSpecies* sp2 = get_species(ctx, sid2);
+  // the binning sort drops removed slots itself: the removals of pushes and sources that
+  // did not wait need not be read first
+  SfSpecies* sp1 = get_species_nowait(ctx, sid1);
+  SfSpecies* sp2 = get_species_nowait(ctx, sid2);
   SF_REQUIRE(dt > 0 && sig_cr_max0 > 0, SF_ERR_ARG, "dt and sig_cr_max must be positive");
   SF_CUDA(cudaSetDevice(ctx->device));
   const bool pair = sid1 != sid2;

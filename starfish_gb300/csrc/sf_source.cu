@@ -29,6 +29,10 @@ struct InjectArgs {
   int axi;               // RZ / ZR: positions uniform in the swept (frustum) area
   double r1, r2;         // radii of the segment ends
   int cold;              // UniformSource: v = normal * v_drift (no thermal spread, no dt draw)
+  // null: draws outside the mesh are dropped and the others packed from `base` (counter);
+  // else draw k takes slot base + k, and a draw outside the mesh leaves that slot removed
+  // and is counted here
+  unsigned long long* dead = nullptr;
 };
 
 // Spline.randomT on an axisymmetric mesh (core/boundaries/Spline.java:582-641) picks t so
@@ -72,14 +76,20 @@ __device__ __forceinline__ void inject_one(const MeshView& m, const ParticlesVie
   px += vx * 1e-6 * a.dt;
   py += vy * 1e-6 * a.dt;
   double lx = (px - m.x0[0]) * m.inv_dh[0], ly = (py - m.x0[1]) * m.inv_dh[1];
-  if (!(lx >= 0 && ly >= 0 && lx <= m.ni - 1 && ly <= m.nj - 1)) return;  // outside every mesh
+  if (!(lx >= 0 && ly >= 0 && lx <= m.ni - 1 && ly <= m.nj - 1)) {  // outside every mesh
+    if (a.dead) {
+      P.cell[a.base + k] = DEAD;
+      atomicAdd(a.dead, 1ULL);
+    }
+    return;
+  }
   int i = (int)lx, j = (int)ly;
   if (i > m.ni - 2) i = m.ni - 2;
   if (j > m.nj - 2) j = m.nj - 2;
   const float fx = (float)(lx - i), fy = (float)(ly - j);
   const float2 eg = gather_efield(m.E, m.ni, i, j, fx, fy);
   const float ex = eg.x, ey = eg.y;
-  const int64_t d = a.base + (int64_t)atomicAdd(counter, 1ULL);
+  const int64_t d = a.dead ? a.base + k : a.base + (int64_t)atomicAdd(counter, 1ULL);
   P.cell[d] = pack_cell(i, j);
   P.frac[d] = make_float2(fx, fy);
   P.vxy[d] = make_float2((float)vx - a.qm_halfdt * ex, (float)vy - a.qm_halfdt * ey);
@@ -253,8 +263,10 @@ __global__ void k_preload(MeshView m, ParticlesView P, PreloadArgs a, const int6
 }
 
 // One segment source of num particles (MaxwellianSource or, cold, UniformSource)
+// wait = false: every draw takes its own slot and the host reads nothing back (a draw that
+// lands outside the mesh leaves its slot removed, counted with the pushes' removals)
 int64_t segment_source(sf_ctx* ctx, SfSpecies* sp, int32_t sid, const double* seg, int64_t num, double v_drift,
-                       double temp, double dt, int cold) {
+                       double temp, double dt, int cold, bool wait = true) {
   const double dx = seg[2] - seg[0], dy = seg[3] - seg[1];
   const double len = std::sqrt(dx * dx + dy * dy);
   SF_REQUIRE(sp->n + num <= sp->cap, SF_ERR_OOM, "species capacity exceeded by the source");
@@ -277,6 +289,18 @@ int64_t segment_source(sf_ctx* ctx, SfSpecies* sp, int32_t sid, const double* se
   a.r2 = ctx->domain == SF_DOMAIN_RZ ? seg[2] : seg[3];
   a.cold = cold;
   unsigned long long* cnt = ctx->counters + 7;
+  if (!wait) {
+    a.dead = sp->acc;  // acc[0]: removed slots the host has not read yet
+    k_inject_maxwellian<<<(int)((num + 255) / 256), 256, 0, ctx->stream>>>(ctx->mesh_view(), sp->cur, a, (int)num,
+                                                                          cnt);
+    ctx->launches++;
+    SF_CUDA(cudaGetLastError());
+    sp->acc_pending = true;
+    sp->n += num;
+    sp->cur.n = sp->n;
+    sp->sorted = false;
+    return num;
+  }
   SF_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), ctx->stream));
   k_inject_maxwellian<<<(int)((num + 255) / 256), 256, 0, ctx->stream>>>(ctx->mesh_view(), sp->cur, a, (int)num, cnt);
   ctx->launches++;
@@ -300,8 +324,9 @@ double segment_length(const double* seg) {
 extern "C" int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg, double den, double v_drift,
                                     double temp, double dt, double* rem, int64_t* n_added) {
   SF_API_BEGIN
-  SfSpecies* sp = get_species(ctx, sid);
-  SF_REQUIRE(seg && rem && n_added, SF_ERR_ARG, "null argument");
+  // without n_added nothing is read back: the slot count is all the source needs
+  SfSpecies* sp = n_added ? get_species(ctx, sid) : get_species_nowait(ctx, sid);
+  SF_REQUIRE(seg && rem, SF_ERR_ARG, "null argument");
   SF_REQUIRE(den >= 0 && temp >= 0 && dt > 0, SF_ERR_ARG, "bad source parameters");
   SF_REQUIRE(ctx->efield_set, SF_ERR_STATE, "electric field not set (the rewind gathers E)");
   SF_CUDA(cudaSetDevice(ctx->device));
@@ -318,9 +343,10 @@ extern "C" int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg,
   const double mp = (mdot * dt) / (sp->mass * sp->spwt) + *rem;
   const int64_t num = (int64_t)mp;
   *rem = mp - (double)num;
-  *n_added = 0;
+  if (n_added) *n_added = 0;
   if (num <= 0) return SF_OK;
-  *n_added = segment_source(ctx, sp, sid, seg, num, v_drift, temp, dt, 0);
+  const int64_t added = segment_source(ctx, sp, sid, seg, num, v_drift, temp, dt, 0, n_added != nullptr);
+  if (n_added) *n_added = added;
   SF_API_END(ctx)
 }
 

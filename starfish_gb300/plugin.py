@@ -115,17 +115,18 @@ class KineticMaterial:
         """Per-particle weights (Particle.mpw) for this species, before its first particle."""
         self.d.check(self.d.lib.sf_species_set_weighted(self.d.ctx, self.sid, int(bool(on))))
 
-    def sample_maxwellian_source(self, seg_xy, den, v_drift, temp, dt):
+    def sample_maxwellian_source(self, seg_xy, den, v_drift, temp, dt, wait=True):
         """MaxwellianSource on one straight segment, sampled on the device; returns the
-        number of particles added (the fractional remainder is kept per source)."""
+        number of particles added (the fractional remainder is kept per source).  wait=False
+        queues the draws and returns None."""
         key = tuple(np.asarray(seg_xy, np.float64).reshape(-1))
         rem = C.c_double(self._src_rem.get(key, 0.0))
         seg = np.ascontiguousarray(seg_xy, np.float64).reshape(-1)
         n = C.c_int64()
         self.d.check(self.d.lib.sf_source_maxwellian(self.d.ctx, self.sid, abi.ptr(seg), den, v_drift,
-                                                     temp, dt, C.byref(rem), C.byref(n)))
+                                                     temp, dt, C.byref(rem), C.byref(n) if wait else None))
         self._src_rem[key] = rem.value
-        return n.value
+        return n.value if wait else None
 
     def sample_uniform_source(self, seg_xy, mdot, v_drift, dt):
         """UniformSource on one straight segment: mass flow rate mdot (kg/s), cold beam

@@ -140,3 +140,29 @@ def test_dsmc_without_count_readback(gpulib):
         assert km.get_np() == n
     finally:
         dom.close()
+
+
+def test_source_without_count_readback(gpulib):
+    """sf_source_maxwellian with n_added NULL: draw k takes slot n + k, a draw outside the
+    mesh leaves its slot removed.  The particles equal those of the counted call as a set;
+    the counts agree once read."""
+    from starfish_gb300.plugin import GpuDomain, KineticMaterial
+    spec = _open_box(65, 33)
+    # a segment reaching past the top of the mesh: part of the draws land outside
+    seg = np.array([spec.x0[0] + 20e-3, spec.x0[1] + 40e-3, spec.x0[0] + 20e-3, spec.x0[1] + 10e-3])
+    out = []
+    for wait in (True, False):
+        dom = GpuDomain(spec)
+        try:
+            dom.set_seed(7)
+            dom.set_efield(np.zeros(spec.nn), np.zeros(spec.nn))
+            km = KineticMaterial(dom, 16 * 1.6605e-27, 1.602e-19, 1e5, capacity=200_000)
+            for _ in range(3):
+                r = km.sample_maxwellian_source(seg, 1e12, 5000.0, 1000.0, 1e-7, wait=wait)
+                assert (r is None) != wait
+            out.append((km.get_np(), _sorted(*km.download())))
+        finally:
+            dom.close()
+    (n0, p0), (n1, p1) = out
+    assert 0 < n0 == n1
+    assert np.array_equal(p0, p1)

@@ -241,7 +241,7 @@ int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg_xy, double 
 /* UniformSource on one straight segment (sources/UniformSource.java:36-80): mass flow rate
  * mdot (kg/s) with the particle count of Source.regenerate; particles at random points of
  * the segment (area-weighted in RZ / ZR), velocity normal * v_drift with no thermal spread;
- * the push off the surface and the rewind as sf_source_maxwellian. */
+ * the push off the surface, the rewind and a null n_added as sf_source_maxwellian. */
 int sf_source_uniform(sf_ctx* ctx, int32_t sid, const double* seg_xy, double mdot, double v_drift,
                       double dt, double* rem, int64_t* n_added);
 /* VolumePreloadSource (sources/VolumePreloadSource.java:44-66) through VolumeSource

@@ -353,8 +353,8 @@ extern "C" int sf_source_maxwellian(sf_ctx* ctx, int32_t sid, const double* seg,
 extern "C" int sf_source_uniform(sf_ctx* ctx, int32_t sid, const double* seg, double mdot, double v_drift, double dt,
                                  double* rem, int64_t* n_added) {
   SF_API_BEGIN
-  SfSpecies* sp = get_species(ctx, sid);
-  SF_REQUIRE(seg && rem && n_added, SF_ERR_ARG, "null argument");
+  SfSpecies* sp = n_added ? get_species(ctx, sid) : get_species_nowait(ctx, sid);
+  SF_REQUIRE(seg && rem, SF_ERR_ARG, "null argument");
   SF_REQUIRE(mdot >= 0 && dt > 0, SF_ERR_ARG, "bad source parameters");
   SF_REQUIRE(ctx->efield_set, SF_ERR_STATE, "electric field not set (the rewind gathers E)");
   SF_CUDA(cudaSetDevice(ctx->device));
@@ -363,9 +363,10 @@ extern "C" int sf_source_uniform(sf_ctx* ctx, int32_t sid, const double* seg, do
   const double mp = (mdot * dt) / (sp->mass * sp->spwt) + *rem;
   const int64_t num = (int64_t)mp;
   *rem = mp - (double)num;
-  *n_added = 0;
+  if (n_added) *n_added = 0;
   if (num <= 0) return SF_OK;
-  *n_added = segment_source(ctx, sp, sid, seg, num, v_drift, 0.0, dt, 1);
+  const int64_t added = segment_source(ctx, sp, sid, seg, num, v_drift, 0.0, dt, 1, n_added != nullptr);
+  if (n_added) *n_added = added;
   SF_API_END(ctx)
 }
 

@@ -216,11 +216,16 @@ __device__ __forceinline__ void level_down_body(const LevelView F, const LevelVi
   }
   __syncthreads();
   tile_sweeps<WX, WY>(sy, sr, sp, st, 0, F.cx, F.cy);
-  // the tile's y (read back by the prolongation), and the residual on it plus one ring,
-  // in place of r (a node reads only its own r)
+  // the tile's y, also into t: the way up reads its tile and halo from t and writes y, so
+  // that no block reads a node another block of the same launch has already written; and
+  // the residual on the tile plus one ring, in place of r (a node reads only its own r)
   for (int k = threadIdx.x; k < TX * TY; k += TILE_NT) {
     const int gi = bx * TX + k % TX, gj = by * TY + k / TX;
-    if (gi < F.ni && gj < F.nj) F.y[gj * F.ni + gi] = sy[(k / TX + H) * WX + k % TX + H];
+    if (gi < F.ni && gj < F.nj) {
+      const float v = sy[(k / TX + H) * WX + k % TX + H];
+      F.y[gj * F.ni + gi] = v;
+      F.t[gj * F.ni + gi] = v;
+    }
   }
   constexpr int RX = TX + 2, RY = TY + 2;
   for (int k = threadIdx.x; k < RX * RY; k += TILE_NT) {
@@ -239,7 +244,8 @@ __device__ __forceinline__ void level_down_body(const LevelView F, const LevelVi
   }
 }
 
-// F.y += prolongation of C.y (not on fixed nodes), then the post-smoothing
+// F.y = F.t (the way down's y) + prolongation of C.y (not on fixed nodes), then the
+// post-smoothing
 template <int TX, int TY>
 __device__ __forceinline__ void level_up_body(const LevelView F, const LevelView C, int bx, int by) {
   constexpr int H = 4, WX = TX + 2 * H, WY = TY + 2 * H, NW = WX * WY, NL = (NW + TILE_NT - 1) / TILE_NT;
@@ -254,7 +260,7 @@ __device__ __forceinline__ void level_up_body(const LevelView F, const LevelView
     const int gi = gi0 + q % WX, gj = gj0 + q / WX;
     const bool in = q < NW && gi >= 0 && gi < F.ni && gj >= 0 && gj < F.nj;
     const int u = in ? gj * F.ni + gi : 0;
-    vy[k] = F.y[u];
+    vy[k] = F.t[u];
     vr[k] = F.r[u];
     vp[k] = F.P[u];
     vt[k] = in ? F.type[u] : TILE_OUT;

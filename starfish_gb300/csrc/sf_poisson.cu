@@ -216,16 +216,13 @@ __device__ __forceinline__ void level_down_body(const LevelView F, const LevelVi
   }
   __syncthreads();
   tile_sweeps<WX, WY>(sy, sr, sp, st, 0, F.cx, F.cy);
-  // the tile's y, also into t: the way up reads its tile and halo from t and writes y, so
-  // that no block reads a node another block of the same launch has already written; and
-  // the residual on the tile plus one ring, in place of r (a node reads only its own r)
+  // the tile's y into the level's scratch t: the way up reads its tile and halo from t and
+  // writes y, so that no block reads a node another block of the same launch has already
+  // written; and the residual on the tile plus one ring, in place of r (a node reads only
+  // its own r)
   for (int k = threadIdx.x; k < TX * TY; k += TILE_NT) {
     const int gi = bx * TX + k % TX, gj = by * TY + k / TX;
-    if (gi < F.ni && gj < F.nj) {
-      const float v = sy[(k / TX + H) * WX + k % TX + H];
-      F.y[gj * F.ni + gi] = v;
-      F.t[gj * F.ni + gi] = v;
-    }
+    if (gi < F.ni && gj < F.nj) F.t[gj * F.ni + gi] = sy[(k / TX + H) * WX + k % TX + H];
   }
   constexpr int RX = TX + 2, RY = TY + 2;
   for (int k = threadIdx.x; k < RX * RY; k += TILE_NT) {

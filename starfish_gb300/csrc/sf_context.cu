@@ -32,6 +32,7 @@ sf::MeshView sf_ctx::mesh_view() const {
   m.inv_dy = (float)(1.0 / dh[1]);
   m.E = E;
   m.seg_dist = seg_dist;
+  m.seg_dist_tile = seg_dist_tile;
   m.node_seg_ptr = node_seg_ptr;
   m.node_seg_idx = node_seg_idx;
   m.seg_xy = d_seg_xy;
@@ -731,6 +732,17 @@ int sf_ctx_create(const sf_mesh_desc* md, int device, sf_ctx** out) {
     SF_CUDA(cudaMemsetAsync(ctx->E, 0, sizeof(float4) * nn, ctx->stream));
     SF_CUDA(cudaMalloc(&ctx->seg_dist, nn));
     copy_wait(ctx->seg_dist, sd.data(), nn, cudaMemcpyHostToDevice, ctx->stream);
+    {
+      const int tx = (ctx->ni + 15) / 16, ty = (ctx->nj + 15) / 16;
+      std::vector<uint8_t> st((size_t)tx * ty, 255);
+      for (int j = 0; j < ctx->nj; j++)
+        for (int i = 0; i < ctx->ni; i++) {
+          uint8_t& t = st[(size_t)(j >> 4) * tx + (i >> 4)];
+          t = std::min(t, sd[(size_t)j * ctx->ni + i]);
+        }
+      SF_CUDA(cudaMalloc(&ctx->seg_dist_tile, st.size()));
+      copy_wait(ctx->seg_dist_tile, st.data(), st.size(), cudaMemcpyHostToDevice, ctx->stream);
+    }
     SF_CUDA(cudaMalloc(&ctx->node_seg_ptr, sizeof(int) * (nn + 1)));
     copy_wait(ctx->node_seg_ptr, ptr.data(), sizeof(int) * (nn + 1), cudaMemcpyHostToDevice, ctx->stream);
     SF_CUDA(cudaMalloc(&ctx->node_seg_idx, sizeof(int) * std::max<size_t>(idx.size(), 1)));
@@ -814,7 +826,7 @@ int sf_ctx_destroy(sf_ctx* ctx) {
       if (p) cudaFree(p);
     delete sp;
   }
-  void* ptrs[] = {ctx->E, ctx->seg_dist, ctx->node_seg_ptr, ctx->node_seg_idx, ctx->d_seg_xy, ctx->d_seg_lc,
+  void* ptrs[] = {ctx->E, ctx->seg_dist, ctx->seg_dist_tile, ctx->node_seg_ptr, ctx->node_seg_idx, ctx->d_seg_xy, ctx->d_seg_lc,
                   ctx->d_seg_btype, ctx->d_face_type, ctx->d_node_vol, ctx->slow_idx, ctx->counters,
                   ctx->stats_partial, ctx->bins, ctx->bins_tmp, ctx->scan_blocks, ctx->dscratch};
   for (void* p : ptrs)

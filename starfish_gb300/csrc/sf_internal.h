@@ -111,6 +111,8 @@ struct MeshView {
   const float4* E;              // ni*nj: node u holds (efi, efj) of u and of u + 1, FP32
   const uint8_t* seg_dist;      // ni*nj Chebyshev distance to the nearest node listing a
                                 // DIRICHLET/SINK segment (255 = none within 255)
+  const uint8_t* seg_dist_tile; // per 16x16-node tile (row of (ni + 15) / 16): the least
+                                // seg_dist of its nodes (a few KB, stays in L1)
   const int* node_seg_ptr;      // ni*nj+1
   const int* node_seg_idx;
   const Seg4* seg_xy;        // x1, y1, x2, y2
@@ -400,6 +402,7 @@ struct sf_ctx {
   int ntx = 0, nty = 0;     // 16x16-cell tiles of the sort key
   int nkeys = 0;            // ntx*nty*256
   uint8_t* seg_dist = nullptr;
+  uint8_t* seg_dist_tile = nullptr;
   int* node_seg_ptr = nullptr;
   int* node_seg_idx = nullptr;
   sf::Seg4* d_seg_xy = nullptr;

@@ -212,7 +212,9 @@ __device__ __forceinline__ void push_tile(const MeshView& m, const ParticlesView
         const int i2 = i + di, j2 = j + dj;
         const int span = max(abs(di), abs(dj)) + 1;
         const bool inside = (i2 >= 0) & (j2 >= 0) & (i2 <= m.ni - 2) & (j2 <= m.nj - 2);
-        bool clear = (int)__ldg(&m.seg_dist[j * m.ni + i]) > span;
+        // the tile's least distance first (L1-resident); the node's own only near segments
+        bool clear = (int)__ldg(&m.seg_dist_tile[(j >> 4) * ((m.ni + 15) >> 4) + (i >> 4)]) > span ||
+                     (int)__ldg(&m.seg_dist[j * m.ni + i]) > span;
         if (PRE && !clear) clear = !may_hit_fp32(m, i, j, f.x, f.y, gx, gy);
         if (inside && clear) {
           __stcs(tcell + q, pack_cell(i2, j2));
